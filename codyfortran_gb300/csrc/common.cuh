@@ -1,0 +1,220 @@
+// common.cuh -- shared types and kernel launchers of the GB300 MCTDHX/TDCI engine.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/cody_gpu.h"
+
+// ---------------------------------------------------------------------------
+// Complex arithmetic on double2 (layout-compatible with Fortran complex(R64)).
+// ---------------------------------------------------------------------------
+typedef double2 z_t;
+
+__host__ __device__ __forceinline__ z_t zmk(double r, double i) { return make_double2(r, i); }
+__host__ __device__ __forceinline__ z_t zadd(z_t a, z_t b) { return make_double2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ z_t zsub(z_t a, z_t b) { return make_double2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ z_t zmul(z_t a, z_t b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ z_t zconj(z_t a) { return make_double2(a.x, -a.y); }
+__host__ __device__ __forceinline__ z_t zscale(z_t a, double s) { return make_double2(a.x * s, a.y * s); }
+// conj(a) * b
+__host__ __device__ __forceinline__ z_t zcmul(z_t a, z_t b) {
+  return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+// a += b * c
+__host__ __device__ __forceinline__ void zfma(z_t& a, z_t b, z_t c) {
+  a.x = fma(b.x, c.x, fma(-b.y, c.y, a.x));
+  a.y = fma(b.x, c.y, fma(b.y, c.x, a.y));
+}
+// multiply by -i
+__host__ __device__ __forceinline__ z_t zmi(z_t a) { return make_double2(a.y, -a.x); }
+// multiply by +i
+__host__ __device__ __forceinline__ z_t zpi(z_t a) { return make_double2(-a.y, a.x); }
+
+#define CODY_MAX_BT 4
+#define CODY_MAX_ORBS 64
+#define CODY_MAX_KRYLOV 64
+
+// ---------------------------------------------------------------------------
+// Per-body-type configuration tables (ConfigList), generated on the device.
+// Layout as the reference: (maxConn, nConf) column-major, 1-based indices.
+// ---------------------------------------------------------------------------
+struct CiTables {
+  int nOrbs, nBodies, nConf, maxS, maxD, shift;
+  int64_t* codes;      // codeFromConfig
+  int* sN;             // singles nConnected
+  int* sExc;           // singles excitedC
+  int* sCode;          // singles orbCode
+  int8_t* sFac;        // singles factor (+-1)
+  int* dN;
+  int* dExc;
+  int* dCode;
+  int8_t* dFac;
+  int* rankTab;        // (nBodies+1) x (nOrbs+1) additive rank table
+};
+
+// Device view of the CI layout for the traversal kernels.
+struct CiView {
+  int nBt, nO, nC;
+  int stride[CODY_MAX_BT];
+  int nConf[CODY_MAX_BT];
+  int maxS[CODY_MAX_BT], maxD[CODY_MAX_BT];
+  const int* sN[CODY_MAX_BT];
+  const int* sExc[CODY_MAX_BT];
+  const int* sCode[CODY_MAX_BT];
+  const int8_t* sFac[CODY_MAX_BT];
+  const int* dN[CODY_MAX_BT];
+  const int* dExc[CODY_MAX_BT];
+  const int* dCode[CODY_MAX_BT];
+  const int8_t* dFac[CODY_MAX_BT];
+};
+
+// ---------------------------------------------------------------------------
+// The context: one system, its device-resident operators, tables and work
+// buffers, and one CUDA stream.  Not reentrant (one host thread at a time),
+// like the reference's module-global state.
+// ---------------------------------------------------------------------------
+struct cgpu_ctx {
+  // sizes
+  int nG = 0, nBt = 0, nO = 0, nOS = 0, nC = 0, nS = 0, restricted = 0, method = 0, precision = 0;
+  int band = 0, nBtK = 1;
+  int nBodies[CODY_MAX_BT] = {0}, nOrbs[CODY_MAX_BT] = {0}, orbStart[CODY_MAX_BT] = {0};
+  double mass[CODY_MAX_BT] = {0};
+  double regEps = 1e-10;
+  int hasPotential = 0, hasInteraction = 0;
+  // laser
+  int laserKind = 0;
+  double E0 = 0, omega = 0, nCycles = 0, cep = 0, tStart = 0, sampleDt = 1, sampleT0 = 0;
+  std::vector<double> samples;
+  // host copies
+  std::vector<double> x, w, V0, band_h;
+  std::vector<int> btOfOrb;
+  // device operators
+  double *x_d = nullptr, *w_d = nullptr, *V0_d = nullptr, *T_d = nullptr, *Vint_d = nullptr, *metric_d = nullptr;
+  double *metricW_d = nullptr, *metricOne_d = nullptr;  // [1 | w per orbital point] and all ones
+  double *metricUser_d = nullptr;                      // caller-supplied SIL metric
+  float* Vint_f = nullptr;
+  int* btOfOrb_d = nullptr;
+  // CI
+  CiTables tab[CODY_MAX_BT];
+  CiView view;
+  z_t *h1Lin_d = nullptr, *h2Lin_d = nullptr, *rdm1Lin_d = nullptr, *rdm2Lin_d = nullptr;
+  z_t *rdm1_d = nullptr, *rdm2_d = nullptr, *h1_d = nullptr, *h2_d = nullptr;
+  // mean-field
+  int nPairs = 0;
+  int *pairL_d = nullptr, *pairK_d = nullptr, *pidx_d = nullptr;
+  z_t *S_d = nullptr, *W_d = nullptr;         // (nG, nPairs) row-major by grid point
+  z_t *Sfull_d = nullptr, *Wfull_d = nullptr; // (nG, nOS*nOS) row-major by grid point
+  z_t *Rp_d = nullptr;                        // (nOS^2, nOS^2) correlation matrix
+  z_t *h2s_d = nullptr;                       // (nOS^2, nOS^2) spatial h2 block
+  z_t *Mreg_d = nullptr;                      // (nOS, nOS)
+  z_t *r1s_d = nullptr, *r2s_d = nullptr;     // spin-summed spatial RDMs
+  // reductions / scratch
+  z_t* partial_d = nullptr;
+  size_t partialCap = 0;
+  z_t *gram_d = nullptr;                      // (nOS, nOS)
+  z_t *orbTmp_d = nullptr;                    // (nG, nOS)
+  double* scal_d = nullptr;                   // misc device scalars
+  // state and integrators
+  z_t *state_d = nullptr, *dstate_d = nullptr, *rkInc_d = nullptr, *rkTmp_d = nullptr, *rkStage_d = nullptr;
+  z_t *basis_d = nullptr, *lw_d = nullptr, *trial_d = nullptr, *work_d = nullptr;
+  int maxKrylov = 0;
+  double* lz_d = nullptr;   // Lanczos scalars: alpha, beta, dots, phi, flags
+  double* lz_h = nullptr;   // pinned mirror
+  // TDCI static data
+  z_t* tdciOrbs_d = nullptr;
+  // stream / graph
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t stepGraph = nullptr;
+  double graphDt = 0;
+  int graphKrylov = 0;
+  std::string lastError;
+  int launches = 0;  // kernels launched by this context (since the last reset)
+  // profiling: CUDA events around every launch of one kernel family
+  int profTarget = 0;
+  std::vector<cudaEvent_t> profEvents;  // start/stop pairs
+  size_t profUsed = 0;
+};
+
+// Records CUDA events on the context stream around the launches of kernel
+// family `id` while profiling of that family is enabled.
+struct ProfScope {
+  cgpu_ctx* c;
+  bool on;
+  ProfScope(cgpu_ctx* ctx, int id) : c(ctx), on(ctx->profTarget == id) {
+    if (on) record();
+  }
+  ~ProfScope() {
+    if (on) record();
+  }
+  void record() {
+    if (c->profUsed >= c->profEvents.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      c->profEvents.push_back(e);
+    }
+    cudaEventRecord(c->profEvents[c->profUsed++], c->stream);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Launchers (defined in the k_*.cu translation units).
+// ---------------------------------------------------------------------------
+// k_onebody.cu
+void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha, int accumulate);
+void launch_gram(cgpu_ctx* c, z_t* G, const z_t* A, const z_t* B, int nCols, int colA0, int colB0, int ldG,
+                 double scale);
+void launch_project_orbs(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs);
+void launch_project_coeffs(cgpu_ctx* c, z_t* dC, const z_t* C);
+void launch_fill_h1_from(cgpu_ctx* c, const z_t* orbs, const z_t* hOrbs, z_t* h1);
+void launch_axpby(cgpu_ctx* c, z_t* y, const z_t* x, z_t a, z_t b, size_t n);  // y = a x + b y
+void launch_rk_stage(cgpu_ctx* c, z_t* inc, z_t* tmp, const z_t* state, const z_t* d, double wInc, double wTmp,
+                     int first, size_t n);
+void launch_scale(cgpu_ctx* c, z_t* y, z_t a, size_t n);
+void launch_orthonormalize(cgpu_ctx* c, z_t* orbs, int col0, int nCols);
+void launch_normalize_coeffs(cgpu_ctx* c, z_t* C);
+void launch_energy(cgpu_ctx* c, double* out_d);
+// k_ci.cu
+void ci_build_tables(cgpu_ctx* c);
+void launch_ci_rdm(cgpu_ctx* c, const z_t* C, int want1, int want2);
+void launch_ci_apply(cgpu_ctx* c, const z_t* C, z_t* dC, int useH1, int useH2);
+void launch_fold_h1(cgpu_ctx* c);
+void launch_fold_h2(cgpu_ctx* c);
+// k_mf.cu
+void launch_pair_potentials(cgpu_ctx* c, const z_t* orbs);
+void launch_correlation(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2);
+void launch_fill_h2(cgpu_ctx* c, const z_t* orbs);
+void launch_expand_h2(cgpu_ctx* c);
+void launch_rdm_inverse(cgpu_ctx* c);
+// k_lanczos.cu
+// The SIL kernels work on c->basis_d, c->lw_d (H v_j), c->work_d (start vector),
+// c->metric_d (current metric) and the scalar block c->lz_d.
+void launch_lanczos_start(cgpu_ctx* c, const z_t* v);
+void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim);
+void launch_lanczos_tail(cgpu_ctx* c, int j, double dt, int evalExp);  // j = 0: use the device mDim
+void launch_lanczos_combine(cgpu_ctx* c, z_t* out);
+void launch_lz_set(cgpu_ctx* c, int idx, double v);
+#define CODY_LZ_ERR 385
+#define CODY_LZ_MDIM 386
+#define CODY_LZ_DONE 387
+#define CODY_LZ_BREAKJ 390
+
+// error helpers
+#define CODY_CUDA(call)                                                                              \
+  do {                                                                                                \
+    cudaError_t e_ = (call);                                                                          \
+    if (e_ != cudaSuccess) throw std::string(#call) + ": " + cudaGetErrorString(e_);                  \
+  } while (0)
+
+#define CODY_LAUNCHED(c) \
+  do {                   \
+    (c)->launches++;     \
+    CODY_CUDA(cudaGetLastError()); \
+  } while (0)
+
+double cody_field_amplitude(const cgpu_ctx* c, double t);

@@ -1,0 +1,394 @@
+// k_lanczos.cu -- short-iterative-Lanczos kernels
+// (PerformLanczosStep / EvaluateExpInSubspace / MetricDot,
+//  src/IntegratorList/Sil/S_IntegratorList_Sil.f90:184-310).
+//
+// Per Krylov iteration j the reference does
+//   w = H v_j - beta_{j-1} v_{j-1};  alpha_j = Re<v_j,w>;  w -= alpha_j v_j;
+//   for k = 1..j: w -= <v_k,w> v_k   (modified Gram-Schmidt);  beta_j = ||w||.
+// With the basis orthonormal, the projections it removes are those of H v_j on
+// v_1..v_j; the kernels remove them in two classical Gram-Schmidt passes
+// (each pass one fused reduction), which reproduces the reference's vectors
+// and coefficients to rounding.  Every reduction is deterministic: per-block
+// partials in a fixed order, re-summed identically by every consumer block.
+//
+// Device scalar block lz[] (doubles):
+#include "common.cuh"
+
+namespace {
+
+constexpr int LZ_ALPHA = 0;     // alpha_j          [0, 64)
+constexpr int LZ_BETA = 64;     // beta_j           [64, 128)
+constexpr int LZ_D = 128;       // dots (complex)   [128, 256)
+constexpr int LZ_PHI = 256;     // phi (complex)    [256, 384)
+constexpr int LZ_NRM = 384;     // state norm
+constexpr int LZ_ERR = 385;     // error estimate
+constexpr int LZ_MDIM = 386;    // subspace dimension used
+constexpr int LZ_DONE = 387;    // breakdown flag (1 = stop growing)
+constexpr int LZ_ZERO = 388;    // zero-norm start (output = input)
+constexpr int LZ_DT = 389;      // dt of the current sub-step
+constexpr int LZ_BREAKJ = 390;  // iteration at which breakdown happened
+
+constexpr int LZ_BLOCKS = 148;
+constexpr int LZ_THREADS = 256;
+
+__device__ z_t block_sum2(z_t v) {
+  __shared__ z_t red[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+  }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  int nw = (blockDim.x + 31) >> 5;
+  v = (threadIdx.x < nw) ? red[threadIdx.x] : zmk(0.0, 0.0);
+  if (wid == 0)
+    for (int o = 16; o > 0; o >>= 1) {
+      v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+  return v;
+}
+
+// part[blk*nVec + k] = sum_{i in blk} conj(V_k[i]) m[i] w[i]
+__global__ void k_mdot(z_t* __restrict__ part, const z_t* __restrict__ V, size_t ldv, int nVec,
+                       const z_t* __restrict__ w, const double* __restrict__ m, size_t n, const double* __restrict__ lz) {
+  if (lz && lz[LZ_DONE] != 0.0) return;
+  for (int k = 0; k < nVec; k++) {
+    z_t s = zmk(0.0, 0.0);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      z_t a = V[ldv * k + i], b = zscale(w[i], m[i]);
+      s.x += a.x * b.x + a.y * b.y;
+      s.y += a.x * b.y - a.y * b.x;
+    }
+    s = block_sum2(s);
+    if (threadIdx.x == 0) part[(size_t)blockIdx.x * nVec + k] = s;
+  }
+}
+
+// Every block re-sums the partials (fixed order) into shared coefficients,
+// subtracts w -= sum_k coef_k V_k, then emits partials for the next pass:
+// mode 0: dots of the new w with V_0..V_{nVec-1}; mode 1: metric norm^2 of the new w.
+// Block 0 stores the coefficients of the first pass at lz[LZ_D].
+__global__ void k_cgs_pass(z_t* __restrict__ w, const z_t* __restrict__ V, size_t ldv, int nVec,
+                           const z_t* __restrict__ partIn, int nBlkIn, z_t* __restrict__ partOut,
+                           const double* __restrict__ m, size_t n, double* __restrict__ lz, int mode, int storeDots) {
+  if (lz[LZ_DONE] != 0.0) return;
+  __shared__ z_t coef[CODY_MAX_KRYLOV];
+  for (int k = threadIdx.x; k < nVec; k += blockDim.x) {
+    z_t s = zmk(0.0, 0.0);
+    for (int b = 0; b < nBlkIn; b++) s = zadd(s, partIn[(size_t)b * nVec + k]);
+    coef[k] = s;
+    if (storeDots && blockIdx.x == 0) {
+      lz[LZ_D + 2 * k] = s.x;
+      lz[LZ_D + 2 * k + 1] = s.y;
+    }
+  }
+  __syncthreads();
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    z_t r = w[i];
+    for (int k = 0; k < nVec; k++) {
+      z_t v = V[ldv * k + i];
+      z_t cf = coef[k];
+      r.x -= cf.x * v.x - cf.y * v.y;
+      r.y -= cf.x * v.y + cf.y * v.x;
+    }
+    w[i] = r;
+  }
+  __syncthreads();
+  if (mode == 0) {
+    for (int k = 0; k < nVec; k++) {
+      z_t s = zmk(0.0, 0.0);
+      for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        z_t a = V[ldv * k + i], b = zscale(w[i], m[i]);
+        s.x += a.x * b.x + a.y * b.y;
+        s.y += a.x * b.y - a.y * b.x;
+      }
+      s = block_sum2(s);
+      if (threadIdx.x == 0) partOut[(size_t)blockIdx.x * nVec + k] = s;
+    }
+  } else {
+    z_t s = zmk(0.0, 0.0);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      z_t b = w[i];
+      s.x += (b.x * b.x + b.y * b.y) * m[i];
+    }
+    s = block_sum2(s);
+    if (threadIdx.x == 0) partOut[blockIdx.x] = s;
+  }
+}
+
+// beta_j = sqrt(sum partials); alpha_j from the first-pass dot; v_{j+1} = w / beta_j.
+// j is 1-based; alpha/beta stored at index j-1.
+__global__ void k_lz_finish(z_t* __restrict__ vNext, const z_t* __restrict__ w, const z_t* __restrict__ partIn,
+                            int nBlkIn, size_t n, double* __restrict__ lz, int j, int maxDim, double zeroThr) {
+  if (lz[LZ_DONE] != 0.0) return;
+  __shared__ double beta;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nBlkIn; b++) s += partIn[b].x;
+    beta = sqrt(s);
+  }
+  __syncthreads();
+  double be = beta;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    lz[LZ_ALPHA + j - 1] = lz[LZ_D + 2 * (j - 1)];
+    lz[LZ_BETA + j - 1] = be;
+  }
+  bool breakdown = be <= zeroThr;
+  if (breakdown || j == maxDim) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      lz[LZ_MDIM] = j;
+      if (breakdown) {
+        lz[LZ_BREAKJ] = j;
+      }
+    }
+    return;
+  }
+  if (vNext == nullptr) return;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    z_t v = w[i];
+    vNext[i] = zmk(v.x / be, v.y / be);
+  }
+}
+
+__global__ void k_lz_mark_done(double* lz, int j) {
+  // executed after k_lz_finish of iteration j: a breakdown stops the growth
+  if (lz[LZ_DONE] == 0.0 && lz[LZ_BREAKJ] == (double)j) lz[LZ_DONE] = 1.0;
+}
+
+// ---------------------------------------------------------------------------
+// EvaluateExpInSubspace: eig of the m x m tridiagonal (one warp, parallel
+// round-robin Jacobi), phi = U exp(-i dt L) U^T e1, err = beta_m |phi_m|.
+// m <= 32.  Writes phi and the error estimate to lz.
+// ---------------------------------------------------------------------------
+__global__ void k_lz_expsub(double* __restrict__ lz, int mFixed, double dt, double tol) {
+  __shared__ double A[32][33];
+  __shared__ double U[32][33];
+  __shared__ double rc[16], rs[16];
+  __shared__ int rp[16], rq[16];
+  int lane = threadIdx.x;
+  int m = mFixed > 0 ? mFixed : (int)lz[LZ_MDIM];
+  if (m > 32) m = 32;
+  for (int i = 0; i < 32; i++) {
+    A[i][lane] = 0.0;
+    U[i][lane] = (i == lane) ? 1.0 : 0.0;
+  }
+  __syncwarp();
+  if (lane < m) {
+    A[lane][lane] = lz[LZ_ALPHA + lane];
+    if (lane + 1 < m) {
+      A[lane][lane + 1] = lz[LZ_BETA + lane];
+      A[lane + 1][lane] = lz[LZ_BETA + lane];
+    }
+  }
+  __syncwarp();
+  int ne = (m + 1) & ~1;
+  int half = ne / 2;
+  for (int sweep = 0; sweep < 60 && m > 1; sweep++) {
+    double off = 0.0, dg = 0.0;
+    if (lane < m)
+      for (int i = 0; i < m; i++) {
+        double a = A[i][lane];
+        if (i == lane) dg += a * a; else off += a * a;
+      }
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      dg += __shfl_xor_sync(0xffffffffu, dg, o);
+    }
+    if (off <= 1e-34 * (dg + off) || off == 0.0) break;
+    for (int r = 0; r < ne - 1; r++) {
+      if (lane < half) {
+        auto pos = [&](int i) { return i == 0 ? 0 : ((i - 1 + r) % (ne - 1)) + 1; };
+        int p = pos(lane), q = pos(ne - 1 - lane);
+        if (p > q) { int t = p; p = q; q = t; }
+        double c = 1.0, s = 0.0;
+        if (q < m) {
+          double g = A[p][q];
+          if (g != 0.0) {
+            double tau = (A[q][q] - A[p][p]) / (2.0 * g);
+            double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + t * t);
+            s = t * c;
+          }
+        } else {
+          q = -1;
+        }
+        rp[lane] = p;
+        rq[lane] = q;
+        rc[lane] = c;
+        rs[lane] = s;
+      }
+      __syncwarp();
+      if (lane < m)
+        for (int k = 0; k < half; k++) {
+          int p = rp[k], q = rq[k];
+          if (q < 0 || rs[k] == 0.0) continue;
+          double c = rc[k], s = rs[k];
+          double akp = A[lane][p], akq = A[lane][q];
+          A[lane][p] = akp * c - akq * s;
+          A[lane][q] = akp * s + akq * c;
+          double vkp = U[lane][p], vkq = U[lane][q];
+          U[lane][p] = vkp * c - vkq * s;
+          U[lane][q] = vkp * s + vkq * c;
+        }
+      __syncwarp();
+      if (lane < m)
+        for (int k = 0; k < half; k++) {
+          int p = rp[k], q = rq[k];
+          if (q < 0 || rs[k] == 0.0) continue;
+          double c = rc[k], s = rs[k];
+          double apk = A[p][lane], aqk = A[q][lane];
+          A[p][lane] = c * apk - s * aqk;
+          A[q][lane] = s * apk + c * aqk;
+        }
+      __syncwarp();
+      if (lane < half) {
+        int p = rp[lane], q = rq[lane];
+        if (q >= 0 && rs[lane] != 0.0) {
+          A[p][q] = 0.0;
+          A[q][p] = 0.0;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  // phi_i = sum_j U(i,j) U(0,j) exp(-i dt lambda_j)
+  if (lane < m) {
+    double pr = 0.0, pi = 0.0;
+    for (int j = 0; j < m; j++) {
+      double lam = A[j][j];
+      double sn, cs;
+      sincos(dt * lam, &sn, &cs);
+      double coef = U[0][j];
+      pr += U[lane][j] * coef * cs;
+      pi -= U[lane][j] * coef * sn;
+    }
+    lz[LZ_PHI + 2 * lane] = pr;
+    lz[LZ_PHI + 2 * lane + 1] = pi;
+    if (lane == m - 1) {
+      double err = lz[LZ_BETA + m - 1] * sqrt(pr * pr + pi * pi);
+      if (lz[LZ_BREAKJ] == (double)m) err = 0.0;
+      lz[LZ_ERR] = err;
+      (void)tol;
+    }
+  }
+}
+
+// out = nrm * sum_{j < mDim} phi_j V_j   (or out = in when the start vector had zero norm)
+__global__ void k_lz_combine(z_t* __restrict__ out, const z_t* __restrict__ in, const z_t* __restrict__ V,
+                             size_t ldv, size_t n, const double* __restrict__ lz) {
+  __shared__ z_t phi[CODY_MAX_KRYLOV];
+  int m = (int)lz[LZ_MDIM];
+  double nrm = lz[LZ_NRM];
+  bool zero = lz[LZ_ZERO] != 0.0;
+  for (int k = threadIdx.x; k < m; k += blockDim.x) phi[k] = zmk(lz[LZ_PHI + 2 * k], lz[LZ_PHI + 2 * k + 1]);
+  __syncthreads();
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if (zero) {
+      out[i] = in[i];
+      continue;
+    }
+    z_t acc = zmk(0.0, 0.0);
+    for (int k = 0; k < m; k++) zfma(acc, V[ldv * k + i], phi[k]);
+    out[i] = zscale(acc, nrm);
+  }
+}
+
+// nrm = sqrt(<s,s>_m); v1 = s / nrm; resets the per-step flags.
+__global__ void k_lz_start(z_t* __restrict__ v1, const z_t* __restrict__ s, const z_t* __restrict__ partIn, int nBlkIn,
+                           size_t n, double* __restrict__ lz, double zeroThr) {
+  __shared__ double nrm;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int b = 0; b < nBlkIn; b++) t += partIn[b].x;
+    nrm = sqrt(t);
+  }
+  __syncthreads();
+  double nr = nrm;
+  bool zero = nr <= zeroThr;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    lz[LZ_NRM] = nr;
+    lz[LZ_ZERO] = zero ? 1.0 : 0.0;
+    lz[LZ_DONE] = zero ? 1.0 : 0.0;
+    lz[LZ_BREAKJ] = -1.0;
+    lz[LZ_MDIM] = 0.0;
+    lz[LZ_ERR] = 0.0;
+  }
+  if (zero) return;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    z_t v = s[i];
+    v1[i] = zmk(v.x / nr, v.y / nr);
+  }
+}
+
+__global__ void k_norm_partial(z_t* __restrict__ part, const z_t* __restrict__ v, const double* __restrict__ m, size_t n) {
+  z_t s = zmk(0.0, 0.0);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    z_t b = v[i];
+    s.x += (b.x * b.x + b.y * b.y) * m[i];
+  }
+  s = block_sum2(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+void ensure_lz_partial(cgpu_ctx* c) {
+  size_t need = (size_t)LZ_BLOCKS * (CODY_MAX_KRYLOV + 1) * 2;
+  if (c->partialCap >= need) return;
+  if (c->partial_d) cudaFree(c->partial_d);
+  CODY_CUDA(cudaMalloc(&c->partial_d, need * sizeof(z_t)));
+  c->partialCap = need;
+}
+
+}  // namespace
+
+// Starts a Lanczos pass from the vector v (device, nS): basis[:,0] = v/|v|.
+void launch_lanczos_start(cgpu_ctx* c, const z_t* v) {
+  ensure_lz_partial(c);
+  k_norm_partial<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(c->partial_d, v, c->metric_d, c->nS);
+  CODY_LAUNCHED(c);
+  k_lz_start<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(c->basis_d, v, c->partial_d, LZ_BLOCKS, c->nS, c->lz_d, 1.0e-14);
+  CODY_LAUNCHED(c);
+}
+
+// After lw_d holds H v_j: CGS2 against v_1..v_j, beta_j, v_{j+1}.
+void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
+  ProfScope prof(c, CGPU_KERNEL_LANCZOS);
+  ensure_lz_partial(c);
+  size_t nS = c->nS;
+  z_t* p1 = c->partial_d;
+  z_t* p2 = c->partial_d + (size_t)LZ_BLOCKS * (CODY_MAX_KRYLOV + 1);
+  k_mdot<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(p1, c->basis_d, nS, j, c->lw_d, c->metric_d, nS, c->lz_d);
+  CODY_LAUNCHED(c);
+  k_cgs_pass<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, nS, j, p1, LZ_BLOCKS, p2, c->metric_d, nS,
+                                                       c->lz_d, 0, 1);
+  CODY_LAUNCHED(c);
+  k_cgs_pass<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, nS, j, p2, LZ_BLOCKS, p1, c->metric_d, nS,
+                                                       c->lz_d, 1, 0);
+  CODY_LAUNCHED(c);
+  z_t* vNext = (j < maxDim) ? c->basis_d + nS * (size_t)j : nullptr;
+  k_lz_finish<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p1, LZ_BLOCKS, nS, c->lz_d, j, maxDim,
+                                                        1.0e-14);
+  CODY_LAUNCHED(c);
+  k_lz_mark_done<<<1, 1, 0, c->stream>>>(c->lz_d, j);
+  CODY_LAUNCHED(c);
+}
+
+void launch_lanczos_tail(cgpu_ctx* c, int j, double dt, int evalExp) {
+  if (!evalExp) return;
+  k_lz_expsub<<<1, 32, 0, c->stream>>>(c->lz_d, j, dt, 0.0);
+  CODY_LAUNCHED(c);
+}
+
+void launch_lanczos_combine(cgpu_ctx* c, z_t* out) {
+  k_lz_combine<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(out, c->work_d, c->basis_d, c->nS, c->nS, c->lz_d);
+  CODY_LAUNCHED(c);
+}
+
+__global__ void k_lz_set(double* lz, int idx, double v) { lz[idx] = v; }
+
+void launch_lz_set(cgpu_ctx* c, int idx, double v) {
+  k_lz_set<<<1, 1, 0, c->stream>>>(c->lz_d, idx, v);
+  CODY_LAUNCHED(c);
+}

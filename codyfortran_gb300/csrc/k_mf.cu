@@ -1,0 +1,452 @@
+// k_mf.cu -- interaction and mean-field kernels (FP64 form).
+//
+// The reference loops over unordered orbital pairs and, per pair, runs an
+// O(nG^2) convolution, multiplies the potential onto every orbital and
+// accumulates into dOrbs / h2 (ApplyCorrelationOp, AccumulateCorrelation,
+// FillH2CorrelationBlock, FillH2: src/Method/Mb/OrbBased/S_Method_Mb_OrbBased.f90:227-329,
+// 491-872).  Here the same sums are three dense contractions:
+//
+//   S[g,(l,k)] = conj(phi_l(g)) phi_k(g) w(g)                 (FillInteractionSrc)
+//   W[g,(l,k)] = sum_g' V(g,g') S[g',(l,k)]    l <= k         (pair potentials, DGEMM)
+//   W[g,(k,l)] = conj(W[g,(l,k)])                             (ConjugateInteractionPotential)
+//   Z[g,(k1,j)] = sum_(l2,k2) W[g,(l2,k2)] R'[(l2,k2),(k1,j)]  (ZGEMM, R' = rho2 x_3 rho^-1)
+//   dphi_j(g) += sum_k1 phi_k1(g) Z[g,(k1,j)]                 (AccumulateCorrelation)
+//   h2[(i1,j1),(l2,k2)] = 1/2 sum_g S[g,(i1,j1)] W[g,(l2,k2)]  (ZGEMM^T, FillH2Block)
+//
+// plus the regularised inverse of the one-body RDM (RdmDiagonalize_Rdm1 +
+// regInvMat, :722-754) by a parallel cyclic Jacobi eigensolver in one CTA.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Pair sources and expansion
+// ---------------------------------------------------------------------------
+__global__ void k_pair_src(z_t* __restrict__ S, const z_t* __restrict__ orbs, const double* __restrict__ w,
+                           const int* __restrict__ pl, const int* __restrict__ pk, int nG, int nP) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)nG * nP) return;
+  int g = (int)(e / nP), p = (int)(e % nP);
+  z_t a = orbs[(size_t)nG * pl[p] + g], b = orbs[(size_t)nG * pk[p] + g];
+  S[e] = zscale(zcmul(a, b), w[g]);
+}
+
+// Wfull[g][a*n+b] = W_(a,b)(g) for same-body-type pairs, Sfull[g][a*n+b] = conj(phi_a) phi_b w.
+__global__ void k_expand(z_t* __restrict__ Wfull, z_t* __restrict__ Sfull, const z_t* __restrict__ W,
+                         const z_t* __restrict__ orbs, const double* __restrict__ w, const int* __restrict__ pidx,
+                         int nG, int n, int nP) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  int Q = n * n;
+  if (e >= (size_t)nG * Q) return;
+  int g = (int)(e / Q), q = (int)(e % Q);
+  int a = q / n, b = q % n;
+  z_t v = zmk(0.0, 0.0);
+  if (a <= b) {
+    int p = pidx[a * n + b];
+    if (p >= 0) v = W[(size_t)g * nP + p];
+  } else {
+    int p = pidx[b * n + a];
+    if (p >= 0) v = zconj(W[(size_t)g * nP + p]);
+  }
+  Wfull[e] = v;
+  if (Sfull) Sfull[e] = zscale(zcmul(orbs[(size_t)nG * a + g], orbs[(size_t)nG * b + g]), w[g]);
+}
+
+// dOrbs[g + nG*j] += sum_k1 orbs[g + nG*k1] * Z[g][k1*n + j]
+__global__ void k_corr_epilogue(z_t* __restrict__ dOrbs, const z_t* __restrict__ orbs, const z_t* __restrict__ Z,
+                                int nG, int n) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  int j = blockIdx.y;
+  if (g >= nG) return;
+  z_t acc = zmk(0.0, 0.0);
+  const z_t* zr = Z + (size_t)g * n * n;
+  for (int k1 = 0; k1 < n; k1++) zfma(acc, orbs[(size_t)nG * k1 + g], zr[k1 * n + j]);
+  size_t o = (size_t)nG * j + g;
+  dOrbs[o] = zadd(dOrbs[o], acc);
+}
+
+// h2 (nO^4, Fortran order) from the spatial block H2s[(i1*n+j1)][(l2*n+k2)]:
+// h2(i1,l2,j1,k2) = H2s, same body type within (i1,j1) and within (l2,k2);
+// restricted runs duplicate the spatial block into the spin blocks.
+__global__ void k_h2_layout(z_t* __restrict__ h2, const z_t* __restrict__ H2s, const int* __restrict__ btOf, int nO,
+                            int n, int restricted) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  size_t N = nO;
+  if (e >= N * N * N * N) return;
+  int i1 = (int)(e % N), l2 = (int)((e / N) % N), j1 = (int)((e / N / N) % N), k2 = (int)(e / N / N / N);
+  z_t v = zmk(0.0, 0.0);
+  if (restricted) {
+    int s1 = i1 / n, s2 = l2 / n, s3 = j1 / n, s4 = k2 / n;
+    if (s1 == s3 && s2 == s4) {
+      int a = i1 % n, b = l2 % n, c = j1 % n, d = k2 % n;
+      v = H2s[(size_t)(a * n + c) * n * n + (b * n + d)];
+    }
+  } else {
+    if (btOf[i1] == btOf[j1] && btOf[l2] == btOf[k2]) v = H2s[(size_t)(i1 * n + j1) * n * n + (l2 * n + k2)];
+  }
+  h2[e] = v;
+}
+
+// ---------------------------------------------------------------------------
+// Tiled GEMMs
+// ---------------------------------------------------------------------------
+// C[M,N] = A[M,K] B[K,N], all row-major, real FP64.  64x64 tile, 256 threads, 4x4 per thread.
+constexpr int DG_BM = 64, DG_BN = 64, DG_BK = 16;
+
+__global__ void __launch_bounds__(256) k_dgemm_nn(int M, int N, int K, const double* __restrict__ A, int lda,
+                                                  const double* __restrict__ B, int ldb, double* __restrict__ C,
+                                                  int ldc) {
+  __shared__ double As[DG_BK][DG_BM + 1];
+  __shared__ double Bs[DG_BK][DG_BN];
+  int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  int m0 = blockIdx.y * DG_BM, n0 = blockIdx.x * DG_BN;
+  double acc[4][4] = {};
+  for (int k0 = 0; k0 < K; k0 += DG_BK) {
+    for (int t = threadIdx.x; t < DG_BM * DG_BK; t += 256) {
+      int r = t / DG_BK, kk = t % DG_BK;
+      int m = m0 + r, k = k0 + kk;
+      As[kk][r] = (m < M && k < K) ? A[(size_t)m * lda + k] : 0.0;
+    }
+    for (int t = threadIdx.x; t < DG_BK * DG_BN; t += 256) {
+      int kk = t / DG_BN, cc = t % DG_BN;
+      int k = k0 + kk, n = n0 + cc;
+      Bs[kk][cc] = (k < K && n < N) ? B[(size_t)k * ldb + n] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < DG_BK; kk++) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      int m = m0 + ty + 16 * i, n = n0 + tx + 16 * j;
+      if (m < M && n < N) C[(size_t)m * ldc + n] = acc[i][j];
+    }
+}
+
+// Complex GEMM, row-major: P[split][m][n] = sum_{k in split} opA(m,k) B[k][n]
+// opA(m,k) = A[m*lda+k] (transA=0) or A[k*lda+m] (transA=1).  32x32 tile, 256 threads, 2x2 per thread.
+constexpr int ZG_BM = 32, ZG_BN = 32, ZG_BK = 8;
+
+__global__ void __launch_bounds__(256) k_zgemm(int transA, int M, int N, int K, int kPerSplit,
+                                               const z_t* __restrict__ A, int lda, const z_t* __restrict__ B,
+                                               int ldb, z_t* __restrict__ P, int ldp) {
+  __shared__ z_t As[ZG_BK][ZG_BM + 1];
+  __shared__ z_t Bs[ZG_BK][ZG_BN];
+  int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  int m0 = blockIdx.y * ZG_BM, n0 = blockIdx.x * ZG_BN;
+  int kBeg = blockIdx.z * kPerSplit, kEnd = min(K, kBeg + kPerSplit);
+  z_t acc[2][2];
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++) acc[i][j] = zmk(0.0, 0.0);
+  for (int k0 = kBeg; k0 < kEnd; k0 += ZG_BK) {
+    {
+      int t = threadIdx.x;  // 256 = 32 x 8
+      int r, kk;
+      if (transA) { r = t % ZG_BM; kk = t / ZG_BM; } else { kk = t % ZG_BK; r = t / ZG_BK; }
+      int m = m0 + r, k = k0 + kk;
+      z_t v = zmk(0.0, 0.0);
+      if (m < M && k < kEnd) v = transA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
+      As[kk][r] = v;
+      int kb = t / ZG_BN, cc = t % ZG_BN;
+      int kq = k0 + kb, n = n0 + cc;
+      Bs[kb][cc] = (kq < kEnd && n < N) ? B[(size_t)kq * ldb + n] : zmk(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < ZG_BK; kk++) {
+      z_t a0 = As[kk][ty], a1 = As[kk][ty + 16];
+      z_t b0 = Bs[kk][tx], b1 = Bs[kk][tx + 16];
+      zfma(acc[0][0], a0, b0);
+      zfma(acc[0][1], a0, b1);
+      zfma(acc[1][0], a1, b0);
+      zfma(acc[1][1], a1, b1);
+    }
+    __syncthreads();
+  }
+  z_t* Pz = P + (size_t)blockIdx.z * M * ldp;
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++) {
+      int m = m0 + ty + 16 * i, n = n0 + tx + 16 * j;
+      if (m < M && n < N) Pz[(size_t)m * ldp + n] = acc[i][j];
+    }
+}
+
+__global__ void k_split_reduce(z_t* __restrict__ C, const z_t* __restrict__ P, int nSplit, size_t MN, double scale) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= MN) return;
+  z_t s = zmk(0.0, 0.0);
+  for (int z = 0; z < nSplit; z++) s = zadd(s, P[(size_t)z * MN + e]);
+  C[e] = zscale(s, scale);
+}
+
+// ---------------------------------------------------------------------------
+// Regularised inverse of the spin-summed one-body RDM (one CTA).
+// Parallel cyclic Jacobi (round-robin pairing), complex Hermitian n <= 32.
+// ---------------------------------------------------------------------------
+constexpr int JB_MAX = 32;
+
+__global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t* __restrict__ r1s,
+                                                     const z_t* __restrict__ rdm1, int nO, int n, int restricted,
+                                                     double reg) {
+  __shared__ z_t A[JB_MAX][JB_MAX + 1];
+  __shared__ z_t V[JB_MAX][JB_MAX + 1];
+  __shared__ double rc[JB_MAX / 2], rs[JB_MAX / 2];
+  __shared__ z_t rph[JB_MAX / 2];
+  __shared__ int rp[JB_MAX / 2], rq[JB_MAX / 2];
+  __shared__ double offs, diags;
+  int tid = threadIdx.x;
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    int i = e % n, j = e / n;
+    z_t v = rdm1[i + (size_t)nO * j];
+    if (restricted) v = zadd(v, rdm1[(n + i) + (size_t)nO * (n + j)]);
+    A[i][j] = v;
+    r1s[e] = v;
+    V[i][j] = zmk(i == j ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  for (int e = tid; e < n; e += blockDim.x) A[e][e].y = 0.0;
+  __syncthreads();
+  int ne = (n + 1) & ~1;
+  int half = ne / 2;
+  for (int sweep = 0; sweep < 60; sweep++) {
+    if (tid == 0) {
+      double off = 0.0, dg = 0.0;
+      for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+          double a2 = A[i][j].x * A[i][j].x + A[i][j].y * A[i][j].y;
+          if (i == j) dg += a2; else off += a2;
+        }
+      offs = off;
+      diags = dg;
+    }
+    __syncthreads();
+    if (offs <= 1e-34 * (diags + offs) || offs == 0.0) break;
+    for (int r = 0; r < ne - 1; r++) {
+      if (tid < half) {
+        int k = tid;
+        auto pos = [&](int i) { return i == 0 ? 0 : ((i - 1 + r) % (ne - 1)) + 1; };
+        int p = pos(k), q = pos(ne - 1 - k);
+        if (p > q) { int t = p; p = q; q = t; }
+        rp[k] = p;
+        rq[k] = q;
+        double c = 1.0, s = 0.0;
+        z_t ph = zmk(1.0, 0.0);
+        if (q < n) {
+          z_t b = A[p][q];
+          double g = sqrt(b.x * b.x + b.y * b.y);
+          if (g != 0.0) {
+            ph = zmk(b.x / g, b.y / g);
+            double tau = (A[q][q].x - A[p][p].x) / (2.0 * g);
+            double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + t * t);
+            s = t * c;
+          }
+        } else {
+          rq[k] = -1;
+        }
+        rc[k] = c;
+        rs[k] = s;
+        rph[k] = ph;
+      }
+      __syncthreads();
+      // columns: A <- A U, V <- V U with U = [[c, s],[-s e^{-i th}, c e^{-i th}]]
+      for (int e = tid; e < n * half; e += blockDim.x) {
+        int i = e % n, k = e / n;
+        int p = rp[k], q = rq[k];
+        if (q < 0 || rs[k] == 0.0) continue;
+        double c = rc[k], s = rs[k];
+        z_t phc = zconj(rph[k]);
+        z_t akp = A[i][p], akq = A[i][q];
+        A[i][p] = zsub(zscale(akp, c), zscale(zmul(akq, phc), s));
+        A[i][q] = zadd(zscale(akp, s), zscale(zmul(akq, phc), c));
+        z_t vkp = V[i][p], vkq = V[i][q];
+        V[i][p] = zsub(zscale(vkp, c), zscale(zmul(vkq, phc), s));
+        V[i][q] = zadd(zscale(vkp, s), zscale(zmul(vkq, phc), c));
+      }
+      __syncthreads();
+      // rows: A <- U^H A
+      for (int e = tid; e < n * half; e += blockDim.x) {
+        int i = e % n, k = e / n;
+        int p = rp[k], q = rq[k];
+        if (q < 0 || rs[k] == 0.0) continue;
+        double c = rc[k], s = rs[k];
+        z_t ph = rph[k];
+        z_t apk = A[p][i], aqk = A[q][i];
+        A[p][i] = zsub(zscale(apk, c), zscale(zmul(ph, aqk), s));
+        A[q][i] = zadd(zscale(apk, s), zscale(zmul(ph, aqk), c));
+      }
+      __syncthreads();
+      if (tid < half) {
+        int p = rp[tid], q = rq[tid];
+        if (q >= 0 && rs[tid] != 0.0) {
+          A[p][q] = zmk(0.0, 0.0);
+          A[q][p] = zmk(0.0, 0.0);
+          A[p][p].y = 0.0;
+          A[q][q].y = 0.0;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // Mreg(k1,j1) = sum_j U(k1,j) n_j/(n_j^2+reg) conj(U(j1,j))
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    int k1 = e % n, j1 = e / n;
+    z_t acc = zmk(0.0, 0.0);
+    for (int j = 0; j < n; j++) {
+      double occ = A[j][j].x;
+      double f = occ / (occ * occ + reg);
+      zfma(acc, zscale(V[k1][j], f), zconj(V[j1][j]));
+    }
+    Mreg[e] = acc;
+  }
+}
+
+// R'[(l2*n+k2)][(k1*n+j)] = sum_k r2s(k1,k2,k,l2) Mreg(k,j), masked by body types.
+// r2s is the spin-summed spatial rdm2 built on the fly from rdm2 (nO^4).
+__global__ void k_build_R(z_t* __restrict__ Rp, const z_t* __restrict__ rdm2, const z_t* __restrict__ Mreg,
+                          const int* __restrict__ btOf, int nO, int n, int restricted) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  size_t Q = (size_t)n * n;
+  if (e >= Q * Q) return;
+  int row = (int)(e / Q), col = (int)(e % Q);
+  int l2 = row / n, k2 = row % n, k1 = col / n, j = col % n;
+  z_t v = zmk(0.0, 0.0);
+  bool ok = restricted || (btOf[l2] == btOf[k2] && btOf[k1] == btOf[j]);
+  if (ok) {
+    size_t N = nO;
+    auto R2 = [&](int a, int b, int c, int d) { return rdm2[a + N * (b + N * (c + N * (size_t)d))]; };
+    for (int k = 0; k < n; k++) {
+      z_t r = R2(k1, k2, k, l2);
+      if (restricted)
+        r = zadd(zadd(zadd(r, R2(n + k1, k2, n + k, l2)), R2(k1, n + k2, k, n + l2)), R2(n + k1, n + k2, n + k, n + l2));
+      zfma(v, r, Mreg[k + (size_t)n * j]);
+    }
+  }
+  Rp[e] = v;
+}
+
+void zgemm(cgpu_ctx* c, int transA, int M, int N, int K, const z_t* A, int lda, const z_t* B, int ldb, z_t* C,
+           int ldc, double scale) {
+  int tilesM = (M + ZG_BM - 1) / ZG_BM, tilesN = (N + ZG_BN - 1) / ZG_BN;
+  int tiles = tilesM * tilesN;
+  int nSplit = 1;
+  if (tiles < 2 * 152 && K > 512) nSplit = std::min((2 * 152 + tiles - 1) / tiles, (K + 255) / 256);
+  if (nSplit == 1 && scale == 1.0) {
+    dim3 grid(tilesN, tilesM, 1);
+    k_zgemm<<<grid, 256, 0, c->stream>>>(transA, M, N, K, K, A, lda, B, ldb, C, ldc);
+    CODY_LAUNCHED(c);
+    return;
+  }
+  int kPer = ((K + nSplit - 1) / nSplit + ZG_BK - 1) / ZG_BK * ZG_BK;
+  nSplit = (K + kPer - 1) / kPer;
+  size_t need = (size_t)nSplit * M * N;
+  if (c->partialCap < need) {
+    if (c->partial_d) cudaFree(c->partial_d);
+    CODY_CUDA(cudaMalloc(&c->partial_d, need * sizeof(z_t)));
+    c->partialCap = need;
+  }
+  dim3 grid(tilesN, tilesM, nSplit);
+  k_zgemm<<<grid, 256, 0, c->stream>>>(transA, M, N, K, kPer, A, lda, B, ldb, c->partial_d, N);
+  CODY_LAUNCHED(c);
+  if (ldc != N) throw std::string("zgemm: split-K output must be dense");
+  size_t MN = (size_t)M * N;
+  k_split_reduce<<<(int)((MN + 255) / 256), 256, 0, c->stream>>>(C, c->partial_d, nSplit, MN, scale);
+  CODY_LAUNCHED(c);
+}
+
+}  // namespace
+
+// W = V S for the unordered same-body-type pairs (FP64).
+void launch_pair_potentials(cgpu_ctx* c, const z_t* orbs) {
+  ProfScope prof(c, CGPU_KERNEL_PAIR_POTENTIALS);
+  size_t nGP = (size_t)c->nG * c->nPairs;
+  k_pair_src<<<(int)((nGP + 255) / 256), 256, 0, c->stream>>>(c->S_d, orbs, c->w_d, c->pairL_d, c->pairK_d, c->nG,
+                                                               c->nPairs);
+  CODY_LAUNCHED(c);
+  int N = 2 * c->nPairs;  // complex columns viewed as interleaved doubles
+  dim3 grid((N + DG_BN - 1) / DG_BN, (c->nG + DG_BM - 1) / DG_BM);
+  k_dgemm_nn<<<grid, 256, 0, c->stream>>>(c->nG, N, c->nG, c->Vint_d, c->nG, (const double*)c->S_d, N,
+                                          (double*)c->W_d, N);
+  CODY_LAUNCHED(c);
+}
+
+static void expand_pairs(cgpu_ctx* c, const z_t* orbs, int wantS) {
+  int n = c->nOS;
+  size_t tot = (size_t)c->nG * n * n;
+  k_expand<<<(int)((tot + 255) / 256), 256, 0, c->stream>>>(c->Wfull_d, wantS ? c->Sfull_d : nullptr, c->W_d, orbs,
+                                                             c->w_d, c->pidx_d, c->nG, n, c->nPairs);
+  CODY_LAUNCHED(c);
+}
+
+static void h2_from_pairs(cgpu_ctx* c) {
+  ProfScope prof(c, CGPU_KERNEL_H2);
+  int n = c->nOS, Q = n * n;
+  // H2s = 1/2 Sfull^T Wfull  (Q x nG)(nG x Q)
+  zgemm(c, 1, Q, Q, c->nG, c->Sfull_d, Q, c->Wfull_d, Q, c->h2s_d, Q, 0.5);
+  size_t n4 = (size_t)c->nO * c->nO * c->nO * c->nO;
+  k_h2_layout<<<(int)((n4 + 255) / 256), 256, 0, c->stream>>>(c->h2_d, c->h2s_d, c->btOfOrb_d, c->nO, n,
+                                                               c->restricted);
+  CODY_LAUNCHED(c);
+}
+
+void launch_rdm_inverse(cgpu_ctx* c) {
+  int n = c->nOS;
+  if (n > JB_MAX) throw std::string("ApplyCorrelationOp: more than 32 stored orbitals is not supported");
+  k_rdm_inverse<<<1, 512, 0, c->stream>>>(c->Mreg_d, c->r1s_d, c->rdm1_d, c->nO, n, c->restricted, c->regEps);
+  CODY_LAUNCHED(c);
+  size_t Q = (size_t)n * n;
+  k_build_R<<<(int)((Q * Q + 255) / 256), 256, 0, c->stream>>>(c->Rp_d, c->rdm2_d, c->Mreg_d, c->btOfOrb_d, c->nO, n,
+                                                                c->restricted);
+  CODY_LAUNCHED(c);
+}
+
+// ApplyCorrelationOp: dOrbs += contraction; h2 (nO^4) filled when wantH2.
+// Requires rdm1_d / rdm2_d to hold the current RDMs.
+void launch_correlation(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
+  launch_rdm_inverse(c);
+  if (!c->hasInteraction) {
+    if (wantH2) CODY_CUDA(cudaMemsetAsync(c->h2_d, 0, sizeof(z_t) * (size_t)c->nO * c->nO * c->nO * c->nO, c->stream));
+    return;
+  }
+  launch_pair_potentials(c, orbs);
+  expand_pairs(c, orbs, wantH2);
+  int n = c->nOS, Q = n * n;
+  // Z = Wfull R'  (nG x Q)(Q x Q), stored in the scratch of Sfull's size
+  z_t* Z = c->Wfull_d + (size_t)c->nG * Q;  // second half of the Wfull allocation
+  {
+    ProfScope prof(c, CGPU_KERNEL_CORRELATION);
+    zgemm(c, 0, c->nG, Q, Q, c->Wfull_d, Q, c->Rp_d, Q, Z, Q, 1.0);
+    dim3 grid((c->nG + 255) / 256, n);
+    k_corr_epilogue<<<grid, 256, 0, c->stream>>>(dOrbs, orbs, Z, c->nG, n);
+    CODY_LAUNCHED(c);
+  }
+  if (wantH2) h2_from_pairs(c);
+}
+
+// FillH2: h2 of the given orbitals.
+void launch_fill_h2(cgpu_ctx* c, const z_t* orbs) {
+  if (!c->hasInteraction) {
+    CODY_CUDA(cudaMemsetAsync(c->h2_d, 0, sizeof(z_t) * (size_t)c->nO * c->nO * c->nO * c->nO, c->stream));
+    return;
+  }
+  launch_pair_potentials(c, orbs);
+  expand_pairs(c, orbs, 1);
+  h2_from_pairs(c);
+}
+
+void launch_expand_h2(cgpu_ctx* c) { h2_from_pairs(c); }

@@ -1,0 +1,355 @@
+"""Host-side mirror of the reference's hot-path interface over the C ABI.
+
+One :class:`Engine` wraps one ``cgpu_ctx`` (include/cody_gpu.h).  Method names
+follow the reference procedures they replace; arrays use the reference
+layouts (Fortran order, complex128).  Errors raise :class:`CodyError` with the
+library's message, the counterpart of the reference's ``error stop``.
+
+The CUDA library is mandatory: if ``libcodygpu.so`` is missing or no GPU is
+present, construction raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .spec import SystemSpec
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libcodygpu.so")
+
+TD_FULL, TD_ORBS_LIN, TD_NONLIN, TD_TDCI = 0, 1, 2, 3
+_WHICH = {"full": TD_FULL, "orbs_lin": TD_ORBS_LIN, "nonlin": TD_NONLIN, "tdci": TD_TDCI}
+
+EXPORTED = [
+    "cgpu_ctx_create", "cgpu_ctx_destroy", "cgpu_last_error", "cgpu_last_global_error", "cgpu_sizes", "cgpu_grid",
+    "cgpu_configlist_tables", "cgpu_synchronize", "cgpu_launch_count", "cgpu_time_derivative",
+    "cgpu_apply_single_body_op", "cgpu_fill_h1", "cgpu_fill_h2", "cgpu_apply_correlation_op", "cgpu_energy",
+    "cgpu_ci_apply_h1_fill_rdm1", "cgpu_ci_apply_h2_fill_rdm2", "cgpu_project_coeffs", "cgpu_normalize_coeffs",
+    "cgpu_project_orbs", "cgpu_orthonormalize_orbs", "cgpu_integrate_rk4", "cgpu_integrate_euler",
+    "cgpu_integrate_sil", "cgpu_propagate_split2", "cgpu_state_upload", "cgpu_state_download",
+    "cgpu_propagate_resident", "cgpu_energy_resident", "cgpu_tdci_set_orbitals", "cgpu_propagate_resident_timed",
+    "cgpu_profile_begin", "cgpu_profile_end",
+]
+
+KERNELS = {"pair_potentials": 1, "correlation": 2, "h2": 3, "ci_apply": 4, "ci_rdm": 5, "onebody": 6, "lanczos": 7}
+
+
+class CodyError(RuntimeError):
+    pass
+
+
+class CgpuDesc(C.Structure):
+    _fields_ = [
+        ("grid_kind", C.c_int), ("xmin", C.c_double), ("xmax", C.c_double), ("n_points", C.c_int),
+        ("n_elements", C.c_int), ("n_locals", C.c_int), ("xmin_excluded", C.c_int), ("xmax_excluded", C.c_int),
+        ("n_body_types", C.c_int), ("n_bodies", C.c_int * 4), ("n_orbs", C.c_int * 4),
+        ("body_mass", C.c_double * 4), ("restricted", C.c_int), ("regularization", C.c_double),
+        ("n_nuclei", C.c_int), ("nuc_position", C.c_double * 8), ("nuc_charge", C.c_double * 8),
+        ("nuc_softening1", C.c_double * 8), ("nuc_softening2", C.c_double * 8), ("nuc_dampening", C.c_double * 8),
+        ("has_interaction", C.c_int), ("int_strength", C.c_double), ("int_softening1", C.c_double),
+        ("int_softening2", C.c_double), ("int_dampening", C.c_double), ("int_kind", C.c_int),
+        ("laser_kind", C.c_int), ("laser_E0", C.c_double), ("laser_omega", C.c_double),
+        ("laser_n_cycles", C.c_double), ("laser_cep", C.c_double), ("laser_t_start", C.c_double),
+        ("field_samples", C.POINTER(C.c_double)), ("n_field_samples", C.c_int), ("field_dt", C.c_double),
+        ("field_t0", C.c_double), ("method", C.c_int), ("precision", C.c_int), ("max_krylov", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libcodygpu.so (built by codyfortran_gb300.build); raise if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise CodyError(f"CUDA library not built: {path} (run codyfortran_gb300.build.build())")
+    lib = C.CDLL(path)
+    for name in EXPORTED:
+        getattr(lib, name)  # AttributeError if a symbol is missing
+    lib.cgpu_last_error.restype = C.c_char_p
+    lib.cgpu_last_error.argtypes = [C.c_void_p]
+    lib.cgpu_last_global_error.restype = C.c_char_p
+    lib.cgpu_launch_count.restype = C.c_long
+    lib.cgpu_launch_count.argtypes = [C.c_void_p, C.c_int]
+    lib.cgpu_ctx_create.argtypes = [C.POINTER(CgpuDesc), C.POINTER(C.c_void_p)]
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _d(v):
+    return C.c_double(float(v))
+
+
+def make_desc(spec: SystemSpec, precision: str = "fp64", max_krylov: int = 32):
+    d = CgpuDesc()
+    d.grid_kind = 0 if spec.grid_kind == "const" else 1
+    d.xmin, d.xmax = spec.xmin, spec.xmax
+    d.n_points, d.n_elements, d.n_locals = spec.n_points, spec.n_elements, spec.n_locals
+    d.xmin_excluded, d.xmax_excluded = int(spec.xmin_excluded), int(spec.xmax_excluded)
+    d.n_body_types = spec.n_bt
+    for b in range(spec.n_bt):
+        d.n_bodies[b] = int(spec.n_bodies[b])
+        d.n_orbs[b] = int(spec.n_orbs[b])
+        d.body_mass[b] = float(spec.masses[b])
+    d.restricted = int(spec.restricted)
+    d.regularization = spec.reg_eps
+    d.n_nuclei = len(spec.nuclei)
+    for i, n in enumerate(spec.nuclei):
+        d.nuc_position[i], d.nuc_charge[i] = n.position, n.charge
+        d.nuc_softening1[i], d.nuc_softening2[i], d.nuc_dampening[i] = n.softening1, n.softening2, n.dampening
+    d.has_interaction = int(spec.has_interaction)
+    d.int_strength, d.int_softening1, d.int_softening2, d.int_dampening = (
+        spec.int_strength, spec.int_s1, spec.int_s2, spec.int_damp)
+    d.int_kind = 0 if spec.int_kind == "toeplitz" else 1
+    L = spec.laser
+    d.laser_kind = {"none": 0, "sin2": 1, "sampled": 2}[L.kind]
+    d.laser_E0, d.laser_omega, d.laser_n_cycles, d.laser_cep, d.laser_t_start = L.E0, L.omega, L.n_cycles, L.cep, L.t_start
+    keep = None
+    if L.kind == "sampled":
+        keep = np.ascontiguousarray(L.samples, dtype=np.float64)
+        d.field_samples = keep.ctypes.data_as(C.POINTER(C.c_double))
+        d.n_field_samples = len(keep)
+        d.field_dt, d.field_t0 = L.sample_dt, L.sample_t0
+    d.method = 1 if spec.method == "tdci" else 0
+    d.precision = {"fp64": 0, "mixed": 1}[precision]
+    d.max_krylov = max_krylov
+    return d, keep
+
+
+class Engine:
+    """The GB300 MCTDHX/TDCI engine for one system (one cgpu_ctx, one CUDA stream)."""
+
+    def __init__(self, spec: SystemSpec, precision: str = "fp64", max_krylov: int = 32):
+        self.lib = load_library()
+        self.spec = spec
+        desc, self._keep = make_desc(spec, precision, max_krylov)
+        h = C.c_void_p()
+        rc = self.lib.cgpu_ctx_create(C.byref(desc), C.byref(h))
+        if rc != 0:
+            raise CodyError(self.lib.cgpu_last_global_error().decode())
+        self.h = h
+        sz = (C.c_int * 6)()
+        self.lib.cgpu_sizes(self.h, sz)
+        self.nG, self.nO, self.nOS, self.nC, self.nBt, self.nS = list(sz)
+        self.x = np.zeros(self.nG)
+        self.w = np.zeros(self.nG)
+        self.lib.cgpu_grid(self.h, _p(self.x), _p(self.w))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cgpu_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise CodyError(self.lib.cgpu_last_error(self.h).decode())
+
+    def launch_count(self, reset=False):
+        return self.lib.cgpu_launch_count(self.h, int(reset))
+
+    # ConfigList --------------------------------------------------------------
+    def tables(self, bt, kind):
+        n_conf, mc = C.c_int(), C.c_int()
+        self._check(self.lib.cgpu_configlist_tables(self.h, bt, kind, C.byref(n_conf), C.byref(mc), None, None, None,
+                                                    None, None))
+        n, m = n_conf.value, mc.value
+        codes = np.zeros(n, dtype=np.int64)
+        ncon = np.zeros(n, dtype=np.int32)
+        exc = np.zeros(max(m, 1) * n, dtype=np.int32)
+        oc = np.zeros(max(m, 1) * n, dtype=np.int32)
+        fac = np.zeros(max(m, 1) * n, dtype=np.float64)
+        self._check(self.lib.cgpu_configlist_tables(self.h, bt, kind, None, None, _p(codes), _p(ncon), _p(exc),
+                                                    _p(oc), _p(fac)))
+        f = lambda a: a[: m * n].reshape(n, m).T
+        return dict(codes=codes, n_connected=ncon, excited_c=f(exc), orb_code=f(oc), factor=f(fac))
+
+    # arrays -------------------------------------------------------------------
+    def _orbs(self, orbs):
+        return np.asfortranarray(orbs, dtype=np.complex128)
+
+    def _new_orbs(self):
+        return np.zeros((self.nG, self.nOS), dtype=np.complex128, order="F")
+
+    def _n4(self):
+        n = self.nO
+        return np.zeros((n, n, n, n), dtype=np.complex128, order="F")
+
+    def _n2(self):
+        return np.zeros((self.nO, self.nO), dtype=np.complex128, order="F")
+
+    # Method / Method_Mb_OrbBased ---------------------------------------------
+    def time_derivative(self, state, t, which="full"):
+        """Method_TimeDerivative / TimeDerivativeOrbsLin / ...CoeffsPlusOrbsNonLin / Tdci."""
+        s = np.ascontiguousarray(state, dtype=np.complex128)
+        d = np.zeros_like(s)
+        self._check(self.lib.cgpu_time_derivative(self.h, _WHICH[which], _p(d), _p(s), _d(t)))
+        return d
+
+    def apply_single_body_op(self, orbs, t, want_h1=False, d_orbs=None):
+        o = self._orbs(orbs)
+        d = self._new_orbs() if d_orbs is None else np.array(d_orbs, dtype=np.complex128, order="F", copy=True)
+        h1 = self._n2() if want_h1 else None
+        self._check(self.lib.cgpu_apply_single_body_op(self.h, _p(d), _p(o), _d(t), _p(h1)))
+        return (d, h1) if want_h1 else d
+
+    def fill_h1(self, orbs, t):
+        o = self._orbs(orbs)
+        h1 = self._n2()
+        self._check(self.lib.cgpu_fill_h1(self.h, _p(h1), _p(o), _d(t)))
+        return h1
+
+    def fill_h2(self, orbs, t):
+        o = self._orbs(orbs)
+        h2 = self._n4()
+        self._check(self.lib.cgpu_fill_h2(self.h, _p(h2), _p(o), _d(t)))
+        return h2
+
+    def apply_correlation_op(self, orbs, rdm1, rdm2, t, d_orbs=None):
+        o = self._orbs(orbs)
+        r1 = np.asfortranarray(rdm1, dtype=np.complex128)
+        r2 = np.asfortranarray(rdm2, dtype=np.complex128)
+        d = self._new_orbs() if d_orbs is None else np.array(d_orbs, dtype=np.complex128, order="F", copy=True)
+        h2 = self._n4()
+        self._check(self.lib.cgpu_apply_correlation_op(self.h, _p(d), _p(o), _p(r1), _p(r2), _d(t), _p(h2)))
+        return d, h2
+
+    def energy(self, state, t=0.0):
+        """Method_GetEnergy."""
+        s = np.ascontiguousarray(state, dtype=np.complex128)
+        e = C.c_double()
+        self._check(self.lib.cgpu_energy(self.h, _p(s), _d(t), C.byref(e)))
+        return e.value
+
+    # Coeffs -------------------------------------------------------------------
+    def rdm1(self, coeffs):
+        c = np.ascontiguousarray(coeffs, dtype=np.complex128)
+        r = self._n2()
+        self._check(self.lib.cgpu_ci_apply_h1_fill_rdm1(self.h, _p(c), _p(r), None, None))
+        return r
+
+    def rdm2(self, coeffs):
+        c = np.ascontiguousarray(coeffs, dtype=np.complex128)
+        r = self._n4()
+        self._check(self.lib.cgpu_ci_apply_h2_fill_rdm2(self.h, _p(c), _p(r), None, None))
+        return r
+
+    def apply_h1(self, coeffs, h1, d_coeffs=None):
+        c = np.ascontiguousarray(coeffs, dtype=np.complex128)
+        h = np.asfortranarray(h1, dtype=np.complex128)
+        d = np.zeros(self.nC, dtype=np.complex128) if d_coeffs is None else np.array(d_coeffs, dtype=np.complex128)
+        self._check(self.lib.cgpu_ci_apply_h1_fill_rdm1(self.h, _p(c), None, _p(d), _p(h)))
+        return d
+
+    def apply_h2(self, coeffs, h2, d_coeffs=None):
+        c = np.ascontiguousarray(coeffs, dtype=np.complex128)
+        h = np.asfortranarray(h2, dtype=np.complex128)
+        d = np.zeros(self.nC, dtype=np.complex128) if d_coeffs is None else np.array(d_coeffs, dtype=np.complex128)
+        self._check(self.lib.cgpu_ci_apply_h2_fill_rdm2(self.h, _p(c), None, _p(d), _p(h)))
+        return d
+
+    def project_coeffs(self, d_coeffs, coeffs):
+        d = np.array(d_coeffs, dtype=np.complex128)
+        c = np.ascontiguousarray(coeffs, dtype=np.complex128)
+        self._check(self.lib.cgpu_project_coeffs(self.h, _p(d), _p(c)))
+        return d
+
+    def normalize_coeffs(self, coeffs):
+        c = np.array(coeffs, dtype=np.complex128)
+        self._check(self.lib.cgpu_normalize_coeffs(self.h, _p(c)))
+        return c
+
+    # Orbs ---------------------------------------------------------------------
+    def project_orbs(self, d_orbs, orbs):
+        d = np.array(d_orbs, dtype=np.complex128, order="F", copy=True)
+        o = self._orbs(orbs)
+        self._check(self.lib.cgpu_project_orbs(self.h, _p(d), _p(o)))
+        return d
+
+    def orthonormalize(self, orbs):
+        o = np.array(orbs, dtype=np.complex128, order="F", copy=True)
+        self._check(self.lib.cgpu_orthonormalize_orbs(self.h, _p(o)))
+        return o
+
+    # integrators / propagator -------------------------------------------------
+    def metric_weights(self):
+        return np.concatenate([np.ones(self.nC), np.tile(self.w, self.nOS)])
+
+    def rk(self, state, t0, t1, integrator="rk4", which="nonlin", imag=False):
+        s = np.array(state, dtype=np.complex128)
+        if integrator == "euler":
+            self._check(self.lib.cgpu_integrate_euler(self.h, _WHICH[which], int(imag), _p(s), _d(t0), _d(t1)))
+        else:
+            self._check(self.lib.cgpu_integrate_rk4(self.h, _WHICH[which], _p(s), _d(t0), _d(t1)))
+        return s
+
+    def sil(self, state, t0, t1, krylov_dim, tol=0.0, max_restarts=0, metric=None, which="orbs_lin"):
+        s = np.array(state, dtype=np.complex128)
+        m = None if metric is None else np.ascontiguousarray(metric, dtype=np.float64)
+        warn = C.c_int()
+        self._check(self.lib.cgpu_integrate_sil(self.h, _WHICH[which], _p(s), _d(t0), _d(t1), krylov_dim, _d(tol),
+                                                max_restarts, _p(m), C.byref(warn)))
+        return s
+
+    def propagate_split2(self, state, t0, t1, krylov_dim=0, tol=0.0, max_restarts=0, use_metric=False):
+        """Propagator_Propagate for SplitStep Order2 (host state in, host state out)."""
+        s = np.array(state, dtype=np.complex128)
+        self._check(self.lib.cgpu_propagate_split2(self.h, _p(s), _d(t0), _d(t1), krylov_dim, _d(tol), max_restarts,
+                                                   int(use_metric)))
+        return s
+
+    # resident state -----------------------------------------------------------
+    def upload(self, state):
+        s = np.ascontiguousarray(state, dtype=np.complex128)
+        self._check(self.lib.cgpu_state_upload(self.h, _p(s)))
+
+    def download(self):
+        s = np.zeros(self.nS, dtype=np.complex128)
+        self._check(self.lib.cgpu_state_download(self.h, _p(s)))
+        return s
+
+    def propagate_resident(self, t0, dt, n_steps, krylov_dim, use_metric=True, use_graph=False):
+        self._check(self.lib.cgpu_propagate_resident(self.h, _d(t0), _d(dt), int(n_steps), int(krylov_dim),
+                                                     int(use_metric), int(use_graph)))
+
+    def propagate_resident_timed(self, t0, dt, n_steps, krylov_dim, use_metric=True, use_graph=False):
+        """Steps on the resident state; returns the device time (ms) from CUDA events on the context stream."""
+        ms = C.c_double()
+        self._check(self.lib.cgpu_propagate_resident_timed(self.h, _d(t0), _d(dt), int(n_steps), int(krylov_dim),
+                                                           int(use_metric), int(use_graph), C.byref(ms)))
+        return ms.value
+
+    def profile_begin(self, kernel):
+        self._check(self.lib.cgpu_profile_begin(self.h, KERNELS[kernel] if isinstance(kernel, str) else int(kernel)))
+
+    def profile_end(self):
+        n, ms = C.c_long(), C.c_double()
+        self._check(self.lib.cgpu_profile_end(self.h, C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def energy_resident(self, t):
+        e = C.c_double()
+        self._check(self.lib.cgpu_energy_resident(self.h, _d(t), C.byref(e)))
+        return e.value
+
+    def synchronize(self):
+        self._check(self.lib.cgpu_synchronize(self.h))
+
+    # TDCI ---------------------------------------------------------------------
+    def tdci_set_orbitals(self, orbs):
+        o = self._orbs(orbs)
+        self._check(self.lib.cgpu_tdci_set_orbitals(self.h, _p(o)))

@@ -1,0 +1,210 @@
+/* cody_gpu.h -- C ABI of the GB300 engine for CodyFortran's MCTDHX/TDCI hot path.
+ *
+ * Every entry point returns an int status (CGPU_OK = 0).  On failure the
+ * message is available from cgpu_last_error(ctx) (or cgpu_last_global_error()
+ * when no context exists); the reference's equivalent is `error stop "<msg>"`.
+ *
+ * Array arguments are HOST pointers in the reference's layouts (Fortran
+ * column-major, complex(R64) = two doubles):
+ *   state   : [C(nC) | orbs(nG, nOS)]   (Method_state,
+ *             src/Method/Mb/OrbBased/Mctdhx/S_Method_Mb_OrbBased_Mctdhx.f90:229-249)
+ *   orbs    : (nG, nOS)
+ *   rdm1/h1 : (nO, nO);  rdm2/h2 : (nO, nO, nO, nO)
+ * The device copies are owned by the context.  The "resident" entry points
+ * keep the state on the GPU between calls.
+ *
+ * One context = one system, one CUDA stream.  A context is not reentrant:
+ * one host thread calls in at a time (the reference's module state is global,
+ * src/Orbs/M_Orbs.f90:25-29).
+ */
+#ifndef CODY_GPU_H
+#define CODY_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CGPU_OK 0
+#define CGPU_ERR_ARG 1
+#define CGPU_ERR_CUDA 2
+#define CGPU_ERR_NUMERIC 3
+#define CGPU_ERR_UNSUPPORTED 4
+
+#define CGPU_GRID_CONST 0 /* grid.linear.const + 8th-order finite differences */
+#define CGPU_GRID_FEDVR 1 /* grid.linear.fedvr + 1D FEDVR kinetic operator      */
+
+#define CGPU_INT_TOEPLITZ 0 /* K(|i-j| dx), dx = x(2)-x(1): the reference's uniform-grid kernel */
+#define CGPU_INT_DENSE 1    /* K(|x_i - x_j|): valid on any grid                            */
+
+#define CGPU_LASER_NONE 0
+#define CGPU_LASER_SIN2 1    /* E(t) = E0 sin^2(pi tau/T) cos(w (tau - T/2) + cep), T = 2 pi n/w */
+#define CGPU_LASER_SAMPLED 2 /* E(t) = E_n on [t0 + n dt, t0 + (n+1) dt)                       */
+
+#define CGPU_METHOD_MCTDHX 0
+#define CGPU_METHOD_TDCI 1
+
+#define CGPU_PREC_FP64 0
+#define CGPU_PREC_MIXED 1
+
+/* Time-derivative selectors (the TimeDerivative procedure pointers). */
+#define CGPU_TD_FULL 0   /* Method_TimeDerivative (Mctdhx :101-149)                        */
+#define CGPU_TD_ORBS_LIN 1   /* TimeDerivativeOrbsLin (Mctdhx :152-177)                    */
+#define CGPU_TD_NONLIN 2 /* TimeDerivativeCoeffsPlusOrbsNonLin (Mctdhx :180-226)           */
+#define CGPU_TD_TDCI 3   /* Tdci TimeDerivative (src/Method/Mb/OrbBased/Tdci/S_Method_Mb_OrbBased_Tdci.f90:75-107) */
+
+typedef struct cgpu_ctx cgpu_ctx;
+
+typedef struct {
+  double re, im;
+} cgpu_complex;
+
+/* The configuration tree of one run (grid, sysKinetic, sysPotential,
+ * sysInteraction, method.mb, orbs); the keys it mirrors are listed beside
+ * each field. */
+typedef struct {
+  int grid_kind;                 /* grid.linear.const | grid.linear.fedvr                     */
+  double xmin, xmax;             /* grid.linear.xmin/xmax (src/Grid/Linear/S_Grid_Linear.f90:29-30) */
+  int n_points;                  /* grid.linear.const.nPoints                                */
+  int n_elements, n_locals;      /* FEDVR elements and GLL points per element (order + 1)    */
+  int xmin_excluded, xmax_excluded;
+  int n_body_types;              /* method.mb.nBodyTypes                                      */
+  int n_bodies[4];               /* method.mb.nBodies                                        */
+  int n_orbs[4];                 /* method.mb.orbBased.nOrbs                                 */
+  double body_mass[4];           /* sysKinetic.linear.laplacian.bodyMass                     */
+  int restricted;                /* orbs.restrictedQ                                         */
+  double regularization;         /* method.mb.orbBased.regularizationParameter (1e-10)       */
+  int n_nuclei;                  /* sysPotential.linear.softYukawa.*                         */
+  double nuc_position[8], nuc_charge[8], nuc_softening1[8], nuc_softening2[8], nuc_dampening[8];
+  int has_interaction;           /* sysInteraction.linear.softYukawa present                 */
+  double int_strength, int_softening1, int_softening2, int_dampening;
+  int int_kind;                  /* CGPU_INT_*                                               */
+  int laser_kind;                /* CGPU_LASER_*                                             */
+  double laser_E0, laser_omega, laser_n_cycles, laser_cep, laser_t_start;
+  const double* field_samples;   /* CGPU_LASER_SAMPLED: copied at creation                   */
+  int n_field_samples;
+  double field_dt, field_t0;
+  int method;                    /* CGPU_METHOD_*                                            */
+  int precision;                 /* CGPU_PREC_*                                              */
+  int max_krylov;                /* largest Krylov dimension the context will be asked for   */
+} cgpu_desc;
+
+/* ---- context (Fabricate + Setup) ---------------------------------------- */
+/* Replaces the *_Fabricate / *_Setup chain of the hot path: Grid_Setup
+ * (src/Grid/Linear/Const/S_Grid_Linear_Const.f90:34-52, src/Utils/M_Utils_Fedvr.f90:76-149),
+ * SysKinetic_Setup, SysPotential/SysInteraction setup, ConfigList_Setup
+ * (src/ConfigList/AllActive/S_ConfigList_AllActive.f90:105-349) and the
+ * Method_state allocation (Mctdhx :40-68). */
+int cgpu_ctx_create(const cgpu_desc* desc, cgpu_ctx** out);
+int cgpu_ctx_destroy(cgpu_ctx* ctx);
+const char* cgpu_last_error(const cgpu_ctx* ctx);
+const char* cgpu_last_global_error(void);
+/* out[0..5] = nG, nO (spin-orbitals), nOS (stored orbitals), nC, nBodyTypes, nState */
+int cgpu_sizes(const cgpu_ctx* ctx, int* out);
+/* Grid_Linear_xCoord / Grid_Linear_weights */
+int cgpu_grid(const cgpu_ctx* ctx, double* x, double* w);
+/* The device-built ConfigList tables of body type bt, copied to the host in the
+ * reference layout (src/ConfigList/M_ConfigList.f90:112-128): kind 0 singles,
+ * 1 doubles; arrays sized (maxConn, nConf) column-major; factor as +-1.0.
+ * Pass NULL arrays to query only max_conn / n_conf. */
+int cgpu_configlist_tables(cgpu_ctx* ctx, int bt, int kind, int* n_conf, int* max_conn, int64_t* codes,
+                           int* n_connected, int* excited_c, int* orb_code, double* factor);
+int cgpu_synchronize(cgpu_ctx* ctx);
+/* Number of CUDA kernels this context launched since the last reset. */
+long cgpu_launch_count(cgpu_ctx* ctx, int reset);
+
+/* ---- equation of motion (Method / Method_Mb_OrbBased pointers) ---------- */
+/* I_Method_TimeDerivative (src/Method/M_Method.f90:82-90) with the selector
+ * CGPU_TD_* choosing among Mctdhx TimeDerivative / OrbsLin / NonLin and Tdci. */
+int cgpu_time_derivative(cgpu_ctx* ctx, int which, cgpu_complex* d_state, const cgpu_complex* state, double time);
+/* ApplySingleBodyOp (src/Method/Mb/OrbBased/S_Method_Mb_OrbBased.f90:976-1034):
+ * d_orbs += (T + V(t)) orbs; h1 (nO, nO) filled when non-NULL. */
+int cgpu_apply_single_body_op(cgpu_ctx* ctx, cgpu_complex* d_orbs, const cgpu_complex* orbs, double time,
+                              cgpu_complex* h1);
+/* FillH1 (S_Method_Mb_OrbBased.f90:164-224) */
+int cgpu_fill_h1(cgpu_ctx* ctx, cgpu_complex* h1, const cgpu_complex* orbs, double time);
+/* FillH2 (S_Method_Mb_OrbBased.f90:227-293) */
+int cgpu_fill_h2(cgpu_ctx* ctx, cgpu_complex* h2, const cgpu_complex* orbs, double time);
+/* ApplyCorrelationOp (S_Method_Mb_OrbBased.f90:647-805): d_orbs += rho^-1 rho2 W orbs;
+ * h2 (nO^4) filled when non-NULL. */
+int cgpu_apply_correlation_op(cgpu_ctx* ctx, cgpu_complex* d_orbs, const cgpu_complex* orbs,
+                              const cgpu_complex* rdm1, const cgpu_complex* rdm2, double time, cgpu_complex* h2);
+/* Method_GetEnergy (S_Method_Mb_OrbBased.f90:132-161) of the given state. */
+int cgpu_energy(cgpu_ctx* ctx, const cgpu_complex* state, double time, double* energy);
+
+/* ---- CI vector (Coeffs pointers) ---------------------------------------- */
+/* I_Coeffs_ApplyH1FillRdm1 (src/Coeffs/M_Coeffs.f90:119-135; Generic :103-178).
+ * NULL optional arguments select the mode, as the Fortran optionals do. */
+int cgpu_ci_apply_h1_fill_rdm1(cgpu_ctx* ctx, const cgpu_complex* coeffs, cgpu_complex* rdm1,
+                               cgpu_complex* d_coeffs, const cgpu_complex* h1);
+/* I_Coeffs_ApplyH2FillRdm2 (src/Coeffs/M_Coeffs.f90:139-156; Generic :197-319). */
+int cgpu_ci_apply_h2_fill_rdm2(cgpu_ctx* ctx, const cgpu_complex* coeffs, cgpu_complex* rdm2,
+                               cgpu_complex* d_coeffs, const cgpu_complex* h2);
+/* Coeffs_ProjectOnSubspace (src/Coeffs/S_Coeffs.f90:105-111) */
+int cgpu_project_coeffs(cgpu_ctx* ctx, cgpu_complex* d_coeffs, const cgpu_complex* coeffs);
+/* Coeffs_Normalize (src/Coeffs/S_Coeffs.f90:84-94) */
+int cgpu_normalize_coeffs(cgpu_ctx* ctx, cgpu_complex* coeffs);
+
+/* ---- orbitals (Orbs / Grid pointers) ------------------------------------ */
+/* Orbs_ProjectOnSubspace (src/Orbs/S_Orbs.f90:198-225 -> src/Grid/S_Grid.f90:170-203) */
+int cgpu_project_orbs(cgpu_ctx* ctx, cgpu_complex* d_orbs, const cgpu_complex* orbs);
+/* Orbs_Orthonormalize (src/Orbs/S_Orbs.f90:145-173 -> src/Grid/S_Grid.f90:120-151) */
+int cgpu_orthonormalize_orbs(cgpu_ctx* ctx, cgpu_complex* orbs);
+
+/* ---- integrators and propagator ----------------------------------------- */
+/* Rk O4Expl Integrate (src/IntegratorList/Rk/O4Expl/S_IntegratorList_Rk_O4Expl.f90:90-141) */
+int cgpu_integrate_rk4(cgpu_ctx* ctx, int which, cgpu_complex* state, double t0, double t1);
+/* Rk O1Expl Integrate (src/IntegratorList/Rk/O1Expl/S_IntegratorList_Rk_O1Expl.f90:50-72);
+ * imag != 0 wraps the derivative as Actions_ImagTimeDerivative (src/Utils/M_Utils_Actions.f90:66-78). */
+int cgpu_integrate_euler(cgpu_ctx* ctx, int which, int imag, cgpu_complex* state, double t0, double t1);
+/* Sil Integrate (src/IntegratorList/Sil/S_IntegratorList_Sil.f90:114-310).  metric:
+ * NULL = Euclidean; otherwise nState weights (metricWeights).  *warnings counts
+ * sub-steps that did not reach the tolerance (the reference prints a warning). */
+int cgpu_integrate_sil(cgpu_ctx* ctx, int which, cgpu_complex* state, double t0, double t1, int krylov_dim,
+                       double tolerance, int max_restarts, const double* metric, int* warnings);
+/* SplitStep Order2 Propagate (src/Propagator/SplitStep/Order2/S_Propagator_SplitStep_Order2.f90:52-77):
+ * integratorList(1) = SIL on OrbsLin (RK4 when krylov_dim <= 0), integratorList(2) = RK4 on NonLin.
+ * use_metric != 0 sets the SIL metric to [1 on C | grid weights on orbitals]. */
+int cgpu_propagate_split2(cgpu_ctx* ctx, cgpu_complex* state, double t0, double t1, int krylov_dim,
+                          double tolerance, int max_restarts, int use_metric);
+
+/* ---- resident state (GPU-native driver loop) ---------------------------- */
+int cgpu_state_upload(cgpu_ctx* ctx, const cgpu_complex* state);
+int cgpu_state_download(cgpu_ctx* ctx, cgpu_complex* state);
+/* n_steps Strang steps of size dt from t0 on the resident state, fixed-order
+ * SIL (krylov_dim, tolerance 0, no restarts).  use_graph != 0 replays one
+ * captured CUDA graph per step. */
+int cgpu_propagate_resident(cgpu_ctx* ctx, double t0, double dt, int n_steps, int krylov_dim, int use_metric,
+                            int use_graph);
+int cgpu_energy_resident(cgpu_ctx* ctx, double time, double* energy);
+
+/* Same as cgpu_propagate_resident, timed with CUDA events recorded on the
+ * context's stream around the n_steps; *elapsed_ms receives the device time. */
+int cgpu_propagate_resident_timed(cgpu_ctx* ctx, double t0, double dt, int n_steps, int krylov_dim, int use_metric,
+                                  int use_graph, double* elapsed_ms);
+
+/* ---- profiling ----------------------------------------------------------- */
+/* Kernel families whose launches can be bracketed by CUDA events. */
+#define CGPU_KERNEL_PAIR_POTENTIALS 1 /* W = V S (interaction potentials of all orbital pairs) */
+#define CGPU_KERNEL_CORRELATION 2     /* rho^-1 rho2 W phi contraction                        */
+#define CGPU_KERNEL_H2 3              /* h2 = 1/2 S^T W                                        */
+#define CGPU_KERNEL_CI_APPLY 4        /* H1/H2 application to the CI vector                    */
+#define CGPU_KERNEL_CI_RDM 5          /* one- and two-body RDM accumulation                    */
+#define CGPU_KERNEL_ONEBODY 6         /* banded kinetic + potential + laser apply              */
+#define CGPU_KERNEL_LANCZOS 7         /* Krylov reorthogonalisation / update                   */
+/* Start recording events around every launch of `kernel` (0 disables). */
+int cgpu_profile_begin(cgpu_ctx* ctx, int kernel);
+/* Stop; *launches and *total_ms receive the bracketed launches and their summed device time. */
+int cgpu_profile_end(cgpu_ctx* ctx, long* launches, double* total_ms);
+
+/* ---- TDCI ---------------------------------------------------------------- */
+/* Tdci Setup (src/Method/Mb/OrbBased/Tdci/S_Method_Mb_OrbBased_Tdci.f90:40-72):
+ * fix the orbitals and fill h1/h2 once. */
+int cgpu_tdci_set_orbitals(cgpu_ctx* ctx, const cgpu_complex* orbs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CODY_GPU_H */
