@@ -536,6 +536,12 @@ int fail(cgpu_ctx* c, const std::string& msg, int code) {
 
 }  // namespace
 
+// Records the message returned by cgpu_last_global_error (for entry points without a context).
+void cody_record_global_error(const std::string& msg) {
+  std::lock_guard<std::mutex> g(g_errMutex);
+  g_lastGlobalError = msg;
+}
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------

@@ -31,7 +31,7 @@ EXPORTED = [
     "cgpu_project_orbs", "cgpu_orthonormalize_orbs", "cgpu_integrate_rk4", "cgpu_integrate_euler",
     "cgpu_integrate_sil", "cgpu_propagate_split2", "cgpu_state_upload", "cgpu_state_download",
     "cgpu_propagate_resident", "cgpu_energy_resident", "cgpu_tdci_set_orbitals", "cgpu_propagate_resident_timed",
-    "cgpu_profile_begin", "cgpu_profile_end",
+    "cgpu_profile_begin", "cgpu_profile_end", "cgpu_weighted_gram_noalloc",
 ]
 
 KERNELS = {"pair_potentials": 1, "correlation": 2, "h2": 3, "ci_apply": 4, "ci_rdm": 5, "onebody": 6, "lanczos": 7}

@@ -203,6 +203,26 @@ int cgpu_profile_end(cgpu_ctx* ctx, long* launches, double* total_ms);
  * fix the orbitals and fill h1/h2 once. */
 int cgpu_tdci_set_orbitals(cgpu_ctx* ctx, const cgpu_complex* orbs);
 
+/* ---- no-allocation variant ---------------------------------------------- */
+/* No counterpart in the reference.  Weighted Gram matrix of two orbital sets,
+ *   gram(i,j) = sum_g conj(a[g + n_grid*i]) * b[g + n_grid*j] * weights[g],
+ * (column-major n_cols x n_cols), the matrix that Grid_InnerProduct builds in
+ * FillH1 and the (1-P) projector.  It is for callers that cannot call
+ * cudaMalloc when they need it: a host program whose device memory belongs
+ * to another component, or code running where allocation is not allowed.
+ * It allocates nothing: a, b, weights and gram are the caller's DEVICE
+ * pointers, and the per-block partial sums live in a fixed 1 MiB __device__
+ * array inside the library, which every GPU that loads the library holds
+ * until exit.  Limits: 1 <= n_cols <= 32, n_grid >= 1; larger sizes are
+ * rejected with CGPU_ERR_ARG and a message in cgpu_last_global_error().
+ * The first call on each device looks up that array's device address (with
+ * the device current); make that first call before any stream capture.
+ * The kernels run asynchronously on `stream` (a cudaStream_t, NULL = legacy
+ * default stream).  All calls share the one array: calls that overlap on the
+ * GPU (concurrent streams) race on it and must be serialised by the caller. */
+int cgpu_weighted_gram_noalloc(const cgpu_complex* a, const cgpu_complex* b, const double* weights, int n_grid,
+                               int n_cols, cgpu_complex* gram, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
