@@ -74,6 +74,8 @@ struct CiView {
   const int8_t* dFac[CODY_MAX_BT];
 };
 
+struct MixedBufs;  // mixed-precision operand buffers (k_mixed.cu)
+
 // ---------------------------------------------------------------------------
 // The context: one system, its device-resident operators, tables and work
 // buffers, and one CUDA stream.  Not reentrant (one host thread at a time),
@@ -135,6 +137,7 @@ struct cgpu_ctx {
   int graphKrylov = 0;
   std::string lastError;
   int launches = 0;  // kernels launched by this context (since the last reset)
+  MixedBufs* mixed = nullptr;
   // profiling: CUDA events around every launch of one kernel family
   int profTarget = 0;
   std::vector<cudaEvent_t> profEvents;  // start/stop pairs
@@ -191,6 +194,13 @@ void launch_correlation(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2);
 void launch_fill_h2(cgpu_ctx* c, const z_t* orbs);
 void launch_expand_h2(cgpu_ctx* c);
 void launch_rdm_inverse(cgpu_ctx* c);
+void launch_corr_epilogue(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, const z_t* Z);
+void launch_h2_layout(cgpu_ctx* c);
+// k_mixed.cu
+void mixed_setup(cgpu_ctx* c);
+void mixed_free(cgpu_ctx* c);
+int mixed_error(cgpu_ctx* c);
+void launch_correlation_mixed(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2);
 // k_lanczos.cu
 // The SIL kernels work on c->basis_d, c->lw_d (H v_j), c->work_d (start vector),
 // c->metric_d (current metric) and the scalar block c->lz_d.

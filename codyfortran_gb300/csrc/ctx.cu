@@ -204,7 +204,8 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* d) {
   if (c->nOS > 64) throw std::string("more than 64 stored orbitals is not supported");
   if (c->method != CGPU_METHOD_TDCI && c->nOS > 32)
     throw std::string("MCTDHX: more than 32 stored orbitals is not supported");
-  if (d->precision != CGPU_PREC_FP64 && d->precision != CGPU_PREC_MIXED) throw std::string("unknown precision");
+  if (d->precision != CGPU_PREC_FP64 && d->precision != CGPU_PREC_MIXED && d->precision != CGPU_PREC_MIXED_X6)
+    throw std::string("unknown precision");
   setup_grid_and_kinetic(c, d);
   int nG = c->nG;
   // potential (src/SysPotential/Linear/SoftYukawa/StdImpl/*.f90:82-113)
@@ -317,6 +318,7 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* d) {
 }
 
 void free_ctx(cgpu_ctx* c) {
+  mixed_free(c);
   if (c->stepGraph) cudaGraphExecDestroy(c->stepGraph);
   for (cudaEvent_t e : c->profEvents) cudaEventDestroy(e);
   void* ptrs[] = {c->x_d, c->w_d, c->V0_d, c->T_d, c->Vint_d, c->metricW_d, c->metricOne_d, c->metricUser_d, c->Vint_f,
@@ -376,7 +378,8 @@ void td_device(cgpu_ctx* c, int which, z_t* out, const z_t* in, double t, z_t po
     launch_fill_h1_from(c, orbs, c->orbTmp_d, c->h1_d);
     CODY_CUDA(cudaMemsetAsync(dOrbs, 0, sizeof(z_t) * nGO, c->stream));
   }
-  launch_correlation(c, dOrbs, orbs, 1);
+  if (c->precision == CGPU_PREC_FP64) launch_correlation(c, dOrbs, orbs, 1);
+  else launch_correlation_mixed(c, dOrbs, orbs, 1);
   launch_fold_h1(c);
   launch_fold_h2(c);
   CODY_CUDA(cudaMemsetAsync(dC, 0, sizeof(z_t) * c->nC, c->stream));
@@ -511,7 +514,10 @@ void up(cgpu_ctx* c, z_t* dst, const cgpu_complex* src, size_t n) {
 void down(cgpu_ctx* c, cgpu_complex* dst, const z_t* src, size_t n) {
   CODY_CUDA(cudaMemcpyAsync(dst, src, sizeof(z_t) * n, cudaMemcpyDeviceToHost, c->stream));
 }
-void sync(cgpu_ctx* c) { CODY_CUDA(cudaStreamSynchronize(c->stream)); }
+void sync(cgpu_ctx* c) {
+  CODY_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->mixed && mixed_error(c)) throw std::string("tensor-core GEMM: a bounded mbarrier wait expired");
+}
 
 int fail(cgpu_ctx* c, const std::string& msg, int code) {
   if (c) c->lastError = msg;
@@ -688,7 +694,8 @@ int cgpu_apply_correlation_op(cgpu_ctx* c, cgpu_complex* d_orbs, const cgpu_comp
   up(c, c->orbTmp_d, d_orbs, n);
   up(c, c->rdm1_d, rdm1, nO2);
   up(c, c->rdm2_d, rdm2, nO2 * nO2);
-  launch_correlation(c, c->orbTmp_d, c->rkStage_d, h2 != nullptr);
+  if (c->precision == CGPU_PREC_FP64) launch_correlation(c, c->orbTmp_d, c->rkStage_d, h2 != nullptr);
+  else launch_correlation_mixed(c, c->orbTmp_d, c->rkStage_d, h2 != nullptr);
   down(c, d_orbs, c->orbTmp_d, n);
   if (h2) down(c, h2, c->h2_d, nO2 * nO2);
   sync(c);

@@ -12,6 +12,8 @@
 // partials in a fixed order, re-summed identically by every consumer block.
 //
 // Device scalar block lz[] (doubles):
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace {
@@ -51,31 +53,66 @@ __device__ z_t block_sum2(z_t v) {
   return v;
 }
 
-// part[blk*nVec + k] = sum_{i in blk} conj(V_k[i]) m[i] w[i]
-__global__ void k_mdot(z_t* __restrict__ part, const z_t* __restrict__ V, size_t ldv, int nVec,
-                       const z_t* __restrict__ w, const double* __restrict__ m, size_t n, const double* __restrict__ lz) {
-  if (lz && lz[LZ_DONE] != 0.0) return;
-  for (int k = 0; k < nVec; k++) {
-    z_t s = zmk(0.0, 0.0);
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-      z_t a = V[ldv * k + i], b = zscale(w[i], m[i]);
-      s.x += a.x * b.x + a.y * b.y;
-      s.y += a.x * b.y - a.y * b.x;
+constexpr int LZ_MAXV = 32;  // Krylov vectors handled per reduction pass
+
+// Block-reduces acc[0..nVec) (register arrays of every thread) into out[0..nVec).
+template <int MAXV>
+__device__ void block_reduce_many(z_t (&acc)[MAXV], int nVec, z_t* __restrict__ out) {
+  __shared__ z_t red[MAXV][LZ_THREADS / 32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < MAXV; k++) {
+    if (k >= nVec) break;
+    z_t v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) {
+      v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_down_sync(0xffffffffu, v.y, o);
     }
-    s = block_sum2(s);
-    if (threadIdx.x == 0) part[(size_t)blockIdx.x * nVec + k] = s;
+    if (lane == 0) red[k][wid] = v;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < nVec; k += blockDim.x) {
+    z_t s = zmk(0.0, 0.0);
+    for (int q = 0; q < LZ_THREADS / 32; q++) s = zadd(s, red[k][q]);
+    out[k] = s;
   }
 }
 
+// part[blk*nVec + k] = sum_{i in blk} conj(V_k[i]) m[i] w[i], all k in one pass over the data.
+template <int MAXV>
+__global__ void __launch_bounds__(LZ_THREADS) k_mdot(z_t* __restrict__ part, const z_t* __restrict__ V, size_t ldv,
+                                                      int nVec, const z_t* __restrict__ w,
+                                                      const double* __restrict__ m, size_t n,
+                                                      const double* __restrict__ lz) {
+  if (lz && lz[LZ_DONE] != 0.0) return;
+  z_t acc[MAXV];
+#pragma unroll
+  for (int k = 0; k < MAXV; k++) acc[k] = zmk(0.0, 0.0);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    z_t b = zscale(w[i], m[i]);
+#pragma unroll
+    for (int k = 0; k < MAXV; k++) {
+      if (k >= nVec) break;
+      z_t a = V[ldv * k + i];
+      acc[k].x += a.x * b.x + a.y * b.y;
+      acc[k].y += a.x * b.y - a.y * b.x;
+    }
+  }
+  block_reduce_many<MAXV>(acc, nVec, part + (size_t)blockIdx.x * nVec);
+}
+
 // Every block re-sums the partials (fixed order) into shared coefficients,
-// subtracts w -= sum_k coef_k V_k, then emits partials for the next pass:
-// mode 0: dots of the new w with V_0..V_{nVec-1}; mode 1: metric norm^2 of the new w.
-// Block 0 stores the coefficients of the first pass at lz[LZ_D].
-__global__ void k_cgs_pass(z_t* __restrict__ w, const z_t* __restrict__ V, size_t ldv, int nVec,
-                           const z_t* __restrict__ partIn, int nBlkIn, z_t* __restrict__ partOut,
-                           const double* __restrict__ m, size_t n, double* __restrict__ lz, int mode, int storeDots) {
+// subtracts w -= sum_k coef_k V_k, and in the same pass emits partials for the
+// next stage: mode 0: dots of the new w with V_0..V_{nVec-1}; mode 1: the
+// metric norm^2 of the new w.  Block 0 stores the first-pass coefficients at lz[LZ_D].
+template <int MAXV>
+__global__ void __launch_bounds__(LZ_THREADS) k_cgs_pass(z_t* __restrict__ w, const z_t* __restrict__ V, size_t ldv,
+                                                          int nVec, const z_t* __restrict__ partIn, int nBlkIn,
+                                                          z_t* __restrict__ partOut, const double* __restrict__ m,
+                                                          size_t n, double* __restrict__ lz, int mode,
+                                                          int storeDots) {
   if (lz[LZ_DONE] != 0.0) return;
-  __shared__ z_t coef[CODY_MAX_KRYLOV];
+  __shared__ z_t coef[MAXV];
   for (int k = threadIdx.x; k < nVec; k += blockDim.x) {
     z_t s = zmk(0.0, 0.0);
     for (int b = 0; b < nBlkIn; b++) s = zadd(s, partIn[(size_t)b * nVec + k]);
@@ -86,36 +123,37 @@ __global__ void k_cgs_pass(z_t* __restrict__ w, const z_t* __restrict__ V, size_
     }
   }
   __syncthreads();
+  z_t acc[MAXV];
+#pragma unroll
+  for (int k = 0; k < MAXV; k++) acc[k] = zmk(0.0, 0.0);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     z_t r = w[i];
-    for (int k = 0; k < nVec; k++) {
+#pragma unroll
+    for (int k = 0; k < MAXV; k++) {
+      if (k >= nVec) break;
       z_t v = V[ldv * k + i];
       z_t cf = coef[k];
       r.x -= cf.x * v.x - cf.y * v.y;
       r.y -= cf.x * v.y + cf.y * v.x;
     }
     w[i] = r;
-  }
-  __syncthreads();
-  if (mode == 0) {
-    for (int k = 0; k < nVec; k++) {
-      z_t s = zmk(0.0, 0.0);
-      for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        z_t a = V[ldv * k + i], b = zscale(w[i], m[i]);
-        s.x += a.x * b.x + a.y * b.y;
-        s.y += a.x * b.y - a.y * b.x;
+    z_t b = zscale(r, m[i]);
+    if (mode == 0) {
+#pragma unroll
+      for (int k = 0; k < MAXV; k++) {
+        if (k >= nVec) break;
+        z_t a = V[ldv * k + i];
+        acc[k].x += a.x * b.x + a.y * b.y;
+        acc[k].y += a.x * b.y - a.y * b.x;
       }
-      s = block_sum2(s);
-      if (threadIdx.x == 0) partOut[(size_t)blockIdx.x * nVec + k] = s;
+    } else {
+      acc[0].x += r.x * b.x + r.y * b.y;
     }
+  }
+  if (mode == 0) {
+    block_reduce_many<MAXV>(acc, nVec, partOut + (size_t)blockIdx.x * nVec);
   } else {
-    z_t s = zmk(0.0, 0.0);
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-      z_t b = w[i];
-      s.x += (b.x * b.x + b.y * b.y) * m[i];
-    }
-    s = block_sum2(s);
-    if (threadIdx.x == 0) partOut[blockIdx.x] = s;
+    block_reduce_many<MAXV>(acc, 1, partOut + blockIdx.x);
   }
 }
 
@@ -186,7 +224,7 @@ __global__ void k_lz_expsub(double* __restrict__ lz, int mFixed, double dt, doub
   __syncwarp();
   int ne = (m + 1) & ~1;
   int half = ne / 2;
-  for (int sweep = 0; sweep < 60 && m > 1; sweep++) {
+  for (int sweep = 0; sweep < 30 && m > 1; sweep++) {
     double off = 0.0, dg = 0.0;
     if (lane < m)
       for (int i = 0; i < m; i++) {
@@ -197,7 +235,7 @@ __global__ void k_lz_expsub(double* __restrict__ lz, int mFixed, double dt, doub
       off += __shfl_xor_sync(0xffffffffu, off, o);
       dg += __shfl_xor_sync(0xffffffffu, dg, o);
     }
-    if (off <= 1e-34 * (dg + off) || off == 0.0) break;
+    if (off <= 1e-28 * (dg + off) || off == 0.0) break;  // rounding floor is ~1e-32
     for (int r = 0; r < ne - 1; r++) {
       if (lane < half) {
         auto pos = [&](int i) { return i == 0 ? 0 : ((i - 1 + r) % (ne - 1)) + 1; };
@@ -359,14 +397,20 @@ void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
   size_t nS = c->nS;
   z_t* p1 = c->partial_d;
   z_t* p2 = c->partial_d + (size_t)LZ_BLOCKS * (CODY_MAX_KRYLOV + 1);
-  k_mdot<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(p1, c->basis_d, nS, j, c->lw_d, c->metric_d, nS, c->lz_d);
-  CODY_LAUNCHED(c);
-  k_cgs_pass<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, nS, j, p1, LZ_BLOCKS, p2, c->metric_d, nS,
-                                                       c->lz_d, 0, 1);
-  CODY_LAUNCHED(c);
-  k_cgs_pass<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, nS, j, p2, LZ_BLOCKS, p1, c->metric_d, nS,
-                                                       c->lz_d, 1, 0);
-  CODY_LAUNCHED(c);
+  auto passes = [&](auto tag) {
+    constexpr int MV = decltype(tag)::value;
+    k_mdot<MV><<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(p1, c->basis_d, nS, j, c->lw_d, c->metric_d, nS, c->lz_d);
+    CODY_LAUNCHED(c);
+    k_cgs_pass<MV><<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, nS, j, p1, LZ_BLOCKS, p2,
+                                                             c->metric_d, nS, c->lz_d, 0, 1);
+    CODY_LAUNCHED(c);
+    k_cgs_pass<MV><<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, nS, j, p2, LZ_BLOCKS, p1,
+                                                             c->metric_d, nS, c->lz_d, 1, 0);
+    CODY_LAUNCHED(c);
+  };
+  if (j <= 8) passes(std::integral_constant<int, 8>());
+  else if (j <= 16) passes(std::integral_constant<int, 16>());
+  else passes(std::integral_constant<int, 32>());
   z_t* vNext = (j < maxDim) ? c->basis_d + nS * (size_t)j : nullptr;
   k_lz_finish<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p1, LZ_BLOCKS, nS, c->lz_d, j, maxDim,
                                                         1.0e-14);

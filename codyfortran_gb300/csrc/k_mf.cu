@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t
   __syncthreads();
   int ne = (n + 1) & ~1;
   int half = ne / 2;
-  for (int sweep = 0; sweep < 60; sweep++) {
+  for (int sweep = 0; sweep < 30; sweep++) {
     if (tid == 0) {
       double off = 0.0, dg = 0.0;
       for (int j = 0; j < n; j++)
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t
       diags = dg;
     }
     __syncthreads();
-    if (offs <= 1e-34 * (diags + offs) || offs == 0.0) break;
+    if (offs <= 1e-28 * (diags + offs) || offs == 0.0) break;  // rounding floor is ~1e-32
     for (int r = 0; r < ne - 1; r++) {
       if (tid < half) {
         int k = tid;
@@ -450,3 +450,16 @@ void launch_fill_h2(cgpu_ctx* c, const z_t* orbs) {
 }
 
 void launch_expand_h2(cgpu_ctx* c) { h2_from_pairs(c); }
+
+void launch_corr_epilogue(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, const z_t* Z) {
+  dim3 grid((c->nG + 255) / 256, c->nOS);
+  k_corr_epilogue<<<grid, 256, 0, c->stream>>>(dOrbs, orbs, Z, c->nG, c->nOS);
+  CODY_LAUNCHED(c);
+}
+
+void launch_h2_layout(cgpu_ctx* c) {
+  size_t n4 = (size_t)c->nO * c->nO * c->nO * c->nO;
+  k_h2_layout<<<(int)((n4 + 255) / 256), 256, 0, c->stream>>>(c->h2_d, c->h2s_d, c->btOfOrb_d, c->nO, c->nOS,
+                                                               c->restricted);
+  CODY_LAUNCHED(c);
+}

@@ -1,0 +1,295 @@
+// k_tc.cu -- tcgen05 tensor-core contractions of the mixed-precision form.
+//
+// One GEMM kernel, C[M,N] (+)= A[M,K] B[N,K]^T with A and B bf16, both
+// K-major, accumulated in FP32 in tensor memory (TMEM):
+//   * operands are staged by TMA (cp.async.bulk.tensor, 128B swizzle) into a
+//     STAGES-deep shared-memory ring guarded by mbarriers;
+//   * one thread issues tcgen05.mma (kind::f16, M=128, N=BN, K=16 per
+//     instruction) and commits each stage back to the producer;
+//   * four warps read the accumulator with tcgen05.ld and store FP32 partial
+//     tiles; split-K partials are summed in FP64 by the consumer kernels.
+// Split precision is expressed in the operands: a value x is carried as
+// hi = bf16(x), lo = bf16(x - hi) (bf16x3: products hi*hi + hi*lo + lo*hi),
+// or as hi/mid/lo (bf16x6: all products of total order <= 2), laid out as
+// consecutive K segments so one accumulation sums all products.
+//
+// Every mbarrier wait is bounded (clock64 limit).  On expiry the kernel sets
+// an error flag, drains its own TMA copies with bounded waits, frees its
+// TMEM and returns; the host reports the flag as an error.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "common.cuh"
+#include "tc.cuh"
+
+namespace {
+
+constexpr int TC_BM = 128;
+constexpr int TC_BK = 64;  // bf16 elements per 128-byte swizzle row
+constexpr long long TC_WAIT_CYCLES = 4000000000LL;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false when the limit expires or another role aborted.
+__device__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abortFlag) {
+  long long t0 = clock64();
+  while (!mbar_test(bar, parity)) {
+    if (*abortFlag) return false;
+    if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+    __nanosleep(32);
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of 1024 bytes.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmemD, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmemD),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+#define TMEM_LD_X16(taddr, r)                                                                                  \
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, " \
+               "[%16];"                                                                                        \
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),            \
+                 "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),        \
+                 "=r"(r[14]), "=r"(r[15])                                                                      \
+               : "r"(taddr))
+
+// P[z][m][n] = sum_{k in split z} A[m][k] B[n][k]; A rows m0.., B rows n0.., bf16 K-major.
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(128, 1)
+    k_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, float* __restrict__ P,
+              int M, int N, int ldp, int kTiles, int kTilesPerSplit, int* __restrict__ err) {
+  constexpr int A_BYTES = TC_BM * TC_BK * 2;
+  constexpr int B_BYTES = BN * TC_BK * 2;
+  constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  constexpr uint32_t TMEM_COLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t fullBar[STAGES];
+  __shared__ __align__(8) uint64_t emptyBar[STAGES];
+  __shared__ __align__(8) uint64_t doneBar;
+  __shared__ uint32_t tmemSlot;
+  __shared__ volatile int abortFlag;
+  __shared__ int consumed;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * BN;
+  const int kt0 = blockIdx.z * kTilesPerSplit;
+  const int kt1 = min(kTiles, kt0 + kTilesPerSplit);
+  const int nk = kt1 - kt0;
+
+  if (threadIdx.x == 0) {
+    abortFlag = 0;
+    consumed = 0;
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(&fullBar[s], 1);
+      mbar_init(&emptyBar[s], 1);
+    }
+    mbar_init(&doneBar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmemSlot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmemSlot;
+
+  int issued = 0;
+  if (nk > 0 && warp == 0 && lane == 0) {
+    // TMA producer
+    for (int i = 0; i < nk; i++) {
+      int s = i % STAGES, r = i / STAGES;
+      if (!mbar_wait(&emptyBar[s], (r & 1) ^ 1, &abortFlag)) {
+        abortFlag = 1;
+        atomicExch(err, 1);
+        break;
+      }
+      mbar_expect_tx(&fullBar[s], STAGE_BYTES);
+      tma_load_2d(smem + s * STAGE_BYTES, &tA, &fullBar[s], (kt0 + i) * TC_BK, m0);
+      tma_load_2d(smem + s * STAGE_BYTES + A_BYTES, &tB, &fullBar[s], (kt0 + i) * TC_BK, n0);
+      issued = i + 1;
+    }
+  } else if (nk > 0 && warp == 1 && lane == 0) {
+    // MMA issuer: instruction descriptor kind::f16, D=F32, A=B=BF16, K-major, N=BN, M=128
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(TC_BM >> 4) << 24);
+    int i = 0;
+    for (; i < nk; i++) {
+      int s = i % STAGES, r = i / STAGES;
+      if (!mbar_wait(&fullBar[s], r & 1, &abortFlag)) {
+        abortFlag = 1;
+        atomicExch(err, 2);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      uint32_t a = smem_u32(smem + s * STAGE_BYTES);
+      uint32_t b = a + A_BYTES;
+#pragma unroll
+      for (int k = 0; k < TC_BK / 16; k++)
+        umma_bf16(tmem, sw128_desc(a + k * 32), sw128_desc(b + k * 32), idesc, (i > 0 || k > 0) ? 1u : 0u);
+      umma_commit(&emptyBar[s]);
+    }
+    consumed = i;
+    umma_commit(&doneBar);
+  }
+  __syncwarp();
+  bool ok = (nk > 0) && mbar_wait(&doneBar, 0, &abortFlag);
+  if (!ok && nk > 0) atomicExch(err, 3);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  __syncwarp();
+  // epilogue: warp w owns TMEM lanes [32w, 32w+32) = tile rows
+  const int row = m0 + warp * 32 + lane;
+  float* Pz = P + (size_t)blockIdx.z * (size_t)M * ldp;
+#pragma unroll 1
+  for (int c = 0; c < BN; c += 16) {
+    uint32_t r[16];
+    TMEM_LD_X16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    if (ok && !abortFlag && row < M) {
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        int col = n0 + c + j;
+        if (col < N) Pz[(size_t)row * ldp + col] = __uint_as_float(r[j]);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  // drain TMA copies that were issued but never consumed (only after an abort)
+  if (warp == 0 && lane == 0 && abortFlag) {
+    volatile int dummy = 0;
+    for (int i = consumed; i < issued; i++) {
+      int s = i % STAGES, r = i / STAGES;
+      mbar_wait(&fullBar[s], r & 1, &dummy);
+    }
+  }
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+void ensure_encode() {
+  if (g_encode) return;
+  cudaDriverEntryPointQueryResult q;
+  void* fn = nullptr;
+  CODY_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+  if (q != cudaDriverEntryPointSuccess || !fn) throw std::string("cuda: cuTensorMapEncodeTiled unavailable");
+  g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+}
+
+// 2D bf16 tensor [rows, kCols] row-major (kCols contiguous, multiple of 64); box = 64 x boxRows.
+CUtensorMap make_tmap(const void* base, int rows, int kCols, int boxRows) {
+  ensure_encode();
+  if ((uintptr_t)base % 16 != 0 || kCols % TC_BK != 0) throw std::string("tensor map: bad alignment");
+  CUtensorMap m;
+  std::memset(&m, 0, sizeof(m));
+  cuuint64_t dims[2] = {(cuuint64_t)kCols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)kCols * 2};
+  cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)boxRows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw std::string("cuda: cuTensorMapEncodeTiled failed");
+  return m;
+}
+
+template <int BN, int STAGES>
+int launch_gemm_t(cgpu_ctx* c, const CUtensorMap& ta, const CUtensorMap& tb, float* P, int M, int N, int kTiles,
+                  int nSplit, int* err) {
+  constexpr int smem = STAGES * (TC_BM * TC_BK * 2 + BN * TC_BK * 2) + 1024;
+  static bool attr = false;
+  if (!attr) {
+    CODY_CUDA(cudaFuncSetAttribute(k_tc_gemm<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr = true;
+  }
+  int per = (kTiles + nSplit - 1) / nSplit;
+  nSplit = (kTiles + per - 1) / per;
+  dim3 grid((M + TC_BM - 1) / TC_BM, (N + BN - 1) / BN, nSplit);
+  k_tc_gemm<BN, STAGES><<<grid, 128, smem, c->stream>>>(ta, tb, P, M, N, N, kTiles, per, err);
+  CODY_LAUNCHED(c);
+  return nSplit;
+}
+
+}  // namespace
+
+int tc_tile_n(int N) {
+  int best = 64, bestCols = ((N + 63) / 64) * 64;
+  for (int bn : {128, 256}) {
+    int cols = ((N + bn - 1) / bn) * bn;
+    if (cols <= bestCols) { best = bn; bestCols = cols; }
+  }
+  return best;
+}
+
+int tc_split_count(int M, int N, int BN, int kTiles) {
+  int tiles = ((M + TC_BM - 1) / TC_BM) * ((N + BN - 1) / BN);
+  int s = std::max(1, (152 + tiles - 1) / tiles);
+  s = std::min(s, std::max(1, kTiles / 2));
+  int per = (kTiles + s - 1) / s;
+  return (kTiles + per - 1) / per;
+}
+
+// P[split][M][N] (fp32) = A[M, K] B[N, K]^T, bf16 operands with K a multiple of 64.
+int tc_gemm(cgpu_ctx* c, const __nv_bfloat16* A, int M, const __nv_bfloat16* B, int N, int K, float* P, int nSplit,
+            int* err) {
+  if (K % TC_BK != 0 || K <= 0) throw std::string("tc_gemm: K must be a positive multiple of 64");
+  int kTiles = K / TC_BK;
+  int bn = tc_tile_n(N);
+  CUtensorMap ta = make_tmap(A, M, K, TC_BM), tb = make_tmap(B, N, K, bn);
+  if (bn == 64) return launch_gemm_t<64, 6>(c, ta, tb, P, M, N, kTiles, nSplit, err);
+  if (bn == 128) return launch_gemm_t<128, 5>(c, ta, tb, P, M, N, kTiles, nSplit, err);
+  return launch_gemm_t<256, 4>(c, ta, tb, P, M, N, kTiles, nSplit, err);
+}

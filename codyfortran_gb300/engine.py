@@ -120,7 +120,7 @@ def make_desc(spec: SystemSpec, precision: str = "fp64", max_krylov: int = 32):
         d.n_field_samples = len(keep)
         d.field_dt, d.field_t0 = L.sample_dt, L.sample_t0
     d.method = 1 if spec.method == "tdci" else 0
-    d.precision = {"fp64": 0, "mixed": 1}[precision]
+    d.precision = {"fp64": 0, "mixed": 1, "mixed6": 2}[precision]
     d.max_krylov = max_krylov
     return d, keep
 

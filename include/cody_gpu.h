@@ -46,7 +46,12 @@ extern "C" {
 #define CGPU_METHOD_TDCI 1
 
 #define CGPU_PREC_FP64 0
+/* Mixed: the pair-potential, correlation and h2 contractions on tcgen05 tensor cores with
+ * split-bf16 operands (hi + lo, three products) and FP32 accumulation; RDMs, rho^-1,
+ * projectors, Lanczos, energy and norm in FP64. */
 #define CGPU_PREC_MIXED 1
+/* As CGPU_PREC_MIXED with three-way split operands (hi + mid + lo, six products). */
+#define CGPU_PREC_MIXED_X6 2
 
 /* Time-derivative selectors (the TimeDerivative procedure pointers). */
 #define CGPU_TD_FULL 0   /* Method_TimeDerivative (Mctdhx :101-149)                        */

@@ -93,7 +93,7 @@ static void jacobi_herm(int n, const cd* Ain, double* evals, cd* evecs) {
         if (i != j) off += std::norm(a(i, j));
         else diag += std::norm(a(i, j));
       }
-    if (off <= 1e-34 * (diag + off) || off == 0.0) break;
+    if (off <= 1e-28 * (diag + off) || off == 0.0) break;  // rounding floor is ~1e-32
     for (int p = 0; p < n - 1; p++)
       for (int q = p + 1; q < n; q++) {
         cd b = a(p, q);
@@ -149,7 +149,7 @@ static void jacobi_sym(int n, const double* Ain, double* evals, double* evecs) {
         if (i != j) off += a(i, j) * a(i, j);
         else diag += a(i, j) * a(i, j);
       }
-    if (off <= 1e-34 * (diag + off) || off == 0.0) break;
+    if (off <= 1e-28 * (diag + off) || off == 0.0) break;  // rounding floor is ~1e-32
     for (int p = 0; p < n - 1; p++)
       for (int q = p + 1; q < n; q++) {
         double g = a(p, q);

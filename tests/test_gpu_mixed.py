@@ -1,0 +1,99 @@
+"""Mixed-precision form: tcgen05 split-bf16 contractions against the FP64 oracle.
+
+Tolerances state the accuracy of the split: bf16x3 (hi + lo operands, three
+products, FP32 accumulation) and bf16x6 (hi + mid + lo, six products).  The
+relative errors measured here are what the form delivers; the propagation
+check compares energy and norm of a mixed trajectory with the FP64 one.
+"""
+import numpy as np
+import pytest
+
+from oracle import Oracle
+from codyfortran_gb300 import init as I
+from codyfortran_gb300 import spec as S
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"mixed": 2e-4, "mixed6": 2e-6}
+
+
+def rel(a, b):
+    return np.linalg.norm((np.asarray(a) - np.asarray(b)).ravel()) / np.linalg.norm(np.asarray(b).ravel())
+
+
+def _systems():
+    he = S.helium_fedvr(20, 6, 4, laser=S.sin2_pulse(0.0534, omega=0.2, n_cycles=2.0))
+    he.xmin, he.xmax = -20.0, 20.0
+    one = S.SystemSpec(grid_kind="fedvr", xmin=-16.0, xmax=16.0, n_elements=16, n_locals=8, n_bodies=(3,),
+                       n_orbs=(6,), masses=(1.0,), stats="f", nuclei=[S.Nucleus(-2.0, 1.5), S.Nucleus(2.0, 1.5)],
+                       int_kind="dense")
+    return {"helium_restricted": he, "single_body_type": one}
+
+
+def _state(sp, o, seed):
+    rng = np.random.default_rng(seed)
+    orbs = I.seeded_gaussian_orbitals(sp, o.x, o.w, seed)
+    c = rng.normal(size=o.nC) + 1j * rng.normal(size=o.nC)
+    c /= np.linalg.norm(c)
+    return c, orbs, I.pack_state(c, orbs)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed6"])
+@pytest.mark.parametrize("name", ["helium_restricted", "single_body_type"])
+def test_mixed_correlation_and_nonlin(name, precision):
+    from codyfortran_gb300.engine import Engine
+    sp = _systems()[name]
+    o = Oracle(sp)
+    e = Engine(sp, precision=precision)
+    c, orbs, st = _state(sp, o, 5)
+    r1, r2 = o.rdm1(c), o.rdm2(c)
+    d_gpu, h2_gpu = e.apply_correlation_op(orbs, r1, r2, 0.0)
+    d_orc, h2_orc = o.apply_correlation_op(orbs, r1, r2, 0.0)
+    assert rel(d_gpu, d_orc) < TOL[precision]
+    assert rel(h2_gpu, h2_orc) < TOL[precision]
+    assert rel(e.time_derivative(st, 1.5, "nonlin"), o.time_derivative(st, 1.5, "nonlin")) < TOL[precision]
+    e.close()
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed6"])
+def test_mixed_nonlin_full_size(precision):
+    """2801 points, 16 orbitals (136 pairs), 8008 determinants."""
+    from codyfortran_gb300.engine import Engine
+    sp = S.cfg_trimer_large()
+    o = Oracle(sp)
+    e = Engine(sp, precision=precision)
+    c, orbs, st = _state(sp, o, 7)
+    a = e.time_derivative(st, 5.0, "nonlin")
+    b = o.time_derivative(st, 5.0, "nonlin")
+    err = rel(a, b)
+    print(f"{precision}: NonLin relative error {err:.3e}")
+    assert err < TOL[precision]
+    e.close()
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed6"])
+def test_mixed_trajectory_energy_norm(precision):
+    """Energy and norm of a mixed-precision trajectory against the FP64 GPU trajectory."""
+    from codyfortran_gb300.engine import Engine
+    sp = S.cfg_helium_small()
+    f = Engine(sp, precision="fp64")
+    m = Engine(sp, precision=precision)
+    orbs = I.seeded_gaussian_orbitals(sp, f.x, f.w, 42)
+    st = I.pack_state(I.unary_coeffs(sp), orbs)
+    f.upload(st)
+    m.upload(st)
+    n_steps, dt = 200, 0.01
+    f.propagate_resident(0.0, dt, n_steps, 12, use_metric=True)
+    m.propagate_resident(0.0, dt, n_steps, 12, use_metric=True)
+    t = n_steps * dt
+    ef, em = f.energy_resident(t), m.energy_resident(t)
+    sf, sm = f.download(), m.download()
+    w = f.metric_weights()
+    nf, nm = np.sqrt(np.sum(np.abs(sf) ** 2 * w)), np.sqrt(np.sum(np.abs(sm) ** 2 * w))
+    de, dn = abs(em - ef) / abs(ef), abs(nm - nf)
+    print(f"{precision}: {n_steps} steps, |dE|/|E| = {de:.3e}, |d norm| = {dn:.3e}")
+    # measured on GB300: bf16x3 |dE|/|E| ~ 2e-6, |d norm| ~ 1e-7 over these 200 steps
+    lim = {"mixed": (1e-5, 1e-6), "mixed6": (2e-6, 2e-7)}[precision]
+    assert de < lim[0] and dn < lim[1]
+    f.close()
+    m.close()
