@@ -36,6 +36,28 @@ __host__ __device__ __forceinline__ z_t zmi(z_t a) { return make_double2(a.y, -a
 // multiply by +i
 __host__ __device__ __forceinline__ z_t zpi(z_t a) { return make_double2(-a.y, a.x); }
 
+// out[k] = sum_{b < nBlk} part[b*stride + k] for k < nk, computed by the whole
+// block (warp per k, lanes over b, fixed order: every block that calls it with
+// the same arguments gets bit-identical sums).  Ends with __syncthreads().
+__device__ __forceinline__ void sum_partials(const double2* __restrict__ part, int nBlk, int stride, int nk,
+                                             double2* out) {
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = wid; k < nk; k += nw) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int b = lane; b < nBlk; b += 32) {
+      double2 p = part[(size_t)b * stride + k];
+      s.x += p.x;
+      s.y += p.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+      s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+    }
+    if (lane == 0) out[k] = s;
+  }
+  __syncthreads();
+}
+
 #define CODY_MAX_BT 4
 #define CODY_MAX_ORBS 64
 #define CODY_MAX_KRYLOV 64
@@ -76,6 +98,15 @@ struct CiView {
 
 struct MixedBufs;  // mixed-precision operand buffers (k_mixed.cu)
 
+// Laser parameters as the device sees them (E(t) is evaluated in the kernels so
+// that a captured step can be replayed at any time).
+struct LaserDev {
+  int kind;
+  double E0, omega, nCycles, cep, tStart, sampleDt, sampleT0;
+  int nSamples;
+  const double* samples;
+};
+
 // ---------------------------------------------------------------------------
 // The context: one system, its device-resident operators, tables and work
 // buffers, and one CUDA stream.  Not reentrant (one host thread at a time),
@@ -115,6 +146,7 @@ struct cgpu_ctx {
   z_t *Rp_d = nullptr;                        // (nOS^2, nOS^2) correlation matrix
   z_t *h2s_d = nullptr;                       // (nOS^2, nOS^2) spatial h2 block
   z_t *Mreg_d = nullptr;                      // (nOS, nOS)
+  z_t *Uprev_d = nullptr;                     // (nOS, nOS) natural orbitals of the previous rho^-1 call
   z_t *r1s_d = nullptr, *r2s_d = nullptr;     // spin-summed spatial RDMs
   // reductions / scratch
   z_t* partial_d = nullptr;
@@ -134,7 +166,18 @@ struct cgpu_ctx {
   cudaStream_t stream = nullptr;
   cudaGraphExec_t stepGraph = nullptr;
   double graphDt = 0;
-  int graphKrylov = 0;
+  int graphKrylov = 0, graphMetric = -1, graphKernels = 0, graphProf = 0;
+  size_t graphProfUsed = 0;
+  // device-side time: kernels evaluate E(*timeBase + offset).  Outside a graph
+  // capture the base is a device zero and the offset the absolute time; inside
+  // one the base is the step-start time stepT_d that the graph advances.
+  LaserDev laserDev;
+  double* samples_d = nullptr;
+  double* zero_d = nullptr;
+  double* stepT_d = nullptr;
+  int inCapture = 0;
+  double captureT0 = 0.0;
+  z_t* warm_d = nullptr;
   std::string lastError;
   int launches = 0;  // kernels launched by this context (since the last reset)
   MixedBufs* mixed = nullptr;
@@ -161,7 +204,9 @@ struct ProfScope {
       cudaEventCreate(&e);
       c->profEvents.push_back(e);
     }
-    cudaEventRecord(c->profEvents[c->profUsed++], c->stream);
+    // inside a stream capture only an external record becomes an event-record node
+    if (c->inCapture) cudaEventRecordWithFlags(c->profEvents[c->profUsed++], c->stream, cudaEventRecordExternal);
+    else cudaEventRecord(c->profEvents[c->profUsed++], c->stream);
   }
 };
 

@@ -231,6 +231,13 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* d) {
   }
   // device operators
   CODY_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  c->zero_d = dalloc<double>(1);
+  c->stepT_d = dalloc<double>(1);
+  CODY_CUDA(cudaMemset(c->zero_d, 0, sizeof(double)));
+  CODY_CUDA(cudaMemset(c->stepT_d, 0, sizeof(double)));
+  if (!c->samples.empty()) c->samples_d = dupload(c->samples);
+  c->laserDev = LaserDev{c->laserKind, c->E0, c->omega, c->nCycles, c->cep, c->tStart, c->sampleDt, c->sampleT0,
+                         (int)c->samples.size(), c->samples_d};
   c->x_d = dupload(c->x);
   c->w_d = dupload(c->w);
   c->V0_d = dupload(c->V0);
@@ -296,6 +303,11 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* d) {
   c->Rp_d = dalloc<z_t>(Q * Q);
   c->h2s_d = dalloc<z_t>(Q * Q);
   c->Mreg_d = dalloc<z_t>(Q);
+  {
+    std::vector<z_t> eye(Q, zmk(0.0, 0.0));
+    for (int i = 0; i < n; i++) eye[(size_t)i * n + i] = zmk(1.0, 0.0);
+    c->Uprev_d = dupload(eye);
+  }
   c->r1s_d = dalloc<z_t>(Q);
   c->gram_d = dalloc<z_t>(Q);
   c->orbTmp_d = dalloc<z_t>((size_t)nG * n);
@@ -326,7 +338,8 @@ void free_ctx(cgpu_ctx* c) {
                   c->h2_d, c->pairL_d, c->pairK_d, c->pidx_d, c->S_d, c->W_d, c->Sfull_d, c->Wfull_d, c->Rp_d,
                   c->h2s_d, c->Mreg_d, c->r1s_d, c->r2s_d, c->partial_d, c->gram_d, c->orbTmp_d, c->scal_d,
                   c->state_d, c->dstate_d, c->rkInc_d, c->rkTmp_d, c->rkStage_d, c->basis_d, c->lw_d, c->trial_d,
-                  c->work_d, c->lz_d, c->tdciOrbs_d};
+                  c->work_d, c->lz_d, c->tdciOrbs_d, c->zero_d, c->stepT_d, c->samples_d, c->warm_d,
+                  c->Uprev_d};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int b = 0; b < CODY_MAX_BT; b++) {
@@ -491,6 +504,53 @@ void split2_device(cgpu_ctx* c, z_t* state, double t0, double t1, int krylov, do
   rk4_device(c, CGPU_TD_NONLIN, state, time1, time1 + 1.0 * dt);
   if (krylov > 0) sil_device(c, CGPU_TD_ORBS_LIN, state, time2, time2 + 0.5 * dt, krylov, tol, maxRestarts, m);
   else rk4_device(c, CGPU_TD_ORBS_LIN, state, time2, time2 + 0.5 * dt);
+}
+
+__global__ void k_advance_time(double* t, double dt) { *t = *t + dt; }
+
+// Captures one fixed-order Strang step on state_d as a CUDA graph.  The step
+// reads its start time from stepT_d (the laser is evaluated on the device) and
+// advances it by dt, so the graph can be replayed for consecutive steps.  A
+// first step on a scratch copy of the state allocates every lazily sized
+// buffer outside the capture.
+void capture_step_graph(cgpu_ctx* c, double t0, double dt, int krylov, int useMetric) {
+  if (c->stepGraph) {
+    cudaGraphExecDestroy(c->stepGraph);
+    c->stepGraph = nullptr;
+  }
+  if (!c->warm_d) c->warm_d = dalloc<z_t>(c->nS);
+  CODY_CUDA(cudaMemcpyAsync(c->warm_d, c->state_d, sizeof(z_t) * c->nS, cudaMemcpyDeviceToDevice, c->stream));
+  split2_device(c, c->warm_d, t0, t0 + dt, krylov, 0.0, 0, useMetric);
+  CODY_CUDA(cudaStreamSynchronize(c->stream));
+  // profiling events of the selected kernel family become event-record nodes of the graph
+  c->profUsed = 0;
+  long before = c->launches;
+  cudaGraph_t g = nullptr;
+  CODY_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  c->inCapture = 1;
+  c->captureT0 = t0;
+  try {
+    split2_device(c, c->state_d, t0, t0 + dt, krylov, 0.0, 0, useMetric);
+    k_advance_time<<<1, 1, 0, c->stream>>>(c->stepT_d, dt);
+    CODY_LAUNCHED(c);
+  } catch (...) {
+    c->inCapture = 0;
+    cudaStreamEndCapture(c->stream, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  c->inCapture = 0;
+  c->graphProf = c->profTarget;
+  c->graphProfUsed = c->profUsed;
+  CODY_CUDA(cudaStreamEndCapture(c->stream, &g));
+  c->graphKernels = (int)(c->launches - before);
+  c->launches = before;
+  cudaError_t e = cudaGraphInstantiate(&c->stepGraph, g, 0);
+  cudaGraphDestroy(g);
+  CODY_CUDA(e);
+  c->graphDt = dt;
+  c->graphKrylov = krylov;
+  c->graphMetric = useMetric;
 }
 
 double energy_device(cgpu_ctx* c, const z_t* state, double t) {
@@ -833,7 +893,19 @@ int cgpu_propagate_split2(cgpu_ctx* c, cgpu_complex* state, double t0, double t1
                           int max_restarts, int use_metric) {
   CODY_API_BEGIN(c)
   up(c, c->state_d, state, c->nS);
-  split2_device(c, c->state_d, t0, t1, krylov_dim, tolerance, max_restarts, use_metric);
+  if (krylov_dim > 0 && tolerance == 0.0 && max_restarts == 0) {
+    // fixed-order SIL: the step has no host-side decisions, replay it as one graph
+    double dt = t1 - t0;
+    if (!c->stepGraph || c->graphDt != dt || c->graphKrylov != krylov_dim || c->graphMetric != use_metric ||
+        c->graphProf != c->profTarget)
+      capture_step_graph(c, t0, dt, krylov_dim, use_metric);
+    if (c->profTarget) c->profUsed = c->graphProfUsed;
+    CODY_CUDA(cudaMemcpyAsync(c->stepT_d, &t0, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CODY_CUDA(cudaGraphLaunch(c->stepGraph, c->stream));
+    c->launches += c->graphKernels;
+  } else {
+    split2_device(c, c->state_d, t0, t1, krylov_dim, tolerance, max_restarts, use_metric);
+  }
   down(c, state, c->state_d, c->nS);
   sync(c);
   CODY_API_END(c)
@@ -856,13 +928,23 @@ int cgpu_state_download(cgpu_ctx* c, cgpu_complex* state) {
 int cgpu_propagate_resident(cgpu_ctx* c, double t0, double dt, int n_steps, int krylov_dim, int use_metric,
                             int use_graph) {
   CODY_API_BEGIN(c)
-  (void)use_graph;
-  double t = t0;
-  for (int s = 0; s < n_steps; s++) {
-    split2_device(c, c->state_d, t, t + dt, krylov_dim, 0.0, 0, use_metric);
-    t = t + dt;
+  if (!use_graph) {
+    double t = t0;
+    for (int s = 0; s < n_steps; s++) {
+      split2_device(c, c->state_d, t, t + dt, krylov_dim, 0.0, 0, use_metric);
+      t = t + dt;
+    }
+    CODY_CUDA(cudaGetLastError());
+  } else {
+    if (!c->stepGraph || c->graphDt != dt || c->graphKrylov != krylov_dim || c->graphMetric != use_metric ||
+        c->graphProf != c->profTarget) {
+      capture_step_graph(c, t0, dt, krylov_dim, use_metric);
+    }
+    if (c->profTarget) c->profUsed = c->graphProfUsed;
+    CODY_CUDA(cudaMemcpyAsync(c->stepT_d, &t0, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    for (int s = 0; s < n_steps; s++) CODY_CUDA(cudaGraphLaunch(c->stepGraph, c->stream));
+    c->launches += n_steps * c->graphKernels;
   }
-  CODY_CUDA(cudaGetLastError());
   CODY_API_END(c)
 }
 

@@ -113,16 +113,12 @@ __global__ void __launch_bounds__(LZ_THREADS) k_cgs_pass(z_t* __restrict__ w, co
                                                           int storeDots) {
   if (lz[LZ_DONE] != 0.0) return;
   __shared__ z_t coef[MAXV];
-  for (int k = threadIdx.x; k < nVec; k += blockDim.x) {
-    z_t s = zmk(0.0, 0.0);
-    for (int b = 0; b < nBlkIn; b++) s = zadd(s, partIn[(size_t)b * nVec + k]);
-    coef[k] = s;
-    if (storeDots && blockIdx.x == 0) {
-      lz[LZ_D + 2 * k] = s.x;
-      lz[LZ_D + 2 * k + 1] = s.y;
+  sum_partials(partIn, nBlkIn, nVec, nVec, coef);
+  if (storeDots && blockIdx.x == 0)
+    for (int k = threadIdx.x; k < nVec; k += blockDim.x) {
+      lz[LZ_D + 2 * k] = coef[k].x;
+      lz[LZ_D + 2 * k + 1] = coef[k].y;
     }
-  }
-  __syncthreads();
   z_t acc[MAXV];
 #pragma unroll
   for (int k = 0; k < MAXV; k++) acc[k] = zmk(0.0, 0.0);
@@ -162,14 +158,9 @@ __global__ void __launch_bounds__(LZ_THREADS) k_cgs_pass(z_t* __restrict__ w, co
 __global__ void k_lz_finish(z_t* __restrict__ vNext, const z_t* __restrict__ w, const z_t* __restrict__ partIn,
                             int nBlkIn, size_t n, double* __restrict__ lz, int j, int maxDim, double zeroThr) {
   if (lz[LZ_DONE] != 0.0) return;
-  __shared__ double beta;
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int b = 0; b < nBlkIn; b++) s += partIn[b].x;
-    beta = sqrt(s);
-  }
-  __syncthreads();
-  double be = beta;
+  __shared__ z_t tot[1];
+  sum_partials(partIn, nBlkIn, 1, 1, tot);
+  double be = sqrt(tot[0].x);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     lz[LZ_ALPHA + j - 1] = lz[LZ_D + 2 * (j - 1)];
     lz[LZ_BETA + j - 1] = be;
@@ -196,123 +187,115 @@ __global__ void k_lz_mark_done(double* lz, int j) {
   if (lz[LZ_DONE] == 0.0 && lz[LZ_BREAKJ] == (double)j) lz[LZ_DONE] = 1.0;
 }
 
-// ---------------------------------------------------------------------------
-// EvaluateExpInSubspace: eig of the m x m tridiagonal (one warp, parallel
-// round-robin Jacobi), phi = U exp(-i dt L) U^T e1, err = beta_m |phi_m|.
-// m <= 32.  Writes phi and the error estimate to lz.
-// ---------------------------------------------------------------------------
+// EvaluateExpInSubspace: phi = exp(-i dt T_m) e1 for the m x m Lanczos
+// tridiagonal T_m and the error estimate beta_m |phi_m|.  The reference
+// diagonalises T_m (DSYEV) and forms U exp(-i dt L) U^T e1; the same vector is
+// computed here without an eigensolver, by the Chebyshev (Jacobi-Anger)
+// expansion of the exponential (Tal-Ezer & Kosloff, J. Chem. Phys. 81, 3967 (1984)):
+//   T' = (T - c)/R with spectrum in [-1, 1] (Gershgorin bounds),
+//   exp(-i z x) = J_0(z) + 2 sum_k (-i)^k J_k(z) T_k(x),  z = dt R,
+//   phi = exp(-i dt c) sum_k a_k q_k,  q_0 = e1, q_1 = T' e1, q_{k+1} = 2 T' q_k - q_{k-1}.
+// The Bessel values J_k(z) come from Miller's backward recurrence normalised
+// by J_0 + 2 sum J_2k = 1.  The series is summed until the coefficients fall
+// below 1e-17 relative, i.e. to machine precision.  One warp, lane i = row i (m <= 32).
 __global__ void k_lz_expsub(double* __restrict__ lz, int mFixed, double dt, double tol) {
-  __shared__ double A[32][33];
-  __shared__ double U[32][33];
-  __shared__ double rc[16], rs[16];
-  __shared__ int rp[16], rq[16];
+  constexpr int KMAX = 1200;
+  __shared__ double J[KMAX + 2];
+  __shared__ int nTerms;
   int lane = threadIdx.x;
   int m = mFixed > 0 ? mFixed : (int)lz[LZ_MDIM];
   if (m > 32) m = 32;
-  for (int i = 0; i < 32; i++) {
-    A[i][lane] = 0.0;
-    U[i][lane] = (i == lane) ? 1.0 : 0.0;
+  if (m < 1) return;
+  double a = (lane < m) ? lz[LZ_ALPHA + lane] : 0.0;
+  double bl = (lane >= 1 && lane < m) ? lz[LZ_BETA + lane - 1] : 0.0;  // beta_{i-1}: couples i-1, i
+  double br = (lane + 1 < m) ? lz[LZ_BETA + lane] : 0.0;               // beta_i:   couples i, i+1
+  double lo = (lane < m) ? a - fabs(bl) - fabs(br) : 1e300;
+  double hi = (lane < m) ? a + fabs(bl) + fabs(br) : -1e300;
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  double c = 0.5 * (hi + lo);
+  double R = 0.5 * (hi - lo);
+  R = R * (1.0 + 1e-12) + 1e-300;
+  double z = fabs(dt) * R;
+  double sgn = dt >= 0.0 ? 1.0 : -1.0;  // exp(-i dt T) with dt < 0 is the complex conjugate series
+  if (lane == 0) {
+    int K = (int)(1.5 * z + 40.0);
+    if (K > KMAX - 20) K = KMAX - 20;
+    if (z < 1e-300) {
+      J[0] = 1.0;
+      for (int k = 1; k <= K; k++) J[k] = 0.0;
+    } else {
+      int N = K + 20;
+      double jp = 0.0, jc = 1e-280, norm = 0.0;
+      for (int k = N; k >= 1; k--) {
+        double jm = (2.0 * k / z) * jc - jp;  // J_{k-1}
+        jp = jc;
+        jc = jm;
+        if (k - 1 <= K) J[k - 1] = jc;
+        if (k - 1 >= 1 && ((k - 1) & 1) == 0) norm += 2.0 * jc;
+        if (fabs(jc) > 1e250) {  // rescale to keep the recurrence finite
+          double s = 1e-250;
+          jc *= s;
+          jp *= s;
+          norm *= s;
+          for (int q = k - 1; q <= K && q <= N; q++) J[q] *= s;
+        }
+      }
+      norm += jc;  // J_0
+      for (int k = 0; k <= K; k++) J[k] /= norm;
+    }
+    int n = K;  // |J_k(z)| <= 1, so an absolute cut-off is relative to the largest term
+    while (n > 1 && fabs(J[n]) < 1e-18 && n > z) n--;
+    nTerms = n;
   }
   __syncwarp();
-  if (lane < m) {
-    A[lane][lane] = lz[LZ_ALPHA + lane];
-    if (lane + 1 < m) {
-      A[lane][lane + 1] = lz[LZ_BETA + lane];
-      A[lane + 1][lane] = lz[LZ_BETA + lane];
+  int K = nTerms;
+  double inv = 1.0 / R;
+  double ta = (a - c) * inv, tl = bl * inv, tr = br * inv;
+  // q_0 = e1, q_1 = T' e1
+  double qm = (lane == 0) ? 1.0 : 0.0;
+  double qlm = __shfl_up_sync(0xffffffffu, qm, 1);
+  double qrm = __shfl_down_sync(0xffffffffu, qm, 1);
+  double q = ta * qm + tl * (lane >= 1 ? qlm : 0.0) + tr * (lane + 1 < m ? qrm : 0.0);
+  if (lane >= m) q = 0.0;
+  double pr = J[0] * qm, pi = 0.0;
+  // a_k = 2 (-i)^k J_k: k = 1 -> -2i J_1
+  pi += -2.0 * J[1] * q;
+  for (int k = 2; k <= K; k++) {
+    double ql = __shfl_up_sync(0xffffffffu, q, 1);
+    double qr = __shfl_down_sync(0xffffffffu, q, 1);
+    double qn = 2.0 * (ta * q + tl * (lane >= 1 ? ql : 0.0) + tr * (lane + 1 < m ? qr : 0.0)) - qm;
+    if (lane >= m) qn = 0.0;
+    qm = q;
+    q = qn;
+    double co = 2.0 * J[k];
+    switch (k & 3) {
+      case 0: pr += co * q; break;   // (-i)^k = 1
+      case 1: pi -= co * q; break;   // -i
+      case 2: pr -= co * q; break;   // -1
+      default: pi += co * q; break;  // +i
     }
   }
-  __syncwarp();
-  int ne = (m + 1) & ~1;
-  int half = ne / 2;
-  for (int sweep = 0; sweep < 30 && m > 1; sweep++) {
-    double off = 0.0, dg = 0.0;
-    if (lane < m)
-      for (int i = 0; i < m; i++) {
-        double a = A[i][lane];
-        if (i == lane) dg += a * a; else off += a * a;
-      }
-    for (int o = 16; o > 0; o >>= 1) {
-      off += __shfl_xor_sync(0xffffffffu, off, o);
-      dg += __shfl_xor_sync(0xffffffffu, dg, o);
-    }
-    if (off <= 1e-28 * (dg + off) || off == 0.0) break;  // rounding floor is ~1e-32
-    for (int r = 0; r < ne - 1; r++) {
-      if (lane < half) {
-        auto pos = [&](int i) { return i == 0 ? 0 : ((i - 1 + r) % (ne - 1)) + 1; };
-        int p = pos(lane), q = pos(ne - 1 - lane);
-        if (p > q) { int t = p; p = q; q = t; }
-        double c = 1.0, s = 0.0;
-        if (q < m) {
-          double g = A[p][q];
-          if (g != 0.0) {
-            double tau = (A[q][q] - A[p][p]) / (2.0 * g);
-            double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-            c = 1.0 / sqrt(1.0 + t * t);
-            s = t * c;
-          }
-        } else {
-          q = -1;
-        }
-        rp[lane] = p;
-        rq[lane] = q;
-        rc[lane] = c;
-        rs[lane] = s;
-      }
-      __syncwarp();
-      if (lane < m)
-        for (int k = 0; k < half; k++) {
-          int p = rp[k], q = rq[k];
-          if (q < 0 || rs[k] == 0.0) continue;
-          double c = rc[k], s = rs[k];
-          double akp = A[lane][p], akq = A[lane][q];
-          A[lane][p] = akp * c - akq * s;
-          A[lane][q] = akp * s + akq * c;
-          double vkp = U[lane][p], vkq = U[lane][q];
-          U[lane][p] = vkp * c - vkq * s;
-          U[lane][q] = vkp * s + vkq * c;
-        }
-      __syncwarp();
-      if (lane < m)
-        for (int k = 0; k < half; k++) {
-          int p = rp[k], q = rq[k];
-          if (q < 0 || rs[k] == 0.0) continue;
-          double c = rc[k], s = rs[k];
-          double apk = A[p][lane], aqk = A[q][lane];
-          A[p][lane] = c * apk - s * aqk;
-          A[q][lane] = s * apk + c * aqk;
-        }
-      __syncwarp();
-      if (lane < half) {
-        int p = rp[lane], q = rq[lane];
-        if (q >= 0 && rs[lane] != 0.0) {
-          A[p][q] = 0.0;
-          A[q][p] = 0.0;
-        }
-      }
-      __syncwarp();
-    }
-  }
-  // phi_i = sum_j U(i,j) U(0,j) exp(-i dt lambda_j)
+  pi *= sgn;
+  // phase exp(-i dt c)
+  double sn, cs;
+  sincos(dt * c, &sn, &cs);
+  double fr = cs * pr + sn * pi;
+  double fi = cs * pi - sn * pr;
   if (lane < m) {
-    double pr = 0.0, pi = 0.0;
-    for (int j = 0; j < m; j++) {
-      double lam = A[j][j];
-      double sn, cs;
-      sincos(dt * lam, &sn, &cs);
-      double coef = U[0][j];
-      pr += U[lane][j] * coef * cs;
-      pi -= U[lane][j] * coef * sn;
-    }
-    lz[LZ_PHI + 2 * lane] = pr;
-    lz[LZ_PHI + 2 * lane + 1] = pi;
-    if (lane == m - 1) {
-      double err = lz[LZ_BETA + m - 1] * sqrt(pr * pr + pi * pi);
-      if (lz[LZ_BREAKJ] == (double)m) err = 0.0;
-      lz[LZ_ERR] = err;
-      (void)tol;
-    }
+    lz[LZ_PHI + 2 * lane] = fr;
+    lz[LZ_PHI + 2 * lane + 1] = fi;
+  }
+  if (lane == m - 1) {
+    double err = lz[LZ_BETA + m - 1] * sqrt(fr * fr + fi * fi);
+    if (lz[LZ_BREAKJ] == (double)m) err = 0.0;
+    lz[LZ_ERR] = err;
+    (void)tol;
   }
 }
+
 
 // out = nrm * sum_{j < mDim} phi_j V_j   (or out = in when the start vector had zero norm)
 __global__ void k_lz_combine(z_t* __restrict__ out, const z_t* __restrict__ in, const z_t* __restrict__ V,
@@ -337,14 +320,9 @@ __global__ void k_lz_combine(z_t* __restrict__ out, const z_t* __restrict__ in, 
 // nrm = sqrt(<s,s>_m); v1 = s / nrm; resets the per-step flags.
 __global__ void k_lz_start(z_t* __restrict__ v1, const z_t* __restrict__ s, const z_t* __restrict__ partIn, int nBlkIn,
                            size_t n, double* __restrict__ lz, double zeroThr) {
-  __shared__ double nrm;
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int b = 0; b < nBlkIn; b++) t += partIn[b].x;
-    nrm = sqrt(t);
-  }
-  __syncthreads();
-  double nr = nrm;
+  __shared__ z_t tot[1];
+  sum_partials(partIn, nBlkIn, 1, 1, tot);
+  double nr = sqrt(tot[0].x);
   bool zero = nr <= zeroThr;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     lz[LZ_NRM] = nr;

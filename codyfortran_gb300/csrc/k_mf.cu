@@ -200,15 +200,24 @@ __global__ void k_split_reduce(z_t* __restrict__ C, const z_t* __restrict__ P, i
 // ---------------------------------------------------------------------------
 constexpr int JB_MAX = 32;
 
+// The eigenvectors of the previous call (Uprev, column-major n x n, identity
+// at start) precondition the problem: Jacobi runs on Uprev^H rho Uprev, which
+// is nearly diagonal between consecutive evaluations, so it converges in a few
+// sweeps; Uprev V is stored for the next call.  Uprev is re-orthonormalised
+// (one modified Gram-Schmidt pass) on load so rounding cannot accumulate.
+// The result Mreg = U f(n) U^H depends only on rho (to rounding).
 __global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t* __restrict__ r1s,
-                                                     const z_t* __restrict__ rdm1, int nO, int n, int restricted,
-                                                     double reg) {
-  __shared__ z_t A[JB_MAX][JB_MAX + 1];
-  __shared__ z_t V[JB_MAX][JB_MAX + 1];
-  __shared__ double rc[JB_MAX / 2], rs[JB_MAX / 2];
+                                                     const z_t* __restrict__ rdm1, z_t* __restrict__ Uprev, int nO,
+                                                     int n, int restricted, double reg) {
+  extern __shared__ z_t jsm[];
+  z_t(*A)[JB_MAX + 1] = reinterpret_cast<z_t(*)[JB_MAX + 1]>(jsm);
+  z_t(*V)[JB_MAX + 1] = reinterpret_cast<z_t(*)[JB_MAX + 1]>(jsm + JB_MAX * (JB_MAX + 1));
+  z_t(*U)[JB_MAX + 1] = reinterpret_cast<z_t(*)[JB_MAX + 1]>(jsm + 2 * JB_MAX * (JB_MAX + 1));
+  __shared__ double rc[JB_MAX / 2], rs[JB_MAX / 2], ev[JB_MAX];
   __shared__ z_t rph[JB_MAX / 2];
   __shared__ int rp[JB_MAX / 2], rq[JB_MAX / 2];
   __shared__ double offs, diags;
+  __shared__ z_t red[JB_MAX];
   int tid = threadIdx.x;
   for (int e = tid; e < n * n; e += blockDim.x) {
     int i = e % n, j = e / n;
@@ -216,10 +225,58 @@ __global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t
     if (restricted) v = zadd(v, rdm1[(n + i) + (size_t)nO * (n + j)]);
     A[i][j] = v;
     r1s[e] = v;
-    V[i][j] = zmk(i == j ? 1.0 : 0.0, 0.0);
+    U[i][j] = Uprev[i + (size_t)n * j];
   }
   __syncthreads();
   for (int e = tid; e < n; e += blockDim.x) A[e][e].y = 0.0;
+  // modified Gram-Schmidt on the columns of U
+  for (int j = 0; j < n; j++) {
+    for (int i = 0; i < j; i++) {
+      if (tid < 32) {
+        z_t s = zmk(0.0, 0.0);
+        for (int r = tid; r < n; r += 32) s = zadd(s, zcmul(U[r][i], U[r][j]));
+        for (int o = 16; o > 0; o >>= 1) {
+          s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+          s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+        }
+        if (tid == 0) red[0] = s;
+      }
+      __syncthreads();
+      z_t ov = red[0];
+      if (tid < n) U[tid][j] = zsub(U[tid][j], zmul(U[tid][i], ov));
+      __syncthreads();
+    }
+    if (tid < 32) {
+      double s = 0.0;
+      for (int r = tid; r < n; r += 32) s += U[r][j].x * U[r][j].x + U[r][j].y * U[r][j].y;
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (tid == 0) red[0] = zmk(s, 0.0);
+    }
+    __syncthreads();
+    double inv = 1.0 / sqrt(red[0].x);
+    if (tid < n) U[tid][j] = zscale(U[tid][j], inv);
+    __syncthreads();
+  }
+  // A <- U^H A U  (V as temporary), then V <- I
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    int i = e % n, j = e / n;
+    z_t s = zmk(0.0, 0.0);
+    for (int k = 0; k < n; k++) zfma(s, A[i][k], U[k][j]);
+    V[i][j] = s;
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    int i = e % n, j = e / n;
+    z_t s = zmk(0.0, 0.0);
+    for (int k = 0; k < n; k++) s = zadd(s, zcmul(U[k][i], V[k][j]));
+    A[i][j] = s;
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    int i = e % n, j = e / n;
+    V[i][j] = zmk(i == j ? 1.0 : 0.0, 0.0);
+    if (i == j) A[i][i].y = 0.0;
+  }
   __syncthreads();
   int ne = (n + 1) & ~1;
   int half = ne / 2;
@@ -303,14 +360,25 @@ __global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t
       __syncthreads();
     }
   }
+  // eigenvalues, eigenvectors U_new = U V (into A), stored for the next call
+  for (int e = tid; e < n; e += blockDim.x) ev[e] = A[e][e].x;
+  __syncthreads();
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    int i = e % n, j = e / n;
+    z_t s = zmk(0.0, 0.0);
+    for (int k = 0; k < n; k++) zfma(s, U[i][k], V[k][j]);
+    A[i][j] = s;
+    Uprev[i + (size_t)n * j] = s;
+  }
+  __syncthreads();
   // Mreg(k1,j1) = sum_j U(k1,j) n_j/(n_j^2+reg) conj(U(j1,j))
   for (int e = tid; e < n * n; e += blockDim.x) {
     int k1 = e % n, j1 = e / n;
     z_t acc = zmk(0.0, 0.0);
     for (int j = 0; j < n; j++) {
-      double occ = A[j][j].x;
+      double occ = ev[j];
       double f = occ / (occ * occ + reg);
-      zfma(acc, zscale(V[k1][j], f), zconj(V[j1][j]));
+      zfma(acc, zscale(A[k1][j], f), zconj(A[j1][j]));
     }
     Mreg[e] = acc;
   }
@@ -407,7 +475,14 @@ static void h2_from_pairs(cgpu_ctx* c) {
 void launch_rdm_inverse(cgpu_ctx* c) {
   int n = c->nOS;
   if (n > JB_MAX) throw std::string("ApplyCorrelationOp: more than 32 stored orbitals is not supported");
-  k_rdm_inverse<<<1, 512, 0, c->stream>>>(c->Mreg_d, c->r1s_d, c->rdm1_d, c->nO, n, c->restricted, c->regEps);
+  constexpr size_t jsmem = 3 * sizeof(z_t) * JB_MAX * (JB_MAX + 1);
+  static bool attr = false;
+  if (!attr) {
+    CODY_CUDA(cudaFuncSetAttribute(k_rdm_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jsmem));
+    attr = true;
+  }
+  k_rdm_inverse<<<1, 512, jsmem, c->stream>>>(c->Mreg_d, c->r1s_d, c->rdm1_d, c->Uprev_d, c->nO, n, c->restricted,
+                                              c->regEps);
   CODY_LAUNCHED(c);
   size_t Q = (size_t)n * n;
   k_build_R<<<(int)((Q * Q + 255) / 256), 256, 0, c->stream>>>(c->Rp_d, c->rdm2_d, c->Mreg_d, c->btOfOrb_d, c->nO, n,

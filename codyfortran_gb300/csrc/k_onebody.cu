@@ -24,10 +24,35 @@ constexpr int RED_BLOCKS = 148;  // partial-sum blocks for grid reductions
 // multiplies orbs[g+d].  One CTA covers OB_THREADS grid points of one orbital;
 // the tile and its halo are staged in shared memory.
 // ---------------------------------------------------------------------------
+// Laser field E(t): sin^2 pulse (pattern of src/SysPotential/Ylm/CoulombLaser/
+// S_SysPotential_Ylm_CoulombLaser.f90:60-83) or piecewise-constant samples.
+__device__ double field_amplitude_dev(const LaserDev& L, double t) {
+  if (L.kind == CGPU_LASER_SIN2) {
+    if (L.omega <= 0.0) return 0.0;
+    const double PI = 3.14159265358979323846264338327950288;
+    double duration = 2.0 * PI * L.nCycles / L.omega;
+    double tRel = t - L.tStart;
+    if (tRel < 0.0 || tRel > duration) return 0.0;
+    double env = sin(PI * tRel / duration);
+    env = env * env;
+    return L.E0 * env * cos(L.omega * (tRel - 0.5 * duration) + L.cep);
+  }
+  if (L.kind == CGPU_LASER_SAMPLED) {
+    double u = (t - L.sampleT0) / L.sampleDt;
+    long n = (long)floor(u + 1e-9);
+    if (n < 0 || n >= L.nSamples) return 0.0;
+    return L.samples[n];
+  }
+  return 0.0;
+}
+
 __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, const double* __restrict__ T,
                           const double* __restrict__ V0, const double* __restrict__ x, const int* __restrict__ btOf,
-                          int nG, int band, int restricted, double E, int hasPot, z_t alpha, int accumulate) {
+                          int nG, int band, int restricted, LaserDev laser, const double* __restrict__ tBase,
+                          double tOff, int hasPot, z_t alpha, int accumulate) {
   extern __shared__ z_t sh[];
+  __shared__ double Eshared;
+  if (threadIdx.x == 0) Eshared = field_amplitude_dev(laser, *tBase + tOff);
   int i = blockIdx.y;
   int g0 = blockIdx.x * OB_THREADS;
   const z_t* f = orbs + (size_t)nG * i;
@@ -50,7 +75,7 @@ __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, c
     acc.y = fma(c, v.y, acc.y);
   }
   if (hasPot) {
-    double pot = V0[g] + E * x[g];
+    double pot = V0[g] + Eshared * x[g];
     z_t v = sh[threadIdx.x + band];
     acc.x = fma(pot, v.x, acc.x);
     acc.y = fma(pot, v.y, acc.y);
@@ -113,15 +138,23 @@ __global__ void k_gram_partial(z_t* __restrict__ part, const z_t* __restrict__ A
   }
 }
 
+// one warp per Gram entry, lanes over the block partials (fixed order)
 __global__ void k_gram_final(z_t* __restrict__ G, const z_t* __restrict__ part, int nBlk, int n, int ldG,
                              double scale) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
   int nn = n * n;
   if (e >= nn) return;
   z_t s = zmk(0.0, 0.0);
-  for (int b = 0; b < nBlk; b++) s = zadd(s, part[(size_t)b * nn + e]);
-  int i = e % n, j = e / n;
-  G[i + (size_t)ldG * j] = zscale(s, scale);
+  for (int b = lane; b < nBlk; b += 32) s = zadd(s, part[(size_t)b * nn + e]);
+  for (int o = 16; o > 0; o >>= 1) {
+    s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+    s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+  }
+  if (lane == 0) {
+    int i = e % n, j = e / n;
+    G[i + (size_t)ldG * j] = zscale(s, scale);
+  }
 }
 
 // dOrbs[:, c0+j] -= sum_i orbs[:, c0+i] * G[i + n*j]
@@ -216,14 +249,9 @@ __global__ void k_dot_partial(z_t* __restrict__ part, const z_t* __restrict__ a,
 // dC -= (sum of partials) * C   (dot_product(coeffs, dCoeffs) = sum conj(C) dC)
 __global__ void k_project_coeffs_apply(z_t* __restrict__ dC, const z_t* __restrict__ C, const z_t* __restrict__ part,
                                        int nBlk, size_t n) {
-  __shared__ z_t ov;
-  if (threadIdx.x == 0) {
-    z_t s = zmk(0.0, 0.0);
-    for (int b = 0; b < nBlk; b++) s = zadd(s, part[b]);
-    ov = s;
-  }
-  __syncthreads();
-  z_t o = ov;
+  __shared__ z_t ov[1];
+  sum_partials(part, nBlk, 1, 1, ov);
+  z_t o = ov[0];
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     z_t r = dC[i];
     z_t c = C[i];
@@ -234,14 +262,9 @@ __global__ void k_project_coeffs_apply(z_t* __restrict__ dC, const z_t* __restri
 }
 
 __global__ void k_normalize_apply(z_t* __restrict__ C, const z_t* __restrict__ part, int nBlk, size_t n) {
-  __shared__ double inv;
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int b = 0; b < nBlk; b++) s += part[b].x;
-    inv = sqrt(s);
-  }
-  __syncthreads();
-  double nr = inv;
+  __shared__ z_t tot[1];
+  sum_partials(part, nBlk, 1, 1, tot);
+  double nr = sqrt(tot[0].x);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     z_t c = C[i];
     C[i] = zmk(c.x / nr, c.y / nr);
@@ -351,12 +374,13 @@ double cody_field_amplitude(const cgpu_ctx* c, double t) {
 
 void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha, int accumulate) {
   ProfScope prof(c, CGPU_KERNEL_ONEBODY);
-  double E = cody_field_amplitude(c, t);
   int hasPot = c->hasPotential || c->laserKind != CGPU_LASER_NONE;
   dim3 grid((c->nG + OB_THREADS - 1) / OB_THREADS, c->nOS);
   size_t sh = sizeof(z_t) * (OB_THREADS + 2 * c->band);
+  const double* base = c->inCapture ? c->stepT_d : c->zero_d;
+  double off = c->inCapture ? t - c->captureT0 : t;
   k_onebody<<<grid, OB_THREADS, sh, c->stream>>>(out, orbs, c->T_d, c->V0_d, c->x_d, c->btOfOrb_d, c->nG, c->band,
-                                                 c->restricted, E, hasPot, alpha, accumulate);
+                                                 c->restricted, c->laserDev, base, off, hasPot, alpha, accumulate);
   CODY_LAUNCHED(c);
 }
 
@@ -369,7 +393,7 @@ void launch_gram(cgpu_ctx* c, z_t* G, const z_t* A, const z_t* B, int n, int col
   if (n * n > GR_PER_THREAD * threads) throw std::string("launch_gram: more than 64 orbitals");
   k_gram_partial<<<nBlk, threads, sh, c->stream>>>(c->partial_d, A, B, c->w_d, c->nG, n, colA0, colB0, chunk);
   CODY_LAUNCHED(c);
-  k_gram_final<<<(n * n + 127) / 128, 128, 0, c->stream>>>(G, c->partial_d, nBlk, n, ldG, scale);
+  k_gram_final<<<(n * n * 32 + 255) / 256, 256, 0, c->stream>>>(G, c->partial_d, nBlk, n, ldG, scale);
   CODY_LAUNCHED(c);
 }
 

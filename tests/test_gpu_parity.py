@@ -194,6 +194,10 @@ def test_resident_propagation_matches_host_api(pair):
     e.upload(st)
     e.propagate_resident(0.0, dt, 2, 10, use_metric=True)
     assert rel(e.download(), a) < 1e-14
+    # one captured step replayed as a CUDA graph
+    e.upload(st)
+    e.propagate_resident(0.0, dt, 2, 10, use_metric=True, use_graph=True)
+    assert rel(e.download(), a) < 1e-13
 
 
 # ---------------------------------------------------------------------------
