@@ -165,6 +165,7 @@ struct cgpu_ctx {
   // stream / graph
   cudaStream_t stream = nullptr;
   cudaGraphExec_t stepGraph = nullptr;
+  cudaGraph_t stepGraphRaw = nullptr;
   double graphDt = 0;
   int graphKrylov = 0, graphMetric = -1, graphKernels = 0, graphProf = 0;
   size_t graphProfUsed = 0;

@@ -177,6 +177,15 @@ double soft_kernel(double s, double s1, double s2, double damp, double dist) {
   return s * std::exp(-dist * damp) / (std::sqrt(dist * dist + s1 * s1) + s2);
 }
 
+__global__ void k_build_vint(double* __restrict__ V, const double* __restrict__ x, int nG, int toeplitz, double dx,
+                             double s, double s1, double s2, double damp) {
+  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (e >= (size_t)nG * nG) return;
+  int i = (int)(e / nG), j = (int)(e % nG);
+  double dist = toeplitz ? (double)abs(i - j) * dx : fabs(x[i] - x[j]);
+  V[e] = s * exp(-dist * damp) / (sqrt(dist * dist + s1 * s1) + s2);
+}
+
 void build_ctx(cgpu_ctx* c, const cgpu_desc* d) {
   if (d->n_body_types < 1 || d->n_body_types > CODY_MAX_BT) throw std::string("method.mb.nBodyTypes out of range");
   c->nBt = d->n_body_types;
@@ -245,16 +254,14 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* d) {
   c->btOfOrb_d = dupload(c->btOfOrb);
   c->hasInteraction = d->has_interaction ? 1 : 0;
   if (c->hasInteraction) {
-    // interaction matrix V(x_i, x_j) (S_SysInteraction_Linear_SoftYukawa.f90:67-73)
-    std::vector<double> V((size_t)nG * nG);
+    // interaction matrix V(x_i, x_j) (S_SysInteraction_Linear_SoftYukawa.f90:67-73), built on the device
     double dx = nG > 1 ? c->x[1] - c->x[0] : 0.0;
-    for (int i = 0; i < nG; i++)
-      for (int j = 0; j < nG; j++) {
-        double dist = d->int_kind == CGPU_INT_TOEPLITZ ? (double)std::abs(i - j) * dx : std::fabs(c->x[i] - c->x[j]);
-        V[(size_t)i * nG + j] =
-            soft_kernel(d->int_strength, d->int_softening1, d->int_softening2, d->int_dampening, dist);
-      }
-    c->Vint_d = dupload(V);
+    c->Vint_d = dalloc<double>((size_t)nG * nG);
+    size_t tot = (size_t)nG * nG;
+    k_build_vint<<<(int)((tot + 255) / 256), 256, 0, c->stream>>>(
+        c->Vint_d, c->x_d, nG, d->int_kind == CGPU_INT_TOEPLITZ, dx, d->int_strength, d->int_softening1,
+        d->int_softening2, d->int_dampening);
+    CODY_LAUNCHED(c);
   }
   // pairs (l <= k, same body type) in the order of the reference's loops
   int n = c->nOS;
@@ -332,6 +339,7 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* d) {
 void free_ctx(cgpu_ctx* c) {
   mixed_free(c);
   if (c->stepGraph) cudaGraphExecDestroy(c->stepGraph);
+  if (c->stepGraphRaw) cudaGraphDestroy(c->stepGraphRaw);
   for (cudaEvent_t e : c->profEvents) cudaEventDestroy(e);
   void* ptrs[] = {c->x_d, c->w_d, c->V0_d, c->T_d, c->Vint_d, c->metricW_d, c->metricOne_d, c->metricUser_d, c->Vint_f,
                   c->btOfOrb_d, c->h1Lin_d, c->h2Lin_d, c->rdm1Lin_d, c->rdm2Lin_d, c->rdm1_d, c->rdm2_d, c->h1_d,
@@ -546,7 +554,8 @@ void capture_step_graph(cgpu_ctx* c, double t0, double dt, int krylov, int useMe
   c->graphKernels = (int)(c->launches - before);
   c->launches = before;
   cudaError_t e = cudaGraphInstantiate(&c->stepGraph, g, 0);
-  cudaGraphDestroy(g);
+  if (c->stepGraphRaw) cudaGraphDestroy(c->stepGraphRaw);
+  c->stepGraphRaw = g;  // kept: a batch embeds it as a child graph
   CODY_CUDA(e);
   c->graphDt = dt;
   c->graphKrylov = krylov;
@@ -1008,6 +1017,126 @@ int cgpu_tdci_set_orbitals(cgpu_ctx* c, const cgpu_complex* orbs) {
   launch_fold_h2(c);
   sync(c);
   CODY_API_END(c)
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched trajectories: one context per trajectory; the step graph of every
+// context is a child node (no dependencies between them) of one batch graph.
+// ---------------------------------------------------------------------------
+struct cgpu_batch {
+  std::vector<cgpu_ctx*> ctx;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  double dt = 0.0;
+  int krylov = -1, metric = -1;
+  long kernelsPerStep = 0;
+  std::vector<double> t0;  // start times the graph was last launched from
+};
+
+namespace {
+void batch_free_graph(cgpu_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  b->kernelsPerStep = 0;
+}
+
+void batch_build_graph(cgpu_batch* b, const double* t0, double dt, int krylov, int useMetric) {
+  batch_free_graph(b);
+  CODY_CUDA(cudaGraphCreate(&b->graph, 0));
+  for (size_t i = 0; i < b->ctx.size(); i++) {
+    cgpu_ctx* c = b->ctx[i];
+    c->profTarget = 0;
+    capture_step_graph(c, t0[i], dt, krylov, useMetric);
+    cudaGraphNode_t node;
+    CODY_CUDA(cudaGraphAddChildGraphNode(&node, b->graph, nullptr, 0, c->stepGraphRaw));
+    b->kernelsPerStep += c->graphKernels;
+  }
+  CODY_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  b->dt = dt;
+  b->krylov = krylov;
+  b->metric = useMetric;
+}
+}  // namespace
+
+#define CODY_BATCH_BEGIN(b)                                          \
+  if (!(b)) return fail(nullptr, "null batch", CGPU_ERR_ARG);        \
+  try {
+
+extern "C" {
+
+int cgpu_batch_create(const cgpu_desc* descs, int n, cgpu_batch** out) {
+  if (!descs || !out || n <= 0) return fail(nullptr, "cgpu_batch_create: bad argument", CGPU_ERR_ARG);
+  *out = nullptr;
+  cgpu_batch* b = new cgpu_batch();
+  for (int i = 0; i < n; i++) {
+    cgpu_ctx* c = nullptr;
+    int rc = cgpu_ctx_create(&descs[i], &c);
+    if (rc != CGPU_OK) {
+      std::string msg = "batch trajectory " + std::to_string(i) + ": " + g_lastGlobalError;
+      cgpu_batch_destroy(b);
+      return fail(nullptr, msg, rc);
+    }
+    b->ctx.push_back(c);
+  }
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cgpu_batch_destroy(b);
+    return fail(nullptr, "cuda: batch stream creation failed", CGPU_ERR_CUDA);
+  }
+  *out = b;
+  return CGPU_OK;
+}
+
+int cgpu_batch_destroy(cgpu_batch* b) {
+  if (!b) return CGPU_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  batch_free_graph(b);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  for (cgpu_ctx* c : b->ctx) cgpu_ctx_destroy(c);
+  delete b;
+  return CGPU_OK;
+}
+
+int cgpu_batch_size(const cgpu_batch* b) { return b ? (int)b->ctx.size() : 0; }
+
+cgpu_ctx* cgpu_batch_context(cgpu_batch* b, int i) {
+  if (!b || i < 0 || i >= (int)b->ctx.size()) return nullptr;
+  return b->ctx[i];
+}
+
+long cgpu_batch_kernels_per_step(const cgpu_batch* b) { return b ? b->kernelsPerStep : 0; }
+
+int cgpu_batch_propagate(cgpu_batch* b, const double* t0, double dt, int n_steps, int krylov_dim, int use_metric,
+                         double* elapsed_ms) {
+  CODY_BATCH_BEGIN(b)
+  if (!t0 || n_steps < 0 || krylov_dim <= 0) throw std::string("batch_propagate: bad argument");
+  // uploads and other work queued on the contexts' own streams come first
+  for (cgpu_ctx* c : b->ctx) CODY_CUDA(cudaStreamSynchronize(c->stream));
+  if (!b->exec || b->dt != dt || b->krylov != krylov_dim || b->metric != use_metric)
+    batch_build_graph(b, t0, dt, krylov_dim, use_metric);
+  for (size_t i = 0; i < b->ctx.size(); i++)
+    CODY_CUDA(cudaMemcpyAsync(b->ctx[i]->stepT_d, &t0[i], sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  cudaEvent_t e0, e1;
+  CODY_CUDA(cudaEventCreate(&e0));
+  CODY_CUDA(cudaEventCreate(&e1));
+  CODY_CUDA(cudaEventRecord(e0, b->stream));
+  for (int s = 0; s < n_steps; s++) CODY_CUDA(cudaGraphLaunch(b->exec, b->stream));
+  CODY_CUDA(cudaEventRecord(e1, b->stream));
+  CODY_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  CODY_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (elapsed_ms) *elapsed_ms = ms;
+  for (cgpu_ctx* c : b->ctx) {
+    c->launches += n_steps * c->graphKernels;
+    if (c->mixed && mixed_error(c)) throw std::string("tensor-core GEMM: a bounded mbarrier wait expired");
+  }
+  CODY_API_END(nullptr)
 }
 
 }  // extern "C"

@@ -32,6 +32,8 @@ EXPORTED = [
     "cgpu_integrate_sil", "cgpu_propagate_split2", "cgpu_state_upload", "cgpu_state_download",
     "cgpu_propagate_resident", "cgpu_energy_resident", "cgpu_tdci_set_orbitals", "cgpu_propagate_resident_timed",
     "cgpu_profile_begin", "cgpu_profile_end", "cgpu_weighted_gram_noalloc",
+    "cgpu_batch_create", "cgpu_batch_destroy", "cgpu_batch_size", "cgpu_batch_context", "cgpu_batch_propagate",
+    "cgpu_batch_kernels_per_step",
 ]
 
 KERNELS = {"pair_potentials": 1, "correlation": 2, "h2": 3, "ci_apply": 4, "ci_rdm": 5, "onebody": 6, "lanczos": 7}
@@ -77,6 +79,11 @@ def load_library(path: str = LIB_PATH):
     lib.cgpu_launch_count.restype = C.c_long
     lib.cgpu_launch_count.argtypes = [C.c_void_p, C.c_int]
     lib.cgpu_ctx_create.argtypes = [C.POINTER(CgpuDesc), C.POINTER(C.c_void_p)]
+    lib.cgpu_batch_create.argtypes = [C.POINTER(CgpuDesc), C.c_int, C.POINTER(C.c_void_p)]
+    lib.cgpu_batch_context.restype = C.c_void_p
+    lib.cgpu_batch_context.argtypes = [C.c_void_p, C.c_int]
+    lib.cgpu_batch_kernels_per_step.restype = C.c_long
+    lib.cgpu_batch_kernels_per_step.argtypes = [C.c_void_p]
     _lib = lib
     return lib
 
@@ -137,6 +144,18 @@ class Engine:
         if rc != 0:
             raise CodyError(self.lib.cgpu_last_global_error().decode())
         self.h = h
+        self._owned = True
+        self._query_sizes()
+
+    @classmethod
+    def _wrap(cls, spec: SystemSpec, handle):
+        """A non-owning Engine over a context that a Batch holds."""
+        e = cls.__new__(cls)
+        e.lib, e.spec, e._keep, e.h, e._owned = load_library(), spec, None, C.c_void_p(handle), False
+        e._query_sizes()
+        return e
+
+    def _query_sizes(self):
         sz = (C.c_int * 6)()
         self.lib.cgpu_sizes(self.h, sz)
         self.nG, self.nO, self.nOS, self.nC, self.nBt, self.nS = list(sz)
@@ -146,7 +165,8 @@ class Engine:
 
     def close(self):
         if getattr(self, "h", None):
-            self.lib.cgpu_ctx_destroy(self.h)
+            if getattr(self, "_owned", True):
+                self.lib.cgpu_ctx_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -353,3 +373,63 @@ class Engine:
     def tdci_set_orbitals(self, orbs):
         o = self._orbs(orbs)
         self._check(self.lib.cgpu_tdci_set_orbitals(self.h, _p(o)))
+
+
+class Batch:
+    """Independent trajectories of arbitrary sizes advanced together: one
+    cgpu_ctx per trajectory, one CUDA-graph launch per time step for the whole
+    batch (cgpu_batch_propagate)."""
+
+    def __init__(self, specs, precision: str = "fp64", max_krylov: int = 32):
+        self.lib = load_library()
+        self.specs = list(specs)
+        n = len(self.specs)
+        descs = (CgpuDesc * n)()
+        self._keep = []
+        for i, sp in enumerate(self.specs):
+            d, keep = make_desc(sp, precision, max_krylov)
+            descs[i] = d
+            self._keep.append(keep)
+        h = C.c_void_p()
+        rc = self.lib.cgpu_batch_create(descs, n, C.byref(h))
+        if rc != 0:
+            raise CodyError(self.lib.cgpu_last_global_error().decode())
+        self.h = h
+        self.engines = [Engine._wrap(sp, self.lib.cgpu_batch_context(self.h, i)) for i, sp in enumerate(self.specs)]
+
+    def __len__(self):
+        return len(self.engines)
+
+    def close(self):
+        if getattr(self, "h", None):
+            for e in self.engines:
+                e.close()
+            self.lib.cgpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, states):
+        for e, s in zip(self.engines, states):
+            e.upload(s)
+
+    def download(self):
+        return [e.download() for e in self.engines]
+
+    def propagate(self, t0, dt, n_steps, krylov_dim, use_metric=True):
+        """n_steps fixed-order Strang steps of every trajectory (start times t0,
+        scalar or one per trajectory); returns the device time in ms."""
+        t = np.broadcast_to(np.asarray(t0, dtype=np.float64), (len(self),)).copy()
+        ms = C.c_double()
+        rc = self.lib.cgpu_batch_propagate(self.h, _p(t), _d(dt), int(n_steps), int(krylov_dim), int(use_metric),
+                                           C.byref(ms))
+        if rc != 0:
+            raise CodyError(self.lib.cgpu_last_global_error().decode())
+        return ms.value
+
+    def kernels_per_step(self):
+        return self.lib.cgpu_batch_kernels_per_step(self.h)

@@ -208,6 +208,28 @@ int cgpu_profile_end(cgpu_ctx* ctx, long* launches, double* total_ms);
  * fix the orbitals and fill h1/h2 once. */
 int cgpu_tdci_set_orbitals(cgpu_ctx* ctx, const cgpu_complex* orbs);
 
+/* ---- batched trajectories ------------------------------------------------ */
+/* No counterpart in the reference, whose module-global state allows one
+ * trajectory per process (src/Method/M_Method.f90:47).  A batch holds n
+ * independent systems of any sizes (pulse scans, uneven grids and orbital
+ * counts), one context each.  cgpu_batch_propagate advances all of them
+ * together by one CUDA-graph launch per time step: each context's
+ * fixed-order Strang step (as cgpu_propagate_resident) is a child graph of
+ * the step graph, so the trajectories run concurrently across the GPU. */
+typedef struct cgpu_batch cgpu_batch;
+int cgpu_batch_create(const cgpu_desc* descs, int n, cgpu_batch** out);
+int cgpu_batch_destroy(cgpu_batch* batch);
+int cgpu_batch_size(const cgpu_batch* batch);
+/* The context of trajectory i: use cgpu_sizes / cgpu_grid / cgpu_state_upload /
+ * cgpu_state_download / cgpu_energy_resident on it. */
+cgpu_ctx* cgpu_batch_context(cgpu_batch* batch, int i);
+/* n_steps steps of size dt; trajectory i starts at t0[i].  *elapsed_ms (may be
+ * NULL) receives the device time from CUDA events around the launches. */
+int cgpu_batch_propagate(cgpu_batch* batch, const double* t0, double dt, int n_steps, int krylov_dim,
+                         int use_metric, double* elapsed_ms);
+/* Kernels launched per batch step (sum over the child graphs). */
+long cgpu_batch_kernels_per_step(const cgpu_batch* batch);
+
 /* ---- no-allocation variant ---------------------------------------------- */
 /* No counterpart in the reference.  Weighted Gram matrix of two orbital sets,
  *   gram(i,j) = sum_g conj(a[g + n_grid*i]) * b[g + n_grid*j] * weights[g],
