@@ -1,4 +1,11 @@
 // common.cuh -- shared types and kernel launchers of the GB300 MCTDHX/TDCI engine.
+//
+// A context holds nb >= 1 independent trajectories ("systems").  The device
+// buffers of trajectory b sit at byte offset b * bs from those of trajectory 0
+// (one arena, the same layout in every block, sized for the largest system),
+// every kernel takes its trajectory from blockIdx.z and its sizes from the
+// TrajShape table, so one launch advances all trajectories.  A plain context
+// is the case nb = 1.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -78,6 +85,14 @@ struct CiTables {
   int* dCode;
   int8_t* dFac;
   int* rankTab;        // (nBodies+1) x (nOrbs+1) additive rank table
+  // the same excitations grouped by orbital code (for the RDM gathers):
+  // code q has value xCode[q] and edges [xStart[q], xStart[q+1]) with
+  // source / target configuration (0-based) and sign
+  int nSc, nDc;        // distinct singles / doubles codes
+  int *sxCode, *sxStart, *sxSrc, *sxDst;
+  int8_t* sxFac;
+  int *dxCode, *dxStart, *dxSrc, *dxDst;
+  int8_t* dxFac;
 };
 
 // Device view of the CI layout for the traversal kernels.
@@ -94,9 +109,15 @@ struct CiView {
   const int* dExc[CODY_MAX_BT];
   const int* dCode[CODY_MAX_BT];
   const int8_t* dFac[CODY_MAX_BT];
+  // code-major excitation lists (CiTables::sx*, dx*)
+  int nSc[CODY_MAX_BT], nDc[CODY_MAX_BT];
+  const int *sxCode[CODY_MAX_BT], *sxStart[CODY_MAX_BT], *sxSrc[CODY_MAX_BT], *sxDst[CODY_MAX_BT];
+  const int8_t* sxFac[CODY_MAX_BT];
+  const int *dxCode[CODY_MAX_BT], *dxStart[CODY_MAX_BT], *dxSrc[CODY_MAX_BT], *dxDst[CODY_MAX_BT];
+  const int8_t* dxFac[CODY_MAX_BT];
 };
 
-struct MixedBufs;  // mixed-precision operand buffers (k_mixed.cu)
+struct MixedBufs;  // mixed-precision operand layout (k_mixed.cu)
 
 // Laser parameters as the device sees them (E(t) is evaluated in the kernels so
 // that a captured step can be replayed at any time).
@@ -107,50 +128,108 @@ struct LaserDev {
   const double* samples;
 };
 
-// ---------------------------------------------------------------------------
-// The context: one system, its device-resident operators, tables and work
-// buffers, and one CUDA stream.  Not reentrant (one host thread at a time),
-// like the reference's module-global state.
-// ---------------------------------------------------------------------------
-struct cgpu_ctx {
-  // sizes
-  int nG = 0, nBt = 0, nO = 0, nOS = 0, nC = 0, nS = 0, restricted = 0, method = 0, precision = 0;
-  int band = 0, nBtK = 1;
+// Sizes and parameters of one trajectory, as the kernels read them.
+struct TrajShape {
+  int nG, nOS, nO, nC, nS, nGO, nPairs, band, restricted, hasPot, nBt;
+  int nCpad;                 // offset of the orbitals in a state vector (the context's largest nC)
+  int nGroups;               // (1-P) projector groups: one when restricted, else one per body type
+  int grpStart[CODY_MAX_BT], grpSize[CODY_MAX_BT];
+  int Kg, Kp;                // mixed form: K of the grid / pair contractions padded to 64
+  double regEps;
+  LaserDev laser;
+  CiView view;
+};
+
+// Pointer p of trajectory 0 moved to the trajectory of this block.
+template <class T>
+__device__ __forceinline__ T* bat(T* p, size_t bs) {
+  return p ? (T*)((char*)p + (size_t)blockIdx.z * bs) : p;
+}
+
+// Pointer p of trajectory b (for kernels that fold more than the trajectory into blockIdx.z).
+template <class T>
+__device__ __forceinline__ T* batn(T* p, size_t bs, int b) {
+  return p ? (T*)((char*)p + (size_t)b * bs) : p;
+}
+
+// A state vector is [C (nC) | unused up to nCpad | orbitals (nG x nOS)]; the
+// vector kernels walk its nS = nC + nG nOS entries through these maps.
+enum { VSEL_STATE = 0, VSEL_COEFFS = 1 };
+__device__ __forceinline__ size_t vlen(const TrajShape& S, int sel) {
+  return sel == VSEL_STATE ? (size_t)S.nS : (size_t)S.nC;
+}
+__device__ __forceinline__ size_t vidx(const TrajShape& S, size_t i) {
+  return i < (size_t)S.nC ? i : i + (size_t)(S.nCpad - S.nC);
+}
+
+// Host-side data of one system (grid, operators, tables).
+struct SysHost {
+  int nG = 0, nO = 0, nOS = 0, nC = 0, nS = 0, nPairs = 0, band = 0, nBtK = 1;
   int nBodies[CODY_MAX_BT] = {0}, nOrbs[CODY_MAX_BT] = {0}, orbStart[CODY_MAX_BT] = {0};
   double mass[CODY_MAX_BT] = {0};
   double regEps = 1e-10;
-  int hasPotential = 0, hasInteraction = 0;
-  // laser
+  int hasPotential = 0;
   int laserKind = 0;
   double E0 = 0, omega = 0, nCycles = 0, cep = 0, tStart = 0, sampleDt = 1, sampleT0 = 0;
   std::vector<double> samples;
-  // host copies
+  double* samples_d = nullptr;
   std::vector<double> x, w, V0, band_h;
-  std::vector<int> btOfOrb;
-  // device operators
+  std::vector<int> btOfOrb, pl, pk, pidx;
+  int intToeplitz = 0;
+  double intS = 0, intS1 = 0, intS2 = 0, intDamp = 0;
+  CiTables tab[CODY_MAX_BT] = {};
+  CiView view = {};
+};
+
+// ---------------------------------------------------------------------------
+// The context: nb systems, their device-resident operators, tables and work
+// buffers, and one CUDA stream.  Not reentrant (one host thread at a time),
+// like the reference's module-global state.  The size fields are the largest
+// over the systems (they size grids and buffers); kernels read the true sizes
+// of their trajectory from shape_d.
+// ---------------------------------------------------------------------------
+struct cgpu_ctx {
+  // batch
+  int nb = 1;
+  size_t bs = 0;                  // bytes between the buffers of consecutive trajectories
+  char* arena = nullptr;
+  std::vector<SysHost> sys;
+  std::vector<TrajShape> shape_h;
+  TrajShape* shape_d = nullptr;
+  // sizes (maxima over the systems; uniform: nBt, restricted, method, precision, hasInteraction)
+  int nG = 0, nBt = 0, nO = 0, nOS = 0, nC = 0, nS = 0, nGO = 0, restricted = 0, method = 0, precision = 0;
+  int band = 0, nBtK = 1, nPairs = 0;
+  int minS = 0;                   // smallest state size (bounds the Krylov order)
+  int ciTasks = 0;                // largest number of RDM gather tasks (warps) of a system
+  int hasInteraction = 0, anyLaser = 0;
+  // packed host states <-> the arena (batched upload / download)
+  std::vector<long> stageOff;     // prefix sums of the systems' state sizes
+  long* stageOff_d = nullptr;
+  z_t* stage_d = nullptr;
+  size_t stageCap = 0;
+  // device operators (trajectory 0; the others at multiples of bs)
   double *x_d = nullptr, *w_d = nullptr, *V0_d = nullptr, *T_d = nullptr, *Vint_d = nullptr, *metric_d = nullptr;
   double *metricW_d = nullptr, *metricOne_d = nullptr;  // [1 | w per orbital point] and all ones
-  double *metricUser_d = nullptr;                      // caller-supplied SIL metric
-  float* Vint_f = nullptr;
+  double *metricUser_d = nullptr;                      // caller-supplied SIL metric (single system)
   int* btOfOrb_d = nullptr;
+  int *pairL_d = nullptr, *pairK_d = nullptr, *pidx_d = nullptr;
   // CI
-  CiTables tab[CODY_MAX_BT];
-  CiView view;
   z_t *h1Lin_d = nullptr, *h2Lin_d = nullptr, *rdm1Lin_d = nullptr, *rdm2Lin_d = nullptr;
   z_t *rdm1_d = nullptr, *rdm2_d = nullptr, *h1_d = nullptr, *h2_d = nullptr;
   // mean-field
-  int nPairs = 0;
-  int *pairL_d = nullptr, *pairK_d = nullptr, *pidx_d = nullptr;
   z_t *S_d = nullptr, *W_d = nullptr;         // (nG, nPairs) row-major by grid point
-  z_t *Sfull_d = nullptr, *Wfull_d = nullptr; // (nG, nOS*nOS) row-major by grid point
+  z_t *Sfull_d = nullptr, *Wfull_d = nullptr; // (nG, nOS*nOS) row-major by grid point; Wfull has a Z half
   z_t *Rp_d = nullptr;                        // (nOS^2, nOS^2) correlation matrix
   z_t *h2s_d = nullptr;                       // (nOS^2, nOS^2) spatial h2 block
   z_t *Mreg_d = nullptr;                      // (nOS, nOS)
   z_t *Uprev_d = nullptr;                     // (nOS, nOS) natural orbitals of the previous rho^-1 call
-  z_t *r1s_d = nullptr, *r2s_d = nullptr;     // spin-summed spatial RDMs
+  z_t *r1s_d = nullptr;                       // spin-summed spatial rdm1
   // reductions / scratch
   z_t* partial_d = nullptr;
-  size_t partialCap = 0;
+  size_t partialCap = 0;                      // complex entries per trajectory
+  int lzBlocks = 148;                         // blocks per trajectory of the Lanczos reductions
+  int lzElems = 1;                            // state entries per thread and chunk in those blocks
+  int redBlocks = 148;                        // blocks per trajectory of the Gram reductions
   z_t *gram_d = nullptr;                      // (nOS, nOS)
   z_t *orbTmp_d = nullptr;                    // (nG, nOS)
   double* scal_d = nullptr;                   // misc device scalars
@@ -159,28 +238,26 @@ struct cgpu_ctx {
   z_t *basis_d = nullptr, *lw_d = nullptr, *trial_d = nullptr, *work_d = nullptr;
   int maxKrylov = 0;
   double* lz_d = nullptr;   // Lanczos scalars: alpha, beta, dots, phi, flags
-  double* lz_h = nullptr;   // pinned mirror
+  double* lz_h = nullptr;   // pinned mirror (trajectory 0)
   // TDCI static data
   z_t* tdciOrbs_d = nullptr;
   // stream / graph
   cudaStream_t stream = nullptr;
   cudaGraphExec_t stepGraph = nullptr;
-  cudaGraph_t stepGraphRaw = nullptr;
   double graphDt = 0;
   int graphKrylov = 0, graphMetric = -1, graphKernels = 0, graphProf = 0;
   size_t graphProfUsed = 0;
   // device-side time: kernels evaluate E(*timeBase + offset).  Outside a graph
   // capture the base is a device zero and the offset the absolute time; inside
   // one the base is the step-start time stepT_d that the graph advances.
-  LaserDev laserDev;
-  double* samples_d = nullptr;
   double* zero_d = nullptr;
   double* stepT_d = nullptr;
   int inCapture = 0;
+  int useStepTime = 0;  // outside a capture: E(*stepT_d + t) per trajectory instead of E(t)
   double captureT0 = 0.0;
   z_t* warm_d = nullptr;
   std::string lastError;
-  int launches = 0;  // kernels launched by this context (since the last reset)
+  long launches = 0;  // kernels launched by this context (since the last reset)
   MixedBufs* mixed = nullptr;
   // profiling: CUDA events around every launch of one kernel family
   int profTarget = 0;
@@ -211,25 +288,45 @@ struct ProfScope {
   }
 };
 
+// Launch configuration helpers: x-extent for n items per trajectory, z = nb.
+inline dim3 bgrid(const cgpu_ctx* c, size_t x, unsigned y = 1) { return dim3((unsigned)(x < 1 ? 1 : x), y, c->nb); }
+inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+// Blocks per trajectory of a grid-stride element-wise kernel over at most nmax
+// items: enough for ~8k resident blocks in total, never more than the items need.
+inline unsigned ew_blocks(const cgpu_ctx* c, size_t nmax, unsigned threads = 256) {
+  size_t need = (nmax + threads - 1) / threads;
+  size_t cap = (size_t)(c->nb > 1 ? (8192 / c->nb > 4 ? 8192 / c->nb : 4) : 8192);
+  return (unsigned)(need < 1 ? 1 : (need < cap ? need : cap));
+}
+// Per-trajectory element counts stay below 2^32, so the loops index in 32 bits.
+#define GRID_STRIDE(e, n) \
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < (unsigned)(n); e += gridDim.x * blockDim.x)
+
+// Zero / copy `bytes` at p in every trajectory (strided by bs).
+void batch_zero(cgpu_ctx* c, void* p, size_t bytes);
+void batch_copy(cgpu_ctx* c, void* dst, const void* src, size_t bytes);
+
 // ---------------------------------------------------------------------------
-// Launchers (defined in the k_*.cu translation units).
+// Launchers (defined in the k_*.cu translation units).  Pointers name the
+// buffers of trajectory 0; every launch covers all trajectories.
 // ---------------------------------------------------------------------------
 // k_onebody.cu
 void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha, int accumulate);
-void launch_gram(cgpu_ctx* c, z_t* G, const z_t* A, const z_t* B, int nCols, int colA0, int colB0, int ldG,
-                 double scale);
 void launch_project_orbs(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs);
 void launch_project_coeffs(cgpu_ctx* c, z_t* dC, const z_t* C);
 void launch_fill_h1_from(cgpu_ctx* c, const z_t* orbs, const z_t* hOrbs, z_t* h1);
-void launch_axpby(cgpu_ctx* c, z_t* y, const z_t* x, z_t a, z_t b, size_t n);  // y = a x + b y
+void launch_axpby(cgpu_ctx* c, z_t* y, const z_t* x, z_t a, z_t b, int sel);  // y = a x + b y
 void launch_rk_stage(cgpu_ctx* c, z_t* inc, z_t* tmp, const z_t* state, const z_t* d, double wInc, double wTmp,
-                     int first, size_t n);
-void launch_scale(cgpu_ctx* c, z_t* y, z_t a, size_t n);
+                     int first);
+void launch_scale(cgpu_ctx* c, z_t* y, z_t a, int sel);
 void launch_orthonormalize(cgpu_ctx* c, z_t* orbs, int col0, int nCols);
 void launch_normalize_coeffs(cgpu_ctx* c, z_t* C);
 void launch_energy(cgpu_ctx* c, double* out_d);
+void launch_set_scalar(cgpu_ctx* c, double* p, double v);
+void launch_add_scalar(cgpu_ctx* c, double* p, double v);
+size_t gram_partial_need(const cgpu_ctx* c, int n);
 // k_ci.cu
-void ci_build_tables(cgpu_ctx* c);
+void ci_build_tables(cgpu_ctx* c, SysHost& s);
 void launch_ci_rdm(cgpu_ctx* c, const z_t* C, int want1, int want2);
 void launch_ci_apply(cgpu_ctx* c, const z_t* C, z_t* dC, int useH1, int useH2);
 void launch_fold_h1(cgpu_ctx* c);
@@ -238,12 +335,14 @@ void launch_fold_h2(cgpu_ctx* c);
 void launch_pair_potentials(cgpu_ctx* c, const z_t* orbs);
 void launch_correlation(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2);
 void launch_fill_h2(cgpu_ctx* c, const z_t* orbs);
-void launch_expand_h2(cgpu_ctx* c);
 void launch_rdm_inverse(cgpu_ctx* c);
 void launch_corr_epilogue(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, const z_t* Z);
 void launch_h2_layout(cgpu_ctx* c);
+void launch_build_vint(cgpu_ctx* c);
+size_t zgemm_partial_need(const cgpu_ctx* c);
 // k_mixed.cu
-void mixed_setup(cgpu_ctx* c);
+size_t mixed_layout(cgpu_ctx* c, char* base, size_t off);  // sizes (base == nullptr) or places the buffers
+void mixed_init(cgpu_ctx* c);
 void mixed_free(cgpu_ctx* c);
 int mixed_error(cgpu_ctx* c);
 void launch_correlation_mixed(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2);
@@ -255,6 +354,7 @@ void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim);
 void launch_lanczos_tail(cgpu_ctx* c, int j, double dt, int evalExp);  // j = 0: use the device mDim
 void launch_lanczos_combine(cgpu_ctx* c, z_t* out);
 void launch_lz_set(cgpu_ctx* c, int idx, double v);
+size_t lanczos_partial_need(const cgpu_ctx* c);
 #define CODY_LZ_ERR 385
 #define CODY_LZ_MDIM 386
 #define CODY_LZ_DONE 387
@@ -273,4 +373,5 @@ void launch_lz_set(cgpu_ctx* c, int idx, double v);
     CODY_CUDA(cudaGetLastError()); \
   } while (0)
 
-double cody_field_amplitude(const cgpu_ctx* c, double t);
+#define TRAJ_ARGS const TrajShape* __restrict__ shp, size_t bs
+#define TRAJ_PASS(c) (c)->shape_d, (c)->bs

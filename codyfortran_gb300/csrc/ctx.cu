@@ -1,5 +1,11 @@
 // ctx.cu -- context set-up (the hot path's Fabricate/Setup chain), the
 // equation-of-motion orchestration, the integrators and the C ABI.
+//
+// A context holds nb >= 1 systems.  Set-up builds each system on the host
+// (grid, kinetic band, potential, pairs, configuration tables), then places
+// the device data of all systems in one arena: trajectory b's buffers sit at
+// byte offset b * bs from trajectory 0's, every buffer sized for the largest
+// system.  The orchestration below is written once for all trajectories.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -15,7 +21,7 @@ std::mutex g_errMutex;
 constexpr double PI = 3.14159265358979323846264338327950288;
 
 // ---------------------------------------------------------------------------
-// Host-side set-up
+// Host-side set-up of one system
 // ---------------------------------------------------------------------------
 // Gauss-Legendre-Lobatto points/weights on [a,b]: interior nodes are the roots
 // of P'_{n-1}, found by Newton's method from Chebyshev-Lobatto guesses;
@@ -71,9 +77,7 @@ double lagrange_dprime(const std::vector<double>& xr, int basis, int node) {
   return r;
 }
 
-// Grid + banded kinetic operator.  T[(bt*(2b+1) + d+b)*nG + g] multiplies
-// orbs[g+d] in (T orbs)[g] = -1/(2 m_bt) (d^2/dx^2 orbs)[g].
-void setup_grid_and_kinetic(cgpu_ctx* c, const cgpu_desc* d) {
+void setup_grid_and_kinetic(SysHost* c, int restricted, int nBt, const cgpu_desc* d) {
   std::vector<double>& x = c->x;
   std::vector<double>& w = c->w;
   std::vector<double> lap;  // (2b+1) x nG second-derivative band (mass independent)
@@ -149,7 +153,7 @@ void setup_grid_and_kinetic(cgpu_ctx* c, const cgpu_desc* d) {
     throw std::string("unknown grid kind");
   }
   int nd = 2 * c->band + 1;
-  c->nBtK = c->restricted ? 1 : c->nBt;
+  c->nBtK = restricted ? 1 : nBt;
   c->band_h.assign((size_t)c->nBtK * nd * c->nG, 0.0);
   for (int bt = 0; bt < c->nBtK; bt++) {
     double m = c->mass[bt];
@@ -157,6 +161,7 @@ void setup_grid_and_kinetic(cgpu_ctx* c, const cgpu_desc* d) {
     for (size_t k = 0; k < (size_t)nd * c->nG; k++) c->band_h[(size_t)bt * nd * c->nG + k] = -0.5 * lap[k] / m;
   }
 }
+
 
 template <typename T>
 T* dalloc(size_t n) {
@@ -186,206 +191,349 @@ __global__ void k_build_vint(double* __restrict__ V, const double* __restrict__ 
   V[e] = s * exp(-dist * damp) / (sqrt(dist * dist + s1 * s1) + s2);
 }
 
-void build_ctx(cgpu_ctx* c, const cgpu_desc* d) {
-  if (d->n_body_types < 1 || d->n_body_types > CODY_MAX_BT) throw std::string("method.mb.nBodyTypes out of range");
-  c->nBt = d->n_body_types;
-  c->restricted = d->restricted ? 1 : 0;
-  c->method = d->method;
-  c->precision = d->precision;
-  c->regEps = d->regularization > 0 ? d->regularization : 1e-10;
-  c->nO = 0;
+__global__ void k_scatter_states(z_t* __restrict__ dst, const z_t* __restrict__ src, const long* __restrict__ off,
+                                 TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  dst = bat(dst, bs);
+  src += off[blockIdx.z];
+  for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < (size_t)S.nS; l += (size_t)gridDim.x * blockDim.x)
+    dst[vidx(S, l)] = src[l];
+}
+
+__global__ void k_gather_states(z_t* __restrict__ dst, const z_t* __restrict__ src, const long* __restrict__ off,
+                                TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  src = bat(src, bs);
+  dst += off[blockIdx.z];
+  for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < (size_t)S.nS; l += (size_t)gridDim.x * blockDim.x)
+    dst[l] = src[vidx(S, l)];
+}
+
+// One system from its descriptor (host data; CI tables on the device).
+void build_system(cgpu_ctx* c, SysHost& s, const cgpu_desc* d) {
+  if (d->n_body_types != c->nBt) throw std::string("batch: every system needs the same number of body types");
+  if ((d->restricted ? 1 : 0) != c->restricted) throw std::string("batch: mixed restricted / unrestricted systems");
+  if (d->method != c->method || d->precision != c->precision)
+    throw std::string("batch: every system needs the same method and precision");
+  if ((d->has_interaction ? 1 : 0) != c->hasInteraction) throw std::string("batch: mixed interaction settings");
+  s.regEps = d->regularization > 0 ? d->regularization : 1e-10;
+  s.nO = 0;
   for (int b = 0; b < c->nBt; b++) {
-    c->nBodies[b] = d->n_bodies[b];
-    c->nOrbs[b] = d->n_orbs[b];
-    c->mass[b] = d->body_mass[b];
-    c->orbStart[b] = c->nO;
-    if (c->nOrbs[b] < 1 || c->nBodies[b] < 0 || c->nBodies[b] > c->nOrbs[b])
+    s.nBodies[b] = d->n_bodies[b];
+    s.nOrbs[b] = d->n_orbs[b];
+    s.mass[b] = d->body_mass[b];
+    s.orbStart[b] = s.nO;
+    if (s.nOrbs[b] < 1 || s.nBodies[b] < 0 || s.nBodies[b] > s.nOrbs[b])
       throw std::string("method.mb: invalid nOrbs / nBodies");
-    for (int i = 0; i < c->nOrbs[b]; i++) c->btOfOrb.push_back(b);
-    c->nO += c->nOrbs[b];
+    for (int i = 0; i < s.nOrbs[b]; i++) s.btOfOrb.push_back(b);
+    s.nO += s.nOrbs[b];
   }
   if (c->restricted) {
     for (int b = 1; b < c->nBt; b++)
-      if (c->nOrbs[b] != c->nOrbs[0]) throw std::string("orbs.restrictedQ needs equal nOrbs per body type");
+      if (s.nOrbs[b] != s.nOrbs[0]) throw std::string("orbs.restrictedQ needs equal nOrbs per body type");
     if (c->nBt != 2) throw std::string("orbs.restrictedQ needs two body types (spins)");
   }
-  c->nOS = c->restricted ? c->nOrbs[0] : c->nO;
-  if (c->nOS > 64) throw std::string("more than 64 stored orbitals is not supported");
-  if (c->method != CGPU_METHOD_TDCI && c->nOS > 32)
+  s.nOS = c->restricted ? s.nOrbs[0] : s.nO;
+  if (s.nOS > 64) throw std::string("more than 64 stored orbitals is not supported");
+  if (c->method != CGPU_METHOD_TDCI && s.nOS > 32)
     throw std::string("MCTDHX: more than 32 stored orbitals is not supported");
-  if (d->precision != CGPU_PREC_FP64 && d->precision != CGPU_PREC_MIXED && d->precision != CGPU_PREC_MIXED_X6)
-    throw std::string("unknown precision");
-  setup_grid_and_kinetic(c, d);
-  int nG = c->nG;
+  setup_grid_and_kinetic(&s, c->restricted, c->nBt, d);
+  for (int bt = 0; bt < s.nBtK; bt++)
+    if (!(s.mass[bt] > 0.0)) throw std::string("sysKinetic: body masses must be positive");
+  int nG = s.nG;
   // potential (src/SysPotential/Linear/SoftYukawa/StdImpl/*.f90:82-113)
-  c->V0.assign(nG, 0.0);
-  c->hasPotential = d->n_nuclei > 0;
+  s.V0.assign(nG, 0.0);
+  s.hasPotential = d->n_nuclei > 0;
   if (d->n_nuclei < 0 || d->n_nuclei > 8) throw std::string("sysPotential: 0..8 nuclei supported");
   for (int k = 0; k < d->n_nuclei; k++)
     for (int g = 0; g < nG; g++)
-      c->V0[g] -= soft_kernel(d->nuc_charge[k], d->nuc_softening1[k], d->nuc_softening2[k], d->nuc_dampening[k],
-                              std::fabs(c->x[g] - d->nuc_position[k]));
+      s.V0[g] -= soft_kernel(d->nuc_charge[k], d->nuc_softening1[k], d->nuc_softening2[k], d->nuc_dampening[k],
+                             std::fabs(s.x[g] - d->nuc_position[k]));
   // laser
-  c->laserKind = d->laser_kind;
-  c->E0 = d->laser_E0;
-  c->omega = d->laser_omega;
-  c->nCycles = d->laser_n_cycles;
-  c->cep = d->laser_cep;
-  c->tStart = d->laser_t_start;
+  s.laserKind = d->laser_kind;
+  s.E0 = d->laser_E0;
+  s.omega = d->laser_omega;
+  s.nCycles = d->laser_n_cycles;
+  s.cep = d->laser_cep;
+  s.tStart = d->laser_t_start;
   if (d->laser_kind == CGPU_LASER_SAMPLED) {
     if (!d->field_samples || d->n_field_samples <= 0) throw std::string("sampled field needs samples");
-    c->samples.assign(d->field_samples, d->field_samples + d->n_field_samples);
-    c->sampleDt = d->field_dt;
-    c->sampleT0 = d->field_t0;
+    s.samples.assign(d->field_samples, d->field_samples + d->n_field_samples);
+    s.sampleDt = d->field_dt;
+    s.sampleT0 = d->field_t0;
+    s.samples_d = dupload(s.samples);
   }
-  // device operators
-  CODY_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-  c->zero_d = dalloc<double>(1);
-  c->stepT_d = dalloc<double>(1);
-  CODY_CUDA(cudaMemset(c->zero_d, 0, sizeof(double)));
-  CODY_CUDA(cudaMemset(c->stepT_d, 0, sizeof(double)));
-  if (!c->samples.empty()) c->samples_d = dupload(c->samples);
-  c->laserDev = LaserDev{c->laserKind, c->E0, c->omega, c->nCycles, c->cep, c->tStart, c->sampleDt, c->sampleT0,
-                         (int)c->samples.size(), c->samples_d};
-  c->x_d = dupload(c->x);
-  c->w_d = dupload(c->w);
-  c->V0_d = dupload(c->V0);
-  c->T_d = dupload(c->band_h);
-  c->btOfOrb_d = dupload(c->btOfOrb);
-  c->hasInteraction = d->has_interaction ? 1 : 0;
-  if (c->hasInteraction) {
-    // interaction matrix V(x_i, x_j) (S_SysInteraction_Linear_SoftYukawa.f90:67-73), built on the device
-    double dx = nG > 1 ? c->x[1] - c->x[0] : 0.0;
-    c->Vint_d = dalloc<double>((size_t)nG * nG);
-    size_t tot = (size_t)nG * nG;
-    k_build_vint<<<(int)((tot + 255) / 256), 256, 0, c->stream>>>(
-        c->Vint_d, c->x_d, nG, d->int_kind == CGPU_INT_TOEPLITZ, dx, d->int_strength, d->int_softening1,
-        d->int_softening2, d->int_dampening);
-    CODY_LAUNCHED(c);
-  }
+  // interaction parameters (S_SysInteraction_Linear_SoftYukawa.f90:67-73)
+  s.intToeplitz = d->int_kind == CGPU_INT_TOEPLITZ;
+  s.intS = d->int_strength;
+  s.intS1 = d->int_softening1;
+  s.intS2 = d->int_softening2;
+  s.intDamp = d->int_dampening;
   // pairs (l <= k, same body type) in the order of the reference's loops
-  int n = c->nOS;
-  std::vector<int> pl, pk, pidx((size_t)n * n, -1);
+  int n = s.nOS;
+  s.pidx.assign((size_t)n * n, -1);
   for (int l = 0; l < n; l++)
     for (int k = l; k < n; k++) {
-      if (!c->restricted && c->btOfOrb[l] != c->btOfOrb[k]) continue;
-      pidx[(size_t)l * n + k] = (int)pl.size();
-      pl.push_back(l);
-      pk.push_back(k);
+      if (!c->restricted && s.btOfOrb[l] != s.btOfOrb[k]) continue;
+      s.pidx[(size_t)l * n + k] = (int)s.pl.size();
+      s.pl.push_back(l);
+      s.pk.push_back(k);
     }
-  c->nPairs = (int)pl.size();
-  c->pairL_d = dupload(pl);
-  c->pairK_d = dupload(pk);
-  c->pidx_d = dupload(pidx);
+  s.nPairs = (int)s.pl.size();
   // CI tables
-  ci_build_tables(c);
-  c->nC = c->view.nC;
-  c->nS = (c->method == CGPU_METHOD_TDCI) ? c->nC : c->nC + nG * n;
+  ci_build_tables(c, s);
+  s.nC = s.view.nC;
+  s.nS = (c->method == CGPU_METHOD_TDCI) ? s.nC : s.nC + nG * n;
+}
+
+size_t take(size_t& off, size_t bytes) {
+  size_t o = (off + 255) & ~(size_t)255;
+  off = o + std::max<size_t>(bytes, 1);
+  return o;
+}
+
+// Sizes (base == nullptr) or places (base = the arena) the buffers of one
+// trajectory block; returns the block size.
+size_t layout(cgpu_ctx* c, char* base) {
+  size_t off = 0;
+  size_t nG = c->nG, nO2 = (size_t)c->nO * c->nO, nO4 = nO2 * nO2, n = c->nOS, Q = n * n, P = std::max(c->nPairs, 1);
   size_t nS = c->nS;
-  std::vector<double> mw(nS, 1.0), m1(nS, 1.0);
-  if (c->method != CGPU_METHOD_TDCI)
-    for (int o = 0; o < n; o++)
-      for (int g = 0; g < nG; g++) mw[(size_t)c->nC + (size_t)o * nG + g] = c->w[g];
-  c->metricW_d = dupload(mw);
-  c->metricOne_d = dupload(m1);
-  c->metric_d = c->metricOne_d;
-  // work buffers
-  size_t nO2 = (size_t)c->nO * c->nO, nO4 = nO2 * nO2, Q = (size_t)n * n;
-  c->h1Lin_d = dalloc<z_t>(nO2 + 1);
-  c->rdm1Lin_d = dalloc<z_t>(nO2 + 1);
-  c->h2Lin_d = dalloc<z_t>(nO4 + 1);
-  c->rdm2Lin_d = dalloc<z_t>(nO4 + 1);
-  CODY_CUDA(cudaMemset(c->h1Lin_d, 0, sizeof(z_t) * (nO2 + 1)));
-  CODY_CUDA(cudaMemset(c->h2Lin_d, 0, sizeof(z_t) * (nO4 + 1)));
-  c->rdm1_d = dalloc<z_t>(nO2);
-  c->h1_d = dalloc<z_t>(nO2);
-  c->rdm2_d = dalloc<z_t>(nO4);
-  c->h2_d = dalloc<z_t>(nO4);
-  CODY_CUDA(cudaMemset(c->h1_d, 0, sizeof(z_t) * nO2));
-  CODY_CUDA(cudaMemset(c->h2_d, 0, sizeof(z_t) * nO4));
-  c->S_d = dalloc<z_t>((size_t)nG * std::max(c->nPairs, 1));
-  c->W_d = dalloc<z_t>((size_t)nG * std::max(c->nPairs, 1));
-  c->Sfull_d = dalloc<z_t>((size_t)nG * Q);
-  c->Wfull_d = dalloc<z_t>(2 * (size_t)nG * Q);
-  c->Rp_d = dalloc<z_t>(Q * Q);
-  c->h2s_d = dalloc<z_t>(Q * Q);
-  c->Mreg_d = dalloc<z_t>(Q);
-  {
-    std::vector<z_t> eye(Q, zmk(0.0, 0.0));
-    for (int i = 0; i < n; i++) eye[(size_t)i * n + i] = zmk(1.0, 0.0);
-    c->Uprev_d = dupload(eye);
+  int nd = 2 * c->band + 1;
+  auto D = [&](double*& p, size_t cnt) { size_t o = take(off, sizeof(double) * cnt); if (base) p = (double*)(base + o); };
+  auto I = [&](int*& p, size_t cnt) { size_t o = take(off, sizeof(int) * cnt); if (base) p = (int*)(base + o); };
+  auto Z = [&](z_t*& p, size_t cnt) { size_t o = take(off, sizeof(z_t) * cnt); if (base) p = (z_t*)(base + o); };
+  D(c->x_d, nG);
+  D(c->w_d, nG);
+  D(c->V0_d, nG);
+  D(c->T_d, (size_t)c->nBtK * nd * nG);
+  if (c->hasInteraction) D(c->Vint_d, nG * nG);
+  D(c->metricW_d, nS);
+  D(c->metricOne_d, nS);
+  D(c->scal_d, 64);
+  D(c->lz_d, 512);
+  D(c->zero_d, 1);
+  D(c->stepT_d, 1);
+  I(c->btOfOrb_d, c->nO);
+  I(c->pairL_d, P);
+  I(c->pairK_d, P);
+  I(c->pidx_d, Q);
+  Z(c->h1Lin_d, nO2 + 1);
+  Z(c->rdm1Lin_d, nO2 + 1);
+  Z(c->h2Lin_d, nO4 + 1);
+  Z(c->rdm2Lin_d, nO4 + 1);
+  Z(c->rdm1_d, nO2);
+  Z(c->h1_d, nO2);
+  Z(c->rdm2_d, nO4);
+  Z(c->h2_d, nO4);
+  Z(c->S_d, nG * P);
+  Z(c->W_d, nG * P);
+  Z(c->Sfull_d, nG * Q);
+  Z(c->Wfull_d, 2 * nG * Q);
+  Z(c->Rp_d, Q * Q);
+  Z(c->h2s_d, Q * Q);
+  Z(c->Mreg_d, Q);
+  Z(c->Uprev_d, Q);
+  Z(c->r1s_d, Q);
+  Z(c->gram_d, Q);
+  Z(c->orbTmp_d, nG * n);
+  Z(c->state_d, nS);
+  Z(c->dstate_d, nS);
+  Z(c->rkInc_d, nS);
+  Z(c->rkTmp_d, nS);
+  Z(c->rkStage_d, nS);
+  Z(c->trial_d, nS);
+  Z(c->work_d, nS);
+  Z(c->lw_d, nS);
+  Z(c->warm_d, nS);
+  Z(c->basis_d, nS * (size_t)c->maxKrylov);
+  if (c->method == CGPU_METHOD_TDCI) Z(c->tdciOrbs_d, nG * n);
+  Z(c->partial_d, c->partialCap);
+  off = mixed_layout(c, base, off);
+  return (off + 1023) & ~(size_t)1023;
+}
+
+template <typename T>
+void put(cgpu_ctx* c, int b, T* dst0, const std::vector<T>& v) {
+  if (v.empty()) return;
+  CODY_CUDA(cudaMemcpy((char*)dst0 + (size_t)b * c->bs, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+}
+
+void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
+  const cgpu_desc* d0 = &descs[0];
+  if (d0->n_body_types < 1 || d0->n_body_types > CODY_MAX_BT) throw std::string("method.mb.nBodyTypes out of range");
+  if (d0->precision != CGPU_PREC_FP64 && d0->precision != CGPU_PREC_MIXED && d0->precision != CGPU_PREC_MIXED_X6)
+    throw std::string("unknown precision");
+  c->nb = nSys;
+  c->nBt = d0->n_body_types;
+  c->restricted = d0->restricted ? 1 : 0;
+  c->method = d0->method;
+  c->precision = d0->precision;
+  c->hasInteraction = d0->has_interaction ? 1 : 0;
+  CODY_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  c->sys.resize(nSys);
+  for (int b = 0; b < nSys; b++) build_system(c, c->sys[b], &descs[b]);
+  // maxima over the systems
+  int nGO = 0, minS = 1 << 30, maxK = 0;
+  for (const SysHost& s : c->sys) {
+    c->nG = std::max(c->nG, s.nG);
+    c->nO = std::max(c->nO, s.nO);
+    c->nOS = std::max(c->nOS, s.nOS);
+    c->nC = std::max(c->nC, s.nC);
+    c->nPairs = std::max(c->nPairs, s.nPairs);
+    c->band = std::max(c->band, s.band);
+    c->nBtK = std::max(c->nBtK, s.nBtK);
+    c->anyLaser |= s.laserKind != CGPU_LASER_NONE;
+    nGO = std::max(nGO, s.nG * s.nOS);
+    minS = std::min(minS, s.nS);
   }
-  c->r1s_d = dalloc<z_t>(Q);
-  c->gram_d = dalloc<z_t>(Q);
-  c->orbTmp_d = dalloc<z_t>((size_t)nG * n);
-  c->scal_d = dalloc<double>(64);
-  c->state_d = dalloc<z_t>(nS);
-  c->dstate_d = dalloc<z_t>(nS);
-  c->rkInc_d = dalloc<z_t>(nS);
-  c->rkTmp_d = dalloc<z_t>(nS);
-  c->rkStage_d = dalloc<z_t>(nS);
-  c->trial_d = dalloc<z_t>(nS);
-  c->work_d = dalloc<z_t>(nS);
-  c->lw_d = dalloc<z_t>(nS);
-  c->maxKrylov = std::max(1, std::min(d->max_krylov > 0 ? d->max_krylov : 32, 32));
-  c->basis_d = dalloc<z_t>(nS * (size_t)c->maxKrylov);
-  c->lz_d = dalloc<double>(512);
-  CODY_CUDA(cudaMemset(c->lz_d, 0, sizeof(double) * 512));
+  for (int b = 0; b < nSys; b++) maxK = std::max(maxK, descs[b].max_krylov);
+  c->nGO = nGO;
+  for (const SysHost& s : c->sys) {
+    const CiView& v = s.view;
+    int nS = 0, nD = 0, nX = 0;
+    for (int b = 0; b < v.nBt; b++) {
+      nS += v.nSc[b];
+      nD += v.nDc[b];
+      for (int b2 = b + 1; b2 < v.nBt; b2++) nX += v.nSc[b] * v.nSc[b2];
+    }
+    c->ciTasks = std::max(c->ciTasks, nS + nD + nX);
+  }
+  c->nS = (c->method == CGPU_METHOD_TDCI) ? c->nC : c->nC + nGO;
+  c->minS = minS;
+  c->maxKrylov = std::max(1, std::min(maxK > 0 ? maxK : 32, 32));
+  // Lanczos reductions: one system spreads 256-entry chunks over up to 4 blocks
+  // per SM; a batch gives each block a 1024-entry chunk of its trajectory.
+  c->lzElems = nSys == 1 ? 1 : 4;
+  {
+    size_t chunk = (size_t)256 * c->lzElems;
+    size_t need = ((size_t)c->nS + chunk - 1) / chunk;
+    c->lzBlocks = (int)std::max<size_t>(1, std::min<size_t>(nSys == 1 ? 4 * 148 : 148, need));
+  }
+  c->partialCap = std::max({lanczos_partial_need(c), gram_partial_need(c, c->nOS), zgemm_partial_need(c),
+                            (size_t)148});
+  // arena
+  c->bs = layout(c, nullptr);
+  size_t total = c->bs * (size_t)nSys;
+  CODY_CUDA(cudaMalloc(&c->arena, total));
+  CODY_CUDA(cudaMemset(c->arena, 0, total));
+  CODY_CUDA(cudaDeviceSynchronize());
+  layout(c, c->arena);
+  // per-system static data
+  c->shape_h.resize(nSys);
+  for (int b = 0; b < nSys; b++) {
+    SysHost& s = c->sys[b];
+    put(c, b, c->x_d, s.x);
+    put(c, b, c->w_d, s.w);
+    put(c, b, c->V0_d, s.V0);
+    put(c, b, c->T_d, s.band_h);
+    put(c, b, c->btOfOrb_d, s.btOfOrb);
+    put(c, b, c->pairL_d, s.pl);
+    put(c, b, c->pairK_d, s.pk);
+    put(c, b, c->pidx_d, s.pidx);
+    std::vector<double> mw(c->nS, 1.0), m1(c->nS, 1.0);
+    if (c->method != CGPU_METHOD_TDCI)
+      for (int o = 0; o < s.nOS; o++)
+        for (int g = 0; g < s.nG; g++) mw[(size_t)c->nC + (size_t)o * s.nG + g] = s.w[g];
+    put(c, b, c->metricW_d, mw);
+    put(c, b, c->metricOne_d, m1);
+    std::vector<z_t> eye((size_t)s.nOS * s.nOS, zmk(0.0, 0.0));
+    for (int i = 0; i < s.nOS; i++) eye[(size_t)i * s.nOS + i] = zmk(1.0, 0.0);
+    put(c, b, c->Uprev_d, eye);
+    if (c->hasInteraction) {
+      double dx = s.nG > 1 ? s.x[1] - s.x[0] : 0.0;
+      size_t tot = (size_t)s.nG * s.nG;
+      double* V = (double*)((char*)c->Vint_d + (size_t)b * c->bs);
+      const double* xb = (const double*)((const char*)c->x_d + (size_t)b * c->bs);
+      k_build_vint<<<(unsigned)((tot + 255) / 256), 256, 0, c->stream>>>(V, xb, s.nG, s.intToeplitz, dx, s.intS,
+                                                                         s.intS1, s.intS2, s.intDamp);
+      CODY_LAUNCHED(c);
+    }
+    TrajShape& t = c->shape_h[b];
+    std::memset(&t, 0, sizeof(t));
+    t.nG = s.nG;
+    t.nOS = s.nOS;
+    t.nO = s.nO;
+    t.nC = s.nC;
+    t.nS = s.nS;
+    t.nGO = s.nG * s.nOS;
+    t.nPairs = s.nPairs;
+    t.band = s.band;
+    t.restricted = c->restricted;
+    t.hasPot = s.hasPotential || s.laserKind != CGPU_LASER_NONE;
+    t.nBt = c->nBt;
+    t.nCpad = c->nC;
+    t.nGroups = c->restricted ? 1 : c->nBt;
+    for (int g = 0; g < t.nGroups; g++) {
+      t.grpStart[g] = c->restricted ? 0 : s.orbStart[g];
+      t.grpSize[g] = c->restricted ? s.nOS : s.nOrbs[g];
+    }
+    t.Kg = (s.nG + 63) / 64 * 64;
+    t.Kp = (2 * s.nPairs + 63) / 64 * 64;
+    t.regEps = s.regEps;
+    t.laser = LaserDev{s.laserKind, s.E0, s.omega, s.nCycles, s.cep, s.tStart, s.sampleDt, s.sampleT0,
+                       (int)s.samples.size(), s.samples_d};
+    t.view = s.view;
+  }
+  CODY_CUDA(cudaMalloc(&c->shape_d, sizeof(TrajShape) * nSys));
+  CODY_CUDA(cudaMemcpy(c->shape_d, c->shape_h.data(), sizeof(TrajShape) * nSys, cudaMemcpyHostToDevice));
+  CODY_CUDA(cudaMalloc(&c->stageOff_d, sizeof(long) * (nSys + 1)));
+  std::vector<long> so(nSys + 1, 0);
+  for (int b = 0; b < nSys; b++) so[b + 1] = so[b] + c->sys[b].nS;
+  c->stageOff = so;
+  CODY_CUDA(cudaMemcpy(c->stageOff_d, so.data(), sizeof(long) * (nSys + 1), cudaMemcpyHostToDevice));
+  mixed_init(c);
   CODY_CUDA(cudaMallocHost(&c->lz_h, sizeof(double) * 512));
-  if (c->method == CGPU_METHOD_TDCI) c->tdciOrbs_d = dalloc<z_t>((size_t)nG * n);
   CODY_CUDA(cudaDeviceSynchronize());
 }
 
 void free_ctx(cgpu_ctx* c) {
   mixed_free(c);
   if (c->stepGraph) cudaGraphExecDestroy(c->stepGraph);
-  if (c->stepGraphRaw) cudaGraphDestroy(c->stepGraphRaw);
   for (cudaEvent_t e : c->profEvents) cudaEventDestroy(e);
-  void* ptrs[] = {c->x_d, c->w_d, c->V0_d, c->T_d, c->Vint_d, c->metricW_d, c->metricOne_d, c->metricUser_d, c->Vint_f,
-                  c->btOfOrb_d, c->h1Lin_d, c->h2Lin_d, c->rdm1Lin_d, c->rdm2Lin_d, c->rdm1_d, c->rdm2_d, c->h1_d,
-                  c->h2_d, c->pairL_d, c->pairK_d, c->pidx_d, c->S_d, c->W_d, c->Sfull_d, c->Wfull_d, c->Rp_d,
-                  c->h2s_d, c->Mreg_d, c->r1s_d, c->r2s_d, c->partial_d, c->gram_d, c->orbTmp_d, c->scal_d,
-                  c->state_d, c->dstate_d, c->rkInc_d, c->rkTmp_d, c->rkStage_d, c->basis_d, c->lw_d, c->trial_d,
-                  c->work_d, c->lz_d, c->tdciOrbs_d, c->zero_d, c->stepT_d, c->samples_d, c->warm_d,
-                  c->Uprev_d};
+  for (SysHost& s : c->sys) {
+    for (int b = 0; b < CODY_MAX_BT; b++) {
+      CiTables& t = s.tab[b];
+      void* tp[] = {t.codes, t.sN,     t.sExc,   t.sCode,  t.sFac,  t.dN,      t.dExc,   t.dCode,
+                    t.dFac,  t.rankTab, t.sxCode, t.sxStart, t.sxSrc, t.sxDst,  t.sxFac,  t.dxCode,
+                    t.dxStart, t.dxSrc, t.dxDst,  t.dxFac};
+      for (void* p : tp)
+        if (p) cudaFree(p);
+    }
+    if (s.samples_d) cudaFree(s.samples_d);
+  }
+  void* ptrs[] = {c->arena, c->shape_d, c->metricUser_d, c->stageOff_d, c->stage_d};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  for (int b = 0; b < CODY_MAX_BT; b++) {
-    CiTables& t = c->tab[b];
-    void* tp[] = {t.codes, t.sN, t.sExc, t.sCode, t.sFac, t.dN, t.dExc, t.dCode, t.dFac, t.rankTab};
-    for (void* p : tp)
-      if (p) cudaFree(p);
-  }
   if (c->lz_h) cudaFreeHost(c->lz_h);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
 // ---------------------------------------------------------------------------
-// Equation of motion on device buffers.  out = post * dState, where dState is
-// the reference's time derivative (carrying its -i).
+// Equation of motion on device buffers (all trajectories).  out = post * dState,
+// where dState is the reference's time derivative (carrying its -i).
 // ---------------------------------------------------------------------------
 void td_device(cgpu_ctx* c, int which, z_t* out, const z_t* in, double t, z_t post) {
   z_t f = zmul(post, zmk(0.0, -1.0));
   bool unit = (f.x == 1.0 && f.y == 0.0);
   if (which == CGPU_TD_TDCI || c->method == CGPU_METHOD_TDCI) {
     if (c->method != CGPU_METHOD_TDCI) throw std::string("TDCI derivative needs a TDCI context");
-    if (c->laserKind != CGPU_LASER_NONE) {  // time-dependent one-body part (Tdci :90-92)
+    if (c->anyLaser) {  // time-dependent one-body part (Tdci :90-92)
       launch_onebody(c, c->orbTmp_d, c->tdciOrbs_d, t, zmk(1.0, 0.0), 0);
       launch_fill_h1_from(c, c->tdciOrbs_d, c->orbTmp_d, c->h1_d);
       launch_fold_h1(c);
     }
-    CODY_CUDA(cudaMemsetAsync(out, 0, sizeof(z_t) * c->nC, c->stream));
+    batch_zero(c, out, sizeof(z_t) * c->nC);
     launch_ci_apply(c, in, out, 1, 1);
-    if (!unit) launch_scale(c, out, f, c->nC);
+    if (!unit) launch_scale(c, out, f, VSEL_COEFFS);
     return;
   }
   const z_t* C = in;
   const z_t* orbs = in + c->nC;
   z_t* dC = out;
   z_t* dOrbs = out + c->nC;
-  size_t nGO = (size_t)c->nG * c->nOS;
+  size_t nGO = c->nGO;
   if (which == CGPU_TD_ORBS_LIN) {
-    CODY_CUDA(cudaMemsetAsync(dC, 0, sizeof(z_t) * c->nC, c->stream));
+    batch_zero(c, dC, sizeof(z_t) * c->nC);
     launch_onebody(c, dOrbs, orbs, t, f, 0);
     return;
   }
@@ -397,41 +545,40 @@ void td_device(cgpu_ctx* c, int which, z_t* out, const z_t* in, double t, z_t po
   } else {
     launch_onebody(c, c->orbTmp_d, orbs, t, zmk(1.0, 0.0), 0);
     launch_fill_h1_from(c, orbs, c->orbTmp_d, c->h1_d);
-    CODY_CUDA(cudaMemsetAsync(dOrbs, 0, sizeof(z_t) * nGO, c->stream));
+    batch_zero(c, dOrbs, sizeof(z_t) * nGO);
   }
   if (c->precision == CGPU_PREC_FP64) launch_correlation(c, dOrbs, orbs, 1);
   else launch_correlation_mixed(c, dOrbs, orbs, 1);
   launch_fold_h1(c);
   launch_fold_h2(c);
-  CODY_CUDA(cudaMemsetAsync(dC, 0, sizeof(z_t) * c->nC, c->stream));
+  batch_zero(c, dC, sizeof(z_t) * c->nC);
   launch_ci_apply(c, C, dC, 1, 1);
   launch_project_coeffs(c, dC, C);
   launch_project_orbs(c, dOrbs, orbs);
-  if (!unit) launch_scale(c, out, f, c->nS);
+  if (!unit) launch_scale(c, out, f, VSEL_STATE);
 }
 
 // RK4 (src/IntegratorList/Rk/O4Expl/S_IntegratorList_Rk_O4Expl.f90:90-141) on state_d-like buffers.
 void rk4_device(cgpu_ctx* c, int which, z_t* state, double t0, double t1) {
   double dt = t1 - t0, dt2 = dt / 2.0, dt3 = dt / 3.0, dt6 = dt / 6.0;
-  size_t n = c->nS;
   z_t one = zmk(1.0, 0.0);
   td_device(c, which, c->dstate_d, state, t0, one);
-  launch_rk_stage(c, c->rkInc_d, c->rkTmp_d, state, c->dstate_d, dt6, dt2, 1, n);
+  launch_rk_stage(c, c->rkInc_d, c->rkTmp_d, state, c->dstate_d, dt6, dt2, 1);
   double tp = t0 + dt2;
   td_device(c, which, c->dstate_d, c->rkTmp_d, tp, one);
-  launch_rk_stage(c, c->rkInc_d, c->rkTmp_d, state, c->dstate_d, dt3, dt2, 0, n);
+  launch_rk_stage(c, c->rkInc_d, c->rkTmp_d, state, c->dstate_d, dt3, dt2, 0);
   td_device(c, which, c->dstate_d, c->rkTmp_d, tp, one);
-  launch_rk_stage(c, c->rkInc_d, c->rkTmp_d, state, c->dstate_d, dt3, dt, 0, n);
+  launch_rk_stage(c, c->rkInc_d, c->rkTmp_d, state, c->dstate_d, dt3, dt, 0);
   tp = t0 + dt;
   td_device(c, which, c->dstate_d, c->rkTmp_d, tp, one);
-  launch_rk_stage(c, c->rkInc_d, nullptr, state, c->dstate_d, dt6, 0.0, 0, n);
-  launch_axpby(c, state, c->rkInc_d, one, one, n);
+  launch_rk_stage(c, c->rkInc_d, nullptr, state, c->dstate_d, dt6, 0.0, 0);
+  launch_axpby(c, state, c->rkInc_d, one, one, VSEL_STATE);
 }
 
 void euler_device(cgpu_ctx* c, int which, int imag, z_t* state, double t0, double t1) {
   z_t post = imag ? zmk(0.0, -1.0) : zmk(1.0, 0.0);
   td_device(c, which, c->dstate_d, state, t0, post);
-  launch_axpby(c, state, c->dstate_d, zmk(t1 - t0, 0.0), zmk(1.0, 0.0), c->nS);
+  launch_axpby(c, state, c->dstate_d, zmk(t1 - t0, 0.0), zmk(1.0, 0.0), VSEL_STATE);
 }
 
 // One PerformLanczosStep on work_d -> trial_d.  Returns converged (adaptive) or -1 (not checked).
@@ -439,6 +586,7 @@ int lanczos_pass(cgpu_ctx* c, int which, double tBase, double dt, int maxDim, do
   launch_lanczos_start(c, c->work_d);
   double tEval = tBase + 0.5 * dt;
   int adaptive = tol > 0.0;
+  if (adaptive && c->nb > 1) throw std::string("SIL: adaptive (tolerance > 0) steps need a single system");
   int converged = -1;
   int mUsed = maxDim;
   for (int j = 1; j <= maxDim; j++) {
@@ -475,11 +623,11 @@ int sil_device(cgpu_ctx* c, int which, z_t* state, double t0, double t1, int kry
                const double* metric_d) {
   const double zeroThreshold = 1.0e-14;
   if (std::fabs(t1 - t0) <= zeroThreshold) return 0;
-  int maxDim = std::max(1, std::min(krylovDim, c->nS));
+  int maxDim = std::max(1, std::min(krylovDim, c->minS));
   if (maxDim > c->maxKrylov) throw std::string("SIL: krylovDim exceeds the context's max_krylov");
   c->metric_d = const_cast<double*>(metric_d);
   int warnings = 0;
-  CODY_CUDA(cudaMemcpyAsync(c->work_d, state, sizeof(z_t) * c->nS, cudaMemcpyDeviceToDevice, c->stream));
+  batch_copy(c, c->work_d, state, sizeof(z_t) * c->nS);
   double tCur = t0, rem = t1 - t0;
   while (std::fabs(rem) > zeroThreshold) {
     double dtS = rem;
@@ -495,11 +643,11 @@ int sil_device(cgpu_ctx* c, int which, z_t* state, double t0, double t1, int kry
       restarts++;
     }
     if (conv != 1) warnings++;
-    CODY_CUDA(cudaMemcpyAsync(c->work_d, c->trial_d, sizeof(z_t) * c->nS, cudaMemcpyDeviceToDevice, c->stream));
+    batch_copy(c, c->work_d, c->trial_d, sizeof(z_t) * c->nS);
     tCur = tCur + dtS;
     rem = rem - dtS;
   }
-  CODY_CUDA(cudaMemcpyAsync(state, c->work_d, sizeof(z_t) * c->nS, cudaMemcpyDeviceToDevice, c->stream));
+  batch_copy(c, state, c->work_d, sizeof(z_t) * c->nS);
   return warnings;
 }
 
@@ -514,20 +662,17 @@ void split2_device(cgpu_ctx* c, z_t* state, double t0, double t1, int krylov, do
   else rk4_device(c, CGPU_TD_ORBS_LIN, state, time2, time2 + 0.5 * dt);
 }
 
-__global__ void k_advance_time(double* t, double dt) { *t = *t + dt; }
-
-// Captures one fixed-order Strang step on state_d as a CUDA graph.  The step
-// reads its start time from stepT_d (the laser is evaluated on the device) and
-// advances it by dt, so the graph can be replayed for consecutive steps.  A
-// first step on a scratch copy of the state allocates every lazily sized
-// buffer outside the capture.
+// Captures one fixed-order Strang step on state_d (every trajectory) as a CUDA
+// graph.  The step reads its start times from stepT_d (the laser is evaluated
+// on the device) and advances them by dt, so the graph can be replayed for
+// consecutive steps.  A first step on a scratch copy of the state makes every
+// launch of the capture valid outside it.
 void capture_step_graph(cgpu_ctx* c, double t0, double dt, int krylov, int useMetric) {
   if (c->stepGraph) {
     cudaGraphExecDestroy(c->stepGraph);
     c->stepGraph = nullptr;
   }
-  if (!c->warm_d) c->warm_d = dalloc<z_t>(c->nS);
-  CODY_CUDA(cudaMemcpyAsync(c->warm_d, c->state_d, sizeof(z_t) * c->nS, cudaMemcpyDeviceToDevice, c->stream));
+  batch_copy(c, c->warm_d, c->state_d, sizeof(z_t) * c->nS);
   split2_device(c, c->warm_d, t0, t0 + dt, krylov, 0.0, 0, useMetric);
   CODY_CUDA(cudaStreamSynchronize(c->stream));
   // profiling events of the selected kernel family become event-record nodes of the graph
@@ -539,8 +684,7 @@ void capture_step_graph(cgpu_ctx* c, double t0, double dt, int krylov, int useMe
   c->captureT0 = t0;
   try {
     split2_device(c, c->state_d, t0, t0 + dt, krylov, 0.0, 0, useMetric);
-    k_advance_time<<<1, 1, 0, c->stream>>>(c->stepT_d, dt);
-    CODY_LAUNCHED(c);
+    launch_add_scalar(c, c->stepT_d, dt);
   } catch (...) {
     c->inCapture = 0;
     cudaStreamEndCapture(c->stream, &g);
@@ -554,15 +698,32 @@ void capture_step_graph(cgpu_ctx* c, double t0, double dt, int krylov, int useMe
   c->graphKernels = (int)(c->launches - before);
   c->launches = before;
   cudaError_t e = cudaGraphInstantiate(&c->stepGraph, g, 0);
-  if (c->stepGraphRaw) cudaGraphDestroy(c->stepGraphRaw);
-  c->stepGraphRaw = g;  // kept: a batch embeds it as a child graph
+  cudaGraphDestroy(g);
   CODY_CUDA(e);
   c->graphDt = dt;
   c->graphKrylov = krylov;
   c->graphMetric = useMetric;
 }
 
-double energy_device(cgpu_ctx* c, const z_t* state, double t) {
+// Step start time of every trajectory (t0s has nb entries).
+void set_step_times(cgpu_ctx* c, const double* t0s) {
+  CODY_CUDA(cudaMemcpy2DAsync(c->stepT_d, c->bs, t0s, sizeof(double), sizeof(double), c->nb, cudaMemcpyHostToDevice,
+                              c->stream));
+}
+
+// n_steps replays of the step graph (captured when dt, order or metric changed).
+void propagate_graph(cgpu_ctx* c, const double* t0s, double dt, int nSteps, int krylov, int useMetric) {
+  if (!c->stepGraph || c->graphDt != dt || c->graphKrylov != krylov || c->graphMetric != useMetric ||
+      c->graphProf != c->profTarget)
+    capture_step_graph(c, t0s[0], dt, krylov, useMetric);
+  if (c->profTarget) c->profUsed = c->graphProfUsed;
+  set_step_times(c, t0s);
+  for (int s = 0; s < nSteps; s++) CODY_CUDA(cudaGraphLaunch(c->stepGraph, c->stream));
+  c->launches += (long)nSteps * c->graphKernels;
+}
+
+// energies of every trajectory (device), E of trajectory b at out_d + b*bs
+void energy_launch(cgpu_ctx* c, const z_t* state, double t) {
   const z_t* C = state;
   const z_t* orbs = (c->method == CGPU_METHOD_TDCI) ? c->tdciOrbs_d : state + c->nC;
   launch_ci_rdm(c, C, 1, 1);
@@ -570,18 +731,39 @@ double energy_device(cgpu_ctx* c, const z_t* state, double t) {
   launch_fill_h1_from(c, orbs, c->orbTmp_d, c->h1_d);
   launch_fill_h2(c, orbs);
   launch_energy(c, c->scal_d + 8);
+}
+
+double energy_device(cgpu_ctx* c, const z_t* state, double t) {
+  energy_launch(c, state, t);
   double e = 0.0;
   CODY_CUDA(cudaMemcpyAsync(&e, c->scal_d + 8, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CODY_CUDA(cudaStreamSynchronize(c->stream));
   return e;
 }
 
-// helpers for host <-> device staging
+// helpers for host <-> device staging (trajectory 0, contiguous)
 void up(cgpu_ctx* c, z_t* dst, const cgpu_complex* src, size_t n) {
   CODY_CUDA(cudaMemcpyAsync(dst, src, sizeof(z_t) * n, cudaMemcpyHostToDevice, c->stream));
 }
 void down(cgpu_ctx* c, cgpu_complex* dst, const z_t* src, size_t n) {
   CODY_CUDA(cudaMemcpyAsync(dst, src, sizeof(z_t) * n, cudaMemcpyDeviceToHost, c->stream));
+}
+// state vector of trajectory b ([C | orbitals], nS_b entries) <-> its device layout
+void up_state(cgpu_ctx* c, int b, z_t* dst0, const cgpu_complex* src) {
+  const SysHost& s = c->sys[b];
+  char* base = (char*)dst0 + (size_t)b * c->bs;
+  CODY_CUDA(cudaMemcpyAsync(base, src, sizeof(z_t) * s.nC, cudaMemcpyHostToDevice, c->stream));
+  if (s.nS > s.nC)
+    CODY_CUDA(cudaMemcpyAsync(base + sizeof(z_t) * c->nC, src + s.nC, sizeof(z_t) * (s.nS - s.nC),
+                              cudaMemcpyHostToDevice, c->stream));
+}
+void down_state(cgpu_ctx* c, int b, cgpu_complex* dst, const z_t* src0) {
+  const SysHost& s = c->sys[b];
+  const char* base = (const char*)src0 + (size_t)b * c->bs;
+  CODY_CUDA(cudaMemcpyAsync(dst, base, sizeof(z_t) * s.nC, cudaMemcpyDeviceToHost, c->stream));
+  if (s.nS > s.nC)
+    CODY_CUDA(cudaMemcpyAsync(dst + s.nC, base + sizeof(z_t) * c->nC, sizeof(z_t) * (s.nS - s.nC),
+                              cudaMemcpyDeviceToHost, c->stream));
 }
 void sync(cgpu_ctx* c) {
   CODY_CUDA(cudaStreamSynchronize(c->stream));
@@ -609,7 +791,39 @@ int fail(cgpu_ctx* c, const std::string& msg, int code) {
   }                                                                             \
   return CGPU_OK;
 
+cgpu_ctx* create_ctx(const cgpu_desc* descs, int n, int* rc) {
+  cgpu_ctx* c = new cgpu_ctx();
+  try {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      throw std::string("cuda: no CUDA device available");
+    }
+    build_ctx(c, descs, n);
+  } catch (const std::string& e) {
+    free_ctx(c);
+    delete c;
+    *rc = fail(nullptr, e, e.find("cuda") != std::string::npos ? CGPU_ERR_CUDA : CGPU_ERR_ARG);
+    return nullptr;
+  } catch (const std::exception& e) {
+    free_ctx(c);
+    delete c;
+    *rc = fail(nullptr, e.what(), CGPU_ERR_ARG);
+    return nullptr;
+  }
+  *rc = CGPU_OK;
+  return c;
+}
+
 }  // namespace
+
+void batch_zero(cgpu_ctx* c, void* p, size_t bytes) {
+  CODY_CUDA(cudaMemset2DAsync(p, c->bs, 0, bytes, c->nb, c->stream));
+}
+
+void batch_copy(cgpu_ctx* c, void* dst, const void* src, size_t bytes) {
+  CODY_CUDA(cudaMemcpy2DAsync(dst, c->bs, src, c->bs, bytes, c->nb, cudaMemcpyDeviceToDevice, c->stream));
+}
 
 // Records the message returned by cgpu_last_global_error (for entry points without a context).
 void cody_record_global_error(const std::string& msg) {
@@ -624,26 +838,9 @@ extern "C" {
 
 int cgpu_ctx_create(const cgpu_desc* desc, cgpu_ctx** out) {
   if (!desc || !out) return fail(nullptr, "cgpu_ctx_create: null argument", CGPU_ERR_ARG);
-  *out = nullptr;
-  cgpu_ctx* c = new cgpu_ctx();
-  try {
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-      cudaGetLastError();
-      throw std::string("cuda: no CUDA device available");
-    }
-    build_ctx(c, desc);
-  } catch (const std::string& e) {
-    free_ctx(c);
-    delete c;
-    return fail(nullptr, e, e.find("cuda") != std::string::npos ? CGPU_ERR_CUDA : CGPU_ERR_ARG);
-  } catch (const std::exception& e) {
-    free_ctx(c);
-    delete c;
-    return fail(nullptr, e.what(), CGPU_ERR_ARG);
-  }
-  *out = c;
-  return CGPU_OK;
+  int rc = CGPU_OK;
+  *out = create_ctx(desc, 1, &rc);
+  return rc;
 }
 
 int cgpu_ctx_destroy(cgpu_ctx* ctx) {
@@ -664,8 +861,9 @@ int cgpu_sizes(const cgpu_ctx* c, int* out) {
 
 int cgpu_grid(const cgpu_ctx* c, double* x, double* w) {
   if (!c) return CGPU_ERR_ARG;
-  if (x) std::memcpy(x, c->x.data(), sizeof(double) * c->nG);
-  if (w) std::memcpy(w, c->w.data(), sizeof(double) * c->nG);
+  const SysHost& s = c->sys[0];
+  if (x) std::memcpy(x, s.x.data(), sizeof(double) * s.nG);
+  if (w) std::memcpy(w, s.w.data(), sizeof(double) * s.nG);
   return CGPU_OK;
 }
 
@@ -673,7 +871,7 @@ int cgpu_configlist_tables(cgpu_ctx* c, int bt, int kind, int* n_conf, int* max_
                            int* n_connected, int* excited_c, int* orb_code, double* factor) {
   CODY_API_BEGIN(c)
   if (bt < 0 || bt >= c->nBt) throw std::string("configlist: body type out of range");
-  CiTables& t = c->tab[bt];
+  CiTables& t = c->sys[0].tab[bt];
   int mc = kind == 0 ? t.maxS : t.maxD;
   if (n_conf) *n_conf = t.nConf;
   if (max_conn) *max_conn = mc;
@@ -850,11 +1048,12 @@ int cgpu_project_orbs(cgpu_ctx* c, cgpu_complex* d_orbs, const cgpu_complex* orb
 
 int cgpu_orthonormalize_orbs(cgpu_ctx* c, cgpu_complex* orbs) {
   CODY_API_BEGIN(c)
+  const SysHost& s = c->sys[0];
   size_t n = (size_t)c->nG * c->nOS;
   up(c, c->orbTmp_d, orbs, n);
   if (c->restricted) launch_orthonormalize(c, c->orbTmp_d, 0, c->nOS);
   else
-    for (int b = 0; b < c->nBt; b++) launch_orthonormalize(c, c->orbTmp_d, c->orbStart[b], c->nOrbs[b]);
+    for (int b = 0; b < c->nBt; b++) launch_orthonormalize(c, c->orbTmp_d, s.orbStart[b], s.nOrbs[b]);
   down(c, orbs, c->orbTmp_d, n);
   int status = 0;
   CODY_CUDA(cudaMemcpyAsync(&status, c->scal_d, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -904,14 +1103,7 @@ int cgpu_propagate_split2(cgpu_ctx* c, cgpu_complex* state, double t0, double t1
   up(c, c->state_d, state, c->nS);
   if (krylov_dim > 0 && tolerance == 0.0 && max_restarts == 0) {
     // fixed-order SIL: the step has no host-side decisions, replay it as one graph
-    double dt = t1 - t0;
-    if (!c->stepGraph || c->graphDt != dt || c->graphKrylov != krylov_dim || c->graphMetric != use_metric ||
-        c->graphProf != c->profTarget)
-      capture_step_graph(c, t0, dt, krylov_dim, use_metric);
-    if (c->profTarget) c->profUsed = c->graphProfUsed;
-    CODY_CUDA(cudaMemcpyAsync(c->stepT_d, &t0, sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    CODY_CUDA(cudaGraphLaunch(c->stepGraph, c->stream));
-    c->launches += c->graphKernels;
+    propagate_graph(c, &t0, t1 - t0, 1, krylov_dim, use_metric);
   } else {
     split2_device(c, c->state_d, t0, t1, krylov_dim, tolerance, max_restarts, use_metric);
   }
@@ -922,14 +1114,14 @@ int cgpu_propagate_split2(cgpu_ctx* c, cgpu_complex* state, double t0, double t1
 
 int cgpu_state_upload(cgpu_ctx* c, const cgpu_complex* state) {
   CODY_API_BEGIN(c)
-  up(c, c->state_d, state, c->nS);
+  up_state(c, 0, c->state_d, state);
   sync(c);
   CODY_API_END(c)
 }
 
 int cgpu_state_download(cgpu_ctx* c, cgpu_complex* state) {
   CODY_API_BEGIN(c)
-  down(c, state, c->state_d, c->nS);
+  down_state(c, 0, state, c->state_d);
   sync(c);
   CODY_API_END(c)
 }
@@ -945,14 +1137,8 @@ int cgpu_propagate_resident(cgpu_ctx* c, double t0, double dt, int n_steps, int 
     }
     CODY_CUDA(cudaGetLastError());
   } else {
-    if (!c->stepGraph || c->graphDt != dt || c->graphKrylov != krylov_dim || c->graphMetric != use_metric ||
-        c->graphProf != c->profTarget) {
-      capture_step_graph(c, t0, dt, krylov_dim, use_metric);
-    }
-    if (c->profTarget) c->profUsed = c->graphProfUsed;
-    CODY_CUDA(cudaMemcpyAsync(c->stepT_d, &t0, sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    for (int s = 0; s < n_steps; s++) CODY_CUDA(cudaGraphLaunch(c->stepGraph, c->stream));
-    c->launches += n_steps * c->graphKernels;
+    std::vector<double> t0s(c->nb, t0);
+    propagate_graph(c, t0s.data(), dt, n_steps, krylov_dim, use_metric);
   }
   CODY_API_END(c)
 }
@@ -1022,121 +1208,147 @@ int cgpu_tdci_set_orbitals(cgpu_ctx* c, const cgpu_complex* orbs) {
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
-// Batched trajectories: one context per trajectory; the step graph of every
-// context is a child node (no dependencies between them) of one batch graph.
+// Batched trajectories: one context with nb systems; every launch of the step
+// covers all of them, and the step is replayed as one CUDA graph.
 // ---------------------------------------------------------------------------
 struct cgpu_batch {
-  std::vector<cgpu_ctx*> ctx;
-  cudaStream_t stream = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  double dt = 0.0;
-  int krylov = -1, metric = -1;
-  long kernelsPerStep = 0;
-  std::vector<double> t0;  // start times the graph was last launched from
+  cgpu_ctx* c = nullptr;
 };
 
 namespace {
-void batch_free_graph(cgpu_batch* b) {
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  if (b->graph) cudaGraphDestroy(b->graph);
-  b->exec = nullptr;
-  b->graph = nullptr;
-  b->kernelsPerStep = 0;
+cgpu_ctx* bctx(const cgpu_batch* b) {
+  if (!b || !b->c) throw std::string("null batch");
+  return b->c;
 }
 
-void batch_build_graph(cgpu_batch* b, const double* t0, double dt, int krylov, int useMetric) {
-  batch_free_graph(b);
-  CODY_CUDA(cudaGraphCreate(&b->graph, 0));
-  for (size_t i = 0; i < b->ctx.size(); i++) {
-    cgpu_ctx* c = b->ctx[i];
-    c->profTarget = 0;
-    capture_step_graph(c, t0[i], dt, krylov, useMetric);
-    cudaGraphNode_t node;
-    CODY_CUDA(cudaGraphAddChildGraphNode(&node, b->graph, nullptr, 0, c->stepGraphRaw));
-    b->kernelsPerStep += c->graphKernels;
-  }
-  CODY_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
-  b->dt = dt;
-  b->krylov = krylov;
-  b->metric = useMetric;
+// device staging area for packed host states (all trajectories, nS_b each)
+void ensure_stage(cgpu_ctx* c) {
+  size_t need = (size_t)c->stageOff.back();
+  if (c->stage_d && c->stageCap >= need) return;
+  if (c->stage_d) cudaFree(c->stage_d);
+  c->stage_d = nullptr;
+  CODY_CUDA(cudaMalloc(&c->stage_d, sizeof(z_t) * std::max<size_t>(need, 1)));
+  c->stageCap = need;
 }
 }  // namespace
 
-#define CODY_BATCH_BEGIN(b)                                          \
-  if (!(b)) return fail(nullptr, "null batch", CGPU_ERR_ARG);        \
-  try {
+#define CODY_BATCH_BEGIN(b) \
+  cgpu_ctx* c_ = nullptr;   \
+  try {                     \
+    c_ = bctx(b);
+#define CODY_BATCH_END CODY_API_END(c_)
 
 extern "C" {
 
 int cgpu_batch_create(const cgpu_desc* descs, int n, cgpu_batch** out) {
   if (!descs || !out || n <= 0) return fail(nullptr, "cgpu_batch_create: bad argument", CGPU_ERR_ARG);
+  if (n > 65535) return fail(nullptr, "cgpu_batch_create: at most 65535 systems", CGPU_ERR_ARG);
   *out = nullptr;
+  int rc = CGPU_OK;
+  cgpu_ctx* c = create_ctx(descs, n, &rc);
+  if (!c) return rc;
   cgpu_batch* b = new cgpu_batch();
-  for (int i = 0; i < n; i++) {
-    cgpu_ctx* c = nullptr;
-    int rc = cgpu_ctx_create(&descs[i], &c);
-    if (rc != CGPU_OK) {
-      std::string msg = "batch trajectory " + std::to_string(i) + ": " + g_lastGlobalError;
-      cgpu_batch_destroy(b);
-      return fail(nullptr, msg, rc);
-    }
-    b->ctx.push_back(c);
-  }
-  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
-    cgpu_batch_destroy(b);
-    return fail(nullptr, "cuda: batch stream creation failed", CGPU_ERR_CUDA);
-  }
+  b->c = c;
   *out = b;
   return CGPU_OK;
 }
 
 int cgpu_batch_destroy(cgpu_batch* b) {
   if (!b) return CGPU_OK;
-  if (b->stream) cudaStreamSynchronize(b->stream);
-  batch_free_graph(b);
-  if (b->stream) cudaStreamDestroy(b->stream);
-  for (cgpu_ctx* c : b->ctx) cgpu_ctx_destroy(c);
+  if (b->c) cgpu_ctx_destroy(b->c);
   delete b;
   return CGPU_OK;
 }
 
-int cgpu_batch_size(const cgpu_batch* b) { return b ? (int)b->ctx.size() : 0; }
+int cgpu_batch_size(const cgpu_batch* b) { return (b && b->c) ? b->c->nb : 0; }
 
-cgpu_ctx* cgpu_batch_context(cgpu_batch* b, int i) {
-  if (!b || i < 0 || i >= (int)b->ctx.size()) return nullptr;
-  return b->ctx[i];
+int cgpu_batch_sizes(const cgpu_batch* b, int i, int* out) {
+  if (!b || !b->c || !out || i < 0 || i >= b->c->nb) return CGPU_ERR_ARG;
+  const SysHost& s = b->c->sys[i];
+  out[0] = s.nG; out[1] = s.nO; out[2] = s.nOS; out[3] = s.nC; out[4] = b->c->nBt; out[5] = s.nS;
+  return CGPU_OK;
 }
 
-long cgpu_batch_kernels_per_step(const cgpu_batch* b) { return b ? b->kernelsPerStep : 0; }
+int cgpu_batch_grid(const cgpu_batch* b, int i, double* x, double* w) {
+  if (!b || !b->c || i < 0 || i >= b->c->nb) return CGPU_ERR_ARG;
+  const SysHost& s = b->c->sys[i];
+  if (x) std::memcpy(x, s.x.data(), sizeof(double) * s.nG);
+  if (w) std::memcpy(w, s.w.data(), sizeof(double) * s.nG);
+  return CGPU_OK;
+}
+
+int cgpu_batch_upload(cgpu_batch* b, const cgpu_complex* states) {
+  CODY_BATCH_BEGIN(b)
+  cgpu_ctx* c = c_;
+  ensure_stage(c);
+  CODY_CUDA(cudaMemcpyAsync(c->stage_d, states, sizeof(z_t) * c->stageOff.back(), cudaMemcpyHostToDevice, c->stream));
+  k_scatter_states<<<bgrid(c, 64), 256, 0, c->stream>>>(c->state_d, c->stage_d, c->stageOff_d, TRAJ_PASS(c));
+  CODY_LAUNCHED(c);
+  sync(c);
+  CODY_BATCH_END
+}
+
+int cgpu_batch_download(cgpu_batch* b, cgpu_complex* states) {
+  CODY_BATCH_BEGIN(b)
+  cgpu_ctx* c = c_;
+  ensure_stage(c);
+  k_gather_states<<<bgrid(c, 64), 256, 0, c->stream>>>(c->stage_d, c->state_d, c->stageOff_d, TRAJ_PASS(c));
+  CODY_LAUNCHED(c);
+  CODY_CUDA(cudaMemcpyAsync(states, c->stage_d, sizeof(z_t) * c->stageOff.back(), cudaMemcpyDeviceToHost, c->stream));
+  sync(c);
+  CODY_BATCH_END
+}
 
 int cgpu_batch_propagate(cgpu_batch* b, const double* t0, double dt, int n_steps, int krylov_dim, int use_metric,
                          double* elapsed_ms) {
   CODY_BATCH_BEGIN(b)
+  cgpu_ctx* c = c_;
   if (!t0 || n_steps < 0 || krylov_dim <= 0) throw std::string("batch_propagate: bad argument");
-  // uploads and other work queued on the contexts' own streams come first
-  for (cgpu_ctx* c : b->ctx) CODY_CUDA(cudaStreamSynchronize(c->stream));
-  if (!b->exec || b->dt != dt || b->krylov != krylov_dim || b->metric != use_metric)
-    batch_build_graph(b, t0, dt, krylov_dim, use_metric);
-  for (size_t i = 0; i < b->ctx.size(); i++)
-    CODY_CUDA(cudaMemcpyAsync(b->ctx[i]->stepT_d, &t0[i], sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  if (!c->stepGraph || c->graphDt != dt || c->graphKrylov != krylov_dim || c->graphMetric != use_metric ||
+      c->graphProf != c->profTarget) {
+    set_step_times(c, t0);
+    capture_step_graph(c, t0[0], dt, krylov_dim, use_metric);
+  }
   cudaEvent_t e0, e1;
   CODY_CUDA(cudaEventCreate(&e0));
   CODY_CUDA(cudaEventCreate(&e1));
-  CODY_CUDA(cudaEventRecord(e0, b->stream));
-  for (int s = 0; s < n_steps; s++) CODY_CUDA(cudaGraphLaunch(b->exec, b->stream));
-  CODY_CUDA(cudaEventRecord(e1, b->stream));
+  set_step_times(c, t0);
+  CODY_CUDA(cudaEventRecord(e0, c->stream));
+  for (int s = 0; s < n_steps; s++) CODY_CUDA(cudaGraphLaunch(c->stepGraph, c->stream));
+  c->launches += (long)n_steps * c->graphKernels;
+  CODY_CUDA(cudaEventRecord(e1, c->stream));
   CODY_CUDA(cudaEventSynchronize(e1));
   float ms = 0.f;
   CODY_CUDA(cudaEventElapsedTime(&ms, e0, e1));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (elapsed_ms) *elapsed_ms = ms;
-  for (cgpu_ctx* c : b->ctx) {
-    c->launches += n_steps * c->graphKernels;
-    if (c->mixed && mixed_error(c)) throw std::string("tensor-core GEMM: a bounded mbarrier wait expired");
-  }
-  CODY_API_END(nullptr)
+  sync(c);
+  CODY_BATCH_END
 }
+
+int cgpu_batch_energies(cgpu_batch* b, const double* t, double* energies) {
+  CODY_BATCH_BEGIN(b)
+  cgpu_ctx* c = c_;
+  if (!t || !energies) throw std::string("batch_energies: null array");
+  // E(t_b) per trajectory: the field reads the per-trajectory time slots
+  set_step_times(c, t);
+  c->useStepTime = 1;
+  try {
+    energy_launch(c, c->state_d, 0.0);
+  } catch (...) {
+    c->useStepTime = 0;
+    throw;
+  }
+  c->useStepTime = 0;
+  CODY_CUDA(cudaMemcpy2DAsync(energies, sizeof(double), c->scal_d + 8, c->bs, sizeof(double), c->nb,
+                              cudaMemcpyDeviceToHost, c->stream));
+  sync(c);
+  CODY_BATCH_END
+}
+
+long cgpu_batch_kernels_per_step(const cgpu_batch* b) { return (b && b->c) ? b->c->graphKernels : 0; }
+
+long cgpu_batch_launch_count(cgpu_batch* b, int reset) { return (b && b->c) ? cgpu_launch_count(b->c, reset) : -1; }
 
 }  // extern "C"

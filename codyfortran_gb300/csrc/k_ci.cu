@@ -14,6 +14,7 @@
 //   * h1/h2 folding and RDM unfolding (FillH1Lin :440-464, FillH2Lin :478-542,
 //     FillRdm1FromRdm1Lin :325-349, FillRdm2FromRdm2Lin :362-434).
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -125,11 +126,16 @@ __device__ __forceinline__ z_t warp_sum(z_t a) {
   return a;
 }
 
-__global__ void k_ci_apply(CiView v, const z_t* __restrict__ C, z_t* __restrict__ dC, const z_t* __restrict__ h1Lin,
-                           const z_t* __restrict__ h2Lin, int useH1, int useH2) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void k_ci_apply(const z_t* __restrict__ C, z_t* __restrict__ dC, const z_t* __restrict__ h1Lin,
+                           const z_t* __restrict__ h2Lin, TRAJ_ARGS, int useH1, int useH2) {
+  const CiView& v = shp[blockIdx.z].view;
   int lane = threadIdx.x & 31;
-  if (warp >= v.nC) return;
+  C = bat(C, bs);
+  dC = bat(dC, bs);
+  h1Lin = bat(h1Lin, bs);
+  h2Lin = bat(h2Lin, bs);
+  const int nWarps = (gridDim.x * blockDim.x) >> 5;
+  for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < v.nC; warp += nWarps) {
   int I = warp + 1;
   int conf[CODY_MAX_BT];
   conf_from_index(v, I, conf);
@@ -159,7 +165,8 @@ __global__ void k_ci_apply(CiView v, const z_t* __restrict__ C, z_t* __restrict_
         if (v.dFac[b][col + k] < 0) hc = zmk(-hc.x, -hc.y);
         acc = zadd(acc, hc);
       }
-      // inter-body-type terms: products of singles on b and b2 > b (Generic :266-300)
+      // inter-body-type terms: products of singles on b and b2 > b (Generic :266-300).
+      // Lane k2 holds an edge of b2, the edges of b are broadcast one by one.
       int n1 = v.sN[b][c - 1];
       size_t col1 = (size_t)v.maxS[b] * (c - 1);
       for (int b2 = b + 1; b2 < v.nBt; b2++) {
@@ -167,87 +174,144 @@ __global__ void k_ci_apply(CiView v, const z_t* __restrict__ C, z_t* __restrict_
         int n2 = v.sN[b2][c2 - 1];
         size_t col2 = (size_t)v.maxS[b2] * (c2 - 1);
         int st2 = v.stride[b2];
-        for (int t = lane; t < n1 * n2; t += 32) {
-          int k1 = t / n2, k2 = t % n2;
-          int oc = (v.sCode[b][col1 + k1] - 1) * nO2 + v.sCode[b2][col2 + k2];
-          int jG = I + (v.sExc[b][col1 + k1] - c) * st + (v.sExc[b2][col2 + k2] - c2) * st2;
-          z_t hc = zmul(h2Lin[oc], C[jG - 1]);
-          if ((v.sFac[b][col1 + k1] * v.sFac[b2][col2 + k2]) < 0) hc = zmk(-hc.x, -hc.y);
-          acc = zadd(acc, hc);
+        for (int k2b = 0; k2b < n2; k2b += 32) {
+          int k2 = k2b + lane;
+          bool has2 = k2 < n2;
+          int oc2 = has2 ? v.sCode[b2][col2 + k2] : 0;
+          int d2 = has2 ? (v.sExc[b2][col2 + k2] - c2) * st2 : 0;
+          int f2 = has2 ? v.sFac[b2][col2 + k2] : 0;
+          for (int k1b = 0; k1b < n1; k1b += 32) {
+            int k1 = k1b + lane;
+            int oc1 = 0, d1 = 0, f1 = 0;
+            if (k1 < n1) {
+              oc1 = v.sCode[b][col1 + k1];
+              d1 = (v.sExc[b][col1 + k1] - c) * st;
+              f1 = v.sFac[b][col1 + k1];
+            }
+            int cnt = min(32, n1 - k1b);
+            for (int u = 0; u < cnt; u++) {
+              int o1 = __shfl_sync(0xffffffffu, oc1, u);
+              int e1 = __shfl_sync(0xffffffffu, d1, u);
+              int g1 = __shfl_sync(0xffffffffu, f1, u);
+              if (has2) {
+                z_t hc = zmul(h2Lin[(o1 - 1) * nO2 + oc2], C[I - 1 + e1 + d2]);
+                if (g1 * f2 < 0) hc = zmk(-hc.x, -hc.y);
+                acc = zadd(acc, hc);
+              }
+            }
+          }
         }
       }
     }
   }
   acc = warp_sum(acc);
   if (lane == 0) dC[warp] = zadd(dC[warp], acc);
+  }
 }
 
-__device__ __forceinline__ void atomic_zadd(z_t* p, z_t v) {
-  atomicAdd(&p->x, v.x);
-  atomicAdd(&p->y, v.y);
-}
-
-__global__ void k_ci_rdm(CiView v, const z_t* __restrict__ C, z_t* __restrict__ r1Lin, z_t* __restrict__ r2Lin,
-                         int want1, int want2) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (warp >= v.nC) return;
-  int I = warp + 1;
-  int conf[CODY_MAX_BT];
-  conf_from_index(v, I, conf);
-  z_t cI = C[warp];
-  if (cI.x == 0.0 && cI.y == 0.0) return;  // every contribution carries the factor C_I
-  int nO2 = v.nO * v.nO;
+// Configuration index (0-based) of the body types other than b1 and b2 (b2 < 0:
+// only b1 excluded), from r in mixed radix over those body types.
+__device__ __forceinline__ int rest_base(const CiView& v, int r, int b1, int b2) {
+  int I = 0;
   for (int b = 0; b < v.nBt; b++) {
-    int c = conf[b];
-    int st = v.stride[b];
-    if (want1) {
-      int n = v.sN[b][c - 1];
-      size_t col = (size_t)v.maxS[b] * (c - 1);
-      for (int k = lane; k < n; k += 32) {
-        int oc = v.sCode[b][col + k];
-        int jG = I + (v.sExc[b][col + k] - c) * st;
-        z_t r = zcmul(C[jG - 1], cI);
-        if (v.sFac[b][col + k] < 0) r = zmk(-r.x, -r.y);
-        atomic_zadd(&r1Lin[oc], r);
+    if (b == b1 || b == b2) continue;
+    int n = v.nConf[b];
+    I += (r % n) * v.stride[b];
+    r /= n;
+  }
+  return I;
+}
+
+// RDMs (ApplyH1FillRdm1 / ApplyH2FillRdm2, S_Coeffs_Generic.f90:103-319) as
+// gathers: rdmLin(oc) = sum over the excitations (I -> J) with orbital code
+// oc of f conj(C_J) C_I.  One warp per code (within a body type) or per pair
+// of codes (singles of two body types, the inter-body-type part of rdm2);
+// every entry has exactly one writer, so there are no atomics.
+__global__ void k_ci_rdm(const z_t* __restrict__ C, z_t* __restrict__ r1Lin, z_t* __restrict__ r2Lin, TRAJ_ARGS,
+                         int want1, int want2) {
+  const CiView& v = shp[blockIdx.z].view;
+  const int lane = threadIdx.x & 31;
+  C = bat(C, bs);
+  r1Lin = bat(r1Lin, bs);
+  r2Lin = bat(r2Lin, bs);
+  int nS = 0, nD = 0, nX = 0;
+  for (int b = 0; b < v.nBt; b++) {
+    nS += v.nSc[b];
+    nD += v.nDc[b];
+    for (int b2 = b + 1; b2 < v.nBt; b2++) nX += v.nSc[b] * v.nSc[b2];
+  }
+  const int nT = (want1 ? nS : 0) + (want2 ? nD + nX : 0);
+  const int nO2 = v.nO * v.nO;
+  const int nWarps = (gridDim.x * blockDim.x) >> 5;
+  for (int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < nT; task += nWarps) {
+    int q = task;
+    z_t acc = zmk(0.0, 0.0);
+    z_t* out;
+    int idx;
+    int kind;  // 0 singles, 1 doubles, 2 inter
+    if (!want1) q += nS;
+    if (q < nS) kind = 0;
+    else if ((q -= nS) < nD) kind = 1;
+    else { q -= nD; kind = 2; }
+    if (kind < 2) {
+      int b = 0;
+      const int* cnt = kind == 0 ? v.nSc : v.nDc;
+      while (q >= cnt[b]) q -= cnt[b++];
+      const int* start = kind == 0 ? v.sxStart[b] : v.dxStart[b];
+      const int* src = kind == 0 ? v.sxSrc[b] : v.dxSrc[b];
+      const int* dst = kind == 0 ? v.sxDst[b] : v.dxDst[b];
+      const int8_t* fac = kind == 0 ? v.sxFac[b] : v.dxFac[b];
+      int e0 = start[q], ne = start[q + 1] - e0;
+      int nRest = v.nC / v.nConf[b], st = v.stride[b];
+      for (int t = lane; t < ne * nRest; t += 32) {
+        int e = e0 + t / nRest, r = t % nRest;
+        int base = rest_base(v, r, b, -1);
+        z_t val = zcmul(C[base + dst[e] * st], C[base + src[e] * st]);
+        if (fac[e] < 0) val = zmk(-val.x, -val.y);
+        acc = zadd(acc, val);
       }
+      out = kind == 0 ? r1Lin : r2Lin;
+      idx = kind == 0 ? v.sxCode[b][q] : v.dxCode[b][q];
+    } else {
+      int b1 = 0, b2 = 1;
+      for (;;) {
+        int seg = v.nSc[b1] * v.nSc[b2];
+        if (q < seg) break;
+        q -= seg;
+        if (++b2 >= v.nBt) { b1++; b2 = b1 + 1; }
+      }
+      int q1 = q / v.nSc[b2], q2 = q % v.nSc[b2];
+      int s1 = v.sxStart[b1][q1], n1 = v.sxStart[b1][q1 + 1] - s1;
+      int s2 = v.sxStart[b2][q2], n2 = v.sxStart[b2][q2 + 1] - s2;
+      int st1 = v.stride[b1], st2 = v.stride[b2];
+      int nRest = v.nC / (v.nConf[b1] * v.nConf[b2]);
+      for (int t = lane; t < n1 * n2 * nRest; t += 32) {
+        int r = t % nRest, u = t / nRest;
+        int e1 = s1 + u / n2, e2 = s2 + u % n2;
+        int base = rest_base(v, r, b1, b2);
+        int I = base + v.sxSrc[b1][e1] * st1 + v.sxSrc[b2][e2] * st2;
+        int J = base + v.sxDst[b1][e1] * st1 + v.sxDst[b2][e2] * st2;
+        z_t val = zcmul(C[J], C[I]);
+        if (v.sxFac[b1][e1] * v.sxFac[b2][e2] < 0) val = zmk(-val.x, -val.y);
+        acc = zadd(acc, val);
+      }
+      out = r2Lin;
+      idx = (v.sxCode[b1][q1] - 1) * nO2 + v.sxCode[b2][q2];
     }
-    if (want2) {
-      int n = v.dN[b][c - 1];
-      size_t col = (size_t)v.maxD[b] * (c - 1);
-      for (int k = lane; k < n; k += 32) {
-        int oc = v.dCode[b][col + k];
-        int jG = I + (v.dExc[b][col + k] - c) * st;
-        z_t r = zcmul(C[jG - 1], cI);
-        if (v.dFac[b][col + k] < 0) r = zmk(-r.x, -r.y);
-        atomic_zadd(&r2Lin[oc], r);
-      }
-      int n1 = v.sN[b][c - 1];
-      size_t col1 = (size_t)v.maxS[b] * (c - 1);
-      for (int b2 = b + 1; b2 < v.nBt; b2++) {
-        int c2 = conf[b2];
-        int n2 = v.sN[b2][c2 - 1];
-        size_t col2 = (size_t)v.maxS[b2] * (c2 - 1);
-        int st2 = v.stride[b2];
-        for (int t = lane; t < n1 * n2; t += 32) {
-          int k1 = t / n2, k2 = t % n2;
-          int oc = (v.sCode[b][col1 + k1] - 1) * nO2 + v.sCode[b2][col2 + k2];
-          int jG = I + (v.sExc[b][col1 + k1] - c) * st + (v.sExc[b2][col2 + k2] - c2) * st2;
-          z_t r = zcmul(C[jG - 1], cI);
-          if ((v.sFac[b][col1 + k1] * v.sFac[b2][col2 + k2]) < 0) r = zmk(-r.x, -r.y);
-          atomic_zadd(&r2Lin[oc], r);
-        }
-      }
-    }
+    acc = warp_sum(acc);
+    if (lane == 0) out[idx] = acc;
   }
 }
 
 // FillH1Lin: h1Lin((i1-1)*nO + j1) = h1(i1, j1)
-__global__ void k_fold_h1(z_t* __restrict__ h1Lin, const z_t* __restrict__ h1, int nO) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nO * nO) return;
-  int i1 = e % nO, j1 = e / nO;  // 0-based
-  h1Lin[i1 * nO + j1 + 1] = h1[e];
+__global__ void k_fold_h1(z_t* __restrict__ h1Lin, const z_t* __restrict__ h1, TRAJ_ARGS) {
+  const int nO = shp[blockIdx.z].nO;
+  h1Lin = bat(h1Lin, bs);
+  h1 = bat(h1, bs);
+  GRID_STRIDE(e, nO * nO) {
+    int i1 = (int)(e % nO), j1 = (int)(e / nO);  // 0-based
+    h1Lin[i1 * nO + j1 + 1] = h1[e];
+  }
 }
 
 __device__ __forceinline__ bool bt_rule_ok(const int* btOf, int i1, int i2, int j1, int j2) {
@@ -258,43 +322,102 @@ __device__ __forceinline__ bool bt_rule_ok(const int* btOf, int i1, int i2, int 
 }
 
 // FillH2Lin (fermions; inter-body-type pairs use the same antisymmetric form)
-__global__ void k_fold_h2(z_t* __restrict__ h2Lin, const z_t* __restrict__ h2, const int* __restrict__ btOf, int nO) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+__global__ void k_fold_h2(z_t* __restrict__ h2Lin, const z_t* __restrict__ h2, const int* __restrict__ btOf,
+                          TRAJ_ARGS) {
+  const int nO = shp[blockIdx.z].nO;
   size_t n4 = (size_t)nO * nO * nO * nO;
-  if (e >= n4) return;
-  // e = orbCode - 1 with orbCode = (((i1-1) nO + j1 - 1) nO + i2 - 1) nO + j2
-  int j2 = (int)(e % nO), i2 = (int)((e / nO) % nO), j1 = (int)((e / nO / nO) % nO), i1 = (int)(e / nO / nO / nO);
-  z_t v = zmk(0.0, 0.0);
-  if (i1 <= i2 && j1 <= j2 && bt_rule_ok(btOf, i1, i2, j1, j2) && i1 != i2 && j1 != j2) {
-    size_t n = nO;
-    auto H = [&](int a, int b, int c, int d) { return h2[a + n * (b + n * (c + n * d))]; };
-    v = zadd(zsub(zsub(H(i1, i2, j1, j2), H(i1, i2, j2, j1)), H(i2, i1, j1, j2)), H(i2, i1, j2, j1));
+  h2Lin = bat(h2Lin, bs);
+  h2 = bat(h2, bs);
+  btOf = bat(btOf, bs);
+  GRID_STRIDE(e, n4) {
+    // e = orbCode - 1 with orbCode = (((i1-1) nO + j1 - 1) nO + i2 - 1) nO + j2
+    int j2 = (int)(e % nO), i2 = (int)((e / nO) % nO), j1 = (int)((e / nO / nO) % nO), i1 = (int)(e / nO / nO / nO);
+    z_t v = zmk(0.0, 0.0);
+    if (i1 <= i2 && j1 <= j2 && bt_rule_ok(btOf, i1, i2, j1, j2) && i1 != i2 && j1 != j2) {
+      size_t n = nO;
+      auto H = [&](int a, int b, int c, int d) { return h2[a + n * (b + n * (c + n * d))]; };
+      v = zadd(zsub(zsub(H(i1, i2, j1, j2), H(i1, i2, j2, j1)), H(i2, i1, j1, j2)), H(i2, i1, j2, j1));
+    }
+    h2Lin[e + 1] = v;
   }
-  h2Lin[e + 1] = v;
 }
 
-__global__ void k_unfold_rdm1(z_t* __restrict__ rdm1, const z_t* __restrict__ lin, int nO) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nO * nO) return;
-  int i1 = e % nO, j1 = e / nO;
-  rdm1[e] = lin[i1 * nO + j1 + 1];
+__global__ void k_unfold_rdm1(z_t* __restrict__ rdm1, const z_t* __restrict__ lin, TRAJ_ARGS) {
+  const int nO = shp[blockIdx.z].nO;
+  rdm1 = bat(rdm1, bs);
+  lin = bat(lin, bs);
+  GRID_STRIDE(e, nO * nO) {
+    int i1 = (int)(e % nO), j1 = (int)(e / nO);
+    rdm1[e] = lin[i1 * nO + j1 + 1];
+  }
 }
 
 // FillRdm2FromRdm2Lin written per output element: rdm2(a,b,c,d) gathers the
 // (up to four) signed lin entries the reference scatters into it.
 __global__ void k_unfold_rdm2(z_t* __restrict__ rdm2, const z_t* __restrict__ lin, const int* __restrict__ btOf,
-                              int nO) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  size_t n = nO;
-  if (e >= n * n * n * n) return;
-  int a = (int)(e % n), b = (int)((e / n) % n), c = (int)((e / n / n) % n), d = (int)(e / n / n / n);
-  auto L = [&](int i1, int j1, int i2, int j2) { return lin[(((size_t)i1 * n + j1) * n + i2) * n + j2 + 1]; };
-  z_t s = zmk(0.0, 0.0);
-  if (a <= b && c <= d && bt_rule_ok(btOf, a, b, c, d)) s = zadd(s, L(a, c, b, d));
-  if (b <= a && c <= d && bt_rule_ok(btOf, b, a, c, d)) s = zsub(s, L(b, c, a, d));
-  if (a <= b && d <= c && bt_rule_ok(btOf, a, b, d, c)) s = zsub(s, L(a, d, b, c));
-  if (b <= a && d <= c && bt_rule_ok(btOf, b, a, d, c)) s = zadd(s, L(b, d, a, c));
-  rdm2[e] = s;
+                              TRAJ_ARGS) {
+  size_t n = shp[blockIdx.z].nO;
+  rdm2 = bat(rdm2, bs);
+  lin = bat(lin, bs);
+  btOf = bat(btOf, bs);
+  GRID_STRIDE(e, n * n * n * n) {
+    int a = (int)(e % n), b = (int)((e / n) % n), c = (int)((e / n / n) % n), d = (int)(e / n / n / n);
+    auto L = [&](int i1, int j1, int i2, int j2) { return lin[(((size_t)i1 * n + j1) * n + i2) * n + j2 + 1]; };
+    z_t s = zmk(0.0, 0.0);
+    if (a <= b && c <= d && bt_rule_ok(btOf, a, b, c, d)) s = zadd(s, L(a, c, b, d));
+    if (b <= a && c <= d && bt_rule_ok(btOf, b, a, c, d)) s = zsub(s, L(b, c, a, d));
+    if (a <= b && d <= c && bt_rule_ok(btOf, a, b, d, c)) s = zsub(s, L(a, d, b, c));
+    if (b <= a && d <= c && bt_rule_ok(btOf, b, a, d, c)) s = zadd(s, L(b, d, a, c));
+    rdm2[e] = s;
+  }
+}
+
+// Groups an excitation table (maxConn x nConf, on the device) by orbital code:
+// distinct codes ascending, edges of one code in table order.
+void group_by_code(int nConf, int maxConn, const int* nConn_d, const int* exc_d, const int* code_d,
+                   const int8_t* fac_d, int& nCodes, int*& xCode, int*& xStart, int*& xSrc, int*& xDst,
+                   int8_t*& xFac) {
+  std::vector<int> n(nConf), exc((size_t)maxConn * nConf), code((size_t)maxConn * nConf);
+  std::vector<int8_t> fac((size_t)maxConn * nConf);
+  CODY_CUDA(cudaMemcpy(n.data(), nConn_d, sizeof(int) * nConf, cudaMemcpyDeviceToHost));
+  CODY_CUDA(cudaMemcpy(exc.data(), exc_d, sizeof(int) * exc.size(), cudaMemcpyDeviceToHost));
+  CODY_CUDA(cudaMemcpy(code.data(), code_d, sizeof(int) * code.size(), cudaMemcpyDeviceToHost));
+  CODY_CUDA(cudaMemcpy(fac.data(), fac_d, fac.size(), cudaMemcpyDeviceToHost));
+  std::vector<int> codes;
+  size_t E = 0;
+  for (int c = 0; c < nConf; c++) E += n[c];
+  codes.reserve(E);
+  for (int c = 0; c < nConf; c++)
+    for (int k = 0; k < n[c]; k++) codes.push_back(code[(size_t)maxConn * c + k]);
+  std::sort(codes.begin(), codes.end());
+  codes.erase(std::unique(codes.begin(), codes.end()), codes.end());
+  nCodes = (int)codes.size();
+  std::vector<int> start(nCodes + 1, 0), src(std::max<size_t>(E, 1)), dst(std::max<size_t>(E, 1));
+  std::vector<int8_t> f(std::max<size_t>(E, 1));
+  auto slot = [&](int oc) { return (int)(std::lower_bound(codes.begin(), codes.end(), oc) - codes.begin()); };
+  for (int c = 0; c < nConf; c++)
+    for (int k = 0; k < n[c]; k++) start[slot(code[(size_t)maxConn * c + k]) + 1]++;
+  for (int q = 0; q < nCodes; q++) start[q + 1] += start[q];
+  std::vector<int> fill(start.begin(), start.end() - 1);
+  for (int c = 0; c < nConf; c++)
+    for (int k = 0; k < n[c]; k++) {
+      size_t at = (size_t)maxConn * c + k;
+      int e = fill[slot(code[at])]++;
+      src[e] = c;
+      dst[e] = exc[at] - 1;
+      f[e] = fac[at];
+    }
+  auto upload = [](auto& dptr, const auto& v) {
+    using T = typename std::remove_reference<decltype(v)>::type::value_type;
+    CODY_CUDA(cudaMalloc(&dptr, sizeof(T) * std::max<size_t>(v.size(), 1)));
+    if (!v.empty()) CODY_CUDA(cudaMemcpy(dptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  };
+  if (codes.empty()) codes.push_back(0);
+  upload(xCode, codes);
+  upload(xStart, start);
+  upload(xSrc, src);
+  upload(xDst, dst);
+  upload(xFac, f);
 }
 
 long long binom_h(int n, int k) {
@@ -306,17 +429,18 @@ long long binom_h(int n, int k) {
 
 }  // namespace
 
-// ConfigList_Setup: codes in GSL lexicographic order on the host, tables on the device.
-void ci_build_tables(cgpu_ctx* c) {
-  c->view.nBt = c->nBt;
-  c->view.nO = c->nO;
+// ConfigList_Setup for one system: codes in GSL lexicographic order on the
+// host, tables on the device (separate allocations, referenced by s.view).
+void ci_build_tables(cgpu_ctx* c, SysHost& s) {
+  s.view.nBt = c->nBt;
+  s.view.nO = s.nO;
   int stride = 1;
   for (int b = 0; b < c->nBt; b++) {
-    CiTables& t = c->tab[b];
-    int M = c->nOrbs[b], N = c->nBodies[b];
+    CiTables& t = s.tab[b];
+    int M = s.nOrbs[b], N = s.nBodies[b];
     t.nOrbs = M;
     t.nBodies = N;
-    t.shift = c->orbStart[b];
+    t.shift = s.orbStart[b];
     if (M > 63 || N > M) throw std::string("ConfigList: unsupported orbital/body counts");
     long long nconf = 0;
     for (int k = 0; k <= N; k++) nconf += binom_h(M - N, k) * binom_h(N, k);
@@ -352,7 +476,7 @@ void ci_build_tables(cgpu_ctx* c) {
     int blocks = (t.nConf * 32 + threads - 1) / threads;
     for (int kind = 0; kind < 2; kind++) {
       int* nConn = kind == 0 ? t.sN : t.dN;
-      k_build_tables<<<blocks, threads, 0, c->stream>>>(kind, 0, t.codes, t.nConf, M, c->nO, t.shift, t.rankTab,
+      k_build_tables<<<blocks, threads, 0, c->stream>>>(kind, 0, t.codes, t.nConf, M, s.nO, t.shift, t.rankTab,
                                                          rankBase, nConn, 0, nullptr, nullptr, nullptr);
       CODY_LAUNCHED(c);
       std::vector<int> h(t.nConf);
@@ -368,12 +492,21 @@ void ci_build_tables(cgpu_ctx* c) {
       CODY_CUDA(cudaMemsetAsync(*exc, 0, sizeof(int) * (size_t)mxa * t.nConf, c->stream));
       CODY_CUDA(cudaMemsetAsync(*oc, 0, sizeof(int) * (size_t)mxa * t.nConf, c->stream));
       CODY_CUDA(cudaMemsetAsync(*fac, 0, sizeof(int8_t) * (size_t)mxa * t.nConf, c->stream));
-      k_build_tables<<<blocks, threads, 0, c->stream>>>(kind, 1, t.codes, t.nConf, M, c->nO, t.shift, t.rankTab,
+      k_build_tables<<<blocks, threads, 0, c->stream>>>(kind, 1, t.codes, t.nConf, M, s.nO, t.shift, t.rankTab,
                                                          rankBase, nConn, mxa, *exc, *oc, *fac);
       CODY_LAUNCHED(c);
       if (kind == 0) t.maxS = mx; else t.maxD = mx;
     }
-    CiView& v = c->view;
+    CODY_CUDA(cudaStreamSynchronize(c->stream));  // the tables are written on the context stream
+    group_by_code(t.nConf, std::max(t.maxS, 1), t.sN, t.sExc, t.sCode, t.sFac, t.nSc, t.sxCode, t.sxStart, t.sxSrc,
+                  t.sxDst, t.sxFac);
+    group_by_code(t.nConf, std::max(t.maxD, 1), t.dN, t.dExc, t.dCode, t.dFac, t.nDc, t.dxCode, t.dxStart, t.dxSrc,
+                  t.dxDst, t.dxFac);
+    CiView& v = s.view;
+    v.nSc[b] = t.nSc;
+    v.nDc[b] = t.nDc;
+    v.sxCode[b] = t.sxCode; v.sxStart[b] = t.sxStart; v.sxSrc[b] = t.sxSrc; v.sxDst[b] = t.sxDst; v.sxFac[b] = t.sxFac;
+    v.dxCode[b] = t.dxCode; v.dxStart[b] = t.dxStart; v.dxSrc[b] = t.dxSrc; v.dxDst[b] = t.dxDst; v.dxFac[b] = t.dxFac;
     v.stride[b] = stride;
     v.nConf[b] = t.nConf;
     v.maxS[b] = std::max(t.maxS, 1);
@@ -382,45 +515,45 @@ void ci_build_tables(cgpu_ctx* c) {
     v.dN[b] = t.dN; v.dExc[b] = t.dExc; v.dCode[b] = t.dCode; v.dFac[b] = t.dFac;
     stride *= t.nConf;
   }
-  c->view.nC = stride;
+  s.view.nC = stride;
   CODY_CUDA(cudaStreamSynchronize(c->stream));
 }
 
 void launch_ci_apply(cgpu_ctx* c, const z_t* C, z_t* dC, int useH1, int useH2) {
   ProfScope prof(c, CGPU_KERNEL_CI_APPLY);
   int threads = 256;
-  int blocks = (int)(((size_t)c->nC * 32 + threads - 1) / threads);
-  k_ci_apply<<<blocks, threads, 0, c->stream>>>(c->view, C, dC, c->h1Lin_d, c->h2Lin_d, useH1, useH2);
+  unsigned blocks = ew_blocks(c, (size_t)c->nC * 32, threads);
+  k_ci_apply<<<bgrid(c, blocks), threads, 0, c->stream>>>(C, dC, c->h1Lin_d, c->h2Lin_d, TRAJ_PASS(c), useH1, useH2);
   CODY_LAUNCHED(c);
 }
 
 void launch_ci_rdm(cgpu_ctx* c, const z_t* C, int want1, int want2) {
   ProfScope prof(c, CGPU_KERNEL_CI_RDM);
   size_t n2 = (size_t)c->nO * c->nO, n4 = n2 * n2;
-  if (want1) CODY_CUDA(cudaMemsetAsync(c->rdm1Lin_d, 0, sizeof(z_t) * (n2 + 1), c->stream));
-  if (want2) CODY_CUDA(cudaMemsetAsync(c->rdm2Lin_d, 0, sizeof(z_t) * (n4 + 1), c->stream));
+  // every code present is written; the other entries of the Lin arrays stay zero
   int threads = 256;
-  int blocks = (int)(((size_t)c->nC * 32 + threads - 1) / threads);
-  k_ci_rdm<<<blocks, threads, 0, c->stream>>>(c->view, C, c->rdm1Lin_d, c->rdm2Lin_d, want1, want2);
+  unsigned blocks = ew_blocks(c, (size_t)c->ciTasks * 32, threads);
+  k_ci_rdm<<<bgrid(c, blocks), threads, 0, c->stream>>>(C, c->rdm1Lin_d, c->rdm2Lin_d, TRAJ_PASS(c), want1, want2);
   CODY_LAUNCHED(c);
   if (want1) {
-    k_unfold_rdm1<<<(int)((n2 + 255) / 256), 256, 0, c->stream>>>(c->rdm1_d, c->rdm1Lin_d, c->nO);
+    k_unfold_rdm1<<<bgrid(c, ew_blocks(c, n2)), 256, 0, c->stream>>>(c->rdm1_d, c->rdm1Lin_d, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
   }
   if (want2) {
-    k_unfold_rdm2<<<(int)((n4 + 255) / 256), 256, 0, c->stream>>>(c->rdm2_d, c->rdm2Lin_d, c->btOfOrb_d, c->nO);
+    k_unfold_rdm2<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(c->rdm2_d, c->rdm2Lin_d, c->btOfOrb_d,
+                                                                       TRAJ_PASS(c));
     CODY_LAUNCHED(c);
   }
 }
 
 void launch_fold_h1(cgpu_ctx* c) {
-  int n2 = c->nO * c->nO;
-  k_fold_h1<<<(n2 + 255) / 256, 256, 0, c->stream>>>(c->h1Lin_d, c->h1_d, c->nO);
+  size_t n2 = (size_t)c->nO * c->nO;
+  k_fold_h1<<<bgrid(c, ew_blocks(c, n2)), 256, 0, c->stream>>>(c->h1Lin_d, c->h1_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
 void launch_fold_h2(cgpu_ctx* c) {
   size_t n4 = (size_t)c->nO * c->nO * c->nO * c->nO;
-  k_fold_h2<<<(int)((n4 + 255) / 256), 256, 0, c->stream>>>(c->h2Lin_d, c->h2_d, c->btOfOrb_d, c->nO);
+  k_fold_h2<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(c->h2Lin_d, c->h2_d, c->btOfOrb_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }

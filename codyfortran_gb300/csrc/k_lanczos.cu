@@ -12,8 +12,6 @@
 // partials in a fixed order, re-summed identically by every consumer block.
 //
 // Device scalar block lz[] (doubles):
-#include <type_traits>
-
 #include "common.cuh"
 
 namespace {
@@ -30,7 +28,6 @@ constexpr int LZ_ZERO = 388;    // zero-norm start (output = input)
 constexpr int LZ_DT = 389;      // dt of the current sub-step
 constexpr int LZ_BREAKJ = 390;  // iteration at which breakdown happened
 
-constexpr int LZ_BLOCKS = 148;
 constexpr int LZ_THREADS = 256;
 
 __device__ z_t block_sum2(z_t v) {
@@ -53,111 +50,154 @@ __device__ z_t block_sum2(z_t v) {
   return v;
 }
 
-constexpr int LZ_MAXV = 32;  // Krylov vectors handled per reduction pass
+constexpr int LZ_WARPS = LZ_THREADS / 32;
+constexpr int LZ_EMAX = 4;                         // state entries per thread and chunk (at most)
+constexpr int LZ_VPW = 32 / LZ_WARPS;              // Krylov vectors per warp (at most 32 vectors)
 
-// Block-reduces acc[0..nVec) (register arrays of every thread) into out[0..nVec).
-template <int MAXV>
-__device__ void block_reduce_many(z_t (&acc)[MAXV], int nVec, z_t* __restrict__ out) {
-  __shared__ z_t red[MAXV][LZ_THREADS / 32];
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+// Chunked reductions against the Krylov basis.  A block walks chunks of
+// LZ_THREADS * E consecutive state entries; the chunk of m * w is staged in
+// shared memory, and warp q forms the dots of the basis vectors q, q + 8, ...
+// with it (lanes over the entries, so every basis load is coalesced and a
+// thread holds at most four accumulators).
+__device__ __forceinline__ void chunk_dots(z_t (&acc)[LZ_VPW], const z_t* __restrict__ V, size_t ldv, int nVec,
+                                           const TrajShape& S, size_t c0, int cn, const z_t* sw) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < MAXV; k++) {
+  for (int q = 0; q < LZ_VPW; q++) {
+    int k = wid + q * LZ_WARPS;
     if (k >= nVec) break;
-    z_t v = acc[k];
-    for (int o = 16; o > 0; o >>= 1) {
-      v.x += __shfl_down_sync(0xffffffffu, v.x, o);
-      v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    const z_t* Vk = V + ldv * k;
+    z_t a = acc[q];
+    for (int t = lane; t < cn; t += 32) {
+      z_t v = Vk[vidx(S, c0 + t)];
+      z_t b = sw[t];
+      a.x += v.x * b.x + v.y * b.y;
+      a.y += v.x * b.y - v.y * b.x;
     }
-    if (lane == 0) red[k][wid] = v;
+    acc[q] = a;
   }
-  __syncthreads();
-  for (int k = threadIdx.x; k < nVec; k += blockDim.x) {
-    z_t s = zmk(0.0, 0.0);
-    for (int q = 0; q < LZ_THREADS / 32; q++) s = zadd(s, red[k][q]);
-    out[k] = s;
+}
+
+// part[blk*nVec + k] = warp sums of acc (one warp per vector k)
+__device__ __forceinline__ void store_dots(z_t (&acc)[LZ_VPW], int nVec, z_t* __restrict__ part) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < LZ_VPW; q++) {
+    int k = wid + q * LZ_WARPS;
+    if (k >= nVec) break;
+    z_t a = acc[q];
+    for (int o = 16; o > 0; o >>= 1) {
+      a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
+      a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
+    }
+    if (lane == 0) part[(size_t)blockIdx.x * nVec + k] = a;
   }
 }
 
 // part[blk*nVec + k] = sum_{i in blk} conj(V_k[i]) m[i] w[i], all k in one pass over the data.
-template <int MAXV>
 __global__ void __launch_bounds__(LZ_THREADS) k_mdot(z_t* __restrict__ part, const z_t* __restrict__ V, size_t ldv,
                                                       int nVec, const z_t* __restrict__ w,
-                                                      const double* __restrict__ m, size_t n,
-                                                      const double* __restrict__ lz) {
-  if (lz && lz[LZ_DONE] != 0.0) return;
-  z_t acc[MAXV];
+                                                      const double* __restrict__ m, TRAJ_ARGS,
+                                                      const double* __restrict__ lz, int E) {
+  const TrajShape& S = shp[blockIdx.z];
+  lz = bat(lz, bs);
+  if (lz[LZ_DONE] != 0.0) return;
+  part = bat(part, bs);
+  V = bat(V, bs);
+  w = bat(w, bs);
+  m = bat(m, bs);
+  __shared__ z_t sw[LZ_THREADS * LZ_EMAX];
+  const size_t n = S.nS;
+  const int CH = LZ_THREADS * E;
+  z_t acc[LZ_VPW];
 #pragma unroll
-  for (int k = 0; k < MAXV; k++) acc[k] = zmk(0.0, 0.0);
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    z_t b = zscale(w[i], m[i]);
-#pragma unroll
-    for (int k = 0; k < MAXV; k++) {
-      if (k >= nVec) break;
-      z_t a = V[ldv * k + i];
-      acc[k].x += a.x * b.x + a.y * b.y;
-      acc[k].y += a.x * b.y - a.y * b.x;
+  for (int q = 0; q < LZ_VPW; q++) acc[q] = zmk(0.0, 0.0);
+  for (size_t c0 = (size_t)blockIdx.x * CH; c0 < n; c0 += (size_t)gridDim.x * CH) {
+    int cn = (int)min((size_t)CH, n - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < cn; t += LZ_THREADS) {
+      size_t i = vidx(S, c0 + t);
+      sw[t] = zscale(w[i], m[i]);
     }
+    __syncthreads();
+    chunk_dots(acc, V, ldv, nVec, S, c0, cn, sw);
   }
-  block_reduce_many<MAXV>(acc, nVec, part + (size_t)blockIdx.x * nVec);
+  store_dots(acc, nVec, part);
 }
 
 // Every block re-sums the partials (fixed order) into shared coefficients,
 // subtracts w -= sum_k coef_k V_k, and in the same pass emits partials for the
-// next stage: mode 0: dots of the new w with V_0..V_{nVec-1}; mode 1: the
-// metric norm^2 of the new w.  Block 0 stores the first-pass coefficients at lz[LZ_D].
-template <int MAXV>
+// next stage: mode 0: dots of the new w with V_0..V_{nVec-1} (the chunk's basis
+// entries are re-read from cache); mode 1: the metric norm^2 of the new w.
+// Block 0 stores the first-pass coefficients at lz[LZ_D].
 __global__ void __launch_bounds__(LZ_THREADS) k_cgs_pass(z_t* __restrict__ w, const z_t* __restrict__ V, size_t ldv,
                                                           int nVec, const z_t* __restrict__ partIn, int nBlkIn,
                                                           z_t* __restrict__ partOut, const double* __restrict__ m,
-                                                          size_t n, double* __restrict__ lz, int mode,
-                                                          int storeDots) {
+                                                          TRAJ_ARGS, double* __restrict__ lz, int mode,
+                                                          int storeDots, int E) {
+  const TrajShape& S = shp[blockIdx.z];
+  lz = bat(lz, bs);
   if (lz[LZ_DONE] != 0.0) return;
-  __shared__ z_t coef[MAXV];
+  w = bat(w, bs);
+  V = bat(V, bs);
+  partIn = bat(partIn, bs);
+  partOut = bat(partOut, bs);
+  m = bat(m, bs);
+  __shared__ z_t coef[32];
+  __shared__ z_t sw[LZ_THREADS * LZ_EMAX];
+  const size_t n = S.nS;
+  const int CH = LZ_THREADS * E;
   sum_partials(partIn, nBlkIn, nVec, nVec, coef);
   if (storeDots && blockIdx.x == 0)
     for (int k = threadIdx.x; k < nVec; k += blockDim.x) {
       lz[LZ_D + 2 * k] = coef[k].x;
       lz[LZ_D + 2 * k + 1] = coef[k].y;
     }
-  z_t acc[MAXV];
+  z_t acc[LZ_VPW];
 #pragma unroll
-  for (int k = 0; k < MAXV; k++) acc[k] = zmk(0.0, 0.0);
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    z_t r = w[i];
-#pragma unroll
-    for (int k = 0; k < MAXV; k++) {
-      if (k >= nVec) break;
-      z_t v = V[ldv * k + i];
-      z_t cf = coef[k];
-      r.x -= cf.x * v.x - cf.y * v.y;
-      r.y -= cf.x * v.y + cf.y * v.x;
-    }
-    w[i] = r;
-    z_t b = zscale(r, m[i]);
-    if (mode == 0) {
-#pragma unroll
-      for (int k = 0; k < MAXV; k++) {
-        if (k >= nVec) break;
-        z_t a = V[ldv * k + i];
-        acc[k].x += a.x * b.x + a.y * b.y;
-        acc[k].y += a.x * b.y - a.y * b.x;
+  for (int q = 0; q < LZ_VPW; q++) acc[q] = zmk(0.0, 0.0);
+  double nacc = 0.0;
+  for (size_t c0 = (size_t)blockIdx.x * CH; c0 < n; c0 += (size_t)gridDim.x * CH) {
+    int cn = (int)min((size_t)CH, n - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < cn; t += LZ_THREADS) {
+      size_t i = vidx(S, c0 + t);
+      z_t r = w[i];
+      for (int k = 0; k < nVec; k++) {
+        z_t v = V[ldv * k + i];
+        z_t cf = coef[k];
+        r.x -= cf.x * v.x - cf.y * v.y;
+        r.y -= cf.x * v.y + cf.y * v.x;
       }
-    } else {
-      acc[0].x += r.x * b.x + r.y * b.y;
+      w[i] = r;
+      z_t b = zscale(r, m[i]);
+      if (mode == 0) sw[t] = b;
+      else nacc += r.x * b.x + r.y * b.y;
+    }
+    if (mode == 0) {
+      __syncthreads();
+      chunk_dots(acc, V, ldv, nVec, S, c0, cn, sw);
     }
   }
   if (mode == 0) {
-    block_reduce_many<MAXV>(acc, nVec, partOut + (size_t)blockIdx.x * nVec);
+    store_dots(acc, nVec, partOut);
   } else {
-    block_reduce_many<MAXV>(acc, 1, partOut + blockIdx.x);
+    z_t t = block_sum2(zmk(nacc, 0.0));
+    if (threadIdx.x == 0) partOut[blockIdx.x] = t;
   }
 }
 
 // beta_j = sqrt(sum partials); alpha_j from the first-pass dot; v_{j+1} = w / beta_j.
 // j is 1-based; alpha/beta stored at index j-1.
 __global__ void k_lz_finish(z_t* __restrict__ vNext, const z_t* __restrict__ w, const z_t* __restrict__ partIn,
-                            int nBlkIn, size_t n, double* __restrict__ lz, int j, int maxDim, double zeroThr) {
+                            int nBlkIn, TRAJ_ARGS, double* __restrict__ lz, int j, int maxDim, double zeroThr) {
+  const TrajShape& S = shp[blockIdx.z];
+  lz = bat(lz, bs);
   if (lz[LZ_DONE] != 0.0) return;
+  vNext = bat(vNext, bs);
+  w = bat(w, bs);
+  partIn = bat(partIn, bs);
+  const size_t n = S.nS;
   __shared__ z_t tot[1];
   sum_partials(partIn, nBlkIn, 1, 1, tot);
   double be = sqrt(tot[0].x);
@@ -176,14 +216,16 @@ __global__ void k_lz_finish(z_t* __restrict__ vNext, const z_t* __restrict__ w, 
     return;
   }
   if (vNext == nullptr) return;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+  for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+    size_t i = vidx(S, l);
     z_t v = w[i];
     vNext[i] = zmk(v.x / be, v.y / be);
   }
 }
 
-__global__ void k_lz_mark_done(double* lz, int j) {
+__global__ void k_lz_mark_done(double* lz, int j, size_t bs) {
   // executed after k_lz_finish of iteration j: a breakdown stops the growth
+  lz = bat(lz, bs);
   if (lz[LZ_DONE] == 0.0 && lz[LZ_BREAKJ] == (double)j) lz[LZ_DONE] = 1.0;
 }
 
@@ -198,8 +240,9 @@ __global__ void k_lz_mark_done(double* lz, int j) {
 // The Bessel values J_k(z) come from Miller's backward recurrence normalised
 // by J_0 + 2 sum J_2k = 1.  The series is summed until the coefficients fall
 // below 1e-17 relative, i.e. to machine precision.  One warp, lane i = row i (m <= 32).
-__global__ void k_lz_expsub(double* __restrict__ lz, int mFixed, double dt, double tol) {
+__global__ void k_lz_expsub(double* __restrict__ lz, int mFixed, double dt, double tol, size_t bs) {
   constexpr int KMAX = 1200;
+  lz = bat(lz, bs);
   __shared__ double J[KMAX + 2];
   __shared__ int nTerms;
   int lane = threadIdx.x;
@@ -299,14 +342,21 @@ __global__ void k_lz_expsub(double* __restrict__ lz, int mFixed, double dt, doub
 
 // out = nrm * sum_{j < mDim} phi_j V_j   (or out = in when the start vector had zero norm)
 __global__ void k_lz_combine(z_t* __restrict__ out, const z_t* __restrict__ in, const z_t* __restrict__ V,
-                             size_t ldv, size_t n, const double* __restrict__ lz) {
+                             size_t ldv, TRAJ_ARGS, const double* __restrict__ lz) {
+  const TrajShape& S = shp[blockIdx.z];
+  out = bat(out, bs);
+  in = bat(in, bs);
+  V = bat(V, bs);
+  lz = bat(lz, bs);
+  const size_t n = S.nS;
   __shared__ z_t phi[CODY_MAX_KRYLOV];
   int m = (int)lz[LZ_MDIM];
   double nrm = lz[LZ_NRM];
   bool zero = lz[LZ_ZERO] != 0.0;
   for (int k = threadIdx.x; k < m; k += blockDim.x) phi[k] = zmk(lz[LZ_PHI + 2 * k], lz[LZ_PHI + 2 * k + 1]);
   __syncthreads();
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+  for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+    size_t i = vidx(S, l);
     if (zero) {
       out[i] = in[i];
       continue;
@@ -319,7 +369,13 @@ __global__ void k_lz_combine(z_t* __restrict__ out, const z_t* __restrict__ in, 
 
 // nrm = sqrt(<s,s>_m); v1 = s / nrm; resets the per-step flags.
 __global__ void k_lz_start(z_t* __restrict__ v1, const z_t* __restrict__ s, const z_t* __restrict__ partIn, int nBlkIn,
-                           size_t n, double* __restrict__ lz, double zeroThr) {
+                           TRAJ_ARGS, double* __restrict__ lz, double zeroThr) {
+  const TrajShape& S = shp[blockIdx.z];
+  v1 = bat(v1, bs);
+  s = bat(s, bs);
+  partIn = bat(partIn, bs);
+  lz = bat(lz, bs);
+  const size_t n = S.nS;
   __shared__ z_t tot[1];
   sum_partials(partIn, nBlkIn, 1, 1, tot);
   double nr = sqrt(tot[0].x);
@@ -333,15 +389,23 @@ __global__ void k_lz_start(z_t* __restrict__ v1, const z_t* __restrict__ s, cons
     lz[LZ_ERR] = 0.0;
   }
   if (zero) return;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+  for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+    size_t i = vidx(S, l);
     z_t v = s[i];
     v1[i] = zmk(v.x / nr, v.y / nr);
   }
 }
 
-__global__ void k_norm_partial(z_t* __restrict__ part, const z_t* __restrict__ v, const double* __restrict__ m, size_t n) {
+__global__ void k_norm_partial(z_t* __restrict__ part, const z_t* __restrict__ v, const double* __restrict__ m,
+                               TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  part = bat(part, bs);
+  v = bat(v, bs);
+  m = bat(m, bs);
+  const size_t n = S.nS;
   z_t s = zmk(0.0, 0.0);
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+  for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+    size_t i = vidx(S, l);
     z_t b = v[i];
     s.x += (b.x * b.x + b.y * b.y) * m[i];
   }
@@ -349,68 +413,56 @@ __global__ void k_norm_partial(z_t* __restrict__ part, const z_t* __restrict__ v
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-void ensure_lz_partial(cgpu_ctx* c) {
-  size_t need = (size_t)LZ_BLOCKS * (CODY_MAX_KRYLOV + 1) * 2;
-  if (c->partialCap >= need) return;
-  if (c->partial_d) cudaFree(c->partial_d);
-  CODY_CUDA(cudaMalloc(&c->partial_d, need * sizeof(z_t)));
-  c->partialCap = need;
-}
-
 }  // namespace
 
-// Starts a Lanczos pass from the vector v (device, nS): basis[:,0] = v/|v|.
+size_t lanczos_partial_need(const cgpu_ctx* c) { return (size_t)c->lzBlocks * (c->maxKrylov + 1) * 2; }
+
+// Starts a Lanczos pass from the vector v (device, state layout): basis[:,0] = v/|v|.
 void launch_lanczos_start(cgpu_ctx* c, const z_t* v) {
-  ensure_lz_partial(c);
-  k_norm_partial<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(c->partial_d, v, c->metric_d, c->nS);
+  int nBlk = c->lzBlocks;
+  k_norm_partial<<<bgrid(c, nBlk), LZ_THREADS, 0, c->stream>>>(c->partial_d, v, c->metric_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
-  k_lz_start<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(c->basis_d, v, c->partial_d, LZ_BLOCKS, c->nS, c->lz_d, 1.0e-14);
+  k_lz_start<<<bgrid(c, nBlk), LZ_THREADS, 0, c->stream>>>(c->basis_d, v, c->partial_d, nBlk, TRAJ_PASS(c), c->lz_d,
+                                                           1.0e-14);
   CODY_LAUNCHED(c);
 }
 
 // After lw_d holds H v_j: CGS2 against v_1..v_j, beta_j, v_{j+1}.
 void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
   ProfScope prof(c, CGPU_KERNEL_LANCZOS);
-  ensure_lz_partial(c);
-  size_t nS = c->nS;
+  size_t ld = c->nS;
+  int nBlk = c->lzBlocks;
   z_t* p1 = c->partial_d;
-  z_t* p2 = c->partial_d + (size_t)LZ_BLOCKS * (CODY_MAX_KRYLOV + 1);
-  auto passes = [&](auto tag) {
-    constexpr int MV = decltype(tag)::value;
-    k_mdot<MV><<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(p1, c->basis_d, nS, j, c->lw_d, c->metric_d, nS, c->lz_d);
-    CODY_LAUNCHED(c);
-    k_cgs_pass<MV><<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, nS, j, p1, LZ_BLOCKS, p2,
-                                                             c->metric_d, nS, c->lz_d, 0, 1);
-    CODY_LAUNCHED(c);
-    k_cgs_pass<MV><<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, nS, j, p2, LZ_BLOCKS, p1,
-                                                             c->metric_d, nS, c->lz_d, 1, 0);
-    CODY_LAUNCHED(c);
-  };
-  if (j <= 8) passes(std::integral_constant<int, 8>());
-  else if (j <= 16) passes(std::integral_constant<int, 16>());
-  else passes(std::integral_constant<int, 32>());
-  z_t* vNext = (j < maxDim) ? c->basis_d + nS * (size_t)j : nullptr;
-  k_lz_finish<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p1, LZ_BLOCKS, nS, c->lz_d, j, maxDim,
-                                                        1.0e-14);
+  z_t* p2 = c->partial_d + (size_t)nBlk * (c->maxKrylov + 1);
+  if (j > 32) throw std::string("SIL: Krylov order above 32");
+  const int E = c->lzElems;
+  k_mdot<<<bgrid(c, nBlk), LZ_THREADS, 0, c->stream>>>(p1, c->basis_d, ld, j, c->lw_d, c->metric_d, TRAJ_PASS(c),
+                                                       c->lz_d, E);
   CODY_LAUNCHED(c);
-  k_lz_mark_done<<<1, 1, 0, c->stream>>>(c->lz_d, j);
+  k_cgs_pass<<<bgrid(c, nBlk), LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, ld, j, p1, nBlk, p2, c->metric_d,
+                                                           TRAJ_PASS(c), c->lz_d, 0, 1, E);
+  CODY_LAUNCHED(c);
+  k_cgs_pass<<<bgrid(c, nBlk), LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, ld, j, p2, nBlk, p1, c->metric_d,
+                                                           TRAJ_PASS(c), c->lz_d, 1, 0, E);
+  CODY_LAUNCHED(c);
+  z_t* vNext = (j < maxDim) ? c->basis_d + ld * (size_t)j : nullptr;
+  k_lz_finish<<<bgrid(c, nBlk), LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p1, nBlk, TRAJ_PASS(c), c->lz_d, j,
+                                                            maxDim, 1.0e-14);
+  CODY_LAUNCHED(c);
+  k_lz_mark_done<<<bgrid(c, 1), 1, 0, c->stream>>>(c->lz_d, j, c->bs);
   CODY_LAUNCHED(c);
 }
 
 void launch_lanczos_tail(cgpu_ctx* c, int j, double dt, int evalExp) {
   if (!evalExp) return;
-  k_lz_expsub<<<1, 32, 0, c->stream>>>(c->lz_d, j, dt, 0.0);
+  k_lz_expsub<<<bgrid(c, 1), 32, 0, c->stream>>>(c->lz_d, j, dt, 0.0, c->bs);
   CODY_LAUNCHED(c);
 }
 
 void launch_lanczos_combine(cgpu_ctx* c, z_t* out) {
-  k_lz_combine<<<LZ_BLOCKS, LZ_THREADS, 0, c->stream>>>(out, c->work_d, c->basis_d, c->nS, c->nS, c->lz_d);
+  k_lz_combine<<<bgrid(c, c->lzBlocks), LZ_THREADS, 0, c->stream>>>(out, c->work_d, c->basis_d, c->nS, TRAJ_PASS(c),
+                                                                    c->lz_d);
   CODY_LAUNCHED(c);
 }
 
-__global__ void k_lz_set(double* lz, int idx, double v) { lz[idx] = v; }
-
-void launch_lz_set(cgpu_ctx* c, int idx, double v) {
-  k_lz_set<<<1, 1, 0, c->stream>>>(c->lz_d, idx, v);
-  CODY_LAUNCHED(c);
-}
+void launch_lz_set(cgpu_ctx* c, int idx, double v) { launch_set_scalar(c, c->lz_d + idx, v); }

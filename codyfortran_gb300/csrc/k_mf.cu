@@ -15,6 +15,7 @@
 //
 // plus the regularised inverse of the one-body RDM (RdmDiagonalize_Rdm1 +
 // regInvMat, :722-754) by a parallel cyclic Jacobi eigensolver in one CTA.
+// Every kernel covers all trajectories of the context (blockIdx.z).
 #include <algorithm>
 
 #include "common.cuh"
@@ -25,41 +26,61 @@ namespace {
 // Pair sources and expansion
 // ---------------------------------------------------------------------------
 __global__ void k_pair_src(z_t* __restrict__ S, const z_t* __restrict__ orbs, const double* __restrict__ w,
-                           const int* __restrict__ pl, const int* __restrict__ pk, int nG, int nP) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= (size_t)nG * nP) return;
-  int g = (int)(e / nP), p = (int)(e % nP);
-  z_t a = orbs[(size_t)nG * pl[p] + g], b = orbs[(size_t)nG * pk[p] + g];
-  S[e] = zscale(zcmul(a, b), w[g]);
+                           const int* __restrict__ pl, const int* __restrict__ pk, TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int nG = T.nG, nP = T.nPairs;
+  S = bat(S, bs);
+  orbs = bat(orbs, bs);
+  w = bat(w, bs);
+  pl = bat(pl, bs);
+  pk = bat(pk, bs);
+  GRID_STRIDE(e, (size_t)nG * nP) {
+    int g = (int)(e / nP), p = (int)(e % nP);
+    z_t a = orbs[(size_t)nG * pl[p] + g], b = orbs[(size_t)nG * pk[p] + g];
+    S[e] = zscale(zcmul(a, b), w[g]);
+  }
 }
 
 // Wfull[g][a*n+b] = W_(a,b)(g) for same-body-type pairs, Sfull[g][a*n+b] = conj(phi_a) phi_b w.
 __global__ void k_expand(z_t* __restrict__ Wfull, z_t* __restrict__ Sfull, const z_t* __restrict__ W,
                          const z_t* __restrict__ orbs, const double* __restrict__ w, const int* __restrict__ pidx,
-                         int nG, int n, int nP) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+                         TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int nG = T.nG, n = T.nOS, nP = T.nPairs;
   int Q = n * n;
-  if (e >= (size_t)nG * Q) return;
-  int g = (int)(e / Q), q = (int)(e % Q);
-  int a = q / n, b = q % n;
-  z_t v = zmk(0.0, 0.0);
-  if (a <= b) {
-    int p = pidx[a * n + b];
-    if (p >= 0) v = W[(size_t)g * nP + p];
-  } else {
-    int p = pidx[b * n + a];
-    if (p >= 0) v = zconj(W[(size_t)g * nP + p]);
+  Wfull = bat(Wfull, bs);
+  Sfull = bat(Sfull, bs);
+  W = bat(W, bs);
+  orbs = bat(orbs, bs);
+  w = bat(w, bs);
+  pidx = bat(pidx, bs);
+  GRID_STRIDE(e, (size_t)nG * Q) {
+    int g = (int)(e / Q), q = (int)(e % Q);
+    int a = q / n, b = q % n;
+    z_t v = zmk(0.0, 0.0);
+    if (a <= b) {
+      int p = pidx[a * n + b];
+      if (p >= 0) v = W[(size_t)g * nP + p];
+    } else {
+      int p = pidx[b * n + a];
+      if (p >= 0) v = zconj(W[(size_t)g * nP + p]);
+    }
+    Wfull[e] = v;
+    if (Sfull) Sfull[e] = zscale(zcmul(orbs[(size_t)nG * a + g], orbs[(size_t)nG * b + g]), w[g]);
   }
-  Wfull[e] = v;
-  if (Sfull) Sfull[e] = zscale(zcmul(orbs[(size_t)nG * a + g], orbs[(size_t)nG * b + g]), w[g]);
 }
 
 // dOrbs[g + nG*j] += sum_k1 orbs[g + nG*k1] * Z[g][k1*n + j]
 __global__ void k_corr_epilogue(z_t* __restrict__ dOrbs, const z_t* __restrict__ orbs, const z_t* __restrict__ Z,
-                                int nG, int n) {
+                                TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int nG = T.nG, n = T.nOS;
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   int j = blockIdx.y;
-  if (g >= nG) return;
+  if (g >= nG || j >= n) return;
+  dOrbs = bat(dOrbs, bs);
+  orbs = bat(orbs, bs);
+  Z = bat(Z, bs);
   z_t acc = zmk(0.0, 0.0);
   const z_t* zr = Z + (size_t)g * n * n;
   for (int k1 = 0; k1 < n; k1++) zfma(acc, orbs[(size_t)nG * k1 + g], zr[k1 * n + j]);
@@ -70,38 +91,49 @@ __global__ void k_corr_epilogue(z_t* __restrict__ dOrbs, const z_t* __restrict__
 // h2 (nO^4, Fortran order) from the spatial block H2s[(i1*n+j1)][(l2*n+k2)]:
 // h2(i1,l2,j1,k2) = H2s, same body type within (i1,j1) and within (l2,k2);
 // restricted runs duplicate the spatial block into the spin blocks.
-__global__ void k_h2_layout(z_t* __restrict__ h2, const z_t* __restrict__ H2s, const int* __restrict__ btOf, int nO,
-                            int n, int restricted) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  size_t N = nO;
-  if (e >= N * N * N * N) return;
-  int i1 = (int)(e % N), l2 = (int)((e / N) % N), j1 = (int)((e / N / N) % N), k2 = (int)(e / N / N / N);
-  z_t v = zmk(0.0, 0.0);
-  if (restricted) {
-    int s1 = i1 / n, s2 = l2 / n, s3 = j1 / n, s4 = k2 / n;
-    if (s1 == s3 && s2 == s4) {
-      int a = i1 % n, b = l2 % n, c = j1 % n, d = k2 % n;
-      v = H2s[(size_t)(a * n + c) * n * n + (b * n + d)];
+__global__ void k_h2_layout(z_t* __restrict__ h2, const z_t* __restrict__ H2s, const int* __restrict__ btOf,
+                            TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int n = T.nOS;
+  size_t N = T.nO;
+  h2 = bat(h2, bs);
+  H2s = bat(H2s, bs);
+  btOf = bat(btOf, bs);
+  GRID_STRIDE(e, N * N * N * N) {
+    int i1 = (int)(e % N), l2 = (int)((e / N) % N), j1 = (int)((e / N / N) % N), k2 = (int)(e / N / N / N);
+    z_t v = zmk(0.0, 0.0);
+    if (T.restricted) {
+      int s1 = i1 / n, s2 = l2 / n, s3 = j1 / n, s4 = k2 / n;
+      if (s1 == s3 && s2 == s4) {
+        int a = i1 % n, b = l2 % n, c = j1 % n, d = k2 % n;
+        v = H2s[(size_t)(a * n + c) * n * n + (b * n + d)];
+      }
+    } else {
+      if (btOf[i1] == btOf[j1] && btOf[l2] == btOf[k2]) v = H2s[(size_t)(i1 * n + j1) * n * n + (l2 * n + k2)];
     }
-  } else {
-    if (btOf[i1] == btOf[j1] && btOf[l2] == btOf[k2]) v = H2s[(size_t)(i1 * n + j1) * n * n + (l2 * n + k2)];
+    h2[e] = v;
   }
-  h2[e] = v;
 }
 
 // ---------------------------------------------------------------------------
 // Tiled GEMMs
 // ---------------------------------------------------------------------------
-// C[M,N] = A[M,K] B[K,N], all row-major, real FP64.  64x64 tile, 256 threads, 4x4 per thread.
+// W[nG, 2P] = V[nG, nG] S[nG, 2P] (the complex pair sources viewed as interleaved
+// doubles), all row-major, real FP64.  64x64 tile, 256 threads, 4x4 per thread.
 constexpr int DG_BM = 64, DG_BN = 64, DG_BK = 16;
 
-__global__ void __launch_bounds__(256) k_dgemm_nn(int M, int N, int K, const double* __restrict__ A, int lda,
-                                                  const double* __restrict__ B, int ldb, double* __restrict__ C,
-                                                  int ldc) {
+__global__ void __launch_bounds__(256) k_dgemm_pairs(const double* __restrict__ A, const double* __restrict__ B,
+                                                     double* __restrict__ C, TRAJ_ARGS) {
   __shared__ double As[DG_BK][DG_BM + 1];
   __shared__ double Bs[DG_BK][DG_BN];
+  const TrajShape& T = shp[blockIdx.z];
+  const int M = T.nG, N = 2 * T.nPairs, K = T.nG, lda = T.nG, ldb = N, ldc = N;
   int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   int m0 = blockIdx.y * DG_BM, n0 = blockIdx.x * DG_BN;
+  if (m0 >= M || n0 >= N) return;
+  A = bat(A, bs);
+  B = bat(B, bs);
+  C = bat(C, bs);
   double acc[4][4] = {};
   for (int k0 = 0; k0 < K; k0 += DG_BK) {
     for (int t = threadIdx.x; t < DG_BM * DG_BK; t += 256) {
@@ -138,18 +170,36 @@ __global__ void __launch_bounds__(256) k_dgemm_nn(int M, int N, int K, const dou
     }
 }
 
-// Complex GEMM, row-major: P[split][m][n] = sum_{k in split} opA(m,k) B[k][n]
-// opA(m,k) = A[m*lda+k] (transA=0) or A[k*lda+m] (transA=1).  32x32 tile, 256 threads, 2x2 per thread.
+// The two complex GEMMs of the mean field, row-major, per trajectory:
+//   ZG_Z : Z[nG, Q]  = Wfull[nG, Q] R'[Q, Q]
+//   ZG_H2: H2s[Q, Q] = Sfull[nG, Q]^T Wfull[nG, Q]   (scaled by 1/2 in the reduction)
+// P[split][m][n] = sum_{k in split} opA(m,k) B[k][n].  32x32 tile, 256 threads,
+// 2x2 per thread; blockIdx.z = trajectory * nSplit + split.
+enum { ZG_Z = 0, ZG_H2 = 1 };
 constexpr int ZG_BM = 32, ZG_BN = 32, ZG_BK = 8;
 
-__global__ void __launch_bounds__(256) k_zgemm(int transA, int M, int N, int K, int kPerSplit,
-                                               const z_t* __restrict__ A, int lda, const z_t* __restrict__ B,
-                                               int ldb, z_t* __restrict__ P, int ldp) {
+__device__ __forceinline__ void zgemm_dims(const TrajShape& T, int mode, int& M, int& N, int& K) {
+  int Q = T.nOS * T.nOS;
+  if (mode == ZG_Z) { M = T.nG; N = Q; K = Q; }
+  else { M = Q; N = Q; K = T.nG; }
+}
+
+__global__ void __launch_bounds__(256) k_zgemm(int mode, int nSplit, int kPerSplit, const z_t* __restrict__ A,
+                                               const z_t* __restrict__ B, z_t* __restrict__ P, TRAJ_ARGS) {
   __shared__ z_t As[ZG_BK][ZG_BM + 1];
   __shared__ z_t Bs[ZG_BK][ZG_BN];
+  const int traj = blockIdx.z / nSplit, split = blockIdx.z % nSplit;
+  const TrajShape& T = shp[traj];
+  int M, N, K;
+  zgemm_dims(T, mode, M, N, K);
+  const int transA = mode == ZG_H2, lda = T.nOS * T.nOS, ldb = lda, ldp = N;
   int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   int m0 = blockIdx.y * ZG_BM, n0 = blockIdx.x * ZG_BN;
-  int kBeg = blockIdx.z * kPerSplit, kEnd = min(K, kBeg + kPerSplit);
+  if (m0 >= M || n0 >= N) return;
+  A = batn(A, bs, traj);
+  B = batn(B, bs, traj);
+  P = batn(P, bs, traj);
+  int kBeg = split * kPerSplit, kEnd = min(K, kBeg + kPerSplit);
   z_t acc[2][2];
   for (int i = 0; i < 2; i++)
     for (int j = 0; j < 2; j++) acc[i][j] = zmk(0.0, 0.0);
@@ -178,7 +228,7 @@ __global__ void __launch_bounds__(256) k_zgemm(int transA, int M, int N, int K, 
     }
     __syncthreads();
   }
-  z_t* Pz = P + (size_t)blockIdx.z * M * ldp;
+  z_t* Pz = P + (size_t)split * M * ldp;
   for (int i = 0; i < 2; i++)
     for (int j = 0; j < 2; j++) {
       int m = m0 + ty + 16 * i, n = n0 + tx + 16 * j;
@@ -186,16 +236,23 @@ __global__ void __launch_bounds__(256) k_zgemm(int transA, int M, int N, int K, 
     }
 }
 
-__global__ void k_split_reduce(z_t* __restrict__ C, const z_t* __restrict__ P, int nSplit, size_t MN, double scale) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= MN) return;
-  z_t s = zmk(0.0, 0.0);
-  for (int z = 0; z < nSplit; z++) s = zadd(s, P[(size_t)z * MN + e]);
-  C[e] = zscale(s, scale);
+__global__ void k_split_reduce(z_t* __restrict__ C, const z_t* __restrict__ P, int nSplit, int mode, double scale,
+                               TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  int M, N, K;
+  zgemm_dims(T, mode, M, N, K);
+  size_t MN = (size_t)M * N;
+  C = bat(C, bs);
+  P = bat(P, bs);
+  GRID_STRIDE(e, MN) {
+    z_t s = zmk(0.0, 0.0);
+    for (int z = 0; z < nSplit; z++) s = zadd(s, P[(size_t)z * MN + e]);
+    C[e] = zscale(s, scale);
+  }
 }
 
 // ---------------------------------------------------------------------------
-// Regularised inverse of the spin-summed one-body RDM (one CTA).
+// Regularised inverse of the spin-summed one-body RDM (one CTA per trajectory).
 // Parallel cyclic Jacobi (round-robin pairing), complex Hermitian n <= 32.
 // ---------------------------------------------------------------------------
 constexpr int JB_MAX = 32;
@@ -207,9 +264,16 @@ constexpr int JB_MAX = 32;
 // (one modified Gram-Schmidt pass) on load so rounding cannot accumulate.
 // The result Mreg = U f(n) U^H depends only on rho (to rounding).
 __global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t* __restrict__ r1s,
-                                                     const z_t* __restrict__ rdm1, z_t* __restrict__ Uprev, int nO,
-                                                     int n, int restricted, double reg) {
+                                                     const z_t* __restrict__ rdm1, z_t* __restrict__ Uprev,
+                                                     TRAJ_ARGS) {
   extern __shared__ z_t jsm[];
+  const TrajShape& T = shp[blockIdx.z];
+  const int nO = T.nO, n = T.nOS, restricted = T.restricted;
+  const double reg = T.regEps;
+  Mreg = bat(Mreg, bs);
+  r1s = bat(r1s, bs);
+  rdm1 = bat(rdm1, bs);
+  Uprev = bat(Uprev, bs);
   z_t(*A)[JB_MAX + 1] = reinterpret_cast<z_t(*)[JB_MAX + 1]>(jsm);
   z_t(*V)[JB_MAX + 1] = reinterpret_cast<z_t(*)[JB_MAX + 1]>(jsm + JB_MAX * (JB_MAX + 1));
   z_t(*U)[JB_MAX + 1] = reinterpret_cast<z_t(*)[JB_MAX + 1]>(jsm + 2 * JB_MAX * (JB_MAX + 1));
@@ -387,89 +451,107 @@ __global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t
 // R'[(l2*n+k2)][(k1*n+j)] = sum_k r2s(k1,k2,k,l2) Mreg(k,j), masked by body types.
 // r2s is the spin-summed spatial rdm2 built on the fly from rdm2 (nO^4).
 __global__ void k_build_R(z_t* __restrict__ Rp, const z_t* __restrict__ rdm2, const z_t* __restrict__ Mreg,
-                          const int* __restrict__ btOf, int nO, int n, int restricted) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+                          const int* __restrict__ btOf, TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int n = T.nOS, restricted = T.restricted;
   size_t Q = (size_t)n * n;
-  if (e >= Q * Q) return;
-  int row = (int)(e / Q), col = (int)(e % Q);
-  int l2 = row / n, k2 = row % n, k1 = col / n, j = col % n;
-  z_t v = zmk(0.0, 0.0);
-  bool ok = restricted || (btOf[l2] == btOf[k2] && btOf[k1] == btOf[j]);
-  if (ok) {
-    size_t N = nO;
-    auto R2 = [&](int a, int b, int c, int d) { return rdm2[a + N * (b + N * (c + N * (size_t)d))]; };
-    for (int k = 0; k < n; k++) {
-      z_t r = R2(k1, k2, k, l2);
-      if (restricted)
-        r = zadd(zadd(zadd(r, R2(n + k1, k2, n + k, l2)), R2(k1, n + k2, k, n + l2)), R2(n + k1, n + k2, n + k, n + l2));
-      zfma(v, r, Mreg[k + (size_t)n * j]);
+  Rp = bat(Rp, bs);
+  rdm2 = bat(rdm2, bs);
+  Mreg = bat(Mreg, bs);
+  btOf = bat(btOf, bs);
+  GRID_STRIDE(e, Q * Q) {
+    int row = (int)(e / Q), col = (int)(e % Q);
+    int l2 = row / n, k2 = row % n, k1 = col / n, j = col % n;
+    z_t v = zmk(0.0, 0.0);
+    bool ok = restricted || (btOf[l2] == btOf[k2] && btOf[k1] == btOf[j]);
+    if (ok) {
+      size_t N = T.nO;
+      auto R2 = [&](int a, int b, int c, int d) { return rdm2[a + N * (b + N * (c + N * (size_t)d))]; };
+      for (int k = 0; k < n; k++) {
+        z_t r = R2(k1, k2, k, l2);
+        if (restricted)
+          r = zadd(zadd(zadd(r, R2(n + k1, k2, n + k, l2)), R2(k1, n + k2, k, n + l2)),
+                   R2(n + k1, n + k2, n + k, n + l2));
+        zfma(v, r, Mreg[k + (size_t)n * j]);
+      }
     }
+    Rp[e] = v;
   }
-  Rp[e] = v;
 }
 
-void zgemm(cgpu_ctx* c, int transA, int M, int N, int K, const z_t* A, int lda, const z_t* B, int ldb, z_t* C,
-           int ldc, double scale) {
+// split count of a complex GEMM with M x N output and inner dimension K
+int zgemm_splits(const cgpu_ctx* c, int M, int N, int K, int* kPer) {
   int tilesM = (M + ZG_BM - 1) / ZG_BM, tilesN = (N + ZG_BN - 1) / ZG_BN;
-  int tiles = tilesM * tilesN;
+  long tiles = (long)tilesM * tilesN * c->nb;
   int nSplit = 1;
-  if (tiles < 2 * 152 && K > 512) nSplit = std::min((2 * 152 + tiles - 1) / tiles, (K + 255) / 256);
+  if (tiles < 2 * 152 && K > 512) nSplit = (int)std::min<long>((2 * 152 + tiles - 1) / tiles, (K + 255) / 256);
+  int per = ((K + nSplit - 1) / nSplit + ZG_BK - 1) / ZG_BK * ZG_BK;
+  nSplit = (K + per - 1) / per;
+  if (kPer) *kPer = per;
+  return std::max(nSplit, 1);
+}
+
+void zgemm(cgpu_ctx* c, int mode, const z_t* A, const z_t* B, z_t* C, double scale) {
+  int Q = c->nOS * c->nOS;
+  int M = mode == ZG_Z ? c->nG : Q, N = Q, K = mode == ZG_Z ? Q : c->nG;
+  int kPer = K;
+  int nSplit = zgemm_splits(c, M, N, K, &kPer);
+  int tilesM = (M + ZG_BM - 1) / ZG_BM, tilesN = (N + ZG_BN - 1) / ZG_BN;
   if (nSplit == 1 && scale == 1.0) {
-    dim3 grid(tilesN, tilesM, 1);
-    k_zgemm<<<grid, 256, 0, c->stream>>>(transA, M, N, K, K, A, lda, B, ldb, C, ldc);
+    dim3 grid(tilesN, tilesM, c->nb);
+    k_zgemm<<<grid, 256, 0, c->stream>>>(mode, 1, K, A, B, C, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
     return;
   }
-  int kPer = ((K + nSplit - 1) / nSplit + ZG_BK - 1) / ZG_BK * ZG_BK;
-  nSplit = (K + kPer - 1) / kPer;
-  size_t need = (size_t)nSplit * M * N;
-  if (c->partialCap < need) {
-    if (c->partial_d) cudaFree(c->partial_d);
-    CODY_CUDA(cudaMalloc(&c->partial_d, need * sizeof(z_t)));
-    c->partialCap = need;
-  }
-  dim3 grid(tilesN, tilesM, nSplit);
-  k_zgemm<<<grid, 256, 0, c->stream>>>(transA, M, N, K, kPer, A, lda, B, ldb, c->partial_d, N);
+  if ((size_t)nSplit * M * N > c->partialCap) throw std::string("internal: zgemm scratch too small");
+  dim3 grid(tilesN, tilesM, (unsigned)(c->nb * nSplit));
+  k_zgemm<<<grid, 256, 0, c->stream>>>(mode, nSplit, kPer, A, B, c->partial_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
-  if (ldc != N) throw std::string("zgemm: split-K output must be dense");
   size_t MN = (size_t)M * N;
-  k_split_reduce<<<(int)((MN + 255) / 256), 256, 0, c->stream>>>(C, c->partial_d, nSplit, MN, scale);
+  k_split_reduce<<<bgrid(c, ew_blocks(c, MN)), 256, 0, c->stream>>>(C, c->partial_d, nSplit, mode, scale,
+                                                                      TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
 }  // namespace
 
+size_t zgemm_partial_need(const cgpu_ctx* c) {
+  int Q = c->nOS * c->nOS;
+  size_t need = 0;
+  // ZG_H2 always goes through the partial buffer (scale 1/2); ZG_Z only when split
+  int s2 = zgemm_splits(c, Q, Q, c->nG, nullptr);
+  need = std::max(need, (size_t)s2 * Q * Q);
+  int s1 = zgemm_splits(c, c->nG, Q, Q, nullptr);
+  if (s1 > 1) need = std::max(need, (size_t)s1 * c->nG * Q);
+  return need;
+}
+
 // W = V S for the unordered same-body-type pairs (FP64).
 void launch_pair_potentials(cgpu_ctx* c, const z_t* orbs) {
   ProfScope prof(c, CGPU_KERNEL_PAIR_POTENTIALS);
   size_t nGP = (size_t)c->nG * c->nPairs;
-  k_pair_src<<<(int)((nGP + 255) / 256), 256, 0, c->stream>>>(c->S_d, orbs, c->w_d, c->pairL_d, c->pairK_d, c->nG,
-                                                               c->nPairs);
+  k_pair_src<<<bgrid(c, ew_blocks(c, nGP)), 256, 0, c->stream>>>(c->S_d, orbs, c->w_d, c->pairL_d, c->pairK_d,
+                                                                   TRAJ_PASS(c));
   CODY_LAUNCHED(c);
   int N = 2 * c->nPairs;  // complex columns viewed as interleaved doubles
-  dim3 grid((N + DG_BN - 1) / DG_BN, (c->nG + DG_BM - 1) / DG_BM);
-  k_dgemm_nn<<<grid, 256, 0, c->stream>>>(c->nG, N, c->nG, c->Vint_d, c->nG, (const double*)c->S_d, N,
-                                          (double*)c->W_d, N);
+  dim3 grid(ceil_div(N, DG_BN), ceil_div(c->nG, DG_BM), c->nb);
+  k_dgemm_pairs<<<grid, 256, 0, c->stream>>>(c->Vint_d, (const double*)c->S_d, (double*)c->W_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
 static void expand_pairs(cgpu_ctx* c, const z_t* orbs, int wantS) {
   int n = c->nOS;
   size_t tot = (size_t)c->nG * n * n;
-  k_expand<<<(int)((tot + 255) / 256), 256, 0, c->stream>>>(c->Wfull_d, wantS ? c->Sfull_d : nullptr, c->W_d, orbs,
-                                                             c->w_d, c->pidx_d, c->nG, n, c->nPairs);
+  k_expand<<<bgrid(c, ew_blocks(c, tot)), 256, 0, c->stream>>>(c->Wfull_d, wantS ? c->Sfull_d : nullptr, c->W_d,
+                                                                 orbs, c->w_d, c->pidx_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
 static void h2_from_pairs(cgpu_ctx* c) {
   ProfScope prof(c, CGPU_KERNEL_H2);
-  int n = c->nOS, Q = n * n;
   // H2s = 1/2 Sfull^T Wfull  (Q x nG)(nG x Q)
-  zgemm(c, 1, Q, Q, c->nG, c->Sfull_d, Q, c->Wfull_d, Q, c->h2s_d, Q, 0.5);
-  size_t n4 = (size_t)c->nO * c->nO * c->nO * c->nO;
-  k_h2_layout<<<(int)((n4 + 255) / 256), 256, 0, c->stream>>>(c->h2_d, c->h2s_d, c->btOfOrb_d, c->nO, n,
-                                                               c->restricted);
-  CODY_LAUNCHED(c);
+  zgemm(c, ZG_H2, c->Sfull_d, c->Wfull_d, c->h2s_d, 0.5);
+  launch_h2_layout(c);
 }
 
 void launch_rdm_inverse(cgpu_ctx* c) {
@@ -481,12 +563,11 @@ void launch_rdm_inverse(cgpu_ctx* c) {
     CODY_CUDA(cudaFuncSetAttribute(k_rdm_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jsmem));
     attr = true;
   }
-  k_rdm_inverse<<<1, 512, jsmem, c->stream>>>(c->Mreg_d, c->r1s_d, c->rdm1_d, c->Uprev_d, c->nO, n, c->restricted,
-                                              c->regEps);
+  k_rdm_inverse<<<bgrid(c, 1), 512, jsmem, c->stream>>>(c->Mreg_d, c->r1s_d, c->rdm1_d, c->Uprev_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
   size_t Q = (size_t)n * n;
-  k_build_R<<<(int)((Q * Q + 255) / 256), 256, 0, c->stream>>>(c->Rp_d, c->rdm2_d, c->Mreg_d, c->btOfOrb_d, c->nO, n,
-                                                                c->restricted);
+  k_build_R<<<bgrid(c, ew_blocks(c, Q * Q)), 256, 0, c->stream>>>(c->Rp_d, c->rdm2_d, c->Mreg_d, c->btOfOrb_d,
+                                                                    TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
@@ -495,20 +576,18 @@ void launch_rdm_inverse(cgpu_ctx* c) {
 void launch_correlation(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   launch_rdm_inverse(c);
   if (!c->hasInteraction) {
-    if (wantH2) CODY_CUDA(cudaMemsetAsync(c->h2_d, 0, sizeof(z_t) * (size_t)c->nO * c->nO * c->nO * c->nO, c->stream));
+    if (wantH2) batch_zero(c, c->h2_d, sizeof(z_t) * (size_t)c->nO * c->nO * c->nO * c->nO);
     return;
   }
   launch_pair_potentials(c, orbs);
   expand_pairs(c, orbs, wantH2);
   int n = c->nOS, Q = n * n;
-  // Z = Wfull R'  (nG x Q)(Q x Q), stored in the scratch of Sfull's size
-  z_t* Z = c->Wfull_d + (size_t)c->nG * Q;  // second half of the Wfull allocation
+  // Z = Wfull R'  (nG x Q)(Q x Q), stored in the second half of the Wfull allocation
+  z_t* Z = c->Wfull_d + (size_t)c->nG * Q;
   {
     ProfScope prof(c, CGPU_KERNEL_CORRELATION);
-    zgemm(c, 0, c->nG, Q, Q, c->Wfull_d, Q, c->Rp_d, Q, Z, Q, 1.0);
-    dim3 grid((c->nG + 255) / 256, n);
-    k_corr_epilogue<<<grid, 256, 0, c->stream>>>(dOrbs, orbs, Z, c->nG, n);
-    CODY_LAUNCHED(c);
+    zgemm(c, ZG_Z, c->Wfull_d, c->Rp_d, Z, 1.0);
+    launch_corr_epilogue(c, dOrbs, orbs, Z);
   }
   if (wantH2) h2_from_pairs(c);
 }
@@ -516,7 +595,7 @@ void launch_correlation(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
 // FillH2: h2 of the given orbitals.
 void launch_fill_h2(cgpu_ctx* c, const z_t* orbs) {
   if (!c->hasInteraction) {
-    CODY_CUDA(cudaMemsetAsync(c->h2_d, 0, sizeof(z_t) * (size_t)c->nO * c->nO * c->nO * c->nO, c->stream));
+    batch_zero(c, c->h2_d, sizeof(z_t) * (size_t)c->nO * c->nO * c->nO * c->nO);
     return;
   }
   launch_pair_potentials(c, orbs);
@@ -524,17 +603,14 @@ void launch_fill_h2(cgpu_ctx* c, const z_t* orbs) {
   h2_from_pairs(c);
 }
 
-void launch_expand_h2(cgpu_ctx* c) { h2_from_pairs(c); }
-
 void launch_corr_epilogue(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, const z_t* Z) {
-  dim3 grid((c->nG + 255) / 256, c->nOS);
-  k_corr_epilogue<<<grid, 256, 0, c->stream>>>(dOrbs, orbs, Z, c->nG, c->nOS);
+  dim3 grid(ceil_div(c->nG, 256), c->nOS, c->nb);
+  k_corr_epilogue<<<grid, 256, 0, c->stream>>>(dOrbs, orbs, Z, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
 void launch_h2_layout(cgpu_ctx* c) {
   size_t n4 = (size_t)c->nO * c->nO * c->nO * c->nO;
-  k_h2_layout<<<(int)((n4 + 255) / 256), 256, 0, c->stream>>>(c->h2_d, c->h2s_d, c->btOfOrb_d, c->nO, c->nOS,
-                                                               c->restricted);
+  k_h2_layout<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(c->h2_d, c->h2s_d, c->btOfOrb_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }

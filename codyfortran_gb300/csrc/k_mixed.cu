@@ -23,13 +23,14 @@
 
 struct MixedBufs {
   int terms = 3;            // 3: bf16x3, 6: bf16x6
-  int Kg = 0, Kp = 0;       // padded K of the grid contraction and of the pair contraction
+  int KgMax = 0, KpMax = 0; // segment pitches: the largest padded K of the grid / pair contractions
+  int bn1 = 64, bn2 = 64, bn3 = 64;
+  int s1 = 1, s2 = 1, s3 = 1;  // K splits of the three GEMMs
   __nv_bfloat16 *VxB = nullptr, *SxA = nullptr, *WxA = nullptr, *WTxB = nullptr, *RxB = nullptr;
   float *P1 = nullptr, *P2 = nullptr, *P3 = nullptr;
-  size_t cap1 = 0, cap2 = 0, cap3 = 0;
   int* err = nullptr;
   double* Zd = nullptr;     // (nG, Q) complex
-  double* Gd = nullptr;     // (2P, 2P)
+  CUtensorMap mV, mS, mSasB, mW, mWT, mR;  // TMA maps (A operands box 128 rows, B operands box BN rows)
 };
 
 namespace {
@@ -56,29 +57,40 @@ __device__ __forceinline__ __nv_bfloat16 split_part(double x, int terms, int par
   return __double2bfloat16(r1 - (double)__bfloat162float(mid));
 }
 
-// out[row][seg*Kpad + k] = part(value(row,k)), zero for k >= K.
-__device__ __forceinline__ void write_split(__nv_bfloat16* out, int row, int k, int K, int Kpad, int terms, int isB,
+// out[row][seg*pitch + k] = part(value(row,k)), zero for k >= K.
+__device__ __forceinline__ void write_split(__nv_bfloat16* out, int row, int k, int K, int pitch, int terms, int isB,
                                             double v) {
-  size_t base = (size_t)row * terms * Kpad;
+  size_t base = (size_t)row * terms * pitch;
   for (int seg = 0; seg < terms; seg++) {
     __nv_bfloat16 h = (k < K) ? split_part(v, terms, seg_part(terms, isB, seg)) : __double2bfloat16(0.0);
-    out[base + (size_t)seg * Kpad + k] = h;
+    out[base + (size_t)seg * pitch + k] = h;
   }
 }
 
-__global__ void k_split_V(__nv_bfloat16* __restrict__ out, const double* __restrict__ V, int nG, int Kpad, int terms) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= (size_t)nG * Kpad) return;
-  int row = (int)(e / Kpad), k = (int)(e % Kpad);
-  double v = (k < nG) ? V[(size_t)row * nG + k] : 0.0;
-  write_split(out, row, k, nG, Kpad, terms, 1, v);
+__global__ void k_split_V(__nv_bfloat16* __restrict__ out, const double* __restrict__ V, int pitch, int terms,
+                          TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int nG = T.nG, Kpad = T.Kg;
+  out = bat(out, bs);
+  V = bat(V, bs);
+  GRID_STRIDE(e, (size_t)nG * Kpad) {
+    int row = (int)(e / Kpad), k = (int)(e % Kpad);
+    double v = (k < nG) ? V[(size_t)row * nG + k] : 0.0;
+    write_split(out, row, k, nG, pitch, terms, 1, v);
+  }
 }
 
 // S_s(p, g) = (re, im)[conj(phi_l) phi_k w] for pair p = (l, k), A pattern.
-__global__ void k_split_S(__nv_bfloat16* __restrict__ outA, const z_t* __restrict__ orbs, const double* __restrict__ w, const int* __restrict__ pl,
-                          const int* __restrict__ pk, int nG, int nP, int Kpad, int terms) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= (size_t)2 * nP * Kpad) return;
+__global__ void k_split_S(__nv_bfloat16* __restrict__ outA, const z_t* __restrict__ orbs, const double* __restrict__ w,
+                          const int* __restrict__ pl, const int* __restrict__ pk, int pitch, int terms, TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int nG = T.nG, nP = T.nPairs, Kpad = T.Kg;
+  outA = bat(outA, bs);
+  orbs = bat(orbs, bs);
+  w = bat(w, bs);
+  pl = bat(pl, bs);
+  pk = bat(pk, bs);
+  GRID_STRIDE(e, (size_t)2 * nP * Kpad) {
   int row = (int)(e / Kpad), g = (int)(e % Kpad);
   int p = row >> 1, s = row & 1;
   double v = 0.0;
@@ -87,37 +99,54 @@ __global__ void k_split_S(__nv_bfloat16* __restrict__ outA, const z_t* __restric
     z_t sv = zscale(zcmul(a, b), w[g]);
     v = s ? sv.y : sv.x;
   }
-  write_split(outA, row, g, nG, Kpad, terms, 0, v);
+  write_split(outA, row, g, nG, pitch, terms, 0, v);
+  }
 }
 
-// W[g][n] = sum_z P1[z][g][n] (FP64), split to WxA (g-major, K = 2P) and WTxB (pair-major, K = nG).
-__global__ void k_split_W(__nv_bfloat16* __restrict__ WxA, __nv_bfloat16* __restrict__ WTxB,
-                          const float* __restrict__ P1, int nSplit, int nG, int N2P, int KpP, int KpG, int terms) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= (size_t)nG * KpP) return;
-  int g = (int)(e / KpP), n = (int)(e % KpP);
-  double v = 0.0;
-  if (n < N2P)
-    for (int z = 0; z < nSplit; z++) v += (double)P1[((size_t)z * nG + g) * N2P + n];
-  write_split(WxA, g, n, N2P, KpP, terms, 0, v);
-  if (n < N2P) write_split(WTxB, n, g, nG, KpG, terms, 1, v);
-}
+// W[g][n] = sum_z P1[z][g][n] (FP64), split to WxA (g-major, K = 2P, zero for
+// n >= 2P) and WTxB (pair-major, K = nG, zero for g >= nG).  A 32 x 32 tile of
+// (g, n) per block: read along n, transposed through shared memory, written
+// along n (WxA) and along g (WTxB).
+constexpr int SW_T = 32;
 
-// zero the K padding columns of WTxB (g in [nG, KpG)) for every pair row
-__global__ void k_pad_WT(__nv_bfloat16* __restrict__ WTxB, int nG, int N2P, int KpG, int terms) {
-  int pad = KpG - nG;
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= (size_t)N2P * pad) return;
-  int n = (int)(e / pad), g = nG + (int)(e % pad);
-  write_split(WTxB, n, g, nG, KpG, terms, 1, 0.0);
+__global__ void __launch_bounds__(256) k_split_W(__nv_bfloat16* __restrict__ WxA, __nv_bfloat16* __restrict__ WTxB,
+                                                 const float* __restrict__ P1, int nSplit, int pitchP, int pitchG,
+                                                 int terms, TRAJ_ARGS) {
+  __shared__ double tile[SW_T][SW_T + 1];
+  const TrajShape& T = shp[blockIdx.z];
+  const int nG = T.nG, N2P = 2 * T.nPairs, KpP = T.Kp, KpG = T.Kg;
+  const int g0 = blockIdx.x * SW_T, n0 = blockIdx.y * SW_T;
+  if (g0 >= KpG || n0 >= KpP) return;
+  WxA = bat(WxA, bs);
+  WTxB = bat(WTxB, bs);
+  P1 = bat(P1, bs);
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  for (int r = ty; r < SW_T; r += 8) {
+    int g = g0 + r, n = n0 + tx;
+    double v = 0.0;
+    if (g < nG && n < N2P)
+      for (int z = 0; z < nSplit; z++) v += (double)P1[((size_t)z * nG + g) * N2P + n];
+    tile[r][tx] = v;
+    if (g < nG && n < KpP) write_split(WxA, g, n, N2P, pitchP, terms, 0, v);
+  }
+  __syncthreads();
+  for (int r = ty; r < SW_T; r += 8) {
+    int n = n0 + r, g = g0 + tx;
+    if (n < N2P && g < KpG) write_split(WTxB, n, g, nG, pitchG, terms, 1, tile[tx][r]);
+  }
 }
 
 // R'' rows n = 2q + s (s: re/im of the output), K = 2p + t (t: a or b of W_p).
 __global__ void k_split_R(__nv_bfloat16* __restrict__ RxB, const z_t* __restrict__ Rp, const int* __restrict__ pl,
-                          const int* __restrict__ pk, int n, int nP, int KpP, int terms) {
+                          const int* __restrict__ pk, int pitchP, int terms, TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int n = T.nOS, nP = T.nPairs, KpP = T.Kp;
   int Q = n * n;
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= (size_t)2 * Q * KpP) return;
+  RxB = bat(RxB, bs);
+  Rp = bat(Rp, bs);
+  pl = bat(pl, bs);
+  pk = bat(pk, bs);
+  GRID_STRIDE(e, (size_t)2 * Q * KpP) {
   int row = (int)(e / KpP), k = (int)(e % KpP);
   int q = row >> 1, s = row & 1;
   double v = 0.0;
@@ -132,13 +161,17 @@ __global__ void k_split_R(__nv_bfloat16* __restrict__ RxB, const z_t* __restrict
     z_t val = t ? Y : X;
     v = s ? val.y : val.x;
   }
-  write_split(RxB, row, k, 2 * nP, KpP, terms, 1, v);
+  write_split(RxB, row, k, 2 * nP, pitchP, terms, 1, v);
+  }
 }
 
 // Z[g][q] (complex) = sum_z P2[z][g][2q+s]
-__global__ void k_reduce_Z(z_t* __restrict__ Z, const float* __restrict__ P2, int nSplit, int nG, int Q) {
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= (size_t)nG * Q) return;
+__global__ void k_reduce_Z(z_t* __restrict__ Z, const float* __restrict__ P2, int nSplit, TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int nG = T.nG, Q = T.nOS * T.nOS;
+  Z = bat(Z, bs);
+  P2 = bat(P2, bs);
+  GRID_STRIDE(e, (size_t)nG * Q) {
   int g = (int)(e / Q), q = (int)(e % Q);
   double re = 0.0, im = 0.0;
   for (int z = 0; z < nSplit; z++) {
@@ -147,14 +180,19 @@ __global__ void k_reduce_Z(z_t* __restrict__ Z, const float* __restrict__ P2, in
     im += (double)r[1];
   }
   Z[e] = zmk(re, im);
+  }
 }
 
 // H2s[(i1*n+j1)][(l2*n+k2)] = 1/2 sum_g S_(i1j1) W_(l2k2) from the unordered-pair products.
-__global__ void k_reduce_H2(z_t* __restrict__ H2s, const float* __restrict__ P3, int nSplit, const int* __restrict__ pidx,
-                            int n, int nP) {
+__global__ void k_reduce_H2(z_t* __restrict__ H2s, const float* __restrict__ P3, int nSplit,
+                            const int* __restrict__ pidx, TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int n = T.nOS, nP = T.nPairs;
   int Q = n * n;
-  size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (e >= (size_t)Q * Q) return;
+  H2s = bat(H2s, bs);
+  P3 = bat(P3, bs);
+  pidx = bat(pidx, bs);
+  GRID_STRIDE(e, (size_t)Q * Q) {
   int row = (int)(e / Q), col = (int)(e % Q);
   int i1 = row / n, j1 = row % n, l2 = col / n, k2 = col % n;
   bool c1 = i1 > j1, c2 = l2 > k2;
@@ -180,58 +218,80 @@ __global__ void k_reduce_H2(z_t* __restrict__ H2s, const float* __restrict__ P3,
     v = zscale(v, 0.5);
   }
   H2s[e] = v;
+  }
 }
 
-template <typename T>
-T* dalloc_t(size_t n) {
-  T* p = nullptr;
-  CODY_CUDA(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
-  return p;
-}
 
-int blocks(size_t n) { return (int)((n + 255) / 256); }
+size_t take(size_t& off, size_t bytes) {
+  size_t o = (off + 255) & ~(size_t)255;
+  off = o + std::max<size_t>(bytes, 1);
+  return o;
+}
 
 }  // namespace
 
-void mixed_free(cgpu_ctx* c) {
+// Sizes (base == nullptr) or places (base = the arena) the mixed-form buffers of
+// one trajectory block starting at byte offset `off`; returns the end offset.
+size_t mixed_layout(cgpu_ctx* c, char* base, size_t off) {
+  if (c->precision == CGPU_PREC_FP64 || !c->hasInteraction) return off;
+  if (!c->mixed) c->mixed = new MixedBufs();
   MixedBufs* m = c->mixed;
-  if (!m) return;
-  void* ptrs[] = {m->VxB, m->SxA, m->WxA, m->WTxB, m->RxB, m->P1, m->P2, m->P3, m->err, m->Zd, m->Gd};
-  for (void* p : ptrs)
-    if (p) cudaFree(p);
-  delete m;
+  m->terms = c->precision == CGPU_PREC_MIXED_X6 ? 6 : 3;
+  int nG = c->nG, nP = c->nPairs, Q = c->nOS * c->nOS, T = m->terms;
+  m->KgMax = (nG + 63) / 64 * 64;
+  m->KpMax = (2 * nP + 63) / 64 * 64;
+  m->bn1 = tc_tile_n(2 * nP);
+  m->bn2 = tc_tile_n(2 * Q);
+  m->bn3 = tc_tile_n(2 * nP);
+  m->s1 = tc_split_count(nG, 2 * nP, m->bn1, T * m->KgMax / 64, c->nb);
+  m->s2 = tc_split_count(nG, 2 * Q, m->bn2, T * m->KpMax / 64, c->nb);
+  m->s3 = tc_split_count(2 * nP, 2 * nP, m->bn3, T * m->KgMax / 64, c->nb);
+  typedef __nv_bfloat16 bf;
+  size_t oV = take(off, sizeof(bf) * (size_t)nG * T * m->KgMax);
+  size_t oS = take(off, sizeof(bf) * (size_t)2 * nP * T * m->KgMax);
+  size_t oW = take(off, sizeof(bf) * (size_t)nG * T * m->KpMax);
+  size_t oWT = take(off, sizeof(bf) * (size_t)2 * nP * T * m->KgMax);
+  size_t oR = take(off, sizeof(bf) * (size_t)2 * Q * T * m->KpMax);
+  size_t o1 = take(off, sizeof(float) * (size_t)m->s1 * nG * 2 * nP);
+  size_t o2 = take(off, sizeof(float) * (size_t)m->s2 * nG * 2 * Q);
+  size_t o3 = take(off, sizeof(float) * (size_t)m->s3 * 2 * nP * 2 * nP);
+  size_t oE = take(off, sizeof(int));
+  size_t oZ = take(off, sizeof(double) * (size_t)2 * nG * Q);
+  if (base) {
+    m->VxB = (bf*)(base + oV);
+    m->SxA = (bf*)(base + oS);
+    m->WxA = (bf*)(base + oW);
+    m->WTxB = (bf*)(base + oWT);
+    m->RxB = (bf*)(base + oR);
+    m->P1 = (float*)(base + o1);
+    m->P2 = (float*)(base + o2);
+    m->P3 = (float*)(base + o3);
+    m->err = (int*)(base + oE);
+    m->Zd = (double*)(base + oZ);
+  }
+  return off;
+}
+
+void mixed_free(cgpu_ctx* c) {
+  delete c->mixed;  // the buffers belong to the arena
   c->mixed = nullptr;
 }
 
-void mixed_setup(cgpu_ctx* c) {
-  if (c->mixed || !c->hasInteraction) return;
-  MixedBufs* m = new MixedBufs();
-  c->mixed = m;
-  m->terms = c->precision == CGPU_PREC_MIXED_X6 ? 6 : 3;
-  int nG = c->nG, nP = c->nPairs, n = c->nOS, Q = n * n, T = m->terms;
-  m->Kg = (nG + 63) / 64 * 64;
-  m->Kp = (2 * nP + 63) / 64 * 64;
-  m->VxB = dalloc_t<__nv_bfloat16>((size_t)nG * T * m->Kg);
-  m->SxA = dalloc_t<__nv_bfloat16>((size_t)2 * nP * T * m->Kg);
-  m->WxA = dalloc_t<__nv_bfloat16>((size_t)nG * T * m->Kp);
-  m->WTxB = dalloc_t<__nv_bfloat16>((size_t)2 * nP * T * m->Kg);
-  m->RxB = dalloc_t<__nv_bfloat16>((size_t)2 * Q * T * m->Kp);
-  m->err = dalloc_t<int>(1);
-  CODY_CUDA(cudaMemset(m->err, 0, sizeof(int)));
-  m->Zd = dalloc_t<double>((size_t)2 * nG * Q);
-  // split-K partial buffers sized for the splits the GEMMs will use
-  int kt1 = T * m->Kg / 64, kt2 = T * m->Kp / 64;
-  int s1 = tc_split_count(nG, 2 * nP, tc_tile_n(2 * nP), kt1);
-  int s2 = tc_split_count(nG, 2 * Q, tc_tile_n(2 * Q), kt2);
-  int s3 = tc_split_count(2 * nP, 2 * nP, tc_tile_n(2 * nP), kt1);
-  m->cap1 = (size_t)s1 * nG * 2 * nP;
-  m->cap2 = (size_t)s2 * nG * 2 * Q;
-  m->cap3 = (size_t)s3 * 2 * nP * 2 * nP;
-  m->P1 = dalloc_t<float>(m->cap1);
-  m->P2 = dalloc_t<float>(m->cap2);
-  m->P3 = dalloc_t<float>(m->cap3);
-  k_split_V<<<blocks((size_t)nG * m->Kg), 256, 0, c->stream>>>(m->VxB, c->Vint_d, nG, m->Kg, T);
+// After the arena holds V: bf16 splits of V (static) and the TMA maps.
+void mixed_init(cgpu_ctx* c) {
+  MixedBufs* m = c->mixed;
+  if (!m) return;
+  int T = m->terms, pG = T * m->KgMax, pP = T * m->KpMax;
+  size_t nGK = (size_t)c->nG * m->KgMax;
+  k_split_V<<<bgrid(c, ew_blocks(c, nGK)), 256, 0, c->stream>>>(m->VxB, c->Vint_d, m->KgMax, T, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
+  int P2 = 2 * c->nPairs, Q2 = 2 * c->nOS * c->nOS;
+  m->mV = tc_make_map(c, m->VxB, c->nG, pG, 128);
+  m->mS = tc_make_map(c, m->SxA, P2, pG, m->bn1);
+  m->mW = tc_make_map(c, m->WxA, c->nG, pP, 128);
+  m->mR = tc_make_map(c, m->RxB, Q2, pP, m->bn2);
+  m->mSasB = tc_make_map(c, m->SxA, P2, pG, 128);
+  m->mWT = tc_make_map(c, m->WTxB, P2, pG, m->bn3);
   CODY_CUDA(cudaStreamSynchronize(c->stream));
 }
 
@@ -246,46 +306,39 @@ int mixed_error(cgpu_ctx* c) {
 void launch_correlation_mixed(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   launch_rdm_inverse(c);
   if (!c->hasInteraction) {
-    if (wantH2) CODY_CUDA(cudaMemsetAsync(c->h2_d, 0, sizeof(z_t) * (size_t)c->nO * c->nO * c->nO * c->nO, c->stream));
+    if (wantH2) batch_zero(c, c->h2_d, sizeof(z_t) * (size_t)c->nO * c->nO * c->nO * c->nO);
     return;
   }
-  mixed_setup(c);
   MixedBufs* m = c->mixed;
   int nG = c->nG, nP = c->nPairs, n = c->nOS, Q = n * n, T = m->terms;
-  int K1 = T * m->Kg, K2 = T * m->Kp;
   {
     ProfScope prof(c, CGPU_KERNEL_PAIR_POTENTIALS);
-    k_split_S<<<blocks((size_t)2 * nP * m->Kg), 256, 0, c->stream>>>(m->SxA, orbs, c->w_d, c->pairL_d, c->pairK_d,
-                                                                      nG, nP, m->Kg, T);
+    k_split_S<<<bgrid(c, ew_blocks(c, (size_t)2 * nP * m->KgMax)), 256, 0, c->stream>>>(
+        m->SxA, orbs, c->w_d, c->pairL_d, c->pairK_d, m->KgMax, T, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
-    int s1 = tc_split_count(nG, 2 * nP, tc_tile_n(2 * nP), K1 / 64);
     // V carries the B split pattern, S the A pattern: hi*hi + lo*hi + hi*lo (x3)
-    s1 = tc_gemm(c, m->VxB, nG, m->SxA, 2 * nP, K1, m->P1, s1, m->err);
-    k_split_W<<<blocks((size_t)nG * m->Kp), 256, 0, c->stream>>>(m->WxA, m->WTxB, m->P1, s1, nG, 2 * nP, m->Kp,
-                                                                  m->Kg, T);
+    tc_gemm(c, TC_GEMM_W, m->mV, m->mS, m->bn1, m->P1, T, m->KgMax, m->s1, nG, 2 * nP, m->err);
+    dim3 gw(ceil_div(m->KgMax, SW_T), ceil_div(m->KpMax, SW_T), c->nb);
+    k_split_W<<<gw, 256, 0, c->stream>>>(m->WxA, m->WTxB, m->P1, m->s1, m->KpMax, m->KgMax, T, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
-    if (m->Kg > nG) {
-      k_pad_WT<<<blocks((size_t)2 * nP * (m->Kg - nG)), 256, 0, c->stream>>>(m->WTxB, nG, 2 * nP, m->Kg, T);
-      CODY_LAUNCHED(c);
-    }
   }
   {
     ProfScope prof(c, CGPU_KERNEL_CORRELATION);
-    k_split_R<<<blocks((size_t)2 * Q * m->Kp), 256, 0, c->stream>>>(m->RxB, c->Rp_d, c->pairL_d, c->pairK_d, n, nP,
-                                                                     m->Kp, T);
+    k_split_R<<<bgrid(c, ew_blocks(c, (size_t)2 * Q * m->KpMax)), 256, 0, c->stream>>>(m->RxB, c->Rp_d, c->pairL_d,
+                                                                                   c->pairK_d, m->KpMax, T,
+                                                                                   TRAJ_PASS(c));
     CODY_LAUNCHED(c);
-    int s2 = tc_split_count(nG, 2 * Q, tc_tile_n(2 * Q), K2 / 64);
-    s2 = tc_gemm(c, m->WxA, nG, m->RxB, 2 * Q, K2, m->P2, s2, m->err);
+    tc_gemm(c, TC_GEMM_Z, m->mW, m->mR, m->bn2, m->P2, T, m->KpMax, m->s2, nG, 2 * Q, m->err);
     z_t* Z = (z_t*)m->Zd;
-    k_reduce_Z<<<blocks((size_t)nG * Q), 256, 0, c->stream>>>(Z, m->P2, s2, nG, Q);
+    k_reduce_Z<<<bgrid(c, ew_blocks(c, (size_t)nG * Q)), 256, 0, c->stream>>>(Z, m->P2, m->s2, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
     launch_corr_epilogue(c, dOrbs, orbs, Z);
   }
   if (wantH2) {
     ProfScope prof(c, CGPU_KERNEL_H2);
-    int s3 = tc_split_count(2 * nP, 2 * nP, tc_tile_n(2 * nP), K1 / 64);
-    s3 = tc_gemm(c, m->SxA, 2 * nP, m->WTxB, 2 * nP, K1, m->P3, s3, m->err);
-    k_reduce_H2<<<blocks((size_t)Q * Q), 256, 0, c->stream>>>(c->h2s_d, m->P3, s3, c->pidx_d, n, nP);
+    tc_gemm(c, TC_GEMM_H2, m->mSasB, m->mWT, m->bn3, m->P3, T, m->KgMax, m->s3, 2 * nP, 2 * nP, m->err);
+    k_reduce_H2<<<bgrid(c, ew_blocks(c, (size_t)Q * Q)), 256, 0, c->stream>>>(c->h2s_d, m->P3, m->s3, c->pidx_d,
+                                                                        TRAJ_PASS(c));
     CODY_LAUNCHED(c);
     launch_h2_layout(c);
   }

@@ -10,13 +10,16 @@
 //     (src/Utils/M_Utils_RdmObservables.f90:17-52)
 //
 // All reductions are deterministic: fixed grids, per-block partials in a
-// fixed order, no floating-point atomics.
+// fixed order, no floating-point atomics.  Every kernel covers all
+// trajectories of the context (blockIdx.z).
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace {
 
 constexpr int OB_THREADS = 256;
-constexpr int RED_BLOCKS = 148;  // partial-sum blocks for grid reductions
+constexpr int RED_BLOCKS = 148;  // partial-sum blocks for grid reductions (one trajectory)
 
 // ---------------------------------------------------------------------------
 // out[:, i] = alpha * ((T_bt + V0 + E x) orbs[:, i]) (+ out[:, i] if accumulate)
@@ -48,13 +51,21 @@ __device__ double field_amplitude_dev(const LaserDev& L, double t) {
 
 __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, const double* __restrict__ T,
                           const double* __restrict__ V0, const double* __restrict__ x, const int* __restrict__ btOf,
-                          int nG, int band, int restricted, LaserDev laser, const double* __restrict__ tBase,
-                          double tOff, int hasPot, z_t alpha, int accumulate) {
+                          TRAJ_ARGS, const double* __restrict__ tBase, double tOff, z_t alpha, int accumulate) {
   extern __shared__ z_t sh[];
   __shared__ double Eshared;
-  if (threadIdx.x == 0) Eshared = field_amplitude_dev(laser, *tBase + tOff);
+  const TrajShape& S = shp[blockIdx.z];
+  const int nG = S.nG, band = S.band;
   int i = blockIdx.y;
   int g0 = blockIdx.x * OB_THREADS;
+  if (i >= S.nOS || g0 >= nG) return;
+  out = bat(out, bs);
+  orbs = bat(orbs, bs);
+  T = bat(T, bs);
+  V0 = bat(V0, bs);
+  x = bat(x, bs);
+  btOf = bat(btOf, bs);
+  if (threadIdx.x == 0) Eshared = field_amplitude_dev(S.laser, *bat(tBase, bs) + tOff);
   const z_t* f = orbs + (size_t)nG * i;
   int nTile = OB_THREADS + 2 * band;
   for (int t = threadIdx.x; t < nTile; t += OB_THREADS) {
@@ -64,7 +75,7 @@ __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, c
   __syncthreads();
   int g = g0 + threadIdx.x;
   if (g >= nG) return;
-  int bt = restricted ? 0 : btOf[i];
+  int bt = S.restricted ? 0 : btOf[i];
   int nd = 2 * band + 1;
   const double* Tb = T + (size_t)bt * nd * nG;
   z_t acc = zmk(0.0, 0.0);
@@ -74,7 +85,7 @@ __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, c
     acc.x = fma(c, v.x, acc.x);
     acc.y = fma(c, v.y, acc.y);
   }
-  if (hasPot) {
+  if (S.hasPot) {
     double pot = V0[g] + Eshared * x[g];
     z_t v = sh[threadIdx.x + band];
     acc.x = fma(pot, v.x, acc.x);
@@ -86,30 +97,52 @@ __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, c
   out[o] = r;
 }
 
+// Column range of a Gram / projector call: group < 0 = all stored orbitals,
+// otherwise projector group `group` (false when the trajectory has none).
+__device__ __forceinline__ bool gram_cols(const TrajShape& S, int group, int& c0, int& n) {
+  if (group < 0) {
+    c0 = 0;
+    n = S.nOS;
+    return true;
+  }
+  if (group >= S.nGroups) return false;
+  c0 = S.grpStart[group];
+  n = S.grpSize[group];
+  return n > 0;
+}
+
 // ---------------------------------------------------------------------------
 // Weighted Gram partials: part[blk][i + n*j] = sum_{g in chunks of blk}
-//   conj(A[g, colA0+i]) * B[g, colB0+j] * w[g]
+//   conj(A[g, c0+i]) * B[g, c0+j] * w[g]
 // ---------------------------------------------------------------------------
 constexpr int GR_CHUNK = 32;
 constexpr int GR_PER_THREAD = 16;  // 256 threads x 16 = 4096 = 64^2 Gram entries
 
 __global__ void k_gram_partial(z_t* __restrict__ part, const z_t* __restrict__ A, const z_t* __restrict__ B,
-                               const double* __restrict__ w, int nG, int n, int colA0, int colB0, int chunk) {
+                               const double* __restrict__ w, TRAJ_ARGS, int group, int chunk) {
   extern __shared__ z_t sh[];
+  const TrajShape& S = shp[blockIdx.z];
+  int c0, n;
+  if (!gram_cols(S, group, c0, n)) return;
+  const int nG = S.nG;
+  part = bat(part, bs);
+  A = bat(A, bs);
+  B = bat(B, bs);
+  w = bat(w, bs);
   z_t* sa = sh;                 // chunk x n
   z_t* sb = sh + chunk * n;     // chunk x n
   int nn = n * n;
   z_t acc[GR_PER_THREAD];
   for (int q = 0; q < GR_PER_THREAD; q++) acc[q] = zmk(0.0, 0.0);
-  for (int c0 = blockIdx.x * chunk; c0 < nG; c0 += gridDim.x * chunk) {
+  for (int r0 = blockIdx.x * chunk; r0 < nG; r0 += gridDim.x * chunk) {
     __syncthreads();
     for (int t = threadIdx.x; t < chunk * n; t += blockDim.x) {
       int col = t / chunk, r = t % chunk;
-      int g = c0 + r;
+      int g = r0 + r;
       z_t a = zmk(0.0, 0.0), b = zmk(0.0, 0.0);
       if (g < nG) {
-        a = A[(size_t)nG * (colA0 + col) + g];
-        b = B[(size_t)nG * (colB0 + col) + g];
+        a = A[(size_t)nG * (c0 + col) + g];
+        b = B[(size_t)nG * (c0 + col) + g];
         b = zscale(b, w[g]);
       }
       sa[r * n + col] = a;
@@ -138,13 +171,18 @@ __global__ void k_gram_partial(z_t* __restrict__ part, const z_t* __restrict__ A
   }
 }
 
-// one warp per Gram entry, lanes over the block partials (fixed order)
-__global__ void k_gram_final(z_t* __restrict__ G, const z_t* __restrict__ part, int nBlk, int n, int ldG,
+// one warp per Gram entry, lanes over the block partials (fixed order); G is n x n
+__global__ void k_gram_final(z_t* __restrict__ G, const z_t* __restrict__ part, int nBlk, TRAJ_ARGS, int group,
                              double scale) {
+  const TrajShape& S = shp[blockIdx.z];
+  int c0, n;
+  if (!gram_cols(S, group, c0, n)) return;
   int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   int nn = n * n;
   if (e >= nn) return;
+  G = bat(G, bs);
+  part = bat(part, bs);
   z_t s = zmk(0.0, 0.0);
   for (int b = lane; b < nBlk; b += 32) s = zadd(s, part[(size_t)b * nn + e]);
   for (int o = 16; o > 0; o >>= 1) {
@@ -153,16 +191,23 @@ __global__ void k_gram_final(z_t* __restrict__ G, const z_t* __restrict__ part, 
   }
   if (lane == 0) {
     int i = e % n, j = e / n;
-    G[i + (size_t)ldG * j] = zscale(s, scale);
+    G[i + (size_t)n * j] = zscale(s, scale);
   }
 }
 
 // dOrbs[:, c0+j] -= sum_i orbs[:, c0+i] * G[i + n*j]
 __global__ void k_project_apply(z_t* __restrict__ dOrbs, const z_t* __restrict__ orbs, const z_t* __restrict__ G,
-                                int nG, int n, int c0) {
+                                TRAJ_ARGS, int group) {
+  const TrajShape& S = shp[blockIdx.z];
+  int c0, n;
+  if (!gram_cols(S, group, c0, n)) return;
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   int j = blockIdx.y;
-  if (g >= nG) return;
+  const int nG = S.nG;
+  if (g >= nG || j >= n) return;
+  dOrbs = bat(dOrbs, bs);
+  orbs = bat(orbs, bs);
+  G = bat(G, bs);
   z_t acc = zmk(0.0, 0.0);
   for (int i = 0; i < n; i++) zfma(acc, orbs[(size_t)nG * (c0 + i) + g], G[i + (size_t)n * j]);
   size_t o = (size_t)nG * (c0 + j) + g;
@@ -171,13 +216,18 @@ __global__ void k_project_apply(z_t* __restrict__ dOrbs, const z_t* __restrict__
 
 // h1 (nO x nO) from the stored-orbital Gram G (nOS x nOS): same body type only,
 // restricted runs duplicate the block for the second spin (FillH1 :203-222).
-__global__ void k_h1_layout(z_t* __restrict__ h1, const z_t* __restrict__ G, const int* __restrict__ btOf, int nO,
-                            int nOS, int restricted) {
+__global__ void k_h1_layout(z_t* __restrict__ h1, const z_t* __restrict__ G, const int* __restrict__ btOf,
+                            TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  const int nO = S.nO, nOS = S.nOS;
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nO * nO) return;
+  h1 = bat(h1, bs);
+  G = bat(G, bs);
+  btOf = bat(btOf, bs);
   int i = e % nO, j = e / nO;
   z_t v = zmk(0.0, 0.0);
-  if (restricted) {
+  if (S.restricted) {
     if ((i < nOS) == (j < nOS)) v = G[(i % nOS) + (size_t)nOS * (j % nOS)];
   } else {
     if (btOf[i] == btOf[j]) v = G[i + (size_t)nOS * j];
@@ -186,26 +236,43 @@ __global__ void k_h1_layout(z_t* __restrict__ h1, const z_t* __restrict__ G, con
 }
 
 // ---------------------------------------------------------------------------
-// Vector kernels
+// Vector kernels over a state vector (sel VSEL_STATE) or its coefficients
 // ---------------------------------------------------------------------------
-__global__ void k_axpby(z_t* __restrict__ y, const z_t* __restrict__ x, z_t a, z_t b, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+__global__ void k_axpby(z_t* __restrict__ y, const z_t* __restrict__ x, z_t a, z_t b, TRAJ_ARGS, int sel) {
+  const TrajShape& S = shp[blockIdx.z];
+  y = bat(y, bs);
+  x = bat(x, bs);
+  size_t n = vlen(S, sel);
+  for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+    size_t i = vidx(S, l);
     z_t r = zmul(b, y[i]);
     zfma(r, a, x[i]);
     y[i] = r;
   }
 }
 
-__global__ void k_scale(z_t* __restrict__ y, z_t a, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+__global__ void k_scale(z_t* __restrict__ y, z_t a, TRAJ_ARGS, int sel) {
+  const TrajShape& S = shp[blockIdx.z];
+  y = bat(y, bs);
+  size_t n = vlen(S, sel);
+  for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+    size_t i = vidx(S, l);
     y[i] = zmul(a, y[i]);
+  }
 }
 
 // RK4 stage bookkeeping (S_IntegratorList_Rk_O4Expl.f90:109-135):
 // inc = (first ? 0 : inc) + d*wInc; tmp = state + d*wTmp
 __global__ void k_rk_stage(z_t* __restrict__ inc, z_t* __restrict__ tmp, const z_t* __restrict__ state,
-                           const z_t* __restrict__ d, double wInc, double wTmp, int first, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+                           const z_t* __restrict__ d, double wInc, double wTmp, int first, TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  inc = bat(inc, bs);
+  tmp = bat(tmp, bs);
+  state = bat(state, bs);
+  d = bat(d, bs);
+  size_t n = S.nS;
+  for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+    size_t i = vidx(S, l);
     z_t di = d[i];
     z_t v = zscale(di, wInc);
     inc[i] = first ? v : zadd(inc[i], v);
@@ -234,8 +301,14 @@ __device__ z_t block_sum(z_t v) {
   return v;  // valid in thread 0
 }
 
-// part[blk] = sum conj(a) b over the block's stride
-__global__ void k_dot_partial(z_t* __restrict__ part, const z_t* __restrict__ a, const z_t* __restrict__ b, size_t n) {
+// part[blk] = sum conj(a) b over the block's stride of the coefficients
+__global__ void k_dot_partial(z_t* __restrict__ part, const z_t* __restrict__ a, const z_t* __restrict__ b,
+                              TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  part = bat(part, bs);
+  a = bat(a, bs);
+  b = bat(b, bs);
+  size_t n = S.nC;
   z_t s = zmk(0.0, 0.0);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     z_t u = a[i], v = b[i];
@@ -248,10 +321,15 @@ __global__ void k_dot_partial(z_t* __restrict__ part, const z_t* __restrict__ a,
 
 // dC -= (sum of partials) * C   (dot_product(coeffs, dCoeffs) = sum conj(C) dC)
 __global__ void k_project_coeffs_apply(z_t* __restrict__ dC, const z_t* __restrict__ C, const z_t* __restrict__ part,
-                                       int nBlk, size_t n) {
+                                       int nBlk, TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  dC = bat(dC, bs);
+  C = bat(C, bs);
+  part = bat(part, bs);
   __shared__ z_t ov[1];
   sum_partials(part, nBlk, 1, 1, ov);
   z_t o = ov[0];
+  size_t n = S.nC;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     z_t r = dC[i];
     z_t c = C[i];
@@ -261,19 +339,29 @@ __global__ void k_project_coeffs_apply(z_t* __restrict__ dC, const z_t* __restri
   }
 }
 
-__global__ void k_normalize_apply(z_t* __restrict__ C, const z_t* __restrict__ part, int nBlk, size_t n) {
+__global__ void k_normalize_apply(z_t* __restrict__ C, const z_t* __restrict__ part, int nBlk, TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  C = bat(C, bs);
+  part = bat(part, bs);
   __shared__ z_t tot[1];
   sum_partials(part, nBlk, 1, 1, tot);
   double nr = sqrt(tot[0].x);
+  size_t n = S.nC;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     z_t c = C[i];
     C[i] = zmk(c.x / nr, c.y / nr);
   }
 }
 
-// Modified Gram-Schmidt, two sweeps, one CTA (src/Grid/S_Grid.f90:120-151).
+// Modified Gram-Schmidt, two sweeps, one CTA per trajectory (src/Grid/S_Grid.f90:120-151).
 // Used only for relaxation / set-up, not in the real-time step.
-__global__ void k_mgs2(z_t* __restrict__ f, const double* __restrict__ w, int nG, int c0, int n, int* status) {
+__global__ void k_mgs2(z_t* __restrict__ f, const double* __restrict__ w, TRAJ_ARGS, int c0, int n, int* status) {
+  const TrajShape& S = shp[blockIdx.z];
+  const int nG = S.nG;
+  f = bat(f, bs);
+  w = bat(w, bs);
+  status = bat(status, bs);
+  if (c0 + n > S.nOS) n = S.nOS - c0;
   for (int i1 = c0; i1 < c0 + n; i1++) {
     for (int pass = 0; pass < 2; pass++)
       for (int j1 = c0; j1 < i1; j1++) {
@@ -321,9 +409,16 @@ __global__ void k_mgs2(z_t* __restrict__ f, const double* __restrict__ w, int nG
 
 // E = Re[ sum h1(k,l) rho1(l,k) + sum h2(k1,k2,l1,l2) rho2(l1,l2,k1,k2) ]
 __global__ void k_energy(double* out, const z_t* __restrict__ h1, const z_t* __restrict__ r1,
-                         const z_t* __restrict__ h2, const z_t* __restrict__ r2, int nO) {
+                         const z_t* __restrict__ h2, const z_t* __restrict__ r2, TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  const size_t nO = S.nO;
+  out = bat(out, bs);
+  h1 = bat(h1, bs);
+  r1 = bat(r1, bs);
+  h2 = bat(h2, bs);
+  r2 = bat(r2, bs);
   z_t s = zmk(0.0, 0.0);
-  size_t n2 = (size_t)nO * nO;
+  size_t n2 = nO * nO;
   for (size_t e = threadIdx.x; e < n2; e += blockDim.x) {
     size_t k = e % nO, l = e / nO;
     zfma(s, h1[k + nO * l], r1[l + nO * k]);
@@ -336,128 +431,147 @@ __global__ void k_energy(double* out, const z_t* __restrict__ h1, const z_t* __r
   if (threadIdx.x == 0) *out = s.x;
 }
 
-int grid_for(size_t n, int threads) {
-  size_t b = (n + threads - 1) / threads;
-  if (b > 152 * 8) b = 152 * 8;
-  if (b < 1) b = 1;
-  return (int)b;
+__global__ void k_set_scalar(double* p, double v, size_t bs) { *bat(p, bs) = v; }
+__global__ void k_add_scalar(double* p, double v, size_t bs) { *bat(p, bs) += v; }
+
+// Blocks per trajectory for a grid-stride kernel over n items.
+unsigned vec_blocks(const cgpu_ctx* c, size_t n) {
+  size_t b = (n + 255) / 256;
+  size_t cap = std::max<size_t>(4, 4864 / (size_t)c->nb);
+  return (unsigned)std::max<size_t>(1, std::min(b, cap));
 }
 
-void ensure_partial(cgpu_ctx* c, size_t n) {
-  if (c->partialCap >= n) return;
-  if (c->partial_d) cudaFree(c->partial_d);
-  CODY_CUDA(cudaMalloc(&c->partial_d, n * sizeof(z_t)));
-  c->partialCap = n;
+int gram_chunk(int n) { return std::max(1, std::min(GR_CHUNK, 1024 / std::max(n, 1))); }  // <= 32 KB shared
+
+int gram_blocks(const cgpu_ctx* c, int chunk) {
+  int nBlk = std::min(RED_BLOCKS, (c->nG + chunk - 1) / chunk);
+  if (c->nb > 1) nBlk = std::max(1, std::min(nBlk, (c->nG + 4 * chunk - 1) / (4 * chunk)));
+  return nBlk;
+}
+
+int coeff_blocks(const cgpu_ctx* c) {
+  return (int)std::min<unsigned>(RED_BLOCKS, vec_blocks(c, c->nC));
+}
+
+void check_partial(const cgpu_ctx* c, size_t need) {
+  if (need > c->partialCap) throw std::string("internal: reduction scratch too small");
+}
+
+// grid/launch of the two-kernel Gram: G (n x n) = scale * A^H W B over the group's columns
+void launch_gram(cgpu_ctx* c, z_t* G, const z_t* A, const z_t* B, int group, int nMax, double scale) {
+  int chunk = gram_chunk(nMax);
+  int nBlk = gram_blocks(c, chunk);
+  check_partial(c, (size_t)nBlk * nMax * nMax);
+  size_t sh = 2 * sizeof(z_t) * chunk * nMax;
+  int threads = 256;
+  if (nMax * nMax > GR_PER_THREAD * threads) throw std::string("launch_gram: more than 64 orbitals");
+  k_gram_partial<<<bgrid(c, nBlk), threads, sh, c->stream>>>(c->partial_d, A, B, c->w_d, TRAJ_PASS(c), group, chunk);
+  CODY_LAUNCHED(c);
+  k_gram_final<<<bgrid(c, ceil_div((size_t)nMax * nMax * 32, 256)), 256, 0, c->stream>>>(G, c->partial_d, nBlk,
+                                                                                         TRAJ_PASS(c), group, scale);
+  CODY_LAUNCHED(c);
+}
+
+int max_group_size(const cgpu_ctx* c, int g) {
+  int m = 0;
+  for (const TrajShape& s : c->shape_h)
+    if (g < s.nGroups) m = std::max(m, s.grpSize[g]);
+  return m;
 }
 
 }  // namespace
 
-double cody_field_amplitude(const cgpu_ctx* c, double t) {
-  if (c->laserKind == CGPU_LASER_SIN2) {
-    if (c->omega <= 0.0) return 0.0;
-    const double PI = 3.14159265358979323846264338327950288;
-    double duration = 2.0 * PI * c->nCycles / c->omega;
-    double tRel = t - c->tStart;
-    if (tRel < 0.0 || tRel > duration) return 0.0;
-    double env = sin(PI * tRel / duration);
-    env = env * env;
-    return c->E0 * env * cos(c->omega * (tRel - 0.5 * duration) + c->cep);
-  }
-  if (c->laserKind == CGPU_LASER_SAMPLED) {
-    double u = (t - c->sampleT0) / c->sampleDt;
-    long n = (long)floor(u + 1e-9);
-    if (n < 0 || n >= (long)c->samples.size()) return 0.0;
-    return c->samples[n];
-  }
-  return 0.0;
+size_t gram_partial_need(const cgpu_ctx* c, int n) {
+  int chunk = gram_chunk(n);
+  return (size_t)gram_blocks(c, chunk) * n * n;
 }
 
 void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha, int accumulate) {
   ProfScope prof(c, CGPU_KERNEL_ONEBODY);
-  int hasPot = c->hasPotential || c->laserKind != CGPU_LASER_NONE;
-  dim3 grid((c->nG + OB_THREADS - 1) / OB_THREADS, c->nOS);
+  dim3 grid(ceil_div(c->nG, OB_THREADS), c->nOS, c->nb);
   size_t sh = sizeof(z_t) * (OB_THREADS + 2 * c->band);
-  const double* base = c->inCapture ? c->stepT_d : c->zero_d;
+  const double* base = (c->inCapture || c->useStepTime) ? c->stepT_d : c->zero_d;
   double off = c->inCapture ? t - c->captureT0 : t;
-  k_onebody<<<grid, OB_THREADS, sh, c->stream>>>(out, orbs, c->T_d, c->V0_d, c->x_d, c->btOfOrb_d, c->nG, c->band,
-                                                 c->restricted, c->laserDev, base, off, hasPot, alpha, accumulate);
+  k_onebody<<<grid, OB_THREADS, sh, c->stream>>>(out, orbs, c->T_d, c->V0_d, c->x_d, c->btOfOrb_d, TRAJ_PASS(c), base,
+                                                 off, alpha, accumulate);
   CODY_LAUNCHED(c);
 }
 
-void launch_gram(cgpu_ctx* c, z_t* G, const z_t* A, const z_t* B, int n, int colA0, int colB0, int ldG, double scale) {
-  int chunk = std::max(1, std::min(GR_CHUNK, 1024 / std::max(n, 1)));  // <= 32 KB of shared memory
-  int nBlk = std::min(RED_BLOCKS, (c->nG + chunk - 1) / chunk);
-  ensure_partial(c, (size_t)nBlk * n * n);
-  size_t sh = 2 * sizeof(z_t) * chunk * n;
-  int threads = 256;
-  if (n * n > GR_PER_THREAD * threads) throw std::string("launch_gram: more than 64 orbitals");
-  k_gram_partial<<<nBlk, threads, sh, c->stream>>>(c->partial_d, A, B, c->w_d, c->nG, n, colA0, colB0, chunk);
-  CODY_LAUNCHED(c);
-  k_gram_final<<<(n * n * 32 + 255) / 256, 256, 0, c->stream>>>(G, c->partial_d, nBlk, n, ldG, scale);
-  CODY_LAUNCHED(c);
-}
-
-// Orbs_ProjectOnSubspace: one block when restricted, otherwise per body type.
+// Orbs_ProjectOnSubspace: one group when restricted, otherwise per body type.
 void launch_project_orbs(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs) {
   int nGroups = c->restricted ? 1 : c->nBt;
-  for (int b = 0; b < nGroups; b++) {
-    int c0 = c->restricted ? 0 : c->orbStart[b];
-    int n = c->restricted ? c->nOS : c->nOrbs[b];
-    launch_gram(c, c->gram_d, orbs, dOrbs, n, c0, c0, n, 1.0);
-    dim3 grid((c->nG + 255) / 256, n);
-    k_project_apply<<<grid, 256, 0, c->stream>>>(dOrbs, orbs, c->gram_d, c->nG, n, c0);
+  for (int g = 0; g < nGroups; g++) {
+    int n = max_group_size(c, g);
+    if (n <= 0) continue;
+    launch_gram(c, c->gram_d, orbs, dOrbs, g, n, 1.0);
+    dim3 grid(ceil_div(c->nG, 256), n, c->nb);
+    k_project_apply<<<grid, 256, 0, c->stream>>>(dOrbs, orbs, c->gram_d, TRAJ_PASS(c), g);
     CODY_LAUNCHED(c);
   }
 }
 
 void launch_project_coeffs(cgpu_ctx* c, z_t* dC, const z_t* C) {
-  int nBlk = std::min(RED_BLOCKS, grid_for(c->nC, 256));
-  ensure_partial(c, nBlk);
-  k_dot_partial<<<nBlk, 256, 0, c->stream>>>(c->partial_d, C, dC, c->nC);
+  int nBlk = coeff_blocks(c);
+  check_partial(c, nBlk);
+  k_dot_partial<<<bgrid(c, nBlk), 256, 0, c->stream>>>(c->partial_d, C, dC, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
-  k_project_coeffs_apply<<<grid_for(c->nC, 256), 256, 0, c->stream>>>(dC, C, c->partial_d, nBlk, c->nC);
+  k_project_coeffs_apply<<<bgrid(c, vec_blocks(c, c->nC)), 256, 0, c->stream>>>(dC, C, c->partial_d, nBlk,
+                                                                                  TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
 void launch_normalize_coeffs(cgpu_ctx* c, z_t* C) {
-  int nBlk = std::min(RED_BLOCKS, grid_for(c->nC, 256));
-  ensure_partial(c, nBlk);
-  k_dot_partial<<<nBlk, 256, 0, c->stream>>>(c->partial_d, C, C, c->nC);
+  int nBlk = coeff_blocks(c);
+  check_partial(c, nBlk);
+  k_dot_partial<<<bgrid(c, nBlk), 256, 0, c->stream>>>(c->partial_d, C, C, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
-  k_normalize_apply<<<grid_for(c->nC, 256), 256, 0, c->stream>>>(C, c->partial_d, nBlk, c->nC);
+  k_normalize_apply<<<bgrid(c, vec_blocks(c, c->nC)), 256, 0, c->stream>>>(C, c->partial_d, nBlk, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
 void launch_fill_h1_from(cgpu_ctx* c, const z_t* orbs, const z_t* hOrbs, z_t* h1) {
-  launch_gram(c, c->gram_d, orbs, hOrbs, c->nOS, 0, 0, c->nOS, 1.0);
+  launch_gram(c, c->gram_d, orbs, hOrbs, -1, c->nOS, 1.0);
   int nn = c->nO * c->nO;
-  k_h1_layout<<<(nn + 127) / 128, 128, 0, c->stream>>>(h1, c->gram_d, c->btOfOrb_d, c->nO, c->nOS, c->restricted);
+  k_h1_layout<<<bgrid(c, ceil_div(nn, 128)), 128, 0, c->stream>>>(h1, c->gram_d, c->btOfOrb_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
-void launch_axpby(cgpu_ctx* c, z_t* y, const z_t* x, z_t a, z_t b, size_t n) {
-  k_axpby<<<grid_for(n, 256), 256, 0, c->stream>>>(y, x, a, b, n);
+void launch_axpby(cgpu_ctx* c, z_t* y, const z_t* x, z_t a, z_t b, int sel) {
+  size_t n = sel == VSEL_STATE ? c->nS : c->nC;
+  k_axpby<<<bgrid(c, vec_blocks(c, n)), 256, 0, c->stream>>>(y, x, a, b, TRAJ_PASS(c), sel);
   CODY_LAUNCHED(c);
 }
 
-void launch_scale(cgpu_ctx* c, z_t* y, z_t a, size_t n) {
-  k_scale<<<grid_for(n, 256), 256, 0, c->stream>>>(y, a, n);
+void launch_scale(cgpu_ctx* c, z_t* y, z_t a, int sel) {
+  size_t n = sel == VSEL_STATE ? c->nS : c->nC;
+  k_scale<<<bgrid(c, vec_blocks(c, n)), 256, 0, c->stream>>>(y, a, TRAJ_PASS(c), sel);
   CODY_LAUNCHED(c);
 }
 
 void launch_rk_stage(cgpu_ctx* c, z_t* inc, z_t* tmp, const z_t* state, const z_t* d, double wInc, double wTmp,
-                     int first, size_t n) {
-  k_rk_stage<<<grid_for(n, 256), 256, 0, c->stream>>>(inc, tmp, state, d, wInc, wTmp, first, n);
+                     int first) {
+  k_rk_stage<<<bgrid(c, vec_blocks(c, c->nS)), 256, 0, c->stream>>>(inc, tmp, state, d, wInc, wTmp, first,
+                                                                      TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
 void launch_orthonormalize(cgpu_ctx* c, z_t* orbs, int col0, int nCols) {
-  CODY_CUDA(cudaMemsetAsync(c->scal_d, 0, sizeof(int), c->stream));
-  k_mgs2<<<1, 1024, 0, c->stream>>>(orbs, c->w_d, c->nG, col0, nCols, (int*)c->scal_d);
+  batch_zero(c, c->scal_d, sizeof(int));
+  k_mgs2<<<bgrid(c, 1), 1024, 0, c->stream>>>(orbs, c->w_d, TRAJ_PASS(c), col0, nCols, (int*)c->scal_d);
   CODY_LAUNCHED(c);
 }
 
 void launch_energy(cgpu_ctx* c, double* out_d) {
-  k_energy<<<1, 1024, 0, c->stream>>>(out_d, c->h1_d, c->rdm1_d, c->h2_d, c->rdm2_d, c->nO);
+  k_energy<<<bgrid(c, 1), 1024, 0, c->stream>>>(out_d, c->h1_d, c->rdm1_d, c->h2_d, c->rdm2_d, TRAJ_PASS(c));
+  CODY_LAUNCHED(c);
+}
+
+void launch_set_scalar(cgpu_ctx* c, double* p, double v) {
+  k_set_scalar<<<bgrid(c, 1), 1, 0, c->stream>>>(p, v, c->bs);
+  CODY_LAUNCHED(c);
+}
+
+void launch_add_scalar(cgpu_ctx* c, double* p, double v) {
+  k_add_scalar<<<bgrid(c, 1), 1, 0, c->stream>>>(p, v, c->bs);
   CODY_LAUNCHED(c);
 }

@@ -63,11 +63,12 @@ __device__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abortFla
   return true;
 }
 
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
+                                            int c2) {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          smem_u32(dst)),
-      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
       : "memory");
 }
 
@@ -99,11 +100,21 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
                  "=r"(r[14]), "=r"(r[15])                                                                      \
                : "r"(taddr))
 
-// P[z][m][n] = sum_{k in split z} A[m][k] B[n][k]; A rows m0.., B rows n0.., bf16 K-major.
+// Per-trajectory sizes of a contraction: M rows of A, N rows of B, K tiles per segment.
+__device__ __forceinline__ void tc_dims(const TrajShape& S, int gemmId, int& M, int& N, int& segTiles) {
+  int P2 = 2 * S.nPairs, Q2 = 2 * S.nOS * S.nOS;
+  if (gemmId == TC_GEMM_W) { M = S.nG; N = P2; segTiles = S.Kg / TC_BK; }
+  else if (gemmId == TC_GEMM_Z) { M = S.nG; N = Q2; segTiles = S.Kp / TC_BK; }
+  else { M = P2; N = P2; segTiles = S.Kg / TC_BK; }
+}
+
+// P[traj][z][m][n] = sum_{k in split z} A[m][k] B[n][k]; A rows m0.., B rows n0.., bf16 K-major.
+// blockIdx.z = trajectory * nSplit + split.  K tile i of the trajectory lies in
+// segment i / segTiles at element (segment * segPitch + (i % segTiles) * 64).
 template <int BN, int STAGES>
 __global__ void __launch_bounds__(128, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, float* __restrict__ P,
-              int M, int N, int ldp, int kTiles, int kTilesPerSplit, int* __restrict__ err) {
+              TRAJ_ARGS, int gemmId, int terms, int segPitch, int nSplit, int* __restrict__ err) {
   constexpr int A_BYTES = TC_BM * TC_BK * 2;
   constexpr int B_BYTES = BN * TC_BK * 2;
   constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
@@ -118,10 +129,25 @@ __global__ void __launch_bounds__(128, 1)
   __shared__ int consumed;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int traj = blockIdx.z / nSplit, split = blockIdx.z % nSplit;
+  int M, N, segTiles;
+  tc_dims(shp[traj], gemmId, M, N, segTiles);
   const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * BN;
-  const int kt0 = blockIdx.z * kTilesPerSplit;
-  const int kt1 = min(kTiles, kt0 + kTilesPerSplit);
-  const int nk = kt1 - kt0;
+  if (m0 >= M || n0 >= N) return;  // tile outside this trajectory's output
+  const int ldp = N;
+  const int kTiles = terms * segTiles;
+  const int per = (kTiles + nSplit - 1) / nSplit;
+  const int kt0 = split * per;
+  const int kt1 = min(kTiles, kt0 + per);
+  const int nk = max(0, kt1 - kt0);
+  float* Pz = batn(P, bs, traj) + (size_t)split * (size_t)M * ldp;
+  if (nk == 0) {  // empty split: its partial is zero
+    for (int e = threadIdx.x; e < TC_BM * BN; e += blockDim.x) {
+      int r = m0 + e / BN, col = n0 + e % BN;
+      if (r < M && col < N) Pz[(size_t)r * ldp + col] = 0.0f;
+    }
+    return;
+  }
 
   if (threadIdx.x == 0) {
     abortFlag = 0;
@@ -155,8 +181,10 @@ __global__ void __launch_bounds__(128, 1)
         break;
       }
       mbar_expect_tx(&fullBar[s], STAGE_BYTES);
-      tma_load_2d(smem + s * STAGE_BYTES, &tA, &fullBar[s], (kt0 + i) * TC_BK, m0);
-      tma_load_2d(smem + s * STAGE_BYTES + A_BYTES, &tB, &fullBar[s], (kt0 + i) * TC_BK, n0);
+      int kt = kt0 + i;
+      int x = (kt / segTiles) * segPitch + (kt % segTiles) * TC_BK;
+      tma_load_3d(smem + s * STAGE_BYTES, &tA, &fullBar[s], x, m0, traj);
+      tma_load_3d(smem + s * STAGE_BYTES + A_BYTES, &tB, &fullBar[s], x, n0, traj);
       issued = i + 1;
     }
   } else if (nk > 0 && warp == 1 && lane == 0) {
@@ -189,7 +217,6 @@ __global__ void __launch_bounds__(128, 1)
   __syncwarp();
   // epilogue: warp w owns TMEM lanes [32w, 32w+32) = tile rows
   const int row = m0 + warp * 32 + lane;
-  float* Pz = P + (size_t)blockIdx.z * (size_t)M * ldp;
 #pragma unroll 1
   for (int c = 0; c < BN; c += 16) {
     uint32_t r[16];
@@ -229,38 +256,19 @@ void ensure_encode() {
   g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
 }
 
-// 2D bf16 tensor [rows, kCols] row-major (kCols contiguous, multiple of 64); box = 64 x boxRows.
-CUtensorMap make_tmap(const void* base, int rows, int kCols, int boxRows) {
-  ensure_encode();
-  if ((uintptr_t)base % 16 != 0 || kCols % TC_BK != 0) throw std::string("tensor map: bad alignment");
-  CUtensorMap m;
-  std::memset(&m, 0, sizeof(m));
-  cuuint64_t dims[2] = {(cuuint64_t)kCols, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)kCols * 2};
-  cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)boxRows};
-  cuuint32_t es[2] = {1, 1};
-  CUresult r = g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) throw std::string("cuda: cuTensorMapEncodeTiled failed");
-  return m;
-}
-
 template <int BN, int STAGES>
-int launch_gemm_t(cgpu_ctx* c, const CUtensorMap& ta, const CUtensorMap& tb, float* P, int M, int N, int kTiles,
-                  int nSplit, int* err) {
+void launch_gemm_t(cgpu_ctx* c, const CUtensorMap& ta, const CUtensorMap& tb, float* P, int gemmId, int terms,
+                   int segPitch, int nSplit, int Mmax, int Nmax, int* err) {
   constexpr int smem = STAGES * (TC_BM * TC_BK * 2 + BN * TC_BK * 2) + 1024;
   static bool attr = false;
   if (!attr) {
     CODY_CUDA(cudaFuncSetAttribute(k_tc_gemm<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     attr = true;
   }
-  int per = (kTiles + nSplit - 1) / nSplit;
-  nSplit = (kTiles + per - 1) / per;
-  dim3 grid((M + TC_BM - 1) / TC_BM, (N + BN - 1) / BN, nSplit);
-  k_tc_gemm<BN, STAGES><<<grid, 128, smem, c->stream>>>(ta, tb, P, M, N, N, kTiles, per, err);
+  dim3 grid(ceil_div(Mmax, TC_BM), ceil_div(Nmax, BN), (unsigned)(c->nb * nSplit));
+  k_tc_gemm<BN, STAGES><<<grid, 128, smem, c->stream>>>(ta, tb, P, TRAJ_PASS(c), gemmId, terms, segPitch, nSplit,
+                                                        err);
   CODY_LAUNCHED(c);
-  return nSplit;
 }
 
 }  // namespace
@@ -274,22 +282,36 @@ int tc_tile_n(int N) {
   return best;
 }
 
-int tc_split_count(int M, int N, int BN, int kTiles) {
-  int tiles = ((M + TC_BM - 1) / TC_BM) * ((N + BN - 1) / BN);
-  int s = std::max(1, (152 + tiles - 1) / tiles);
+int tc_split_count(int M, int N, int BN, int kTiles, int nb) {
+  long tiles = (long)((M + TC_BM - 1) / TC_BM) * ((N + BN - 1) / BN) * nb;
+  int s = (int)std::max<long>(1, (152 + tiles - 1) / tiles);
   s = std::min(s, std::max(1, kTiles / 2));
   int per = (kTiles + s - 1) / s;
   return (kTiles + per - 1) / per;
 }
 
-// P[split][M][N] (fp32) = A[M, K] B[N, K]^T, bf16 operands with K a multiple of 64.
-int tc_gemm(cgpu_ctx* c, const __nv_bfloat16* A, int M, const __nv_bfloat16* B, int N, int K, float* P, int nSplit,
-            int* err) {
-  if (K % TC_BK != 0 || K <= 0) throw std::string("tc_gemm: K must be a positive multiple of 64");
-  int kTiles = K / TC_BK;
-  int bn = tc_tile_n(N);
-  CUtensorMap ta = make_tmap(A, M, K, TC_BM), tb = make_tmap(B, N, K, bn);
-  if (bn == 64) return launch_gemm_t<64, 6>(c, ta, tb, P, M, N, kTiles, nSplit, err);
-  if (bn == 128) return launch_gemm_t<128, 5>(c, ta, tb, P, M, N, kTiles, nSplit, err);
-  return launch_gemm_t<256, 4>(c, ta, tb, P, M, N, kTiles, nSplit, err);
+// 3D bf16 tensor [nb][rowsMax][pitch] (pitch contiguous, multiple of 64, trajectories bs bytes apart).
+CUtensorMap tc_make_map(const cgpu_ctx* c, const __nv_bfloat16* base, int rowsMax, int pitch, int boxRows) {
+  ensure_encode();
+  if ((uintptr_t)base % 16 != 0 || pitch % TC_BK != 0 || c->bs % 16 != 0)
+    throw std::string("tensor map: bad alignment");
+  CUtensorMap m;
+  std::memset(&m, 0, sizeof(m));
+  cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)rowsMax, (cuuint64_t)c->nb};
+  cuuint64_t strides[2] = {(cuuint64_t)pitch * 2, (cuuint64_t)c->bs};
+  cuuint32_t box[3] = {(cuuint32_t)TC_BK, (cuuint32_t)boxRows, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(base), dims, strides, box,
+                        es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw std::string("cuda: cuTensorMapEncodeTiled failed");
+  return m;
+}
+
+void tc_gemm(cgpu_ctx* c, int gemmId, const CUtensorMap& ta, const CUtensorMap& tb, int bn, float* P, int terms,
+             int segPitch, int nSplit, int Mmax, int Nmax, int* err) {
+  if (segPitch % TC_BK != 0) throw std::string("tc_gemm: segment pitch must be a multiple of 64");
+  if (bn == 64) launch_gemm_t<64, 6>(c, ta, tb, P, gemmId, terms, segPitch, nSplit, Mmax, Nmax, err);
+  else if (bn == 128) launch_gemm_t<128, 5>(c, ta, tb, P, gemmId, terms, segPitch, nSplit, Mmax, Nmax, err);
+  else launch_gemm_t<256, 4>(c, ta, tb, P, gemmId, terms, segPitch, nSplit, Mmax, Nmax, err);
 }

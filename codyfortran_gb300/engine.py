@@ -32,8 +32,9 @@ EXPORTED = [
     "cgpu_integrate_sil", "cgpu_propagate_split2", "cgpu_state_upload", "cgpu_state_download",
     "cgpu_propagate_resident", "cgpu_energy_resident", "cgpu_tdci_set_orbitals", "cgpu_propagate_resident_timed",
     "cgpu_profile_begin", "cgpu_profile_end", "cgpu_weighted_gram_noalloc",
-    "cgpu_batch_create", "cgpu_batch_destroy", "cgpu_batch_size", "cgpu_batch_context", "cgpu_batch_propagate",
-    "cgpu_batch_kernels_per_step",
+    "cgpu_batch_create", "cgpu_batch_destroy", "cgpu_batch_size", "cgpu_batch_sizes", "cgpu_batch_grid",
+    "cgpu_batch_upload", "cgpu_batch_download", "cgpu_batch_propagate", "cgpu_batch_energies",
+    "cgpu_batch_kernels_per_step", "cgpu_batch_launch_count",
 ]
 
 KERNELS = {"pair_potentials": 1, "correlation": 2, "h2": 3, "ci_apply": 4, "ci_rdm": 5, "onebody": 6, "lanczos": 7}
@@ -80,10 +81,10 @@ def load_library(path: str = LIB_PATH):
     lib.cgpu_launch_count.argtypes = [C.c_void_p, C.c_int]
     lib.cgpu_ctx_create.argtypes = [C.POINTER(CgpuDesc), C.POINTER(C.c_void_p)]
     lib.cgpu_batch_create.argtypes = [C.POINTER(CgpuDesc), C.c_int, C.POINTER(C.c_void_p)]
-    lib.cgpu_batch_context.restype = C.c_void_p
-    lib.cgpu_batch_context.argtypes = [C.c_void_p, C.c_int]
     lib.cgpu_batch_kernels_per_step.restype = C.c_long
     lib.cgpu_batch_kernels_per_step.argtypes = [C.c_void_p]
+    lib.cgpu_batch_launch_count.restype = C.c_long
+    lib.cgpu_batch_launch_count.argtypes = [C.c_void_p, C.c_int]
     _lib = lib
     return lib
 
@@ -144,18 +145,6 @@ class Engine:
         if rc != 0:
             raise CodyError(self.lib.cgpu_last_global_error().decode())
         self.h = h
-        self._owned = True
-        self._query_sizes()
-
-    @classmethod
-    def _wrap(cls, spec: SystemSpec, handle):
-        """A non-owning Engine over a context that a Batch holds."""
-        e = cls.__new__(cls)
-        e.lib, e.spec, e._keep, e.h, e._owned = load_library(), spec, None, C.c_void_p(handle), False
-        e._query_sizes()
-        return e
-
-    def _query_sizes(self):
         sz = (C.c_int * 6)()
         self.lib.cgpu_sizes(self.h, sz)
         self.nG, self.nO, self.nOS, self.nC, self.nBt, self.nS = list(sz)
@@ -165,8 +154,7 @@ class Engine:
 
     def close(self):
         if getattr(self, "h", None):
-            if getattr(self, "_owned", True):
-                self.lib.cgpu_ctx_destroy(self.h)
+            self.lib.cgpu_ctx_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -375,10 +363,19 @@ class Engine:
         self._check(self.lib.cgpu_tdci_set_orbitals(self.h, _p(o)))
 
 
+class BatchSystem:
+    """Sizes and grid of one system of a Batch."""
+
+    def __init__(self, spec, sizes, x, w):
+        self.spec = spec
+        self.nG, self.nO, self.nOS, self.nC, self.nBt, self.nS = sizes
+        self.x, self.w = x, w
+
+
 class Batch:
-    """Independent trajectories of arbitrary sizes advanced together: one
-    cgpu_ctx per trajectory, one CUDA-graph launch per time step for the whole
-    batch (cgpu_batch_propagate)."""
+    """Independent systems of arbitrary sizes advanced together: every kernel
+    of the step covers all systems in one launch, one CUDA-graph launch per
+    time step (cgpu_batch_propagate)."""
 
     def __init__(self, specs, precision: str = "fp64", max_krylov: int = 32):
         self.lib = load_library()
@@ -395,15 +392,20 @@ class Batch:
         if rc != 0:
             raise CodyError(self.lib.cgpu_last_global_error().decode())
         self.h = h
-        self.engines = [Engine._wrap(sp, self.lib.cgpu_batch_context(self.h, i)) for i, sp in enumerate(self.specs)]
+        self.systems = []
+        for i, sp in enumerate(self.specs):
+            sz = (C.c_int * 6)()
+            self.lib.cgpu_batch_sizes(self.h, i, sz)
+            x, w = np.zeros(sz[0]), np.zeros(sz[0])
+            self.lib.cgpu_batch_grid(self.h, i, _p(x), _p(w))
+            self.systems.append(BatchSystem(sp, list(sz), x, w))
+        self.offsets = np.concatenate([[0], np.cumsum([s.nS for s in self.systems])]).astype(np.int64)
 
     def __len__(self):
-        return len(self.engines)
+        return len(self.systems)
 
     def close(self):
         if getattr(self, "h", None):
-            for e in self.engines:
-                e.close()
             self.lib.cgpu_batch_destroy(self.h)
             self.h = None
 
@@ -413,23 +415,46 @@ class Batch:
         except Exception:
             pass
 
-    def upload(self, states):
-        for e, s in zip(self.engines, states):
-            e.upload(s)
-
-    def download(self):
-        return [e.download() for e in self.engines]
-
-    def propagate(self, t0, dt, n_steps, krylov_dim, use_metric=True):
-        """n_steps fixed-order Strang steps of every trajectory (start times t0,
-        scalar or one per trajectory); returns the device time in ms."""
-        t = np.broadcast_to(np.asarray(t0, dtype=np.float64), (len(self),)).copy()
-        ms = C.c_double()
-        rc = self.lib.cgpu_batch_propagate(self.h, _p(t), _d(dt), int(n_steps), int(krylov_dim), int(use_metric),
-                                           C.byref(ms))
+    def _check(self, rc):
         if rc != 0:
             raise CodyError(self.lib.cgpu_last_global_error().decode())
+
+    def pack(self, states):
+        return np.ascontiguousarray(np.concatenate([np.asarray(s, dtype=np.complex128) for s in states]))
+
+    def upload(self, states):
+        """states: list of per-system state vectors, or one packed array."""
+        buf = states if isinstance(states, np.ndarray) and states.ndim == 1 and states.size == self.offsets[-1] \
+            else self.pack(states)
+        buf = np.ascontiguousarray(buf, dtype=np.complex128)
+        self._check(self.lib.cgpu_batch_upload(self.h, _p(buf)))
+
+    def download_packed(self, out=None):
+        buf = out if out is not None else np.zeros(int(self.offsets[-1]), dtype=np.complex128)
+        self._check(self.lib.cgpu_batch_download(self.h, _p(buf)))
+        return buf
+
+    def download(self):
+        buf = self.download_packed()
+        return [buf[self.offsets[i]:self.offsets[i + 1]].copy() for i in range(len(self))]
+
+    def propagate(self, t0, dt, n_steps, krylov_dim, use_metric=True):
+        """n_steps fixed-order Strang steps of every system (start times t0,
+        scalar or one per system); returns the device time in ms."""
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(t0, dtype=np.float64), (len(self),)))
+        ms = C.c_double()
+        self._check(self.lib.cgpu_batch_propagate(self.h, _p(t), _d(dt), int(n_steps), int(krylov_dim),
+                                                  int(use_metric), C.byref(ms)))
         return ms.value
+
+    def energies(self, t):
+        tt = np.ascontiguousarray(np.broadcast_to(np.asarray(t, dtype=np.float64), (len(self),)))
+        e = np.zeros(len(self))
+        self._check(self.lib.cgpu_batch_energies(self.h, _p(tt), _p(e)))
+        return e
 
     def kernels_per_step(self):
         return self.lib.cgpu_batch_kernels_per_step(self.h)
+
+    def launch_count(self, reset=False):
+        return self.lib.cgpu_batch_launch_count(self.h, int(reset))

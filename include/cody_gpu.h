@@ -212,23 +212,30 @@ int cgpu_tdci_set_orbitals(cgpu_ctx* ctx, const cgpu_complex* orbs);
 /* No counterpart in the reference, whose module-global state allows one
  * trajectory per process (src/Method/M_Method.f90:47).  A batch holds n
  * independent systems of any sizes (pulse scans, uneven grids and orbital
- * counts), one context each.  cgpu_batch_propagate advances all of them
- * together by one CUDA-graph launch per time step: each context's
- * fixed-order Strang step (as cgpu_propagate_resident) is a child graph of
- * the step graph, so the trajectories run concurrently across the GPU. */
+ * counts) with the same body-type layout, method and precision.  Every kernel
+ * of the step covers all systems in one launch, and cgpu_batch_propagate
+ * replays the fixed-order Strang step (as cgpu_propagate_resident) as one
+ * CUDA graph per time step. */
 typedef struct cgpu_batch cgpu_batch;
 int cgpu_batch_create(const cgpu_desc* descs, int n, cgpu_batch** out);
 int cgpu_batch_destroy(cgpu_batch* batch);
 int cgpu_batch_size(const cgpu_batch* batch);
-/* The context of trajectory i: use cgpu_sizes / cgpu_grid / cgpu_state_upload /
- * cgpu_state_download / cgpu_energy_resident on it. */
-cgpu_ctx* cgpu_batch_context(cgpu_batch* batch, int i);
-/* n_steps steps of size dt; trajectory i starts at t0[i].  *elapsed_ms (may be
+/* cgpu_sizes / cgpu_grid of system i */
+int cgpu_batch_sizes(const cgpu_batch* batch, int i, int* sizes6);
+int cgpu_batch_grid(const cgpu_batch* batch, int i, double* x, double* w);
+/* All states, concatenated in system order (nS_i entries each, layout
+ * [C | orbitals] as cgpu_state_upload). */
+int cgpu_batch_upload(cgpu_batch* batch, const cgpu_complex* states);
+int cgpu_batch_download(cgpu_batch* batch, cgpu_complex* states);
+/* n_steps steps of size dt; system i starts at t0[i].  *elapsed_ms (may be
  * NULL) receives the device time from CUDA events around the launches. */
 int cgpu_batch_propagate(cgpu_batch* batch, const double* t0, double dt, int n_steps, int krylov_dim,
                          int use_metric, double* elapsed_ms);
-/* Kernels launched per batch step (sum over the child graphs). */
+/* energies[i] = GetEnergy of system i at time t[i] */
+int cgpu_batch_energies(cgpu_batch* batch, const double* t, double* energies);
+/* Kernels launched per step (all systems); launches so far (reset if nonzero). */
 long cgpu_batch_kernels_per_step(const cgpu_batch* batch);
+long cgpu_batch_launch_count(cgpu_batch* batch, int reset);
 
 /* ---- no-allocation variant ---------------------------------------------- */
 /* No counterpart in the reference.  Weighted Gram matrix of two orbital sets,

@@ -1,6 +1,6 @@
-"""Batched trajectories (cgpu_batch_*): uneven systems advanced together by one
-graph launch per step must give what each system gives alone, and the FP64
-batch must match the CPU oracle."""
+"""Batched trajectories (cgpu_batch_*): uneven systems advanced together (every
+kernel covers all systems, one graph launch per step) must give what each
+system gives alone, and the FP64 batch must match the CPU oracle."""
 import numpy as np
 import pytest
 
@@ -40,12 +40,16 @@ def _states(engines, seed):
     return out
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("mixed", 1e-12)])
-def test_batch_matches_individual_contexts(precision, tol):
+# FP64: the batch sums its reductions over other block counts than a single
+# system, so agreement is to rounding.  Mixed: the split-K partitions of the
+# FP32-accumulated contractions differ too, so agreement is to the mixed form's
+# own accuracy.
+@pytest.mark.parametrize("precision,tol,etol", [("fp64", 1e-12, 1e-12), ("mixed", 2e-5, 1e-6)])
+def test_batch_matches_individual_contexts(precision, tol, etol):
     from codyfortran_gb300.engine import Batch, Engine
     specs = S.batch_trajectory_specs(512, 1234)[:3] + [_small_helium(), _two_per_spin()]
     b = Batch(specs, precision, max_krylov=16)
-    st = _states(b.engines, 5)
+    st = _states(b.systems, 5)
     b.upload(st)
     t0 = np.array([0.0, 3.0, 7.5, 1.0, 0.25])
     dt, n, K = 0.02, 3, 12
@@ -54,13 +58,16 @@ def test_batch_matches_individual_contexts(precision, tol):
     # a second call continues from the advanced states on the same batch graph
     b.propagate(t0 + n * dt, dt, n, K)
     got = b.download()
+    E = b.energies(t0 + 2 * n * dt)
     for k, sp in enumerate(specs):
         e = Engine(sp, precision, max_krylov=16)
         e.upload(st[k])
         e.propagate_resident(t0[k], dt, 2 * n, K, use_metric=True, use_graph=True)
         ref = e.download()
+        e_ref = e.energy_resident(t0[k] + 2 * n * dt)
         e.close()
         assert rel(got[k], ref) <= tol, (k, rel(got[k], ref))
+        assert abs(E[k] - e_ref) <= etol * abs(e_ref), (k, E[k], e_ref)
     b.close()
 
 
@@ -68,7 +75,7 @@ def test_batch_fp64_matches_oracle():
     from codyfortran_gb300.engine import Batch
     specs = [_small_helium(), _two_per_spin()]
     b = Batch(specs, "fp64")
-    st = _states(b.engines, 17)
+    st = _states(b.systems, 17)
     b.upload(st)
     t0 = np.array([0.5, 0.0])
     dt, n, K = 0.01, 3, 10
