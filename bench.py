@@ -1,29 +1,39 @@
 #!/usr/bin/env python
 """Benchmark: MCTDHF trajectory-steps/s on one GB300.
 
-One step = one Strang split step Propagate(t, t+dt): short-iterative-Lanczos
-half steps on the one-body part (fixed Krylov order, grid-weighted metric)
-around an RK4 step of the nonlinear part (CI H.C, RDMs, pair potentials,
-mean-field contraction, (1-P) projector).
+One trajectory-step = one Strang split step Propagate(t, t+dt) of one
+trajectory: short-iterative-Lanczos half steps on the one-body part (fixed
+Krylov order, grid-weighted metric) around an RK4 step of the nonlinear part
+(CI H.C, RDMs, pair potentials, mean-field contraction, (1-P) projector).
 
-Default workload: three soft-Coulomb nuclei, FEDVR 400 elements x 8 points on
-[-400, 400] (2801 points), N=6 fermions in 16 spin-orbitals (8008
-determinants), dt = 0.02, Krylov order 16, sin^2 laser pulse E0 = 0.0755 au.
-Synthetic seeded inputs: Gaussian orbitals (seed 7) and random normalised CI
+Default workload (batch512): 512 independent 1D soft-Coulomb MCTDHF
+trajectories drawn from seed 1234 -- N in {2,4} electrons as two restricted
+spin body types, M uniform in 4..12 spatial orbitals, FEDVR 100..400 elements
+x 6 points on [-nE, nE], sin^2 4-cycle pulses at omega = 0.057 au with
+log-uniform intensity 1e13..1e15 W/cm^2 and uniform CEP; dt = 0.02, Krylov
+order 12; mixed precision (split-bf16 tcgen05 contractions, FP64 elsewhere).
+All trajectories advance together: every kernel of the step covers the whole
+batch and the step is one CUDA-graph launch.  The same batch in the plain FP64
+form is timed beside it (the "vs FP64 GPU" leg of the metric).
+
+Other workload: trimer_large -- three soft-Coulomb nuclei, FEDVR 400 x 8
+points on [-400, 400] (2801 points), N=6 fermions in 16 spin-orbitals (8008
+determinants), dt = 0.02, Krylov order 16, E0 = 0.0755 au.
+
+Synthetic seeded inputs: Gaussian orbitals and random normalised CI
 coefficients (the step cost does not depend on the values).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload batch512|trimer_large] [--precision mixed|mixed6|fp64]
 """
 from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -34,14 +44,18 @@ sys.path.insert(0, ROOT)
 METRIC = "MCTDHF traj-steps/s: mixed-prec batched vs FP64 GPU at ≤1e-8 energy/norm err"
 UNIT = "traj-steps/s"
 L2_BYTES = 129 * 1024 * 1024
+FAMILIES = ("pair_potentials", "correlation", "h2", "ci_apply", "ci_rdm", "onebody", "lanczos", "rdm_inverse",
+            "projectors", "fold", "vector")
 
 
 def workload(name: str):
     from codyfortran_gb300 import spec as S
+    if name == "batch512":
+        return S.batch_trajectory_specs(512, 1234), dict(dt=0.02, krylov=12, seed=1234)
     if name == "trimer_large":
-        return S.cfg_trimer_large(), dict(dt=0.02, krylov=16, seed=7)
+        return [S.cfg_trimer_large()], dict(dt=0.02, krylov=16, seed=7)
     if name == "helium_small":
-        return S.cfg_helium_small(), dict(dt=0.01, krylov=12, seed=42)
+        return [S.cfg_helium_small()], dict(dt=0.01, krylov=12, seed=42)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -139,78 +153,204 @@ def barrier_max(value: float, world: int) -> float:
     return float(t.item())
 
 
-def cpu_sample(sp, cfg, state, n_threads, budget_s=25.0, max_steps=None):
-    """Strang steps of the oracle (CPU port) on the host cores: bounded sample."""
+def oracle_traj_steps(specs, cfg, n_threads, budget_s, max_traj=None):
+    """Strang steps of the oracle (the CPU port of the reference algorithm) on the
+    host cores, over the first trajectories of the workload: returns (steps, seconds, trajectories)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from oracle import Oracle
-    o = Oracle(sp, n_threads=n_threads)
-    m = o.metric_weights()
-    st = state.copy()
-    t = 0.0
-    steps, t0 = 0, time.perf_counter()
-    while True:
-        st = o.propagate_split2(st, t, t + cfg["dt"], krylov_dim=cfg["krylov"], metric=m)
-        t += cfg["dt"]
-        steps += 1
-        el = time.perf_counter() - t0
-        if el > budget_s or (max_steps and steps >= max_steps):
+    steps, el, used = 0, 0.0, 0
+    t_start = time.perf_counter()
+    for k, sp in enumerate(specs[:max_traj] if max_traj else specs):
+        o = Oracle(sp, n_threads=n_threads)
+        m = o.metric_weights()
+        st = initial_state(sp, o.x, o.w, cfg["seed"] + k)
+        t = 0.0
+        t0 = time.perf_counter()
+        n = 0
+        while True:
+            st = o.propagate_split2(st, t, t + cfg["dt"], krylov_dim=cfg["krylov"], metric=m)
+            t += cfg["dt"]
+            n += 1
+            if time.perf_counter() - t0 > budget_s / max(1, min(len(specs), 8)) or n >= 3:
+                break
+        el += time.perf_counter() - t0
+        steps += n
+        used += 1
+        if time.perf_counter() - t_start > budget_s:
             break
-    return steps, el
+    return steps, el, used
 
 
 def run_reference(args):
-    """The reference's algorithm on the host CPU (the oracle port; the Fortran reference cannot be built here)."""
+    """The reference's algorithm on the host CPU (the oracle port; the Fortran
+    reference cannot be built in this environment), on the workload's trajectories."""
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
-    sp, cfg = workload(args.workload)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    from oracle import Oracle
-    o = Oracle(sp, n_threads=os.cpu_count())
-    st = initial_state(sp, o.x, o.w, cfg["seed"])
-    m = o.metric_weights()
-    t = 0.0
-    tw0 = time.perf_counter()
-    warm = 0
-    for _ in range(max(args.warmup, 1)):
-        st = o.propagate_split2(st, t, t + cfg["dt"], krylov_dim=cfg["krylov"], metric=m)
-        t += cfg["dt"]
-        warm += 1
-        if time.perf_counter() - tw0 > 60.0:
-            break
-    per = (time.perf_counter() - tw0) / warm
-    k = max(1, min(args.steps, int(120.0 / max(per, 1e-9))))
-    t0 = time.perf_counter()
-    for _ in range(k):
-        st = o.propagate_split2(st, t, t + cfg["dt"], krylov_dim=cfg["krylov"], metric=m)
-        t += cfg["dt"]
-    el = time.perf_counter() - t0
-    val = k / el
+    specs, cfg = workload(args.workload)
+    budget = 60.0
+    steps, el, used = oracle_traj_steps(specs, cfg, os.cpu_count(), budget)
+    val = steps / el
     line = {
-        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": k,
-        "warmup": warm, "ms_per_step": 1e3 * el / k, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "complex128", "data": "synthetic",
-        "config": {"workload": args.workload, "n_grid": o.nG, "n_determinants": o.nC, "krylov_order": cfg["krylov"],
-                   "dt": cfg["dt"], "form": "CPU port of the reference algorithm (FP64)"},
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+        "warmup": 0, "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "complex128", "data": "synthetic (seeded Gaussian orbitals, random CI vector)",
+        "config": {"workload": args.workload, "trajectories": len(specs), "krylov_order": cfg["krylov"],
+                   "dt": cfg["dt"], "form": "CPU port of the reference algorithm (FP64), one trajectory at a time"},
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"{k} Strang steps of {args.workload} on {os.cpu_count()} host threads"},
+                         "sample": f"{steps} Strang steps over the first {used} trajectories of {args.workload} "
+                                   f"on {os.cpu_count()} host threads"},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
 
 
-def run_ours(args):
+def lanczos_work(systems, K, sil_per_step=2):
+    """Algorithmic bytes and FP64 flops of the Lanczos family in one step: at
+    iteration j the update reads the j basis vectors three times (dots, two
+    Gram-Schmidt passes) and w / v_{j+1} seven times; every basis entry costs
+    one complex multiply-add (8 flops) per pass."""
+    nS = sum(s.nS for s in systems)
+    passes = sum(3 * j + 7 for j in range(1, K + 1)) * sil_per_step
+    flops = sum(3 * j * 8 + 8 for j in range(1, K + 1)) * sil_per_step * nS
+    return passes * nS * 16.0, float(flops)
+
+
+def dense_flops(systems, fam):
+    """Algorithmic flops of one NonLin evaluation's dense contraction (four per step)."""
+    tot = 0.0
+    for s in systems:
+        n = s.nOS
+        P = n * (n + 1) // 2
+        if fam == "pair_potentials":
+            tot += 4.0 * s.nG * s.nG * P
+        elif fam in ("correlation", "h2"):
+            tot += 8.0 * s.nG * n ** 4
+    return 4.0 * tot
+
+
+def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=False, e2e=True):
+    from codyfortran_gb300.engine import Batch
+    dt, K = cfg["dt"], cfg["krylov"]
+    b = Batch(specs, precision, max_krylov=K)
+    states = [initial_state(sp, s.x, s.w, cfg["seed"] + k) for k, (sp, s) in enumerate(zip(specs, b.systems))]
+    host = b.pack(states)
+    b.upload(host)
+    t = 0.0
+    b.propagate(t, dt, warmup, K)
+    t += warmup * dt
+    fam_ms = {}
+    if profile:
+        for fam in FAMILIES:
+            b.profile_begin(fam)
+            b.propagate(t, dt, 1, K)
+            t += dt
+            fam_ms[fam] = b.profile_end()
+    dom = max(fam_ms, key=lambda k: fam_ms[k][1]) if fam_ms else None
+    if dom:
+        b.profile_begin(dom)
+        b.propagate(t, dt, 1, K)  # capture the graph with the dominant family's events, untimed
+        t += dt
+    b.launch_count(reset=True)
+    clk = ClockSampler(0) if clock else None
+    if clk:
+        clk.__enter__()
+    ms = b.propagate(t, dt, steps, K)
+    if clk:
+        clk.__exit__()
+    t += steps * dt
+    n_dom, ms_dom = b.profile_end() if dom else (0, 0.0)
+    launches = b.launch_count()
+    out = dict(ms=ms, fam_ms=fam_ms, dom=dom, n_dom=n_dom, ms_dom=ms_dom, launches=launches,
+               clocks=clk.summary() if clk else None, systems=b.systems, kps=b.kernels_per_step())
+    if e2e:
+        # end to end through the C ABI: packed host states in, one step, packed states out
+        n_e2e = max(1, min(steps, 5))
+        buf = host.copy()
+        te0 = time.perf_counter()
+        for _ in range(n_e2e):
+            b.upload(buf)
+            b.propagate(t, dt, 1, K)
+            b.download_packed(buf)
+            t += dt
+        out["e2e_s"] = (time.perf_counter() - te0) / n_e2e
+        out["e2e_bytes"] = int(buf.nbytes)
+        out["energy"] = float(b.energies(t)[0])
+    b.close()
+    return out
+
+
+def run_batch(args):
     rank, world, local = dist_info()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if world > 1 else None
+    specs, cfg = workload(args.workload)
+    precision = args.precision or "mixed"
+    n = len(specs)
+    r = run_batch_leg(specs, cfg, precision, args.steps, args.warmup, profile=True, clock=True)
+    ms = barrier_max(r["ms"], world)
+    value = world * n * args.steps / (ms / 1e3)
+    # the same batch in the plain FP64 form (short timed region)
+    fp64 = None
+    if precision != "fp64" and not args.no_fp64_leg:
+        f = run_batch_leg(specs, cfg, "fp64", max(1, min(args.steps, 2)), 1, profile=False, e2e=False)
+        fp64 = n * max(1, min(args.steps, 2)) / (f["ms"] / 1e3)
+    # roofline of the dominant kernel family
+    hbm, bf16, src = measured_peaks()
+    dom, n_dom = r["dom"], max(r["n_dom"], 1)
+    avg_s = r["ms_dom"] / n_dom / 1e3
+    systems = r["systems"]
+    roof = {"kernel": dom, "launches": r["n_dom"], "avg_launch_us": avg_s * 1e6, "peak_source": src, "traffic": None}
+    if dom in ("pair_potentials", "correlation", "h2"):
+        work = dense_flops(systems, dom) / n_dom
+        roof.update(bound="tensor", achieved=work / avg_s / 1e12, peak=bf16, unit="TFLOP/s", work_per_launch=work)
+    elif dom == "lanczos":
+        byts, flops = lanczos_work(systems, cfg["krylov"])
+        byts /= n_dom
+        roof.update(bound="hbm", achieved=byts / avg_s / 1e9, peak=hbm, unit="GB/s", work_per_launch=byts,
+                    fp64_tflops=flops / n_dom / avg_s / 1e12)
+    else:
+        byts = sum(s.nS for s in systems) * 16.0 * 4
+        roof.update(bound="hbm", achieved=byts / avg_s / 1e9, peak=hbm, unit="GB/s", work_per_launch=byts)
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    e2e = world * n / r["e2e_s"]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "complex128" if precision == "fp64" else
+                 f"mixed (bf16x{6 if precision == 'mixed6' else 3} tcgen05 contractions with fp32 accumulation, fp64 rest)",
+        "data": "synthetic (seeded Gaussian orbitals, random normalised CI vectors)",
+        "config": {"workload": args.workload, "trajectories": n, "krylov_order": cfg["krylov"], "dt": cfg["dt"],
+                   "precision": precision, "parallelism": f"batch of {n} per GPU, replicas x{world}",
+                   "n_grid_range": [min(s.nG for s in systems), max(s.nG for s in systems)],
+                   "n_determinants_range": [min(s.nC for s in systems), max(s.nC for s in systems)],
+                   "l2": f"per-step working set {sum(s.nS for s in systems) * 16 * (cfg['krylov'] + 8) / 1e9:.1f} GB "
+                         f"of states and Krylov vectors > L2 ({L2_BYTES / 1e6:.0f} MB): inputs larger than L2, no flush"},
+        "fp64_gpu": {"value": fp64, "unit": UNIT, "ratio": (value / fp64) if fp64 else None,
+                     "note": "same batch, plain FP64 form, same GPU"},
+        "clocks": r["clocks"],
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": r["e2e_bytes"], "d2h_bytes_per_step": r["e2e_bytes"],
+                "call": "cgpu_batch_upload + cgpu_batch_propagate(1 step) + cgpu_batch_download, pageable host buffers"},
+        "gpu_launches": int(r["launches"]),
+        "kernels_per_step": r["kps"],
+        "roofline": roof,
+        "kernel_ms_per_step": {k: v[1] for k, v in r["fam_ms"].items()},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        steps_cpu, el, used = oracle_traj_steps(specs, cfg, os.cpu_count(), args.cpu_budget)
+        line["cpu_baseline"] = {"value": steps_cpu / el, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{steps_cpu} Strang steps over the first {used} trajectories "
+                                          f"({el:.1f} s, one trajectory at a time)"}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def run_single(args):
+    rank, world, local = dist_info()
     from codyfortran_gb300.engine import Engine
-    from codyfortran_gb300 import build as B
-    B.build()
-    sp, cfg = workload(args.workload)
-    precision = args.precision
+    specs, cfg = workload(args.workload)
+    sp = specs[0]
+    precision = args.precision or "fp64"
     e = Engine(sp, precision=precision, max_krylov=cfg["krylov"])
     st = initial_state(sp, e.x, e.w, cfg["seed"])
     dt, K = cfg["dt"], cfg["krylov"]
@@ -220,69 +360,54 @@ def run_ours(args):
     e.propagate_resident(t, dt, args.warmup, K, use_metric=True, use_graph=graph)
     t += args.warmup * dt
     e.synchronize()
-    # dominant kernel: the family with the largest device time in one step (CUDA events
-    # around each of its launches, recorded on the library's stream; inside the graph
-    # they are event-record nodes, so the times are those of the last replayed step)
     fam_ms = {}
-    for fam in ("pair_potentials", "correlation", "h2", "ci_apply", "ci_rdm", "onebody", "lanczos"):
+    for fam in FAMILIES:
         e.profile_begin(fam)
         e.propagate_resident(t, dt, 1, K, use_metric=True, use_graph=graph)
         t += dt
-        n, ms = e.profile_end()
-        fam_ms[fam] = (n, ms)
+        fam_ms[fam] = e.profile_end()
     dom = max(fam_ms, key=lambda k: fam_ms[k][1])
     e.profile_begin(dom)
     e.propagate_resident(t, dt, 1, K, use_metric=True, use_graph=graph)  # capture with the events, untimed
     t += dt
-    # timed region
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
     e.launch_count(reset=True)
-    with ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]) if world > 1 else 0) as clk:
+    with ClockSampler(0) as clk:
         ms = e.propagate_resident_timed(t, dt, args.steps, K, use_metric=True, use_graph=graph)
     n_dom, ms_dom = e.profile_end()
     launches = e.launch_count()
     t += args.steps * dt
     ms = barrier_max(ms, world)
     value = world * args.steps / (ms / 1e3)
-    # end-to-end through the host-buffer C-ABI call (H2D + step + D2H per step)
     host = e.download()
     n_e2e = max(1, min(args.steps, 20))
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
     te0 = time.perf_counter()
     for _ in range(n_e2e):
         host = e.propagate_split2(host, t, t + dt, krylov_dim=K, use_metric=True)
         t += dt
     te = barrier_max(time.perf_counter() - te0, world)
     e2e = world * n_e2e / te
-    # roofline of the dominant kernel
     hbm, bf16, src = measured_peaks()
     nG, P, Q, nC = e.nG, e.nOS * (e.nOS + 1) // 2, e.nOS * e.nOS, e.nC
     avg_s = (ms_dom / max(n_dom, 1)) / 1e3
     if dom == "pair_potentials":
-        work, bound = 2.0 * nG * nG * 2 * P, "tensor"       # W = V S, real GEMM nG x nG x 2P
+        work, bound = 2.0 * nG * nG * 2 * P, "tensor"
     elif dom in ("correlation", "h2"):
-        work, bound = 8.0 * nG * Q * Q, "tensor"            # complex GEMM nG x Q x Q
+        work, bound = 8.0 * nG * Q * Q, "tensor"
     else:
-        work, bound = 16.0 * e.nS * 4, "hbm"                # streaming estimate
+        work, bound = 16.0 * e.nS * 4, "hbm"
     if bound == "tensor":
         achieved, peak, unit = work / avg_s / 1e12, bf16, "TFLOP/s"
     else:
         achieved, peak, unit = work / avg_s / 1e9, hbm, "GB/s"
-    clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "complex128" if precision == "fp64" else "mixed(bf16x3/fp32 contractions, fp64 rest)",
+        "dtype": "complex128" if precision == "fp64" else "mixed(bf16 split tcgen05 contractions, fp64 rest)",
         "data": "synthetic (seeded Gaussian orbitals, random normalised CI vector)",
         "config": {"workload": args.workload, "n_grid": nG, "n_orbitals": e.nOS, "n_determinants": nC,
                    "krylov_order": K, "dt": dt, "precision": precision, "parallelism": f"replicas x{world}",
-                   "l2": f"per-step working set {(nG * nG * 8 + 71e6 + (K + 8) * e.nS * 16) / 1e6:.0f} MB > L2 "
-                         f"({L2_BYTES / 1e6:.0f} MB): inputs larger than L2, no flush"},
-        "clocks": clocks,
+                   "l2": "inputs larger than L2, no flush"},
+        "clocks": clk.summary(),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": e.nS * 16, "d2h_bytes_per_step": e.nS * 16,
                 "steps": n_e2e, "call": "cgpu_propagate_split2 (host state in/out)"},
         "gpu_launches": int(launches),
@@ -292,7 +417,7 @@ def run_ours(args):
         "kernel_ms_per_step": {k: v[1] for k, v in fam_ms.items()},
     }
     if rank == 0 and not args.no_cpu_baseline:
-        steps_cpu, el = cpu_sample(sp, cfg, st, os.cpu_count(), budget_s=args.cpu_budget, max_steps=3)
+        steps_cpu, el, used = oracle_traj_steps(specs, cfg, os.cpu_count(), args.cpu_budget)
         line["cpu_baseline"] = {"value": steps_cpu / el, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"{steps_cpu} Strang step(s) of {args.workload} ({el:.1f} s)"}
     if rank == 0:
@@ -307,9 +432,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="trimer_large")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed6"])
+    ap.add_argument("--workload", default="batch512", choices=["batch512", "trimer_large", "helium_small"])
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed", "mixed6"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-leg", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=25.0)
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one instead of a step graph")
     args = ap.parse_args()
@@ -317,7 +443,15 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
-    return run_ours(args)
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    from codyfortran_gb300 import build as B
+    B.build()
+    if args.workload == "batch512":
+        return run_batch(args)
+    return run_single(args)
 
 
 if __name__ == "__main__":

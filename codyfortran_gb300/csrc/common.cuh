@@ -38,6 +38,17 @@ __host__ __device__ __forceinline__ void zfma(z_t& a, z_t b, z_t c) {
   a.x = fma(b.x, c.x, fma(-b.y, c.y, a.x));
   a.y = fma(b.x, c.y, fma(b.y, c.x, a.y));
 }
+// a with its sign flipped when neg (integer operation on the sign bits, no FP64 instruction)
+__device__ __forceinline__ z_t zsign(z_t a, bool neg) {
+  long long m = neg ? (long long)0x8000000000000000ULL : 0LL;
+  return make_double2(__longlong_as_double(__double_as_longlong(a.x) ^ m),
+                      __longlong_as_double(__double_as_longlong(a.y) ^ m));
+}
+// a += conj(b) * c
+__host__ __device__ __forceinline__ void zcfma(z_t& a, z_t b, z_t c) {
+  a.x = fma(b.x, c.x, fma(b.y, c.y, a.x));
+  a.y = fma(b.x, c.y, fma(-b.y, c.x, a.y));
+}
 // multiply by -i
 __host__ __device__ __forceinline__ z_t zmi(z_t a) { return make_double2(a.y, -a.x); }
 // multiply by +i
@@ -179,6 +190,13 @@ struct SysHost {
   double intS = 0, intS1 = 0, intS2 = 0, intDamp = 0;
   CiTables tab[CODY_MAX_BT] = {};
   CiView view = {};
+  // host copies for the work lists: connections per configuration, code-list starts
+  std::vector<int> hsN[CODY_MAX_BT], hdN[CODY_MAX_BT], hsxStart[CODY_MAX_BT], hdxStart[CODY_MAX_BT];
+};
+
+// One block's share of a CI kernel: trajectory and task range [t0, t1).
+struct CiWork {
+  int traj, t0, t1;
 };
 
 // ---------------------------------------------------------------------------
@@ -200,7 +218,10 @@ struct cgpu_ctx {
   int nG = 0, nBt = 0, nO = 0, nOS = 0, nC = 0, nS = 0, nGO = 0, restricted = 0, method = 0, precision = 0;
   int band = 0, nBtK = 1, nPairs = 0;
   int minS = 0;                   // smallest state size (bounds the Krylov order)
-  int ciTasks = 0;                // largest number of RDM gather tasks (warps) of a system
+  // CI work lists (blocks balanced by the number of terms; see ci_build_work)
+  CiWork *applyWork_d = nullptr, *rdmWork_d = nullptr, *pairWork_d = nullptr;
+  int nApplyWork = 0, nRdmWork = 0, nPairWork = 0;
+  int ciSmem = 0;                 // bytes of shared memory for a CI vector (0: read it from global memory)
   int hasInteraction = 0, anyLaser = 0;
   // packed host states <-> the arena (batched upload / download)
   std::vector<long> stageOff;     // prefix sums of the systems' state sizes
@@ -327,6 +348,7 @@ void launch_add_scalar(cgpu_ctx* c, double* p, double v);
 size_t gram_partial_need(const cgpu_ctx* c, int n);
 // k_ci.cu
 void ci_build_tables(cgpu_ctx* c, SysHost& s);
+void ci_build_work(cgpu_ctx* c);
 void launch_ci_rdm(cgpu_ctx* c, const z_t* C, int want1, int want2);
 void launch_ci_apply(cgpu_ctx* c, const z_t* C, z_t* dC, int useH1, int useH2);
 void launch_fold_h1(cgpu_ctx* c);

@@ -388,16 +388,7 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
   }
   for (int b = 0; b < nSys; b++) maxK = std::max(maxK, descs[b].max_krylov);
   c->nGO = nGO;
-  for (const SysHost& s : c->sys) {
-    const CiView& v = s.view;
-    int nS = 0, nD = 0, nX = 0;
-    for (int b = 0; b < v.nBt; b++) {
-      nS += v.nSc[b];
-      nD += v.nDc[b];
-      for (int b2 = b + 1; b2 < v.nBt; b2++) nX += v.nSc[b] * v.nSc[b2];
-    }
-    c->ciTasks = std::max(c->ciTasks, nS + nD + nX);
-  }
+  ci_build_work(c);
   c->nS = (c->method == CGPU_METHOD_TDCI) ? c->nC : c->nC + nGO;
   c->minS = minS;
   c->maxKrylov = std::max(1, std::min(maxK > 0 ? maxK : 32, 32));
@@ -501,7 +492,8 @@ void free_ctx(cgpu_ctx* c) {
     }
     if (s.samples_d) cudaFree(s.samples_d);
   }
-  void* ptrs[] = {c->arena, c->shape_d, c->metricUser_d, c->stageOff_d, c->stage_d};
+  void* ptrs[] = {c->arena, c->shape_d, c->metricUser_d, c->stageOff_d, c->stage_d, c->applyWork_d, c->rdmWork_d,
+                  c->pairWork_d};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->lz_h) cudaFreeHost(c->lz_h);
@@ -818,10 +810,12 @@ cgpu_ctx* create_ctx(const cgpu_desc* descs, int n, int* rc) {
 }  // namespace
 
 void batch_zero(cgpu_ctx* c, void* p, size_t bytes) {
+  ProfScope prof(c, CGPU_KERNEL_VECTOR);
   CODY_CUDA(cudaMemset2DAsync(p, c->bs, 0, bytes, c->nb, c->stream));
 }
 
 void batch_copy(cgpu_ctx* c, void* dst, const void* src, size_t bytes) {
+  ProfScope prof(c, CGPU_KERNEL_VECTOR);
   CODY_CUDA(cudaMemcpy2DAsync(dst, c->bs, src, c->bs, bytes, c->nb, cudaMemcpyDeviceToDevice, c->stream));
 }
 
@@ -1309,6 +1303,7 @@ int cgpu_batch_propagate(cgpu_batch* b, const double* t0, double dt, int n_steps
     set_step_times(c, t0);
     capture_step_graph(c, t0[0], dt, krylov_dim, use_metric);
   }
+  if (c->profTarget) c->profUsed = c->graphProfUsed;
   cudaEvent_t e0, e1;
   CODY_CUDA(cudaEventCreate(&e0));
   CODY_CUDA(cudaEventCreate(&e1));
@@ -1350,5 +1345,15 @@ int cgpu_batch_energies(cgpu_batch* b, const double* t, double* energies) {
 long cgpu_batch_kernels_per_step(const cgpu_batch* b) { return (b && b->c) ? b->c->graphKernels : 0; }
 
 long cgpu_batch_launch_count(cgpu_batch* b, int reset) { return (b && b->c) ? cgpu_launch_count(b->c, reset) : -1; }
+
+int cgpu_batch_profile_begin(cgpu_batch* b, int kernel) {
+  if (!b || !b->c) return fail(nullptr, "null batch", CGPU_ERR_ARG);
+  return cgpu_profile_begin(b->c, kernel);
+}
+
+int cgpu_batch_profile_end(cgpu_batch* b, long* launches, double* total_ms) {
+  if (!b || !b->c) return fail(nullptr, "null batch", CGPU_ERR_ARG);
+  return cgpu_profile_end(b->c, launches, total_ms);
+}
 
 }  // extern "C"

@@ -126,16 +126,31 @@ __device__ __forceinline__ z_t warp_sum(z_t a) {
   return a;
 }
 
-__global__ void k_ci_apply(const z_t* __restrict__ C, z_t* __restrict__ dC, const z_t* __restrict__ h1Lin,
-                           const z_t* __restrict__ h2Lin, TRAJ_ARGS, int useH1, int useH2) {
-  const CiView& v = shp[blockIdx.z].view;
-  int lane = threadIdx.x & 31;
-  C = bat(C, bs);
-  dC = bat(dC, bs);
-  h1Lin = bat(h1Lin, bs);
-  h2Lin = bat(h2Lin, bs);
-  const int nWarps = (gridDim.x * blockDim.x) >> 5;
-  for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < v.nC; warp += nWarps) {
+// The CI vector of the block's trajectory: staged in shared memory when it fits
+// (random gathers of C then hit shared memory), else read from global memory.
+__device__ __forceinline__ const z_t* stage_coeffs(const z_t* __restrict__ Cg, int nC, z_t* sm, int useSmem) {
+  if (!useSmem) return Cg;
+  for (int i = threadIdx.x; i < nC; i += blockDim.x) sm[i] = Cg[i];
+  __syncthreads();
+  return sm;
+}
+
+// H.C: one warp per configuration, the configurations of one trajectory in a
+// block (work[blockIdx.x] = trajectory and range, balanced by the number of terms).
+__global__ void k_ci_apply(const z_t* __restrict__ C0, z_t* __restrict__ dC0, const z_t* __restrict__ h1Lin0,
+                           const z_t* __restrict__ h2Lin0, TRAJ_ARGS, const CiWork* __restrict__ work, int useSmem,
+                           int useH1, int useH2) {
+  extern __shared__ z_t csm[];
+  const CiWork wk = work[blockIdx.x];
+  const int tb = wk.traj;
+  const CiView& v = shp[tb].view;
+  const z_t* C = stage_coeffs(batn(C0, bs, tb), v.nC, csm, useSmem);
+  z_t* dC = batn(dC0, bs, tb);
+  const z_t* h1Lin = batn(h1Lin0, bs, tb);
+  const z_t* h2Lin = batn(h2Lin0, bs, tb);
+  const int lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  for (int warp = wk.t0 + (threadIdx.x >> 5); warp < wk.t1; warp += nw) {
   int I = warp + 1;
   int conf[CODY_MAX_BT];
   conf_from_index(v, I, conf);
@@ -150,9 +165,7 @@ __global__ void k_ci_apply(const z_t* __restrict__ C, z_t* __restrict__ dC, cons
       for (int k = lane; k < n; k += 32) {
         int oc = v.sCode[b][col + k];
         int jG = I + (v.sExc[b][col + k] - c) * st;
-        z_t hc = zmul(h1Lin[oc], C[jG - 1]);
-        if (v.sFac[b][col + k] < 0) hc = zmk(-hc.x, -hc.y);
-        acc = zadd(acc, hc);
+        zfma(acc, h1Lin[oc], zsign(C[jG - 1], v.sFac[b][col + k] < 0));
       }
     }
     if (useH2) {
@@ -161,9 +174,7 @@ __global__ void k_ci_apply(const z_t* __restrict__ C, z_t* __restrict__ dC, cons
       for (int k = lane; k < n; k += 32) {
         int oc = v.dCode[b][col + k];
         int jG = I + (v.dExc[b][col + k] - c) * st;
-        z_t hc = zmul(h2Lin[oc], C[jG - 1]);
-        if (v.dFac[b][col + k] < 0) hc = zmk(-hc.x, -hc.y);
-        acc = zadd(acc, hc);
+        zfma(acc, h2Lin[oc], zsign(C[jG - 1], v.dFac[b][col + k] < 0));
       }
       // inter-body-type terms: products of singles on b and b2 > b (Generic :266-300).
       // Lane k2 holds an edge of b2, the edges of b are broadcast one by one.
@@ -189,14 +200,13 @@ __global__ void k_ci_apply(const z_t* __restrict__ C, z_t* __restrict__ dC, cons
               f1 = v.sFac[b][col1 + k1];
             }
             int cnt = min(32, n1 - k1b);
+#pragma unroll 4
             for (int u = 0; u < cnt; u++) {
               int o1 = __shfl_sync(0xffffffffu, oc1, u);
               int e1 = __shfl_sync(0xffffffffu, d1, u);
               int g1 = __shfl_sync(0xffffffffu, f1, u);
               if (has2) {
-                z_t hc = zmul(h2Lin[(o1 - 1) * nO2 + oc2], C[I - 1 + e1 + d2]);
-                if (g1 * f2 < 0) hc = zmk(-hc.x, -hc.y);
-                acc = zadd(acc, hc);
+                zfma(acc, h2Lin[(o1 - 1) * nO2 + oc2], zsign(C[I - 1 + e1 + d2], g1 * f2 < 0));
               }
             }
           }
@@ -224,82 +234,91 @@ __device__ __forceinline__ int rest_base(const CiView& v, int r, int b1, int b2)
 
 // RDMs (ApplyH1FillRdm1 / ApplyH2FillRdm2, S_Coeffs_Generic.f90:103-319) as
 // gathers: rdmLin(oc) = sum over the excitations (I -> J) with orbital code
-// oc of f conj(C_J) C_I.  One warp per code (within a body type) or per pair
-// of codes (singles of two body types, the inter-body-type part of rdm2);
-// every entry has exactly one writer, so there are no atomics.
-__global__ void k_ci_rdm(const z_t* __restrict__ C, z_t* __restrict__ r1Lin, z_t* __restrict__ r2Lin, TRAJ_ARGS,
-                         int want1, int want2) {
-  const CiView& v = shp[blockIdx.z].view;
-  const int lane = threadIdx.x & 31;
-  C = bat(C, bs);
-  r1Lin = bat(r1Lin, bs);
-  r2Lin = bat(r2Lin, bs);
-  int nS = 0, nD = 0, nX = 0;
-  for (int b = 0; b < v.nBt; b++) {
-    nS += v.nSc[b];
-    nD += v.nDc[b];
-    for (int b2 = b + 1; b2 < v.nBt; b2++) nX += v.nSc[b] * v.nSc[b2];
-  }
-  const int nT = (want1 ? nS : 0) + (want2 ? nD + nX : 0);
-  const int nO2 = v.nO * v.nO;
-  const int nWarps = (gridDim.x * blockDim.x) >> 5;
-  for (int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < nT; task += nWarps) {
+// oc of f conj(C_J) C_I.  Every entry has exactly one writer, so there are no
+// atomics.  k_ci_rdm_codes: one warp per code of one body type (singles ->
+// rdm1, doubles -> rdm2), lanes over the code's excitations (and over the
+// configurations of the other body types); k_ci_rdm_pairs: one thread per pair
+// of singles codes of two body types (the inter-body-type part of rdm2).
+__global__ void k_ci_rdm_codes(const z_t* __restrict__ C0, z_t* __restrict__ r1Lin0, z_t* __restrict__ r2Lin0,
+                               TRAJ_ARGS, const CiWork* __restrict__ work, int useSmem, int want1, int want2) {
+  extern __shared__ z_t csm[];
+  const CiWork wk = work[blockIdx.x];
+  const int tb = wk.traj;
+  const CiView& v = shp[tb].view;
+  const z_t* C = stage_coeffs(batn(C0, bs, tb), v.nC, csm, useSmem);
+  z_t* r1Lin = batn(r1Lin0, bs, tb);
+  z_t* r2Lin = batn(r2Lin0, bs, tb);
+  int nS = 0;
+  for (int b = 0; b < v.nBt; b++) nS += v.nSc[b];
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int task = wk.t0 + (threadIdx.x >> 5); task < wk.t1; task += nw) {
     int q = task;
+    const int kind = q < nS ? 0 : 1;
+    if (kind == 1) q -= nS;
+    if ((kind == 0 && !want1) || (kind == 1 && !want2)) continue;
+    int b = 0;
+    const int* cnt = kind == 0 ? v.nSc : v.nDc;
+    while (q >= cnt[b]) q -= cnt[b++];
+    const int* start = kind == 0 ? v.sxStart[b] : v.dxStart[b];
+    const int* src = kind == 0 ? v.sxSrc[b] : v.dxSrc[b];
+    const int* dst = kind == 0 ? v.sxDst[b] : v.dxDst[b];
+    const int8_t* fac = kind == 0 ? v.sxFac[b] : v.dxFac[b];
+    const int e0 = start[q], e1 = start[q + 1];
+    const int nRest = v.nC / v.nConf[b], st = v.stride[b];
     z_t acc = zmk(0.0, 0.0);
-    z_t* out;
-    int idx;
-    int kind;  // 0 singles, 1 doubles, 2 inter
-    if (!want1) q += nS;
-    if (q < nS) kind = 0;
-    else if ((q -= nS) < nD) kind = 1;
-    else { q -= nD; kind = 2; }
-    if (kind < 2) {
-      int b = 0;
-      const int* cnt = kind == 0 ? v.nSc : v.nDc;
-      while (q >= cnt[b]) q -= cnt[b++];
-      const int* start = kind == 0 ? v.sxStart[b] : v.dxStart[b];
-      const int* src = kind == 0 ? v.sxSrc[b] : v.dxSrc[b];
-      const int* dst = kind == 0 ? v.sxDst[b] : v.dxDst[b];
-      const int8_t* fac = kind == 0 ? v.sxFac[b] : v.dxFac[b];
-      int e0 = start[q], ne = start[q + 1] - e0;
-      int nRest = v.nC / v.nConf[b], st = v.stride[b];
-      for (int t = lane; t < ne * nRest; t += 32) {
+    if (nRest == 1) {
+      for (int e = e0 + lane; e < e1; e += 32) zcfma(acc, C[dst[e] * st], zsign(C[src[e] * st], fac[e] < 0));
+    } else {
+      for (int t = lane; t < (e1 - e0) * nRest; t += 32) {
         int e = e0 + t / nRest, r = t % nRest;
         int base = rest_base(v, r, b, -1);
-        z_t val = zcmul(C[base + dst[e] * st], C[base + src[e] * st]);
-        if (fac[e] < 0) val = zmk(-val.x, -val.y);
-        acc = zadd(acc, val);
+        zcfma(acc, C[base + dst[e] * st], zsign(C[base + src[e] * st], fac[e] < 0));
       }
-      out = kind == 0 ? r1Lin : r2Lin;
-      idx = kind == 0 ? v.sxCode[b][q] : v.dxCode[b][q];
-    } else {
-      int b1 = 0, b2 = 1;
-      for (;;) {
-        int seg = v.nSc[b1] * v.nSc[b2];
-        if (q < seg) break;
-        q -= seg;
-        if (++b2 >= v.nBt) { b1++; b2 = b1 + 1; }
-      }
-      int q1 = q / v.nSc[b2], q2 = q % v.nSc[b2];
-      int s1 = v.sxStart[b1][q1], n1 = v.sxStart[b1][q1 + 1] - s1;
-      int s2 = v.sxStart[b2][q2], n2 = v.sxStart[b2][q2 + 1] - s2;
-      int st1 = v.stride[b1], st2 = v.stride[b2];
-      int nRest = v.nC / (v.nConf[b1] * v.nConf[b2]);
-      for (int t = lane; t < n1 * n2 * nRest; t += 32) {
-        int r = t % nRest, u = t / nRest;
-        int e1 = s1 + u / n2, e2 = s2 + u % n2;
-        int base = rest_base(v, r, b1, b2);
-        int I = base + v.sxSrc[b1][e1] * st1 + v.sxSrc[b2][e2] * st2;
-        int J = base + v.sxDst[b1][e1] * st1 + v.sxDst[b2][e2] * st2;
-        z_t val = zcmul(C[J], C[I]);
-        if (v.sxFac[b1][e1] * v.sxFac[b2][e2] < 0) val = zmk(-val.x, -val.y);
-        acc = zadd(acc, val);
-      }
-      out = r2Lin;
-      idx = (v.sxCode[b1][q1] - 1) * nO2 + v.sxCode[b2][q2];
     }
     acc = warp_sum(acc);
-    if (lane == 0) out[idx] = acc;
+    if (lane == 0) (kind == 0 ? r1Lin : r2Lin)[kind == 0 ? v.sxCode[b][q] : v.dxCode[b][q]] = acc;
+  }
+}
+
+__global__ void k_ci_rdm_pairs(const z_t* __restrict__ C0, z_t* __restrict__ r2Lin0, TRAJ_ARGS,
+                               const CiWork* __restrict__ work, int useSmem) {
+  extern __shared__ z_t csm[];
+  const CiWork wk = work[blockIdx.x];
+  const int tb = wk.traj;
+  const CiView& v = shp[tb].view;
+  const z_t* C = stage_coeffs(batn(C0, bs, tb), v.nC, csm, useSmem);
+  z_t* r2Lin = batn(r2Lin0, bs, tb);
+  const int nO2 = v.nO * v.nO;
+  for (int task = wk.t0 + threadIdx.x; task < wk.t1; task += blockDim.x) {
+    int q = task, b1 = 0, b2 = 1;
+    for (;;) {
+      int seg = v.nSc[b1] * v.nSc[b2];
+      if (q < seg) break;
+      q -= seg;
+      if (++b2 >= v.nBt) { b1++; b2 = b1 + 1; }
+    }
+    int q1 = q / v.nSc[b2], q2 = q % v.nSc[b2];
+    int s1 = v.sxStart[b1][q1], n1 = v.sxStart[b1][q1 + 1] - s1;
+    int s2 = v.sxStart[b2][q2], n2 = v.sxStart[b2][q2 + 1] - s2;
+    int st1 = v.stride[b1], st2 = v.stride[b2];
+    int nRest = v.nC / (v.nConf[b1] * v.nConf[b2]);
+    const int *src1 = v.sxSrc[b1], *dst1 = v.sxDst[b1], *src2 = v.sxSrc[b2], *dst2 = v.sxDst[b2];
+    const int8_t *fac1 = v.sxFac[b1], *fac2 = v.sxFac[b2];
+    z_t acc = zmk(0.0, 0.0);
+    for (int e1 = s1; e1 < s1 + n1; e1++) {
+      int i1 = src1[e1] * st1, j1 = dst1[e1] * st1;
+      bool g1 = fac1[e1] < 0;
+#pragma unroll 4
+      for (int e2 = s2; e2 < s2 + n2; e2++) {
+        int i2 = src2[e2] * st2, j2 = dst2[e2] * st2;
+        bool neg = g1 != (fac2[e2] < 0);
+        for (int r = 0; r < nRest; r++) {
+          int base = nRest == 1 ? 0 : rest_base(v, r, b1, b2);
+          zcfma(acc, C[base + j1 + j2], zsign(C[base + i1 + i2], neg));
+        }
+      }
+    }
+    r2Lin[(v.sxCode[b1][q1] - 1) * nO2 + v.sxCode[b2][q2]] = acc;
   }
 }
 
@@ -376,7 +395,7 @@ __global__ void k_unfold_rdm2(z_t* __restrict__ rdm2, const z_t* __restrict__ li
 // distinct codes ascending, edges of one code in table order.
 void group_by_code(int nConf, int maxConn, const int* nConn_d, const int* exc_d, const int* code_d,
                    const int8_t* fac_d, int& nCodes, int*& xCode, int*& xStart, int*& xSrc, int*& xDst,
-                   int8_t*& xFac) {
+                   int8_t*& xFac, std::vector<int>& nHost, std::vector<int>& startHost) {
   std::vector<int> n(nConf), exc((size_t)maxConn * nConf), code((size_t)maxConn * nConf);
   std::vector<int8_t> fac((size_t)maxConn * nConf);
   CODY_CUDA(cudaMemcpy(n.data(), nConn_d, sizeof(int) * nConf, cudaMemcpyDeviceToHost));
@@ -418,6 +437,8 @@ void group_by_code(int nConf, int maxConn, const int* nConn_d, const int* exc_d,
   upload(xSrc, src);
   upload(xDst, dst);
   upload(xFac, f);
+  nHost = n;
+  startHost = start;
 }
 
 long long binom_h(int n, int k) {
@@ -499,9 +520,9 @@ void ci_build_tables(cgpu_ctx* c, SysHost& s) {
     }
     CODY_CUDA(cudaStreamSynchronize(c->stream));  // the tables are written on the context stream
     group_by_code(t.nConf, std::max(t.maxS, 1), t.sN, t.sExc, t.sCode, t.sFac, t.nSc, t.sxCode, t.sxStart, t.sxSrc,
-                  t.sxDst, t.sxFac);
+                  t.sxDst, t.sxFac, s.hsN[b], s.hsxStart[b]);
     group_by_code(t.nConf, std::max(t.maxD, 1), t.dN, t.dExc, t.dCode, t.dFac, t.nDc, t.dxCode, t.dxStart, t.dxSrc,
-                  t.dxDst, t.dxFac);
+                  t.dxDst, t.dxFac, s.hdN[b], s.hdxStart[b]);
     CiView& v = s.view;
     v.nSc[b] = t.nSc;
     v.nDc[b] = t.nDc;
@@ -519,11 +540,96 @@ void ci_build_tables(cgpu_ctx* c, SysHost& s) {
   CODY_CUDA(cudaStreamSynchronize(c->stream));
 }
 
+// Work lists of the CI kernels: per trajectory, the configurations (H.C) and the
+// RDM tasks, cut into blocks of about the same number of terms.
+void ci_build_work(cgpu_ctx* c) {
+  std::vector<CiWork> apply, rdm, pairs;
+  std::vector<std::vector<long>> aw(c->nb), rw(c->nb), pw(c->nb);
+  long aTot = 0, rTot = 0, pTot = 0;
+  for (int t = 0; t < c->nb; t++) {
+    const SysHost& s = c->sys[t];
+    const CiView& v = s.view;
+    aw[t].resize(s.nC);
+    for (int I = 0; I < s.nC; I++) {
+      int conf[CODY_MAX_BT], r = I;
+      for (int b = 0; b < v.nBt; b++) {
+        conf[b] = r % v.nConf[b];
+        r /= v.nConf[b];
+      }
+      long w = 1;
+      for (int b = 0; b < v.nBt; b++) {
+        w += s.hsN[b][conf[b]] + s.hdN[b][conf[b]];
+        for (int b2 = b + 1; b2 < v.nBt; b2++) w += (long)s.hsN[b][conf[b]] * s.hsN[b2][conf[b2]];
+      }
+      aw[t][I] = w;
+      aTot += w;
+    }
+    for (int b = 0; b < v.nBt; b++)
+      for (int q = 0; q < v.nSc[b]; q++)
+        rw[t].push_back(1 + (long)(s.hsxStart[b][q + 1] - s.hsxStart[b][q]) * (v.nC / v.nConf[b]));
+    for (int b = 0; b < v.nBt; b++)
+      for (int q = 0; q < v.nDc[b]; q++)
+        rw[t].push_back(1 + (long)(s.hdxStart[b][q + 1] - s.hdxStart[b][q]) * (v.nC / v.nConf[b]));
+    for (int b1 = 0; b1 < v.nBt; b1++)
+      for (int b2 = b1 + 1; b2 < v.nBt; b2++) {
+        long nRest = v.nC / ((long)v.nConf[b1] * v.nConf[b2]);
+        for (int q1 = 0; q1 < v.nSc[b1]; q1++)
+          for (int q2 = 0; q2 < v.nSc[b2]; q2++)
+            pw[t].push_back(1 + (long)(s.hsxStart[b1][q1 + 1] - s.hsxStart[b1][q1]) *
+                                    (s.hsxStart[b2][q2 + 1] - s.hsxStart[b2][q2]) * nRest);
+      }
+    for (long w : rw[t]) rTot += w;
+    for (long w : pw[t]) pTot += w;
+  }
+  // about 8 blocks per SM in total; a block never spans two trajectories
+  auto cut = [](const std::vector<std::vector<long>>& wts, long target, int maxItems, std::vector<CiWork>& out) {
+    for (int t = 0; t < (int)wts.size(); t++) {
+      int n = (int)wts[t].size(), t0 = 0;
+      long acc = 0;
+      for (int i = 0; i < n; i++) {
+        acc += wts[t][i];
+        if (acc >= target || i + 1 - t0 >= maxItems || i == n - 1) {
+          out.push_back(CiWork{t, t0, i + 1});
+          t0 = i + 1;
+          acc = 0;
+        }
+      }
+    }
+  };
+  // a block holds at least ~8 configurations (one per warp) / ~128 RDM tasks (one per thread) on average
+  long nConfTot = 0, nTaskTot = 0, nPairTot = 0;
+  for (int t = 0; t < c->nb; t++) {
+    nConfTot += (long)aw[t].size();
+    nTaskTot += (long)rw[t].size();
+    nPairTot += (long)pw[t].size();
+  }
+  cut(aw, std::max({64L, aTot / (8 * 152), 8 * aTot / std::max(1L, nConfTot)}), 1 << 20, apply);
+  cut(rw, std::max({64L, rTot / (8 * 152), 8 * rTot / std::max(1L, nTaskTot)}), 1 << 20, rdm);
+  cut(pw, std::max({64L, pTot / (8 * 152), 128 * pTot / std::max(1L, nPairTot)}), 1 << 20, pairs);
+  c->nApplyWork = (int)apply.size();
+  c->nRdmWork = (int)rdm.size();
+  c->nPairWork = (int)pairs.size();
+  auto put = [](CiWork*& d, const std::vector<CiWork>& h) {
+    CODY_CUDA(cudaMalloc(&d, sizeof(CiWork) * std::max<size_t>(h.size(), 1)));
+    if (!h.empty()) CODY_CUDA(cudaMemcpy(d, h.data(), sizeof(CiWork) * h.size(), cudaMemcpyHostToDevice));
+  };
+  put(c->applyWork_d, apply);
+  put(c->rdmWork_d, rdm);
+  put(c->pairWork_d, pairs);
+  // the CI vector of one trajectory in shared memory when it fits
+  size_t need = sizeof(z_t) * (size_t)c->nC;
+  c->ciSmem = need <= 72 * 1024 ? (int)need : 0;  // leaves room for three blocks per SM
+  if (c->ciSmem > 48 * 1024) {
+    CODY_CUDA(cudaFuncSetAttribute(k_ci_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
+    CODY_CUDA(cudaFuncSetAttribute(k_ci_rdm_codes, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
+    CODY_CUDA(cudaFuncSetAttribute(k_ci_rdm_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
+  }
+}
+
 void launch_ci_apply(cgpu_ctx* c, const z_t* C, z_t* dC, int useH1, int useH2) {
   ProfScope prof(c, CGPU_KERNEL_CI_APPLY);
-  int threads = 256;
-  unsigned blocks = ew_blocks(c, (size_t)c->nC * 32, threads);
-  k_ci_apply<<<bgrid(c, blocks), threads, 0, c->stream>>>(C, dC, c->h1Lin_d, c->h2Lin_d, TRAJ_PASS(c), useH1, useH2);
+  k_ci_apply<<<c->nApplyWork, 256, c->ciSmem, c->stream>>>(C, dC, c->h1Lin_d, c->h2Lin_d, TRAJ_PASS(c), c->applyWork_d,
+                                                          c->ciSmem > 0, useH1, useH2);
   CODY_LAUNCHED(c);
 }
 
@@ -531,10 +637,16 @@ void launch_ci_rdm(cgpu_ctx* c, const z_t* C, int want1, int want2) {
   ProfScope prof(c, CGPU_KERNEL_CI_RDM);
   size_t n2 = (size_t)c->nO * c->nO, n4 = n2 * n2;
   // every code present is written; the other entries of the Lin arrays stay zero
-  int threads = 256;
-  unsigned blocks = ew_blocks(c, (size_t)c->ciTasks * 32, threads);
-  k_ci_rdm<<<bgrid(c, blocks), threads, 0, c->stream>>>(C, c->rdm1Lin_d, c->rdm2Lin_d, TRAJ_PASS(c), want1, want2);
-  CODY_LAUNCHED(c);
+  if (c->nRdmWork > 0) {
+    k_ci_rdm_codes<<<c->nRdmWork, 256, c->ciSmem, c->stream>>>(C, c->rdm1Lin_d, c->rdm2Lin_d, TRAJ_PASS(c),
+                                                               c->rdmWork_d, c->ciSmem > 0, want1, want2);
+    CODY_LAUNCHED(c);
+  }
+  if (want2 && c->nPairWork > 0) {
+    k_ci_rdm_pairs<<<c->nPairWork, 128, c->ciSmem, c->stream>>>(C, c->rdm2Lin_d, TRAJ_PASS(c), c->pairWork_d,
+                                                                c->ciSmem > 0);
+    CODY_LAUNCHED(c);
+  }
   if (want1) {
     k_unfold_rdm1<<<bgrid(c, ew_blocks(c, n2)), 256, 0, c->stream>>>(c->rdm1_d, c->rdm1Lin_d, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
@@ -547,12 +659,14 @@ void launch_ci_rdm(cgpu_ctx* c, const z_t* C, int want1, int want2) {
 }
 
 void launch_fold_h1(cgpu_ctx* c) {
+  ProfScope prof(c, CGPU_KERNEL_FOLD);
   size_t n2 = (size_t)c->nO * c->nO;
   k_fold_h1<<<bgrid(c, ew_blocks(c, n2)), 256, 0, c->stream>>>(c->h1Lin_d, c->h1_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
 void launch_fold_h2(cgpu_ctx* c) {
+  ProfScope prof(c, CGPU_KERNEL_FOLD);
   size_t n4 = (size_t)c->nO * c->nO * c->nO * c->nO;
   k_fold_h2<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(c->h2Lin_d, c->h2_d, c->btOfOrb_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);

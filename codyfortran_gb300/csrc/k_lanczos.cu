@@ -78,8 +78,8 @@ __device__ __forceinline__ void chunk_dots(z_t (&acc)[LZ_VPW], const z_t* __rest
   }
 }
 
-// part[blk*nVec + k] = warp sums of acc (one warp per vector k)
-__device__ __forceinline__ void store_dots(z_t (&acc)[LZ_VPW], int nVec, z_t* __restrict__ part) {
+// part[blk*stride + k] = warp sums of acc (one warp per vector k)
+__device__ __forceinline__ void store_dots(z_t (&acc)[LZ_VPW], int nVec, z_t* __restrict__ part, int stride) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int q = 0; q < LZ_VPW; q++) {
@@ -90,18 +90,35 @@ __device__ __forceinline__ void store_dots(z_t (&acc)[LZ_VPW], int nVec, z_t* __
       a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
       a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
     }
-    if (lane == 0) part[(size_t)blockIdx.x * nVec + k] = a;
+    if (lane == 0) part[(size_t)blockIdx.x * stride + k] = a;
   }
 }
 
-// part[blk*nVec + k] = sum_{i in blk} conj(V_k[i]) m[i] w[i], all k in one pass over the data.
-__global__ void __launch_bounds__(LZ_THREADS) k_mdot(z_t* __restrict__ part, const z_t* __restrict__ V, size_t ldv,
-                                                      int nVec, const z_t* __restrict__ w,
+// Second Gram-Schmidt pass needed?  True when the first pass cancelled most of
+// w: ||w1||^2 <= eta^2 ||w0||^2 (w0 = H v_j before, w1 after the projections),
+// the classical criterion for a loss of orthogonality beyond rounding.  Every
+// block sums the same partials in the same order, so all blocks agree.
+constexpr double LZ_ETA2 = 1.0e-2;
+__device__ bool reorth_needed(const z_t* __restrict__ w0n, int stride, const z_t* __restrict__ w1n, int nBlk) {
+  __shared__ z_t g[2];
+  sum_partials(w0n, nBlk, stride, 1, g);
+  sum_partials(w1n, nBlk, 1, 1, g + 1);
+  return g[1].x <= LZ_ETA2 * g[0].x;
+}
+
+// part[blk*stride + k] = sum_{i in blk} conj(V_k[i]) m[i] w[i] for k < nVec, in
+// one pass over the data; with withNorm also part[blk*stride + nVec] = ||w||_m^2.
+// Gated (gate0 != null): only when the reorthogonalisation test says so.
+__global__ void __launch_bounds__(LZ_THREADS) k_mdot(z_t* __restrict__ part, int stride, const z_t* __restrict__ V,
+                                                      size_t ldv, int nVec, const z_t* __restrict__ w,
                                                       const double* __restrict__ m, TRAJ_ARGS,
-                                                      const double* __restrict__ lz, int E) {
+                                                      const double* __restrict__ lz, int E, int withNorm,
+                                                      const z_t* __restrict__ gate0, int gateStride,
+                                                      const z_t* __restrict__ gate1, int nBlkGate) {
   const TrajShape& S = shp[blockIdx.z];
   lz = bat(lz, bs);
   if (lz[LZ_DONE] != 0.0) return;
+  if (gate0 && !reorth_needed(bat(gate0, bs), gateStride, bat(gate1, bs), nBlkGate)) return;
   part = bat(part, bs);
   V = bat(V, bs);
   w = bat(w, bs);
@@ -112,54 +129,59 @@ __global__ void __launch_bounds__(LZ_THREADS) k_mdot(z_t* __restrict__ part, con
   z_t acc[LZ_VPW];
 #pragma unroll
   for (int q = 0; q < LZ_VPW; q++) acc[q] = zmk(0.0, 0.0);
+  double nacc = 0.0;
   for (size_t c0 = (size_t)blockIdx.x * CH; c0 < n; c0 += (size_t)gridDim.x * CH) {
     int cn = (int)min((size_t)CH, n - c0);
     __syncthreads();
     for (int t = threadIdx.x; t < cn; t += LZ_THREADS) {
       size_t i = vidx(S, c0 + t);
-      sw[t] = zscale(w[i], m[i]);
+      z_t wi = w[i];
+      z_t b = zscale(wi, m[i]);
+      sw[t] = b;
+      nacc += wi.x * b.x + wi.y * b.y;
     }
     __syncthreads();
     chunk_dots(acc, V, ldv, nVec, S, c0, cn, sw);
   }
-  store_dots(acc, nVec, part);
+  store_dots(acc, nVec, part, stride);
+  if (withNorm) {
+    z_t t = block_sum2(zmk(nacc, 0.0));
+    if (threadIdx.x == 0) part[(size_t)blockIdx.x * stride + nVec] = t;
+  }
 }
 
-// Every block re-sums the partials (fixed order) into shared coefficients,
-// subtracts w -= sum_k coef_k V_k, and in the same pass emits partials for the
-// next stage: mode 0: dots of the new w with V_0..V_{nVec-1} (the chunk's basis
-// entries are re-read from cache); mode 1: the metric norm^2 of the new w.
-// Block 0 stores the first-pass coefficients at lz[LZ_D].
+// Every block re-sums the dot partials (fixed order) into shared coefficients,
+// subtracts w -= sum_k coef_k V_k and emits the partials of the metric norm^2
+// of the new w.  Block 0 stores the coefficients at lz[LZ_D] (storeDots).
+// Gated as k_mdot.
 __global__ void __launch_bounds__(LZ_THREADS) k_cgs_pass(z_t* __restrict__ w, const z_t* __restrict__ V, size_t ldv,
-                                                          int nVec, const z_t* __restrict__ partIn, int nBlkIn,
-                                                          z_t* __restrict__ partOut, const double* __restrict__ m,
-                                                          TRAJ_ARGS, double* __restrict__ lz, int mode,
-                                                          int storeDots, int E) {
+                                                          int nVec, const z_t* __restrict__ partIn, int inStride,
+                                                          int nBlkIn, z_t* __restrict__ partOut,
+                                                          const double* __restrict__ m, TRAJ_ARGS,
+                                                          double* __restrict__ lz, int storeDots, int E,
+                                                          const z_t* __restrict__ gate0, int gateStride,
+                                                          const z_t* __restrict__ gate1) {
   const TrajShape& S = shp[blockIdx.z];
   lz = bat(lz, bs);
   if (lz[LZ_DONE] != 0.0) return;
+  if (gate0 && !reorth_needed(bat(gate0, bs), gateStride, bat(gate1, bs), nBlkIn)) return;
   w = bat(w, bs);
   V = bat(V, bs);
   partIn = bat(partIn, bs);
   partOut = bat(partOut, bs);
   m = bat(m, bs);
   __shared__ z_t coef[32];
-  __shared__ z_t sw[LZ_THREADS * LZ_EMAX];
   const size_t n = S.nS;
   const int CH = LZ_THREADS * E;
-  sum_partials(partIn, nBlkIn, nVec, nVec, coef);
+  sum_partials(partIn, nBlkIn, inStride, nVec, coef);
   if (storeDots && blockIdx.x == 0)
     for (int k = threadIdx.x; k < nVec; k += blockDim.x) {
       lz[LZ_D + 2 * k] = coef[k].x;
       lz[LZ_D + 2 * k + 1] = coef[k].y;
     }
-  z_t acc[LZ_VPW];
-#pragma unroll
-  for (int q = 0; q < LZ_VPW; q++) acc[q] = zmk(0.0, 0.0);
   double nacc = 0.0;
   for (size_t c0 = (size_t)blockIdx.x * CH; c0 < n; c0 += (size_t)gridDim.x * CH) {
     int cn = (int)min((size_t)CH, n - c0);
-    __syncthreads();
     for (int t = threadIdx.x; t < cn; t += LZ_THREADS) {
       size_t i = vidx(S, c0 + t);
       z_t r = w[i];
@@ -170,26 +192,20 @@ __global__ void __launch_bounds__(LZ_THREADS) k_cgs_pass(z_t* __restrict__ w, co
         r.y -= cf.x * v.y + cf.y * v.x;
       }
       w[i] = r;
-      z_t b = zscale(r, m[i]);
-      if (mode == 0) sw[t] = b;
-      else nacc += r.x * b.x + r.y * b.y;
-    }
-    if (mode == 0) {
-      __syncthreads();
-      chunk_dots(acc, V, ldv, nVec, S, c0, cn, sw);
+      double mi = m[i];
+      nacc += (r.x * r.x + r.y * r.y) * mi;
     }
   }
-  if (mode == 0) {
-    store_dots(acc, nVec, partOut);
-  } else {
-    z_t t = block_sum2(zmk(nacc, 0.0));
-    if (threadIdx.x == 0) partOut[blockIdx.x] = t;
-  }
+  z_t t = block_sum2(zmk(nacc, 0.0));
+  if (threadIdx.x == 0) partOut[blockIdx.x] = t;
 }
 
 // beta_j = sqrt(sum partials); alpha_j from the first-pass dot; v_{j+1} = w / beta_j.
 // j is 1-based; alpha/beta stored at index j-1.
+// The norm partials are those of the first pass (partIn) or, when the
+// reorthogonalisation test fired, of the second (partAlt).
 __global__ void k_lz_finish(z_t* __restrict__ vNext, const z_t* __restrict__ w, const z_t* __restrict__ partIn,
+                            const z_t* __restrict__ partAlt, const z_t* __restrict__ gate0, int gateStride,
                             int nBlkIn, TRAJ_ARGS, double* __restrict__ lz, int j, int maxDim, double zeroThr) {
   const TrajShape& S = shp[blockIdx.z];
   lz = bat(lz, bs);
@@ -197,6 +213,7 @@ __global__ void k_lz_finish(z_t* __restrict__ vNext, const z_t* __restrict__ w, 
   vNext = bat(vNext, bs);
   w = bat(w, bs);
   partIn = bat(partIn, bs);
+  if (reorth_needed(bat(gate0, bs), gateStride, partIn, nBlkIn)) partIn = bat(partAlt, bs);
   const size_t n = S.nS;
   __shared__ z_t tot[1];
   sum_partials(partIn, nBlkIn, 1, 1, tot);
@@ -216,10 +233,10 @@ __global__ void k_lz_finish(z_t* __restrict__ vNext, const z_t* __restrict__ w, 
     return;
   }
   if (vNext == nullptr) return;
+  const double inv = 1.0 / be;
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
     size_t i = vidx(S, l);
-    z_t v = w[i];
-    vNext[i] = zmk(v.x / be, v.y / be);
+    vNext[i] = zscale(w[i], inv);
   }
 }
 
@@ -389,10 +406,10 @@ __global__ void k_lz_start(z_t* __restrict__ v1, const z_t* __restrict__ s, cons
     lz[LZ_ERR] = 0.0;
   }
   if (zero) return;
+  const double inv = 1.0 / nr;
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
     size_t i = vidx(S, l);
-    z_t v = s[i];
-    v1[i] = zmk(v.x / nr, v.y / nr);
+    v1[i] = zscale(s[i], inv);
   }
 }
 
@@ -415,10 +432,11 @@ __global__ void k_norm_partial(z_t* __restrict__ part, const z_t* __restrict__ v
 
 }  // namespace
 
-size_t lanczos_partial_need(const cgpu_ctx* c) { return (size_t)c->lzBlocks * (c->maxKrylov + 1) * 2; }
+size_t lanczos_partial_need(const cgpu_ctx* c) { return (size_t)c->lzBlocks * (2 * (c->maxKrylov + 1) + 2); }
 
 // Starts a Lanczos pass from the vector v (device, state layout): basis[:,0] = v/|v|.
 void launch_lanczos_start(cgpu_ctx* c, const z_t* v) {
+  ProfScope prof(c, CGPU_KERNEL_VECTOR);
   int nBlk = c->lzBlocks;
   k_norm_partial<<<bgrid(c, nBlk), LZ_THREADS, 0, c->stream>>>(c->partial_d, v, c->metric_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
@@ -432,34 +450,44 @@ void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
   ProfScope prof(c, CGPU_KERNEL_LANCZOS);
   size_t ld = c->nS;
   int nBlk = c->lzBlocks;
+  // p1: pass-1 dots with v_1..v_j and ||w0||^2 (stride j+1); p2: ||w1||^2 after
+  // pass 1; p3, p4: dots and norm of the gated second pass
   z_t* p1 = c->partial_d;
-  z_t* p2 = c->partial_d + (size_t)nBlk * (c->maxKrylov + 1);
+  z_t* p2 = p1 + (size_t)nBlk * (c->maxKrylov + 1);
+  z_t* p3 = p2 + nBlk;
+  z_t* p4 = p3 + (size_t)nBlk * (c->maxKrylov + 1);
   if (j > 32) throw std::string("SIL: Krylov order above 32");
-  const int E = c->lzElems;
-  k_mdot<<<bgrid(c, nBlk), LZ_THREADS, 0, c->stream>>>(p1, c->basis_d, ld, j, c->lw_d, c->metric_d, TRAJ_PASS(c),
-                                                       c->lz_d, E);
+  const int E = c->lzElems, s1 = j + 1;
+  dim3 g = bgrid(c, nBlk);
+  k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p1, s1, c->basis_d, ld, j, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 1,
+                                          nullptr, 0, nullptr, nBlk);
   CODY_LAUNCHED(c);
-  k_cgs_pass<<<bgrid(c, nBlk), LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, ld, j, p1, nBlk, p2, c->metric_d,
-                                                           TRAJ_PASS(c), c->lz_d, 0, 1, E);
+  k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, ld, j, p1, s1, nBlk, p2, c->metric_d, TRAJ_PASS(c),
+                                              c->lz_d, 1, E, nullptr, 0, nullptr);
   CODY_LAUNCHED(c);
-  k_cgs_pass<<<bgrid(c, nBlk), LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, ld, j, p2, nBlk, p1, c->metric_d,
-                                                           TRAJ_PASS(c), c->lz_d, 1, 0, E);
+  k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p3, j, c->basis_d, ld, j, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 0,
+                                          p1 + j, s1, p2, nBlk);
+  CODY_LAUNCHED(c);
+  k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, ld, j, p3, j, nBlk, p4, c->metric_d, TRAJ_PASS(c),
+                                              c->lz_d, 0, E, p1 + j, s1, p2);
   CODY_LAUNCHED(c);
   z_t* vNext = (j < maxDim) ? c->basis_d + ld * (size_t)j : nullptr;
-  k_lz_finish<<<bgrid(c, nBlk), LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p1, nBlk, TRAJ_PASS(c), c->lz_d, j,
-                                                            maxDim, 1.0e-14);
+  k_lz_finish<<<g, LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p2, p4, p1 + j, s1, nBlk, TRAJ_PASS(c), c->lz_d, j,
+                                               maxDim, 1.0e-14);
   CODY_LAUNCHED(c);
   k_lz_mark_done<<<bgrid(c, 1), 1, 0, c->stream>>>(c->lz_d, j, c->bs);
   CODY_LAUNCHED(c);
 }
 
 void launch_lanczos_tail(cgpu_ctx* c, int j, double dt, int evalExp) {
+  ProfScope prof(c, CGPU_KERNEL_VECTOR);
   if (!evalExp) return;
   k_lz_expsub<<<bgrid(c, 1), 32, 0, c->stream>>>(c->lz_d, j, dt, 0.0, c->bs);
   CODY_LAUNCHED(c);
 }
 
 void launch_lanczos_combine(cgpu_ctx* c, z_t* out) {
+  ProfScope prof(c, CGPU_KERNEL_VECTOR);
   k_lz_combine<<<bgrid(c, c->lzBlocks), LZ_THREADS, 0, c->stream>>>(out, c->work_d, c->basis_d, c->nS, TRAJ_PASS(c),
                                                                     c->lz_d);
   CODY_LAUNCHED(c);

@@ -555,6 +555,7 @@ static void h2_from_pairs(cgpu_ctx* c) {
 }
 
 void launch_rdm_inverse(cgpu_ctx* c) {
+  ProfScope prof(c, CGPU_KERNEL_RDM_INVERSE);
   int n = c->nOS;
   if (n > JB_MAX) throw std::string("ApplyCorrelationOp: more than 32 stored orbitals is not supported");
   constexpr size_t jsmem = 3 * sizeof(z_t) * JB_MAX * (JB_MAX + 1);

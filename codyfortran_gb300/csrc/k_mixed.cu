@@ -67,6 +67,33 @@ __device__ __forceinline__ void write_split(__nv_bfloat16* out, int row, int k, 
   }
 }
 
+// FP64 -> FP32 by truncating the significand (integer operations only: the FP64
+// pipes are the scarce resource).  |x| below the FP32 normal range flushes to
+// zero; relative error < 2^-23, below the bf16x3 form's ~2^-16.
+__device__ __forceinline__ float f64_to_f32(double x) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  unsigned hi = (unsigned)(u >> 32);
+  unsigned sign = hi & 0x80000000u;
+  int e = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;
+  if (e <= 0) return __int_as_float((int)sign);
+  if (e >= 255) return __int_as_float((int)(sign | 0x7F800000u));
+  unsigned mant = ((hi & 0xFFFFFu) << 3) | (unsigned)((u >> 29) & 7u);
+  return __int_as_float((int)(sign | ((unsigned)e << 23) | mant));
+}
+
+// bf16x3 split in FP32: hi = bf16(v), lo = bf16(v - hi); A rows [hi,hi,lo], B rows [hi,lo,hi].
+__device__ __forceinline__ void write_split3(__nv_bfloat16* out, int row, int k, int K, int pitch, int isB, float v) {
+  size_t base = (size_t)row * 3 * pitch + k;
+  __nv_bfloat16 hi = __float2bfloat16_rn(0.0f), lo = hi;
+  if (k < K) {
+    hi = __float2bfloat16_rn(v);
+    lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+  }
+  out[base] = hi;
+  out[base + pitch] = isB ? lo : hi;
+  out[base + 2 * (size_t)pitch] = isB ? hi : lo;
+}
+
 __global__ void k_split_V(__nv_bfloat16* __restrict__ out, const double* __restrict__ V, int pitch, int terms,
                           TRAJ_ARGS) {
   const TrajShape& T = shp[blockIdx.z];
@@ -91,15 +118,26 @@ __global__ void k_split_S(__nv_bfloat16* __restrict__ outA, const z_t* __restric
   pl = bat(pl, bs);
   pk = bat(pk, bs);
   GRID_STRIDE(e, (size_t)2 * nP * Kpad) {
-  int row = (int)(e / Kpad), g = (int)(e % Kpad);
-  int p = row >> 1, s = row & 1;
-  double v = 0.0;
-  if (g < nG) {
-    z_t a = orbs[(size_t)nG * pl[p] + g], b = orbs[(size_t)nG * pk[p] + g];
-    z_t sv = zscale(zcmul(a, b), w[g]);
-    v = s ? sv.y : sv.x;
-  }
-  write_split(outA, row, g, nG, pitch, terms, 0, v);
+    int row = (int)(e / Kpad), g = (int)(e % Kpad);
+    int p = row >> 1, s = row & 1;
+    if (terms == 3) {
+      float v = 0.0f;
+      if (g < nG) {
+        z_t a = orbs[(size_t)nG * pl[p] + g], b = orbs[(size_t)nG * pk[p] + g];
+        float ar = f64_to_f32(a.x), ai = f64_to_f32(a.y), br = f64_to_f32(b.x), bi = f64_to_f32(b.y);
+        float wg = f64_to_f32(w[g]);
+        v = s ? (ar * bi - ai * br) * wg : (ar * br + ai * bi) * wg;
+      }
+      write_split3(outA, row, g, nG, pitch, 0, v);
+    } else {
+      double v = 0.0;
+      if (g < nG) {
+        z_t a = orbs[(size_t)nG * pl[p] + g], b = orbs[(size_t)nG * pk[p] + g];
+        z_t sv = zscale(zcmul(a, b), w[g]);
+        v = s ? sv.y : sv.x;
+      }
+      write_split(outA, row, g, nG, pitch, terms, 0, v);
+    }
   }
 }
 
@@ -127,12 +165,18 @@ __global__ void __launch_bounds__(256) k_split_W(__nv_bfloat16* __restrict__ WxA
     if (g < nG && n < N2P)
       for (int z = 0; z < nSplit; z++) v += (double)P1[((size_t)z * nG + g) * N2P + n];
     tile[r][tx] = v;
-    if (g < nG && n < KpP) write_split(WxA, g, n, N2P, pitchP, terms, 0, v);
+    if (g < nG && n < KpP) {
+      if (terms == 3) write_split3(WxA, g, n, N2P, pitchP, 0, (float)v);
+      else write_split(WxA, g, n, N2P, pitchP, terms, 0, v);
+    }
   }
   __syncthreads();
   for (int r = ty; r < SW_T; r += 8) {
     int n = n0 + r, g = g0 + tx;
-    if (n < N2P && g < KpG) write_split(WTxB, n, g, nG, pitchG, terms, 1, tile[tx][r]);
+    if (n < N2P && g < KpG) {
+      if (terms == 3) write_split3(WTxB, n, g, nG, pitchG, 1, (float)tile[tx][r]);
+      else write_split(WTxB, n, g, nG, pitchG, terms, 1, tile[tx][r]);
+    }
   }
 }
 
@@ -147,21 +191,21 @@ __global__ void k_split_R(__nv_bfloat16* __restrict__ RxB, const z_t* __restrict
   pl = bat(pl, bs);
   pk = bat(pk, bs);
   GRID_STRIDE(e, (size_t)2 * Q * KpP) {
-  int row = (int)(e / KpP), k = (int)(e % KpP);
-  int q = row >> 1, s = row & 1;
-  double v = 0.0;
-  if (k < 2 * nP) {
-    int p = k >> 1, t = k & 1;
-    int l = pl[p], kk = pk[p];
-    z_t R1 = Rp[(size_t)(l * n + kk) * Q + q];
-    z_t R2 = (l < kk) ? Rp[(size_t)(kk * n + l) * Q + q] : zmk(0.0, 0.0);
-    z_t X = zadd(R1, R2);
-    z_t D = zsub(R1, R2);
-    z_t Y = zmk(-D.y, D.x);
-    z_t val = t ? Y : X;
-    v = s ? val.y : val.x;
-  }
-  write_split(RxB, row, k, 2 * nP, pitchP, terms, 1, v);
+    int row = (int)(e / KpP), k = (int)(e % KpP);
+    int q = row >> 1, s = row & 1;
+    double v = 0.0;
+    if (k < 2 * nP) {
+      int p = k >> 1, t = k & 1;
+      int l = pl[p], kk = pk[p];
+      z_t R1 = Rp[(size_t)(l * n + kk) * Q + q];
+      z_t R2 = (l < kk) ? Rp[(size_t)(kk * n + l) * Q + q] : zmk(0.0, 0.0);
+      // X = R1 + R2, Y = i (R1 - R2): re/im parts of the selected one
+      double r1 = s ? (t ? R1.x : R1.y) : (t ? -R1.y : R1.x);
+      double r2 = s ? (t ? R2.x : R2.y) : (t ? -R2.y : R2.x);
+      v = t ? r1 - r2 : r1 + r2;
+    }
+    if (terms == 3) write_split3(RxB, row, k, 2 * nP, pitchP, 1, f64_to_f32(v));
+    else write_split(RxB, row, k, 2 * nP, pitchP, terms, 1, v);
   }
 }
 

@@ -49,11 +49,16 @@ __device__ double field_amplitude_dev(const LaserDev& L, double t) {
   return 0.0;
 }
 
+// Eout (one slot per trajectory) = E(*tBase + tOff) for every trajectory.
+__global__ void k_field(double* __restrict__ Eout, TRAJ_ARGS, const double* __restrict__ tBase, double tOff) {
+  Eout = bat(Eout, bs);
+  *Eout = field_amplitude_dev(shp[blockIdx.z].laser, *bat(tBase, bs) + tOff);
+}
+
 __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, const double* __restrict__ T,
                           const double* __restrict__ V0, const double* __restrict__ x, const int* __restrict__ btOf,
-                          TRAJ_ARGS, const double* __restrict__ tBase, double tOff, z_t alpha, int accumulate) {
+                          TRAJ_ARGS, const double* __restrict__ Efield, z_t alpha, int accumulate) {
   extern __shared__ z_t sh[];
-  __shared__ double Eshared;
   const TrajShape& S = shp[blockIdx.z];
   const int nG = S.nG, band = S.band;
   int i = blockIdx.y;
@@ -65,7 +70,7 @@ __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, c
   V0 = bat(V0, bs);
   x = bat(x, bs);
   btOf = bat(btOf, bs);
-  if (threadIdx.x == 0) Eshared = field_amplitude_dev(S.laser, *bat(tBase, bs) + tOff);
+  const double E = *bat(Efield, bs);
   const z_t* f = orbs + (size_t)nG * i;
   int nTile = OB_THREADS + 2 * band;
   for (int t = threadIdx.x; t < nTile; t += OB_THREADS) {
@@ -86,12 +91,13 @@ __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, c
     acc.y = fma(c, v.y, acc.y);
   }
   if (S.hasPot) {
-    double pot = V0[g] + Eshared * x[g];
+    double pot = V0[g] + E * x[g];
     z_t v = sh[threadIdx.x + band];
     acc.x = fma(pot, v.x, acc.x);
     acc.y = fma(pot, v.y, acc.y);
   }
-  z_t r = zmul(alpha, acc);
+  // alpha is 1 or -i on the propagation paths: no FP64 multiply for those
+  z_t r = (alpha.x == 1.0 && alpha.y == 0.0) ? acc : (alpha.x == 0.0 && alpha.y == -1.0) ? zmi(acc) : zmul(alpha, acc);
   size_t o = (size_t)nG * i + g;
   if (accumulate) r = zadd(out[o], r);
   out[o] = r;
@@ -492,13 +498,17 @@ void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha,
   size_t sh = sizeof(z_t) * (OB_THREADS + 2 * c->band);
   const double* base = (c->inCapture || c->useStepTime) ? c->stepT_d : c->zero_d;
   double off = c->inCapture ? t - c->captureT0 : t;
-  k_onebody<<<grid, OB_THREADS, sh, c->stream>>>(out, orbs, c->T_d, c->V0_d, c->x_d, c->btOfOrb_d, TRAJ_PASS(c), base,
-                                                 off, alpha, accumulate);
+  double* E = c->scal_d + 16;
+  k_field<<<bgrid(c, 1), 1, 0, c->stream>>>(E, TRAJ_PASS(c), base, off);
+  CODY_LAUNCHED(c);
+  k_onebody<<<grid, OB_THREADS, sh, c->stream>>>(out, orbs, c->T_d, c->V0_d, c->x_d, c->btOfOrb_d, TRAJ_PASS(c), E,
+                                                 alpha, accumulate);
   CODY_LAUNCHED(c);
 }
 
 // Orbs_ProjectOnSubspace: one group when restricted, otherwise per body type.
 void launch_project_orbs(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs) {
+  ProfScope prof(c, CGPU_KERNEL_PROJECTORS);
   int nGroups = c->restricted ? 1 : c->nBt;
   for (int g = 0; g < nGroups; g++) {
     int n = max_group_size(c, g);
@@ -511,6 +521,7 @@ void launch_project_orbs(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs) {
 }
 
 void launch_project_coeffs(cgpu_ctx* c, z_t* dC, const z_t* C) {
+  ProfScope prof(c, CGPU_KERNEL_PROJECTORS);
   int nBlk = coeff_blocks(c);
   check_partial(c, nBlk);
   k_dot_partial<<<bgrid(c, nBlk), 256, 0, c->stream>>>(c->partial_d, C, dC, TRAJ_PASS(c));
@@ -530,6 +541,7 @@ void launch_normalize_coeffs(cgpu_ctx* c, z_t* C) {
 }
 
 void launch_fill_h1_from(cgpu_ctx* c, const z_t* orbs, const z_t* hOrbs, z_t* h1) {
+  ProfScope prof(c, CGPU_KERNEL_PROJECTORS);
   launch_gram(c, c->gram_d, orbs, hOrbs, -1, c->nOS, 1.0);
   int nn = c->nO * c->nO;
   k_h1_layout<<<bgrid(c, ceil_div(nn, 128)), 128, 0, c->stream>>>(h1, c->gram_d, c->btOfOrb_d, TRAJ_PASS(c));
@@ -537,12 +549,14 @@ void launch_fill_h1_from(cgpu_ctx* c, const z_t* orbs, const z_t* hOrbs, z_t* h1
 }
 
 void launch_axpby(cgpu_ctx* c, z_t* y, const z_t* x, z_t a, z_t b, int sel) {
+  ProfScope prof(c, CGPU_KERNEL_VECTOR);
   size_t n = sel == VSEL_STATE ? c->nS : c->nC;
   k_axpby<<<bgrid(c, vec_blocks(c, n)), 256, 0, c->stream>>>(y, x, a, b, TRAJ_PASS(c), sel);
   CODY_LAUNCHED(c);
 }
 
 void launch_scale(cgpu_ctx* c, z_t* y, z_t a, int sel) {
+  ProfScope prof(c, CGPU_KERNEL_VECTOR);
   size_t n = sel == VSEL_STATE ? c->nS : c->nC;
   k_scale<<<bgrid(c, vec_blocks(c, n)), 256, 0, c->stream>>>(y, a, TRAJ_PASS(c), sel);
   CODY_LAUNCHED(c);
@@ -550,6 +564,7 @@ void launch_scale(cgpu_ctx* c, z_t* y, z_t a, int sel) {
 
 void launch_rk_stage(cgpu_ctx* c, z_t* inc, z_t* tmp, const z_t* state, const z_t* d, double wInc, double wTmp,
                      int first) {
+  ProfScope prof(c, CGPU_KERNEL_VECTOR);
   k_rk_stage<<<bgrid(c, vec_blocks(c, c->nS)), 256, 0, c->stream>>>(inc, tmp, state, d, wInc, wTmp, first,
                                                                       TRAJ_PASS(c));
   CODY_LAUNCHED(c);

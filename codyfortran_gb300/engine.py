@@ -34,10 +34,11 @@ EXPORTED = [
     "cgpu_profile_begin", "cgpu_profile_end", "cgpu_weighted_gram_noalloc",
     "cgpu_batch_create", "cgpu_batch_destroy", "cgpu_batch_size", "cgpu_batch_sizes", "cgpu_batch_grid",
     "cgpu_batch_upload", "cgpu_batch_download", "cgpu_batch_propagate", "cgpu_batch_energies",
-    "cgpu_batch_kernels_per_step", "cgpu_batch_launch_count",
+    "cgpu_batch_kernels_per_step", "cgpu_batch_launch_count", "cgpu_batch_profile_begin", "cgpu_batch_profile_end",
 ]
 
-KERNELS = {"pair_potentials": 1, "correlation": 2, "h2": 3, "ci_apply": 4, "ci_rdm": 5, "onebody": 6, "lanczos": 7}
+KERNELS = {"pair_potentials": 1, "correlation": 2, "h2": 3, "ci_apply": 4, "ci_rdm": 5, "onebody": 6, "lanczos": 7,
+           "rdm_inverse": 8, "projectors": 9, "fold": 10, "vector": 11}
 
 
 class CodyError(RuntimeError):
@@ -455,6 +456,14 @@ class Batch:
 
     def kernels_per_step(self):
         return self.lib.cgpu_batch_kernels_per_step(self.h)
+
+    def profile_begin(self, kernel):
+        self._check(self.lib.cgpu_batch_profile_begin(self.h, KERNELS[kernel] if isinstance(kernel, str) else int(kernel)))
+
+    def profile_end(self):
+        n, ms = C.c_long(), C.c_double()
+        self._check(self.lib.cgpu_batch_profile_end(self.h, C.byref(n), C.byref(ms)))
+        return n.value, ms.value
 
     def launch_count(self, reset=False):
         return self.lib.cgpu_batch_launch_count(self.h, int(reset))

@@ -198,6 +198,10 @@ int cgpu_propagate_resident_timed(cgpu_ctx* ctx, double t0, double dt, int n_ste
 #define CGPU_KERNEL_CI_RDM 5          /* one- and two-body RDM accumulation                    */
 #define CGPU_KERNEL_ONEBODY 6         /* banded kinetic + potential + laser apply              */
 #define CGPU_KERNEL_LANCZOS 7         /* Krylov reorthogonalisation / update                   */
+#define CGPU_KERNEL_RDM_INVERSE 8     /* regularised rho^-1 and the correlation matrix R'      */
+#define CGPU_KERNEL_PROJECTORS 9      /* Gram matrices: h1, (1-P) on orbitals, P on coefficients */
+#define CGPU_KERNEL_FOLD 10           /* h1/h2 folding into the CI code layout                 */
+#define CGPU_KERNEL_VECTOR 11         /* state-vector updates: RK stages, Lanczos start/combine, copies */
 /* Start recording events around every launch of `kernel` (0 disables). */
 int cgpu_profile_begin(cgpu_ctx* ctx, int kernel);
 /* Stop; *launches and *total_ms receive the bracketed launches and their summed device time. */
@@ -235,6 +239,9 @@ int cgpu_batch_propagate(cgpu_batch* batch, const double* t0, double dt, int n_s
 int cgpu_batch_energies(cgpu_batch* batch, const double* t, double* energies);
 /* Kernels launched per step (all systems); launches so far (reset if nonzero). */
 long cgpu_batch_kernels_per_step(const cgpu_batch* batch);
+/* As cgpu_profile_begin / cgpu_profile_end, for the launches of a batch step. */
+int cgpu_batch_profile_begin(cgpu_batch* batch, int kernel);
+int cgpu_batch_profile_end(cgpu_batch* batch, long* launches, double* total_ms);
 long cgpu_batch_launch_count(cgpu_batch* batch, int reset);
 
 /* ---- no-allocation variant ---------------------------------------------- */
