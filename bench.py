@@ -44,6 +44,7 @@ sys.path.insert(0, ROOT)
 METRIC = "MCTDHF traj-steps/s: mixed-prec batched vs FP64 GPU at ≤1e-8 energy/norm err"
 UNIT = "traj-steps/s"
 L2_BYTES = 129 * 1024 * 1024
+ACC_STEPS = 10
 FAMILIES = ("pair_potentials", "correlation", "h2", "ci_apply", "ci_rdm", "onebody", "lanczos", "rdm_inverse",
             "projectors", "fold", "vector")
 
@@ -230,7 +231,12 @@ def dense_flops(systems, fam):
     return 4.0 * tot
 
 
-def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=False, e2e=True):
+def batch_norms(b, packed):
+    """||C|| of every trajectory (orthonormal orbitals: the MCTDHF norm)."""
+    return np.array([np.linalg.norm(packed[b.offsets[i]:b.offsets[i] + b.systems[i].nC]) for i in range(len(b))])
+
+
+def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=False, e2e=True, acc_steps=0):
     from codyfortran_gb300.engine import Batch
     dt, K = cfg["dt"], cfg["krylov"]
     b = Batch(specs, precision, max_krylov=K)
@@ -276,7 +282,12 @@ def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=Fals
             t += dt
         out["e2e_s"] = (time.perf_counter() - te0) / n_e2e
         out["e2e_bytes"] = int(buf.nbytes)
-        out["energy"] = float(b.energies(t)[0])
+    if acc_steps:
+        # accuracy leg: acc_steps steps from the initial states, energies and norms at the end
+        b.upload(host)
+        b.propagate(0.0, dt, acc_steps, K)
+        out["acc_energy"] = b.energies(acc_steps * dt)
+        out["acc_norm"] = batch_norms(b, b.download_packed())
     b.close()
     return out
 
@@ -286,14 +297,23 @@ def run_batch(args):
     specs, cfg = workload(args.workload)
     precision = args.precision or "mixed"
     n = len(specs)
-    r = run_batch_leg(specs, cfg, precision, args.steps, args.warmup, profile=True, clock=True)
+    acc_steps = 0 if args.no_fp64_leg or precision == "fp64" else ACC_STEPS
+    r = run_batch_leg(specs, cfg, precision, args.steps, args.warmup, profile=True, clock=True, acc_steps=acc_steps)
     ms = barrier_max(r["ms"], world)
     value = world * n * args.steps / (ms / 1e3)
-    # the same batch in the plain FP64 form (short timed region)
-    fp64 = None
-    if precision != "fp64" and not args.no_fp64_leg:
-        f = run_batch_leg(specs, cfg, "fp64", max(1, min(args.steps, 2)), 1, profile=False, e2e=False)
+    # the same batch in the plain FP64 form (short timed region), and the
+    # deviation of the mixed form from it after ACC_STEPS steps from the same states
+    fp64, accuracy = None, None
+    if acc_steps:
+        f = run_batch_leg(specs, cfg, "fp64", max(1, min(args.steps, 2)), 1, profile=False, e2e=False,
+                          acc_steps=acc_steps)
         fp64 = n * max(1, min(args.steps, 2)) / (f["ms"] / 1e3)
+        dE = np.abs(r["acc_energy"] - f["acc_energy"]) / np.abs(f["acc_energy"])
+        dN = np.abs(r["acc_norm"] - f["acc_norm"])
+        accuracy = {"steps": acc_steps, "energy_rel_max": float(dE.max()), "energy_rel_median": float(np.median(dE)),
+                    "norm_abs_max": float(dN.max()), "norm_abs_median": float(np.median(dN)),
+                    "target": 1e-8, "reference": "same batch, plain FP64 form on the GPU (parity-tested against "
+                                                  "the CPU port to 1e-12)"}
     # roofline of the dominant kernel family
     hbm, bf16, src = measured_peaks()
     dom, n_dom = r["dom"], max(r["n_dom"], 1)
@@ -327,6 +347,7 @@ def run_batch(args):
                          f"of states and Krylov vectors > L2 ({L2_BYTES / 1e6:.0f} MB): inputs larger than L2, no flush"},
         "fp64_gpu": {"value": fp64, "unit": UNIT, "ratio": (value / fp64) if fp64 else None,
                      "note": "same batch, plain FP64 form, same GPU"},
+        "accuracy_vs_fp64": accuracy,
         "clocks": r["clocks"],
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": r["e2e_bytes"], "d2h_bytes_per_step": r["e2e_bytes"],
                 "call": "cgpu_batch_upload + cgpu_batch_propagate(1 step) + cgpu_batch_download, pageable host buffers"},

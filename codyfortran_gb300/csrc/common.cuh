@@ -368,6 +368,9 @@ void mixed_init(cgpu_ctx* c);
 void mixed_free(cgpu_ctx* c);
 int mixed_error(cgpu_ctx* c);
 void launch_correlation_mixed(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2);
+// k_adjoint.cu
+void adjoint_tdci(cgpu_ctx* c, const z_t* C0_h, const double* E_h, int nT, double dt, int K, double* J,
+                  double* aOut, z_t* CN_h, double* grad_h);
 // k_lanczos.cu
 // The SIL kernels work on c->basis_d, c->lw_d (H v_j), c->work_d (start vector),
 // c->metric_d (current metric) and the scalar block c->lz_d.

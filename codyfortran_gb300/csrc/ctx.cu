@@ -1199,6 +1199,15 @@ int cgpu_tdci_set_orbitals(cgpu_ctx* c, const cgpu_complex* orbs) {
   CODY_API_END(c)
 }
 
+int cgpu_tdci_adjoint(cgpu_ctx* c, const cgpu_complex* c0, const double* field, int n_steps, double dt,
+                      int checkpoint, double* objective, double* overlap, cgpu_complex* c_final, double* d_objective) {
+  CODY_API_BEGIN(c)
+  if (!c0 || !field || !objective) throw std::string("tdci_adjoint: null argument");
+  adjoint_tdci(c, (const z_t*)c0, field, n_steps, dt, checkpoint > 0 ? checkpoint : 64, objective, overlap,
+               (z_t*)c_final, d_objective);
+  CODY_API_END(c)
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

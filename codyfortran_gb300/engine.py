@@ -35,6 +35,7 @@ EXPORTED = [
     "cgpu_batch_create", "cgpu_batch_destroy", "cgpu_batch_size", "cgpu_batch_sizes", "cgpu_batch_grid",
     "cgpu_batch_upload", "cgpu_batch_download", "cgpu_batch_propagate", "cgpu_batch_energies",
     "cgpu_batch_kernels_per_step", "cgpu_batch_launch_count", "cgpu_batch_profile_begin", "cgpu_batch_profile_end",
+    "cgpu_tdci_adjoint",
 ]
 
 KERNELS = {"pair_potentials": 1, "correlation": 2, "h2": 3, "ci_apply": 4, "ci_rdm": 5, "onebody": 6, "lanczos": 7,
@@ -362,6 +363,19 @@ class Engine:
     def tdci_set_orbitals(self, orbs):
         o = self._orbs(orbs)
         self._check(self.lib.cgpu_tdci_set_orbitals(self.h, _p(o)))
+
+    def tdci_adjoint(self, c0, field, dt, checkpoint=64, gradient=True):
+        """J = 1 - |<c0|C_N>|^2 after len(field) RK4 steps (field constant per
+        step) and, with gradient, dJ/dfield from the adjoint sweep.
+        Returns (J, overlap, C_N, grad or None)."""
+        c0 = np.ascontiguousarray(c0, dtype=np.complex128)
+        f = np.ascontiguousarray(field, dtype=np.float64)
+        J, ov = C.c_double(), (C.c_double * 2)()
+        cn = np.zeros(self.nC, dtype=np.complex128)
+        g = np.zeros(len(f)) if gradient else None
+        self._check(self.lib.cgpu_tdci_adjoint(self.h, _p(c0), _p(f), len(f), _d(dt), int(checkpoint), C.byref(J), ov,
+                                               _p(cn), _p(g)))
+        return J.value, complex(ov[0], ov[1]), cn, g
 
 
 class BatchSystem:

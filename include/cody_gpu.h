@@ -212,6 +212,19 @@ int cgpu_profile_end(cgpu_ctx* ctx, long* launches, double* total_ms);
  * fix the orbitals and fill h1/h2 once. */
 int cgpu_tdci_set_orbitals(cgpu_ctx* ctx, const cgpu_complex* orbs);
 
+/* ---- pulse gradient (adjoint) ------------------------------------------- */
+/* No counterpart in the reference.  For a TDCI context (orbitals set with
+ * cgpu_tdci_set_orbitals, at most 64 configurations): propagates c0 over
+ * n_steps RK4 steps of dt with the field constant over step n (field[n]), and
+ * returns objective = 1 - |overlap|^2, overlap = c0^H C_N, the final
+ * coefficients c_final (may be NULL) and, if d_objective is not NULL, the
+ * exact gradient of the discrete map d objective / d field[n] from the
+ * adjoint sweep (states checkpointed every `checkpoint` steps, 0 = 64).
+ * The context's one-body integrals are restored to t = 0 afterwards. */
+int cgpu_tdci_adjoint(cgpu_ctx* ctx, const cgpu_complex* c0, const double* field, int n_steps, double dt,
+                      int checkpoint, double* objective, double* overlap, cgpu_complex* c_final,
+                      double* d_objective);
+
 /* ---- batched trajectories ------------------------------------------------ */
 /* No counterpart in the reference, whose module-global state allows one
  * trajectory per process (src/Method/M_Method.f90:47).  A batch holds n
