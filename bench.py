@@ -231,6 +231,10 @@ def dense_flops(systems, fam):
     return 4.0 * tot
 
 
+def systems_of(r):
+    return r["systems"]
+
+
 def batch_norms(b, packed):
     """||C|| of every trajectory (orthonormal orbitals: the MCTDHF norm)."""
     return np.array([np.linalg.norm(packed[b.offsets[i]:b.offsets[i] + b.systems[i].nC]) for i in range(len(b))])
@@ -308,9 +312,15 @@ def run_batch(args):
         f = run_batch_leg(specs, cfg, "fp64", max(1, min(args.steps, 2)), 1, profile=False, e2e=False,
                           acc_steps=acc_steps)
         fp64 = n * max(1, min(args.steps, 2)) / (f["ms"] / 1e3)
-        dE = np.abs(r["acc_energy"] - f["acc_energy"]) / np.abs(f["acc_energy"])
+        dA = np.abs(r["acc_energy"] - f["acc_energy"])
+        dE = dA / np.abs(f["acc_energy"])
         dN = np.abs(r["acc_norm"] - f["acc_norm"])
+        worst = int(np.argmax(dE))
         accuracy = {"steps": acc_steps, "energy_rel_max": float(dE.max()), "energy_rel_median": float(np.median(dE)),
+                    "energy_rel_p99": float(np.quantile(dE, 0.99)), "energy_abs_max": float(dA.max()),
+                    "worst": {"trajectory": worst, "energy_fp64": float(f["acc_energy"][worst]),
+                              "n_orbitals": int(systems_of(r)[worst].nOS), "n_grid": int(systems_of(r)[worst].nG),
+                              "n_determinants": int(systems_of(r)[worst].nC)},
                     "norm_abs_max": float(dN.max()), "norm_abs_median": float(np.median(dN)),
                     "target": 1e-8, "reference": "same batch, plain FP64 form on the GPU (parity-tested against "
                                                   "the CPU port to 1e-12)"}

@@ -245,6 +245,7 @@ struct cgpu_ctx {
   z_t *Mreg_d = nullptr;                      // (nOS, nOS)
   z_t *Uprev_d = nullptr;                     // (nOS, nOS) natural orbitals of the previous rho^-1 call
   z_t *r1s_d = nullptr;                       // spin-summed spatial rdm1
+  z_t *r2s_d = nullptr;                       // spin-summed spatial rdm2 (nOS^2 x nOS^2)
   // reductions / scratch
   z_t* partial_d = nullptr;
   size_t partialCap = 0;                      // complex entries per trajectory

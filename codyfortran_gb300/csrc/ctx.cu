@@ -334,6 +334,7 @@ size_t layout(cgpu_ctx* c, char* base) {
   Z(c->Mreg_d, Q);
   Z(c->Uprev_d, Q);
   Z(c->r1s_d, Q);
+  Z(c->r2s_d, Q * Q);
   Z(c->gram_d, Q);
   Z(c->orbTmp_d, nG * n);
   Z(c->state_d, nS);
@@ -394,11 +395,15 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
   c->maxKrylov = std::max(1, std::min(maxK > 0 ? maxK : 32, 32));
   // Lanczos reductions: one system spreads 256-entry chunks over up to 4 blocks
   // per SM; a batch gives each block a 1024-entry chunk of its trajectory.
+  // Lanczos reductions: one system spreads 256-entry chunks over up to 4 blocks
+  // per SM; a batch gives each trajectory a few blocks of 1024-entry chunks
+  // (about 4k blocks in total: few partials, little per-block overhead).
   c->lzElems = nSys == 1 ? 1 : 4;
   {
     size_t chunk = (size_t)256 * c->lzElems;
     size_t need = ((size_t)c->nS + chunk - 1) / chunk;
-    c->lzBlocks = (int)std::max<size_t>(1, std::min<size_t>(nSys == 1 ? 4 * 148 : 148, need));
+    size_t cap = nSys == 1 ? 4 * 148 : std::max<size_t>(2, 4096 / (size_t)nSys);
+    c->lzBlocks = (int)std::max<size_t>(1, std::min(cap, need));
   }
   c->partialCap = std::max({lanczos_partial_need(c), gram_partial_need(c, c->nOS), zgemm_partial_need(c),
                             (size_t)148});

@@ -281,7 +281,6 @@ __global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t
   __shared__ z_t rph[JB_MAX / 2];
   __shared__ int rp[JB_MAX / 2], rq[JB_MAX / 2];
   __shared__ double offs, diags;
-  __shared__ z_t red[JB_MAX];
   int tid = threadIdx.x;
   for (int e = tid; e < n * n; e += blockDim.x) {
     int i = e % n, j = e / n;
@@ -293,32 +292,27 @@ __global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t
   }
   __syncthreads();
   for (int e = tid; e < n; e += blockDim.x) A[e][e].y = 0.0;
-  // modified Gram-Schmidt on the columns of U
-  for (int j = 0; j < n; j++) {
-    for (int i = 0; i < j; i++) {
-      if (tid < 32) {
-        z_t s = zmk(0.0, 0.0);
-        for (int r = tid; r < n; r += 32) s = zadd(s, zcmul(U[r][i], U[r][j]));
-        for (int o = 16; o > 0; o >>= 1) {
-          s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
-          s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
-        }
-        if (tid == 0) red[0] = s;
-      }
-      __syncthreads();
-      z_t ov = red[0];
-      if (tid < n) U[tid][j] = zsub(U[tid][j], zmul(U[tid][i], ov));
-      __syncthreads();
-    }
-    if (tid < 32) {
-      double s = 0.0;
-      for (int r = tid; r < n; r += 32) s += U[r][j].x * U[r][j].x + U[r][j].y * U[r][j].y;
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (tid == 0) red[0] = zmk(s, 0.0);
+  // re-orthonormalise U (unitary to rounding) by one Newton-Schulz polar
+  // step, U <- U (3 I - U^H U) / 2: the deviation from orthonormality squares
+  {
+    for (int e = tid; e < n * n; e += blockDim.x) {
+      int i = e % n, j = e / n;
+      z_t g = zmk(0.0, 0.0);
+      for (int k = 0; k < n; k++) zcfma(g, U[k][i], U[k][j]);
+      V[i][j] = zmk((i == j ? 1.5 : 0.0) - 0.5 * g.x, -0.5 * g.y);
     }
     __syncthreads();
-    double inv = 1.0 / sqrt(red[0].x);
-    if (tid < n) U[tid][j] = zscale(U[tid][j], inv);
+    z_t un[(JB_MAX * JB_MAX + 511) / 512];
+    int q = 0;
+    for (int e = tid; e < n * n; e += blockDim.x, q++) {
+      int i = e % n, j = e / n;
+      z_t s = zmk(0.0, 0.0);
+      for (int k = 0; k < n; k++) zfma(s, U[i][k], V[k][j]);
+      un[q] = s;
+    }
+    __syncthreads();
+    q = 0;
+    for (int e = tid; e < n * n; e += blockDim.x, q++) U[e % n][e / n] = un[q];
     __syncthreads();
   }
   // A <- U^H A U  (V as temporary), then V <- I
@@ -448,15 +442,39 @@ __global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t
   }
 }
 
-// R'[(l2*n+k2)][(k1*n+j)] = sum_k r2s(k1,k2,k,l2) Mreg(k,j), masked by body types.
-// r2s is the spin-summed spatial rdm2 built on the fly from rdm2 (nO^4).
-__global__ void k_build_R(z_t* __restrict__ Rp, const z_t* __restrict__ rdm2, const z_t* __restrict__ Mreg,
+// r2s[(l2*n+k2)][(k1*n+k)] = rdm2(k1,k2,k,l2) summed over the spin blocks
+// (restricted), or the spatial block masked by body types (unrestricted).
+__global__ void k_build_r2s(z_t* __restrict__ r2s, const z_t* __restrict__ rdm2, const int* __restrict__ btOf,
+                            TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int n = T.nOS, restricted = T.restricted;
+  size_t Q = (size_t)n * n;
+  r2s = bat(r2s, bs);
+  rdm2 = bat(rdm2, bs);
+  btOf = bat(btOf, bs);
+  const size_t N = T.nO;
+  auto R2 = [&](int a, int b, int c, int d) { return rdm2[a + N * (b + N * (c + N * (size_t)d))]; };
+  GRID_STRIDE(e, Q * Q) {
+    int row = (int)(e / Q), col = (int)(e % Q);
+    int l2 = row / n, k2 = row % n, k1 = col / n, k = col % n;
+    z_t r = zmk(0.0, 0.0);
+    if (restricted)
+      r = zadd(zadd(zadd(R2(k1, k2, k, l2), R2(n + k1, k2, n + k, l2)), R2(k1, n + k2, k, n + l2)),
+               R2(n + k1, n + k2, n + k, n + l2));
+    else if (btOf[l2] == btOf[k2] && btOf[k1] == btOf[k])
+      r = R2(k1, k2, k, l2);
+    r2s[e] = r;
+  }
+}
+
+// R'[(l2*n+k2)][(k1*n+j)] = sum_k r2s[(l2,k2)][(k1,k)] Mreg(k,j), masked by body types.
+__global__ void k_build_R(z_t* __restrict__ Rp, const z_t* __restrict__ r2s, const z_t* __restrict__ Mreg,
                           const int* __restrict__ btOf, TRAJ_ARGS) {
   const TrajShape& T = shp[blockIdx.z];
   const int n = T.nOS, restricted = T.restricted;
   size_t Q = (size_t)n * n;
   Rp = bat(Rp, bs);
-  rdm2 = bat(rdm2, bs);
+  r2s = bat(r2s, bs);
   Mreg = bat(Mreg, bs);
   btOf = bat(btOf, bs);
   GRID_STRIDE(e, Q * Q) {
@@ -465,15 +483,8 @@ __global__ void k_build_R(z_t* __restrict__ Rp, const z_t* __restrict__ rdm2, co
     z_t v = zmk(0.0, 0.0);
     bool ok = restricted || (btOf[l2] == btOf[k2] && btOf[k1] == btOf[j]);
     if (ok) {
-      size_t N = T.nO;
-      auto R2 = [&](int a, int b, int c, int d) { return rdm2[a + N * (b + N * (c + N * (size_t)d))]; };
-      for (int k = 0; k < n; k++) {
-        z_t r = R2(k1, k2, k, l2);
-        if (restricted)
-          r = zadd(zadd(zadd(r, R2(n + k1, k2, n + k, l2)), R2(k1, n + k2, k, n + l2)),
-                   R2(n + k1, n + k2, n + k, n + l2));
-        zfma(v, r, Mreg[k + (size_t)n * j]);
-      }
+      const z_t* rr = r2s + (size_t)row * Q + (size_t)k1 * n;
+      for (int k = 0; k < n; k++) zfma(v, rr[k], Mreg[k + (size_t)n * j]);
     }
     Rp[e] = v;
   }
@@ -567,7 +578,9 @@ void launch_rdm_inverse(cgpu_ctx* c) {
   k_rdm_inverse<<<bgrid(c, 1), 512, jsmem, c->stream>>>(c->Mreg_d, c->r1s_d, c->rdm1_d, c->Uprev_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
   size_t Q = (size_t)n * n;
-  k_build_R<<<bgrid(c, ew_blocks(c, Q * Q)), 256, 0, c->stream>>>(c->Rp_d, c->rdm2_d, c->Mreg_d, c->btOfOrb_d,
+  k_build_r2s<<<bgrid(c, ew_blocks(c, Q * Q)), 256, 0, c->stream>>>(c->r2s_d, c->rdm2_d, c->btOfOrb_d, TRAJ_PASS(c));
+  CODY_LAUNCHED(c);
+  k_build_R<<<bgrid(c, ew_blocks(c, Q * Q)), 256, 0, c->stream>>>(c->Rp_d, c->r2s_d, c->Mreg_d, c->btOfOrb_d,
                                                                     TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }

@@ -284,7 +284,9 @@ size_t mixed_layout(cgpu_ctx* c, char* base, size_t off) {
   int nG = c->nG, nP = c->nPairs, Q = c->nOS * c->nOS, T = m->terms;
   m->KgMax = (nG + 63) / 64 * 64;
   m->KpMax = (2 * nP + 63) / 64 * 64;
-  m->bn1 = tc_tile_n(2 * nP);
+  // W = V S: in a batch one N tile of 256 covers all pairs (2P <= 156 for 12
+  // orbitals), so the large V operand streams once per trajectory
+  m->bn1 = (c->nb > 1 && 2 * nP <= 256) ? 256 : tc_tile_n(2 * nP);
   m->bn2 = tc_tile_n(2 * Q);
   m->bn3 = tc_tile_n(2 * nP);
   m->s1 = tc_split_count(nG, 2 * nP, m->bn1, T * m->KgMax / 64, c->nb);
