@@ -332,6 +332,15 @@ void batch_copy(cgpu_ctx* c, void* dst, const void* src, size_t bytes);
 // Launchers (defined in the k_*.cu translation units).  Pointers name the
 // buffers of trajectory 0; every launch covers all trajectories.
 // ---------------------------------------------------------------------------
+// Per-trajectory scalar slots in scal_d (64 doubles): MGS status (int), energy,
+// norm, dipole, laser field, natural occupations (up to 32).
+#define CODY_SCAL_STATUS 0
+#define CODY_SCAL_ENERGY 8
+#define CODY_SCAL_NORM 9
+#define CODY_SCAL_DIPOLE 10
+#define CODY_SCAL_FIELD 16
+#define CODY_SCAL_OCC 24
+
 // k_onebody.cu
 void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha, int accumulate);
 void launch_project_orbs(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs);
@@ -341,7 +350,8 @@ void launch_axpby(cgpu_ctx* c, z_t* y, const z_t* x, z_t a, z_t b, int sel);  //
 void launch_rk_stage(cgpu_ctx* c, z_t* inc, z_t* tmp, const z_t* state, const z_t* d, double wInc, double wTmp,
                      int first);
 void launch_scale(cgpu_ctx* c, z_t* y, z_t a, int sel);
-void launch_orthonormalize(cgpu_ctx* c, z_t* orbs, int col0, int nCols);
+void launch_orthonormalize(cgpu_ctx* c, z_t* orbs, int col0, int nCols, int resetStatus = 1);
+void launch_norm_dipole(cgpu_ctx* c, const z_t* state);  // after the RDMs of state: norm and <x> slots
 void launch_normalize_coeffs(cgpu_ctx* c, z_t* C);
 void launch_energy(cgpu_ctx* c, double* out_d);
 void launch_set_scalar(cgpu_ctx* c, double* p, double v);

@@ -727,13 +727,13 @@ void energy_launch(cgpu_ctx* c, const z_t* state, double t) {
   launch_onebody(c, c->orbTmp_d, orbs, t, zmk(1.0, 0.0), 0);
   launch_fill_h1_from(c, orbs, c->orbTmp_d, c->h1_d);
   launch_fill_h2(c, orbs);
-  launch_energy(c, c->scal_d + 8);
+  launch_energy(c, c->scal_d + CODY_SCAL_ENERGY);
 }
 
 double energy_device(cgpu_ctx* c, const z_t* state, double t) {
   energy_launch(c, state, t);
   double e = 0.0;
-  CODY_CUDA(cudaMemcpyAsync(&e, c->scal_d + 8, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CODY_CUDA(cudaMemcpyAsync(&e, c->scal_d + CODY_SCAL_ENERGY, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CODY_CUDA(cudaStreamSynchronize(c->stream));
   return e;
 }
@@ -810,6 +810,41 @@ cgpu_ctx* create_ctx(const cgpu_desc* descs, int n, int* rc) {
   }
   *rc = CGPU_OK;
   return c;
+}
+
+// Observables of every trajectory (RDM observables, src/Utils/M_Utils_RdmObservables.f90:17-52,
+// and the printers' quantities, src/Utils/M_Utils_PrinterObservableLinear.f90:25-103):
+// out[b*stride + 0..2] = energy, ||C||, <x>; then the natural occupations in
+// descending order (zeros past the trajectory's orbital count).  stride = 3 + nOS(max).
+void observables(cgpu_ctx* c, const double* tHost, double* out) {
+  const int stride = 3 + c->nOS;
+  set_step_times(c, tHost);
+  c->useStepTime = 1;
+  try {
+    energy_launch(c, c->state_d, 0.0);
+  } catch (...) {
+    c->useStepTime = 0;
+    throw;
+  }
+  c->useStepTime = 0;
+  const bool occ = c->method != CGPU_METHOD_TDCI && c->nOS <= 32;
+  if (occ) launch_rdm_inverse(c);
+  launch_norm_dipole(c, c->state_d);
+  std::vector<double> rows((size_t)c->nb * 64);
+  CODY_CUDA(cudaMemcpy2DAsync(rows.data(), 64 * sizeof(double), c->scal_d, c->bs, 64 * sizeof(double), c->nb,
+                              cudaMemcpyDeviceToHost, c->stream));
+  sync(c);
+  for (int b = 0; b < c->nb; b++) {
+    const double* r = rows.data() + (size_t)b * 64;
+    double* o = out + (size_t)b * stride;
+    o[0] = r[CODY_SCAL_ENERGY];
+    o[1] = r[CODY_SCAL_NORM];
+    o[2] = r[CODY_SCAL_DIPOLE];
+    int n = c->sys[b].nOS;
+    std::vector<double> ev(occ ? r + CODY_SCAL_OCC : r, occ ? r + CODY_SCAL_OCC + n : r);
+    std::sort(ev.begin(), ev.end(), [](double a, double bb) { return a > bb; });
+    for (int k = 0; k < c->nOS; k++) o[3 + k] = k < (int)ev.size() ? ev[k] : 0.0;
+  }
 }
 
 }  // namespace
@@ -1204,6 +1239,54 @@ int cgpu_tdci_set_orbitals(cgpu_ctx* c, const cgpu_complex* orbs) {
   CODY_API_END(c)
 }
 
+int cgpu_observables(cgpu_ctx* c, double time, double* out) {
+  CODY_API_BEGIN(c)
+  if (!out) throw std::string("observables: null output");
+  std::vector<double> t(c->nb, time);
+  observables(c, t.data(), out);
+  CODY_API_END(c)
+}
+
+// Imaginary-time relaxation (T_He1d_04_ImagTimePropagationMctdhx.f90:82-99 with
+// M_Utils_Actions.f90:66-78): n_inner Euler steps on the imaginary-time
+// derivative, each followed by Coeffs_Normalize and Orbs_Orthonormalize (MGS
+// twice), then GetEnergy; stop when |dE| <= conv_thresh or after max_outer rounds.
+int cgpu_relax(cgpu_ctx* c, cgpu_complex* state, double dt, int n_inner, double conv_thresh, int max_outer,
+               double* energy, int* n_outer) {
+  CODY_API_BEGIN(c)
+  if (c->nb != 1) throw std::string("relax: a single system (use the context of one trajectory)");
+  if (c->method == CGPU_METHOD_TDCI) throw std::string("relax: MCTDHX contexts only");
+  if (!state || n_inner <= 0) throw std::string("relax: bad argument");
+  const SysHost& s = c->sys[0];
+  up_state(c, 0, c->state_d, state);
+  z_t* orbs = c->state_d + c->nC;
+  double eNew = 0.0, eOld = 0.0, conv = 1.0, time = 0.0;
+  int outer = 0;
+  while (std::fabs(conv) > conv_thresh && outer < max_outer) {
+    outer++;
+    batch_zero(c, c->scal_d, sizeof(int));
+    for (int k = 0; k < n_inner; k++) {
+      euler_device(c, CGPU_TD_FULL, 1, c->state_d, time, time + dt);
+      time = time + dt;
+      launch_normalize_coeffs(c, c->state_d);
+      if (c->restricted) launch_orthonormalize(c, orbs, 0, c->nOS, 0);
+      else
+        for (int b = 0; b < c->nBt; b++) launch_orthonormalize(c, orbs, s.orbStart[b], s.nOrbs[b], 0);
+    }
+    int status = 0;
+    CODY_CUDA(cudaMemcpyAsync(&status, c->scal_d, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    eOld = eNew;
+    eNew = energy_device(c, c->state_d, time);
+    if (status) throw std::string("relax: Orthonormalize met a vector with non-positive norm");
+    conv = eNew - eOld;
+  }
+  down_state(c, 0, state, c->state_d);
+  sync(c);
+  if (energy) *energy = eNew;
+  if (n_outer) *n_outer = outer;
+  CODY_API_END(c)
+}
+
 int cgpu_tdci_adjoint(cgpu_ctx* c, const cgpu_complex* c0, const double* field, int n_steps, double dt,
                       int checkpoint, double* objective, double* overlap, cgpu_complex* c_final, double* d_objective) {
   CODY_API_BEGIN(c)
@@ -1350,9 +1433,16 @@ int cgpu_batch_energies(cgpu_batch* b, const double* t, double* energies) {
     throw;
   }
   c->useStepTime = 0;
-  CODY_CUDA(cudaMemcpy2DAsync(energies, sizeof(double), c->scal_d + 8, c->bs, sizeof(double), c->nb,
+  CODY_CUDA(cudaMemcpy2DAsync(energies, sizeof(double), c->scal_d + CODY_SCAL_ENERGY, c->bs, sizeof(double), c->nb,
                               cudaMemcpyDeviceToHost, c->stream));
   sync(c);
+  CODY_BATCH_END
+}
+
+int cgpu_batch_observables(cgpu_batch* b, const double* t, double* out) {
+  CODY_BATCH_BEGIN(b)
+  if (!t || !out) throw std::string("batch_observables: null array");
+  observables(c_, t, out);
   CODY_BATCH_END
 }
 

@@ -265,7 +265,7 @@ constexpr int JB_MAX = 32;
 // The result Mreg = U f(n) U^H depends only on rho (to rounding).
 __global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t* __restrict__ r1s,
                                                      const z_t* __restrict__ rdm1, z_t* __restrict__ Uprev,
-                                                     TRAJ_ARGS) {
+                                                     double* __restrict__ occ, TRAJ_ARGS) {
   extern __shared__ z_t jsm[];
   const TrajShape& T = shp[blockIdx.z];
   const int nO = T.nO, n = T.nOS, restricted = T.restricted;
@@ -419,7 +419,11 @@ __global__ void __launch_bounds__(512) k_rdm_inverse(z_t* __restrict__ Mreg, z_t
     }
   }
   // eigenvalues, eigenvectors U_new = U V (into A), stored for the next call
-  for (int e = tid; e < n; e += blockDim.x) ev[e] = A[e][e].x;
+  occ = bat(occ, bs);
+  for (int e = tid; e < n; e += blockDim.x) {
+    ev[e] = A[e][e].x;
+    occ[e] = ev[e];  // natural occupations (eigenvalues of the spin-summed rho1, unsorted)
+  }
   __syncthreads();
   for (int e = tid; e < n * n; e += blockDim.x) {
     int i = e % n, j = e / n;
@@ -575,7 +579,8 @@ void launch_rdm_inverse(cgpu_ctx* c) {
     CODY_CUDA(cudaFuncSetAttribute(k_rdm_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jsmem));
     attr = true;
   }
-  k_rdm_inverse<<<bgrid(c, 1), 512, jsmem, c->stream>>>(c->Mreg_d, c->r1s_d, c->rdm1_d, c->Uprev_d, TRAJ_PASS(c));
+  k_rdm_inverse<<<bgrid(c, 1), 512, jsmem, c->stream>>>(c->Mreg_d, c->r1s_d, c->rdm1_d, c->Uprev_d,
+                                                        c->scal_d + CODY_SCAL_OCC, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
   size_t Q = (size_t)n * n;
   k_build_r2s<<<bgrid(c, ew_blocks(c, Q * Q)), 256, 0, c->stream>>>(c->r2s_d, c->rdm2_d, c->btOfOrb_d, TRAJ_PASS(c));

@@ -437,6 +437,40 @@ __global__ void k_energy(double* out, const z_t* __restrict__ h1, const z_t* __r
   if (threadIdx.x == 0) *out = s.x;
 }
 
+// out[:, i] = x * orbs[:, i] (dipole operator on the orbitals)
+__global__ void k_x_apply(z_t* __restrict__ out, const z_t* __restrict__ orbs, const double* __restrict__ x,
+                          TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  out = bat(out, bs);
+  orbs = bat(orbs, bs);
+  x = bat(x, bs);
+  GRID_STRIDE(e, (size_t)S.nG * S.nOS) out[e] = zscale(orbs[e], x[e % S.nG]);
+}
+
+// scal[NORM] = ||C||, scal[DIPOLE] = Re sum_kl xm(k,l) rho1(l,k) (xm: the dipole
+// matrix in the spin-orbital layout of h1)
+__global__ void k_norm_dipole(double* __restrict__ scal, const z_t* __restrict__ C, const z_t* __restrict__ xm,
+                              const z_t* __restrict__ r1, TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  scal = bat(scal, bs);
+  C = bat(C, bs);
+  xm = bat(xm, bs);
+  r1 = bat(r1, bs);
+  z_t s = zmk(0.0, 0.0);
+  for (int i = threadIdx.x; i < S.nC; i += blockDim.x) s.x += C[i].x * C[i].x + C[i].y * C[i].y;
+  const size_t nO = S.nO;
+  for (size_t e = threadIdx.x; e < nO * nO; e += blockDim.x) {
+    size_t k = e % nO, l = e / nO;
+    z_t p = zmul(xm[k + nO * l], r1[l + nO * k]);
+    s.y += p.x;
+  }
+  s = block_sum(s);
+  if (threadIdx.x == 0) {
+    scal[CODY_SCAL_NORM] = sqrt(s.x);
+    scal[CODY_SCAL_DIPOLE] = s.y;
+  }
+}
+
 __global__ void k_set_scalar(double* p, double v, size_t bs) { *bat(p, bs) = v; }
 __global__ void k_add_scalar(double* p, double v, size_t bs) { *bat(p, bs) += v; }
 
@@ -498,7 +532,7 @@ void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha,
   size_t sh = sizeof(z_t) * (OB_THREADS + 2 * c->band);
   const double* base = (c->inCapture || c->useStepTime) ? c->stepT_d : c->zero_d;
   double off = c->inCapture ? t - c->captureT0 : t;
-  double* E = c->scal_d + 16;
+  double* E = c->scal_d + CODY_SCAL_FIELD;
   k_field<<<bgrid(c, 1), 1, 0, c->stream>>>(E, TRAJ_PASS(c), base, off);
   CODY_LAUNCHED(c);
   k_onebody<<<grid, OB_THREADS, sh, c->stream>>>(out, orbs, c->T_d, c->V0_d, c->x_d, c->btOfOrb_d, TRAJ_PASS(c), E,
@@ -570,9 +604,19 @@ void launch_rk_stage(cgpu_ctx* c, z_t* inc, z_t* tmp, const z_t* state, const z_
   CODY_LAUNCHED(c);
 }
 
-void launch_orthonormalize(cgpu_ctx* c, z_t* orbs, int col0, int nCols) {
-  batch_zero(c, c->scal_d, sizeof(int));
+void launch_orthonormalize(cgpu_ctx* c, z_t* orbs, int col0, int nCols, int resetStatus) {
+  if (resetStatus) batch_zero(c, c->scal_d, sizeof(int));
   k_mgs2<<<bgrid(c, 1), 1024, 0, c->stream>>>(orbs, c->w_d, TRAJ_PASS(c), col0, nCols, (int*)c->scal_d);
+  CODY_LAUNCHED(c);
+}
+
+void launch_norm_dipole(cgpu_ctx* c, const z_t* state) {
+  const z_t* orbs = (c->method == CGPU_METHOD_TDCI) ? c->tdciOrbs_d : state + c->nC;
+  k_x_apply<<<bgrid(c, ew_blocks(c, (size_t)c->nG * c->nOS)), 256, 0, c->stream>>>(c->orbTmp_d, orbs, c->x_d,
+                                                                                    TRAJ_PASS(c));
+  CODY_LAUNCHED(c);
+  launch_fill_h1_from(c, orbs, c->orbTmp_d, c->h1_d);  // h1 <- dipole matrix
+  k_norm_dipole<<<bgrid(c, 1), 256, 0, c->stream>>>(c->scal_d, state, c->h1_d, c->rdm1_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 

@@ -35,7 +35,7 @@ EXPORTED = [
     "cgpu_batch_create", "cgpu_batch_destroy", "cgpu_batch_size", "cgpu_batch_sizes", "cgpu_batch_grid",
     "cgpu_batch_upload", "cgpu_batch_download", "cgpu_batch_propagate", "cgpu_batch_energies",
     "cgpu_batch_kernels_per_step", "cgpu_batch_launch_count", "cgpu_batch_profile_begin", "cgpu_batch_profile_end",
-    "cgpu_tdci_adjoint",
+    "cgpu_tdci_adjoint", "cgpu_observables", "cgpu_relax", "cgpu_batch_observables",
 ]
 
 KERNELS = {"pair_potentials": 1, "correlation": 2, "h2": 3, "ci_apply": 4, "ci_rdm": 5, "onebody": 6, "lanczos": 7,
@@ -359,6 +359,20 @@ class Engine:
     def synchronize(self):
         self._check(self.lib.cgpu_synchronize(self.h))
 
+    def observables(self, t):
+        """Resident state at time t: dict(energy, norm, dipole, occupations)."""
+        out = np.zeros(3 + self.nOS)
+        self._check(self.lib.cgpu_observables(self.h, _d(t), _p(out)))
+        return dict(energy=out[0], norm=out[1], dipole=out[2], occupations=out[3:].copy())
+
+    def relax(self, state, dt, n_inner, conv_thresh, max_outer=100000):
+        """Imaginary-time relaxation on the GPU; returns (energy, state, rounds)."""
+        s = np.array(state, dtype=np.complex128)
+        e, n = C.c_double(), C.c_int()
+        self._check(self.lib.cgpu_relax(self.h, _p(s), _d(dt), int(n_inner), _d(conv_thresh), int(max_outer),
+                                        C.byref(e), C.byref(n)))
+        return e.value, s, n.value
+
     # TDCI ---------------------------------------------------------------------
     def tdci_set_orbitals(self, orbs):
         o = self._orbs(orbs)
@@ -461,6 +475,14 @@ class Batch:
         self._check(self.lib.cgpu_batch_propagate(self.h, _p(t), _d(dt), int(n_steps), int(krylov_dim),
                                                   int(use_metric), C.byref(ms)))
         return ms.value
+
+    def observables(self, t):
+        """(energy, norm, dipole, occupations[nOSmax]) arrays over the systems at times t."""
+        tt = np.ascontiguousarray(np.broadcast_to(np.asarray(t, dtype=np.float64), (len(self),)))
+        nmax = max(s.nOS for s in self.systems)
+        out = np.zeros((len(self), 3 + nmax))
+        self._check(self.lib.cgpu_batch_observables(self.h, _p(tt), _p(out)))
+        return out[:, 0], out[:, 1], out[:, 2], out[:, 3:]
 
     def energies(self, t):
         tt = np.ascontiguousarray(np.broadcast_to(np.asarray(t, dtype=np.float64), (len(self),)))

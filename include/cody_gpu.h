@@ -212,6 +212,21 @@ int cgpu_profile_end(cgpu_ctx* ctx, long* launches, double* total_ms);
  * fix the orbitals and fill h1/h2 once. */
 int cgpu_tdci_set_orbitals(cgpu_ctx* ctx, const cgpu_complex* orbs);
 
+/* ---- observables and relaxation ------------------------------------------ */
+/* Observables of the resident state at `time` (GetEnergy and the RDM
+ * observables the printers use, src/Utils/M_Utils_RdmObservables.f90:17-52,
+ * src/Utils/M_Utils_PrinterObservableLinear.f90:25-103):
+ * out[0] = energy, out[1] = ||C||, out[2] = <x> (dipole, sum rho1 x), then the
+ * nOS natural occupations (eigenvalues of the spin-summed rho1, descending;
+ * zero for TDCI contexts).  out has 3 + nOS entries. */
+int cgpu_observables(cgpu_ctx* ctx, double time, double* out);
+/* Imaginary-time relaxation of a host state (T_He1d_04_ImagTimePropagationMctdhx.f90:82-99):
+ * n_inner Euler steps, each followed by Coeffs_Normalize and Orbs_Orthonormalize,
+ * then GetEnergy; repeated until |dE| <= conv_thresh or max_outer rounds.
+ * Replaces state; returns the final energy and the number of rounds. */
+int cgpu_relax(cgpu_ctx* ctx, cgpu_complex* state, double dt, int n_inner, double conv_thresh, int max_outer,
+               double* energy, int* n_outer);
+
 /* ---- pulse gradient (adjoint) ------------------------------------------- */
 /* No counterpart in the reference.  For a TDCI context (orbitals set with
  * cgpu_tdci_set_orbitals, at most 64 configurations): propagates c0 over
@@ -250,6 +265,9 @@ int cgpu_batch_propagate(cgpu_batch* batch, const double* t0, double dt, int n_s
                          int use_metric, double* elapsed_ms);
 /* energies[i] = GetEnergy of system i at time t[i] */
 int cgpu_batch_energies(cgpu_batch* batch, const double* t, double* energies);
+/* cgpu_observables of every system at t[i]: out[i * (3 + nOSmax) + ...],
+ * nOSmax the largest orbital count of the batch (cgpu_batch_sizes). */
+int cgpu_batch_observables(cgpu_batch* batch, const double* t, double* out);
 /* Kernels launched per step (all systems); launches so far (reset if nonzero). */
 long cgpu_batch_kernels_per_step(const cgpu_batch* batch);
 /* As cgpu_profile_begin / cgpu_profile_end, for the launches of a batch step. */

@@ -1,0 +1,85 @@
+"""On-device observables (cgpu_observables / cgpu_batch_observables) and the
+GPU imaginary-time relaxation (cgpu_relax), against the CPU oracle."""
+import numpy as np
+import pytest
+
+from oracle import Oracle
+from codyfortran_gb300 import init as I
+from codyfortran_gb300 import spec as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _helium():
+    sp = S.helium_fedvr(20, 6, 4, laser=S.sin2_pulse(0.0534, omega=0.2, n_cycles=2.0, cep=0.3))
+    sp.xmin, sp.xmax = -20.0, 20.0
+    return sp
+
+
+def _state(sp, x, w, seed, nC):
+    rng = np.random.default_rng(seed)
+    orbs = I.seeded_gaussian_orbitals(sp, x, w, seed)
+    c = rng.normal(size=nC) + 1j * rng.normal(size=nC)
+    return I.pack_state(c / np.linalg.norm(c), orbs), orbs, c / np.linalg.norm(c)
+
+
+def test_observables_match_oracle():
+    from codyfortran_gb300.engine import Engine
+    sp = _helium()
+    o, e = Oracle(sp), Engine(sp)
+    st, orbs, c = _state(sp, o.x, o.w, 3, o.nC)
+    t = 7.3
+    e.upload(st)
+    obs = e.observables(t)
+    assert abs(obs["energy"] - o.energy(st, t)) <= 1e-12 * abs(o.energy(st, t))
+    assert abs(obs["norm"] - np.linalg.norm(c)) < 1e-13
+    r1 = o.rdm1(c)
+    n = e.nOS
+    xs = (orbs.conj() * (o.x * o.w)[:, None]).T @ orbs          # spatial <phi_i| x |phi_j>_w
+    X = np.zeros((2 * n, 2 * n), dtype=complex)
+    X[:n, :n] = xs
+    X[n:, n:] = xs
+    dip = np.real(np.sum(X * r1.T))
+    assert abs(obs["dipole"] - dip) <= 1e-12 * max(1.0, abs(dip))
+    occ = np.sort(np.linalg.eigvalsh(r1[:n, :n] + r1[n:, n:]))[::-1]
+    assert np.max(np.abs(obs["occupations"] - occ)) < 1e-12
+    assert abs(np.sum(occ) - 2.0) < 1e-12                       # two electrons
+    e.close()
+
+
+def test_batch_observables_match_single_systems():
+    from codyfortran_gb300.engine import Batch, Engine
+    specs = S.batch_trajectory_specs(512, 1234)[:3] + [_helium()]
+    b = Batch(specs, "fp64")
+    states = [_state(sp, s.x, s.w, 11 + k, s.nC)[0] for k, (sp, s) in enumerate(zip(specs, b.systems))]
+    b.upload(states)
+    t = np.array([0.0, 12.5, 3.0, 7.3])
+    E, N, D, O = b.observables(t)
+    for k, sp in enumerate(specs):
+        e = Engine(sp)
+        e.upload(states[k])
+        ob = e.observables(t[k])
+        e.close()
+        assert abs(E[k] - ob["energy"]) <= 1e-12 * abs(ob["energy"])
+        assert abs(N[k] - ob["norm"]) < 1e-13
+        assert abs(D[k] - ob["dipole"]) <= 1e-12 * max(1.0, abs(ob["dipole"]))
+        n = len(ob["occupations"])
+        assert np.max(np.abs(O[k, :n] - ob["occupations"])) < 1e-12
+        assert np.all(O[k, n:] == 0.0)
+    b.close()
+
+
+def test_relax_matches_oracle_and_golden(golden):
+    """He1d_04 (unrestricted MCTDHF, 21-point grid): relaxation entirely on the GPU."""
+    from codyfortran_gb300.engine import Engine
+    sp = S.he1d_findiff((4, 4), False)
+    o, e = Oracle(sp), Engine(sp)
+    orbs = I.orthonormalize_state_orbitals(sp, I.harmonic_orbitals(sp, e.x), e.w)
+    st = I.pack_state(I.unary_coeffs(sp), orbs)
+    eg, sg, ng = e.relax(st, 0.01, 10, 1e-12, 1000)
+    eo, so, no = o.relax(st, 0.01, 10, 1e-12, 1000)
+    assert ng == no
+    assert abs(eg - eo) < 1e-11
+    g04 = golden["he1d_04_mctdhf_imag"]["checks"][0]["golden"]
+    assert abs(eg - g04) < 1e-8
+    e.close()
