@@ -8,6 +8,7 @@
 // system.  The orchestration below is written once for all trajectories.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 
@@ -1284,6 +1285,92 @@ int cgpu_relax(cgpu_ctx* c, cgpu_complex* state, double dt, int n_inner, double 
   sync(c);
   if (energy) *energy = eNew;
   if (n_outer) *n_outer = outer;
+  CODY_API_END(c)
+}
+
+// Restart files in the reference's raw format (src/Utils/M_Utils_DataStorage.f90:20-106:
+// unformatted stream of the complex(R64) array): coeffs.in (S_Coeffs.f90:167-175),
+// orbBB_II.in per stored orbital (S_Orbs.f90:251-276; restricted runs store
+// body type 1 only) and, when asked, rdm2BtXX_YY.in body-type blocks of rho2
+// (S_Coeffs.f90:177-214).  `dir` is a directory prefix ("" = current).
+int cgpu_save_restart(cgpu_ctx* c, const char* dir, int with_rdm2) {
+  CODY_API_BEGIN(c)
+  if (c->nb != 1) throw std::string("save_restart: a single system");
+  const SysHost& s = c->sys[0];
+  std::string pre = dir ? std::string(dir) : std::string();
+  if (!pre.empty() && pre.back() != '/') pre += '/';
+  std::vector<cgpu_complex> st(s.nS);
+  down_state(c, 0, st.data(), c->state_d);
+  sync(c);
+  auto write = [&](const std::string& name, const void* p, size_t bytes) {
+    FILE* f = std::fopen((pre + name).c_str(), "wb");
+    if (!f) throw std::string("save_restart: cannot open ") + pre + name;
+    size_t w = std::fwrite(p, 1, bytes, f);
+    std::fclose(f);
+    if (w != bytes) throw std::string("save_restart: short write to ") + pre + name;
+  };
+  write("coeffs.in", st.data(), sizeof(cgpu_complex) * s.nC);
+  if (c->method != CGPU_METHOD_TDCI) {
+    int nBt = c->restricted ? 1 : c->nBt, i1 = 0;
+    for (int bt = 0; bt < nBt; bt++)
+      for (int k = 0; k < s.nOrbs[bt]; k++, i1++) {
+        char name[32];
+        std::snprintf(name, sizeof(name), "orb%02d_%02d.in", bt + 1, k + 1);
+        write(name, st.data() + s.nC + (size_t)i1 * s.nG, sizeof(cgpu_complex) * s.nG);
+      }
+  }
+  if (with_rdm2) {
+    launch_ci_rdm(c, c->state_d, 0, 1);
+    const size_t nO = s.nO;
+    std::vector<cgpu_complex> r2(nO * nO * nO * nO);
+    down(c, r2.data(), c->rdm2_d, r2.size());
+    sync(c);
+    for (int b1 = 0; b1 < c->nBt; b1++)
+      for (int b2 = 0; b2 < c->nBt; b2++) {
+        const int s1 = s.orbStart[b1], n1 = s.nOrbs[b1], s2 = s.orbStart[b2], n2 = s.nOrbs[b2];
+        std::vector<cgpu_complex> blk((size_t)n1 * n2 * n1 * n2);
+        size_t q = 0;
+        for (int l = 0; l < n2; l++)
+          for (int k = 0; k < n1; k++)
+            for (int j = 0; j < n2; j++)
+              for (int i = 0; i < n1; i++, q++)
+                blk[q] = r2[(s1 + i) + nO * ((s2 + j) + nO * ((s1 + k) + nO * (size_t)(s2 + l)))];
+        char name[32];
+        std::snprintf(name, sizeof(name), "rdm2Bt%02d_%02d.in", b1 + 1, b2 + 1);
+        write(name, blk.data(), sizeof(cgpu_complex) * blk.size());
+      }
+  }
+  CODY_API_END(c)
+}
+
+// Loads coeffs.in and the orbital files written by cgpu_save_restart (or by the
+// reference) into the resident state (CoeffsInit / OrbsInit with "load").
+int cgpu_load_restart(cgpu_ctx* c, const char* dir) {
+  CODY_API_BEGIN(c)
+  if (c->nb != 1) throw std::string("load_restart: a single system");
+  const SysHost& s = c->sys[0];
+  std::string pre = dir ? std::string(dir) : std::string();
+  if (!pre.empty() && pre.back() != '/') pre += '/';
+  std::vector<cgpu_complex> st(s.nS);
+  auto read = [&](const std::string& name, void* p, size_t bytes) {
+    FILE* f = std::fopen((pre + name).c_str(), "rb");
+    if (!f) throw std::string("load_restart: cannot open ") + pre + name;
+    size_t r = std::fread(p, 1, bytes, f);
+    std::fclose(f);
+    if (r != bytes) throw std::string("load_restart: more data requested than stored in ") + pre + name;
+  };
+  read("coeffs.in", st.data(), sizeof(cgpu_complex) * s.nC);
+  if (c->method != CGPU_METHOD_TDCI) {
+    int nBt = c->restricted ? 1 : c->nBt, i1 = 0;
+    for (int bt = 0; bt < nBt; bt++)
+      for (int k = 0; k < s.nOrbs[bt]; k++, i1++) {
+        char name[32];
+        std::snprintf(name, sizeof(name), "orb%02d_%02d.in", bt + 1, k + 1);
+        read(name, st.data() + s.nC + (size_t)i1 * s.nG, sizeof(cgpu_complex) * s.nG);
+      }
+  }
+  up_state(c, 0, c->state_d, st.data());
+  sync(c);
   CODY_API_END(c)
 }
 

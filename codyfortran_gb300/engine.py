@@ -35,7 +35,8 @@ EXPORTED = [
     "cgpu_batch_create", "cgpu_batch_destroy", "cgpu_batch_size", "cgpu_batch_sizes", "cgpu_batch_grid",
     "cgpu_batch_upload", "cgpu_batch_download", "cgpu_batch_propagate", "cgpu_batch_energies",
     "cgpu_batch_kernels_per_step", "cgpu_batch_launch_count", "cgpu_batch_profile_begin", "cgpu_batch_profile_end",
-    "cgpu_tdci_adjoint", "cgpu_observables", "cgpu_relax", "cgpu_batch_observables",
+    "cgpu_tdci_adjoint", "cgpu_observables", "cgpu_relax", "cgpu_batch_observables", "cgpu_save_restart",
+    "cgpu_load_restart",
 ]
 
 KERNELS = {"pair_potentials": 1, "correlation": 2, "h2": 3, "ci_apply": 4, "ci_rdm": 5, "onebody": 6, "lanczos": 7,
@@ -87,6 +88,8 @@ def load_library(path: str = LIB_PATH):
     lib.cgpu_batch_kernels_per_step.argtypes = [C.c_void_p]
     lib.cgpu_batch_launch_count.restype = C.c_long
     lib.cgpu_batch_launch_count.argtypes = [C.c_void_p, C.c_int]
+    lib.cgpu_save_restart.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
+    lib.cgpu_load_restart.argtypes = [C.c_void_p, C.c_char_p]
     _lib = lib
     return lib
 
@@ -364,6 +367,12 @@ class Engine:
         out = np.zeros(3 + self.nOS)
         self._check(self.lib.cgpu_observables(self.h, _d(t), _p(out)))
         return dict(energy=out[0], norm=out[1], dipole=out[2], occupations=out[3:].copy())
+
+    def save_restart(self, directory, with_rdm2=False):
+        self._check(self.lib.cgpu_save_restart(self.h, str(directory).encode(), int(with_rdm2)))
+
+    def load_restart(self, directory):
+        self._check(self.lib.cgpu_load_restart(self.h, str(directory).encode()))
 
     def relax(self, state, dt, n_inner, conv_thresh, max_outer=100000):
         """Imaginary-time relaxation on the GPU; returns (energy, state, rounds)."""

@@ -227,6 +227,13 @@ int cgpu_observables(cgpu_ctx* ctx, double time, double* out);
 int cgpu_relax(cgpu_ctx* ctx, cgpu_complex* state, double dt, int n_inner, double conv_thresh, int max_outer,
                double* energy, int* n_outer);
 
+/* Restart files of the resident state in the reference's raw format
+ * (src/Utils/M_Utils_DataStorage.f90:20-106): coeffs.in, orbBB_II.in per
+ * stored orbital (src/Orbs/S_Orbs.f90:251-276) and, with with_rdm2,
+ * rdm2BtXX_YY.in (src/Coeffs/S_Coeffs.f90:177-214), under the directory `dir`. */
+int cgpu_save_restart(cgpu_ctx* ctx, const char* dir, int with_rdm2);
+int cgpu_load_restart(cgpu_ctx* ctx, const char* dir);
+
 /* ---- pulse gradient (adjoint) ------------------------------------------- */
 /* No counterpart in the reference.  For a TDCI context (orbitals set with
  * cgpu_tdci_set_orbitals, at most 64 configurations): propagates c0 over

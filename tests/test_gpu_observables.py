@@ -1,5 +1,6 @@
-"""On-device observables (cgpu_observables / cgpu_batch_observables) and the
-GPU imaginary-time relaxation (cgpu_relax), against the CPU oracle."""
+"""On-device observables (cgpu_observables / cgpu_batch_observables), the GPU
+imaginary-time relaxation (cgpu_relax) against the CPU oracle, and restart
+files in the reference's raw format (cgpu_save_restart / cgpu_load_restart)."""
 import numpy as np
 import pytest
 
@@ -83,3 +84,28 @@ def test_relax_matches_oracle_and_golden(golden):
     g04 = golden["he1d_04_mctdhf_imag"]["checks"][0]["golden"]
     assert abs(eg - g04) < 1e-8
     e.close()
+
+
+def test_restart_files_round_trip(tmp_path):
+    from codyfortran_gb300.engine import Engine
+    sp = S.he1d_findiff((4, 4), False)             # unrestricted: two body types of orbital files
+    e = Engine(sp)
+    st, orbs, c = _state(sp, e.x, e.w, 5, e.nC)
+    e.upload(st)
+    e.save_restart(tmp_path, with_rdm2=True)
+    coeffs = np.fromfile(tmp_path / "coeffs.in", dtype=np.complex128)
+    assert np.array_equal(coeffs, st[:e.nC])
+    i1 = 0
+    for bt in range(2):
+        for k in range(4):
+            f = np.fromfile(tmp_path / f"orb{bt + 1:02d}_{k + 1:02d}.in", dtype=np.complex128)
+            assert np.array_equal(f, st[e.nC + i1 * e.nG:e.nC + (i1 + 1) * e.nG])
+            i1 += 1
+    r2 = e.rdm2(st[:e.nC])                          # nO^4, Fortran order
+    blk = np.fromfile(tmp_path / "rdm2Bt01_02.in", dtype=np.complex128).reshape((4, 4, 4, 4), order="F")
+    assert np.array_equal(blk, r2[0:4, 4:8, 0:4, 4:8])
+    e2 = Engine(sp)
+    e2.load_restart(tmp_path)
+    assert np.array_equal(e2.download(), st)
+    e.close()
+    e2.close()
