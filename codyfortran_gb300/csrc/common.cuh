@@ -232,6 +232,8 @@ struct cgpu_ctx {
   double *x_d = nullptr, *w_d = nullptr, *V0_d = nullptr, *T_d = nullptr, *Vint_d = nullptr, *metric_d = nullptr;
   double *metricW_d = nullptr, *metricOne_d = nullptr;  // [1 | w per orbital point] and all ones
   double *metricUser_d = nullptr;                      // caller-supplied SIL metric (single system)
+  double *mask_d = nullptr;                            // absorber mask per grid point (1 = none)
+  int absorbEachStep = 0, graphAbsorb = -1;
   int* btOfOrb_d = nullptr;
   int *pairL_d = nullptr, *pairK_d = nullptr, *pidx_d = nullptr;
   // CI
@@ -355,6 +357,8 @@ void launch_norm_dipole(cgpu_ctx* c, const z_t* state);  // after the RDMs of st
 void launch_normalize_coeffs(cgpu_ctx* c, z_t* C);
 void launch_energy(cgpu_ctx* c, double* out_d);
 void launch_set_scalar(cgpu_ctx* c, double* p, double v);
+void launch_absorber_setup(cgpu_ctx* c, double onset, double order);
+void launch_absorber_apply(cgpu_ctx* c, z_t* orbs);
 void launch_add_scalar(cgpu_ctx* c, double* p, double v);
 size_t gram_partial_need(const cgpu_ctx* c, int n);
 // k_ci.cu

@@ -304,6 +304,7 @@ size_t layout(cgpu_ctx* c, char* base) {
   auto I = [&](int*& p, size_t cnt) { size_t o = take(off, sizeof(int) * cnt); if (base) p = (int*)(base + o); };
   auto Z = [&](z_t*& p, size_t cnt) { size_t o = take(off, sizeof(z_t) * cnt); if (base) p = (z_t*)(base + o); };
   D(c->x_d, nG);
+  D(c->mask_d, nG);
   D(c->w_d, nG);
   D(c->V0_d, nG);
   D(c->T_d, (size_t)c->nBtK * nd * nG);
@@ -420,6 +421,7 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
   for (int b = 0; b < nSys; b++) {
     SysHost& s = c->sys[b];
     put(c, b, c->x_d, s.x);
+    put(c, b, c->mask_d, std::vector<double>(s.nG, 1.0));
     put(c, b, c->w_d, s.w);
     put(c, b, c->V0_d, s.V0);
     put(c, b, c->T_d, s.band_h);
@@ -682,6 +684,7 @@ void capture_step_graph(cgpu_ctx* c, double t0, double dt, int krylov, int useMe
   c->captureT0 = t0;
   try {
     split2_device(c, c->state_d, t0, t0 + dt, krylov, 0.0, 0, useMetric);
+    if (c->absorbEachStep && c->method != CGPU_METHOD_TDCI) launch_absorber_apply(c, c->state_d + c->nC);
     launch_add_scalar(c, c->stepT_d, dt);
   } catch (...) {
     c->inCapture = 0;
@@ -701,6 +704,7 @@ void capture_step_graph(cgpu_ctx* c, double t0, double dt, int krylov, int useMe
   c->graphDt = dt;
   c->graphKrylov = krylov;
   c->graphMetric = useMetric;
+  c->graphAbsorb = c->absorbEachStep;
 }
 
 // Step start time of every trajectory (t0s has nb entries).
@@ -712,7 +716,7 @@ void set_step_times(cgpu_ctx* c, const double* t0s) {
 // n_steps replays of the step graph (captured when dt, order or metric changed).
 void propagate_graph(cgpu_ctx* c, const double* t0s, double dt, int nSteps, int krylov, int useMetric) {
   if (!c->stepGraph || c->graphDt != dt || c->graphKrylov != krylov || c->graphMetric != useMetric ||
-      c->graphProf != c->profTarget)
+      c->graphProf != c->profTarget || c->graphAbsorb != c->absorbEachStep)
     capture_step_graph(c, t0s[0], dt, krylov, useMetric);
   if (c->profTarget) c->profUsed = c->graphProfUsed;
   set_step_times(c, t0s);
@@ -1168,6 +1172,7 @@ int cgpu_propagate_resident(cgpu_ctx* c, double t0, double dt, int n_steps, int 
     double t = t0;
     for (int s = 0; s < n_steps; s++) {
       split2_device(c, c->state_d, t, t + dt, krylov_dim, 0.0, 0, use_metric);
+      if (c->absorbEachStep && c->method != CGPU_METHOD_TDCI) launch_absorber_apply(c, c->state_d + c->nC);
       t = t + dt;
     }
     CODY_CUDA(cudaGetLastError());
@@ -1374,6 +1379,23 @@ int cgpu_load_restart(cgpu_ctx* c, const char* dir) {
   CODY_API_END(c)
 }
 
+int cgpu_absorber_setup(cgpu_ctx* c, double onset, double order, int apply_each_step) {
+  CODY_API_BEGIN(c)
+  if (!(order > 0.0)) throw std::string("absorber: order must be positive");
+  launch_absorber_setup(c, onset, order);
+  c->absorbEachStep = apply_each_step ? 1 : 0;
+  sync(c);
+  CODY_API_END(c)
+}
+
+int cgpu_absorber_apply(cgpu_ctx* c) {
+  CODY_API_BEGIN(c)
+  if (c->method == CGPU_METHOD_TDCI) throw std::string("absorber: no orbitals in a TDCI state");
+  launch_absorber_apply(c, c->state_d + c->nC);
+  sync(c);
+  CODY_API_END(c)
+}
+
 int cgpu_tdci_adjoint(cgpu_ctx* c, const cgpu_complex* c0, const double* field, int n_steps, double dt,
                       int checkpoint, double* objective, double* overlap, cgpu_complex* c_final, double* d_objective) {
   CODY_API_BEGIN(c)
@@ -1483,7 +1505,7 @@ int cgpu_batch_propagate(cgpu_batch* b, const double* t0, double dt, int n_steps
   cgpu_ctx* c = c_;
   if (!t0 || n_steps < 0 || krylov_dim <= 0) throw std::string("batch_propagate: bad argument");
   if (!c->stepGraph || c->graphDt != dt || c->graphKrylov != krylov_dim || c->graphMetric != use_metric ||
-      c->graphProf != c->profTarget) {
+      c->graphProf != c->profTarget || c->graphAbsorb != c->absorbEachStep) {
     set_step_times(c, t0);
     capture_step_graph(c, t0[0], dt, krylov_dim, use_metric);
   }
@@ -1524,6 +1546,11 @@ int cgpu_batch_energies(cgpu_batch* b, const double* t, double* energies) {
                               cudaMemcpyDeviceToHost, c->stream));
   sync(c);
   CODY_BATCH_END
+}
+
+int cgpu_batch_absorber_setup(cgpu_batch* b, double onset, double order, int apply_each_step) {
+  if (!b || !b->c) return fail(nullptr, "null batch", CGPU_ERR_ARG);
+  return cgpu_absorber_setup(b->c, onset, order, apply_each_step);
 }
 
 int cgpu_batch_observables(cgpu_batch* b, const double* t, double* out) {

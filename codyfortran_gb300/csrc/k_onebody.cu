@@ -471,6 +471,30 @@ __global__ void k_norm_dipole(double* __restrict__ scal, const z_t* __restrict__
   }
 }
 
+// Absorber mask (src/Absorber/Linear/Cosinus/S_Absorber_Linear_Cosinus.f90:75-104):
+// 1 inside |x| < onset, cos(pi/2 xi)^(1/order) outside, xi = (|x| - onset) / (x_last - onset).
+__global__ void k_absorber_mask(double* __restrict__ mask, const double* __restrict__ x, double onset, double order,
+                                TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  mask = bat(mask, bs);
+  x = bat(x, bs);
+  const double xMax = x[S.nG - 1];
+  const double PI = 3.14159265358979323846264338327950288;
+  GRID_STRIDE(g, S.nG) {
+    double xi = fabs(x[g]);
+    double t = (xi - onset) / (xMax - onset);
+    mask[g] = xi < onset ? 1.0 : pow(cos(0.5 * PI * t), 1.0 / order);
+  }
+}
+
+// ApplyAbsorber (:115-128): every stored orbital times the mask
+__global__ void k_absorber_apply(z_t* __restrict__ orbs, const double* __restrict__ mask, TRAJ_ARGS) {
+  const TrajShape& S = shp[blockIdx.z];
+  orbs = bat(orbs, bs);
+  mask = bat(mask, bs);
+  GRID_STRIDE(e, (size_t)S.nG * S.nOS) orbs[e] = zscale(orbs[e], mask[e % S.nG]);
+}
+
 __global__ void k_set_scalar(double* p, double v, size_t bs) { *bat(p, bs) = v; }
 __global__ void k_add_scalar(double* p, double v, size_t bs) { *bat(p, bs) += v; }
 
@@ -632,5 +656,18 @@ void launch_set_scalar(cgpu_ctx* c, double* p, double v) {
 
 void launch_add_scalar(cgpu_ctx* c, double* p, double v) {
   k_add_scalar<<<bgrid(c, 1), 1, 0, c->stream>>>(p, v, c->bs);
+  CODY_LAUNCHED(c);
+}
+
+void launch_absorber_setup(cgpu_ctx* c, double onset, double order) {
+  k_absorber_mask<<<bgrid(c, ew_blocks(c, c->nG)), 256, 0, c->stream>>>(c->mask_d, c->x_d, onset, order,
+                                                                          TRAJ_PASS(c));
+  CODY_LAUNCHED(c);
+}
+
+void launch_absorber_apply(cgpu_ctx* c, z_t* orbs) {
+  ProfScope prof(c, CGPU_KERNEL_VECTOR);
+  k_absorber_apply<<<bgrid(c, ew_blocks(c, (size_t)c->nG * c->nOS)), 256, 0, c->stream>>>(orbs, c->mask_d,
+                                                                                            TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }

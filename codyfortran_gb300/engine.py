@@ -36,7 +36,7 @@ EXPORTED = [
     "cgpu_batch_upload", "cgpu_batch_download", "cgpu_batch_propagate", "cgpu_batch_energies",
     "cgpu_batch_kernels_per_step", "cgpu_batch_launch_count", "cgpu_batch_profile_begin", "cgpu_batch_profile_end",
     "cgpu_tdci_adjoint", "cgpu_observables", "cgpu_relax", "cgpu_batch_observables", "cgpu_save_restart",
-    "cgpu_load_restart",
+    "cgpu_load_restart", "cgpu_absorber_setup", "cgpu_absorber_apply", "cgpu_batch_absorber_setup",
 ]
 
 KERNELS = {"pair_potentials": 1, "correlation": 2, "h2": 3, "ci_apply": 4, "ci_rdm": 5, "onebody": 6, "lanczos": 7,
@@ -367,6 +367,12 @@ class Engine:
         out = np.zeros(3 + self.nOS)
         self._check(self.lib.cgpu_observables(self.h, _d(t), _p(out)))
         return dict(energy=out[0], norm=out[1], dipole=out[2], occupations=out[3:].copy())
+
+    def absorber(self, onset, order, apply_each_step=False):
+        self._check(self.lib.cgpu_absorber_setup(self.h, _d(onset), _d(order), int(apply_each_step)))
+
+    def absorber_apply(self):
+        self._check(self.lib.cgpu_absorber_apply(self.h))
 
     def save_restart(self, directory, with_rdm2=False):
         self._check(self.lib.cgpu_save_restart(self.h, str(directory).encode(), int(with_rdm2)))

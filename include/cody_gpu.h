@@ -234,6 +234,14 @@ int cgpu_relax(cgpu_ctx* ctx, cgpu_complex* state, double dt, int n_inner, doubl
 int cgpu_save_restart(cgpu_ctx* ctx, const char* dir, int with_rdm2);
 int cgpu_load_restart(cgpu_ctx* ctx, const char* dir);
 
+/* Cosine absorber (src/Absorber/Linear/Cosinus/S_Absorber_Linear_Cosinus.f90:75-128):
+ * mask 1 for |x| < onset, cos(pi/2 xi)^(1/order) beyond, xi = (|x| - onset) /
+ * (x_last - onset).  cgpu_absorber_apply multiplies the resident orbitals by it
+ * once (Absorber_ApplyAbsorber); with apply_each_step the resident / graph
+ * propagations apply it after every step. */
+int cgpu_absorber_setup(cgpu_ctx* ctx, double onset, double order, int apply_each_step);
+int cgpu_absorber_apply(cgpu_ctx* ctx);
+
 /* ---- pulse gradient (adjoint) ------------------------------------------- */
 /* No counterpart in the reference.  For a TDCI context (orbitals set with
  * cgpu_tdci_set_orbitals, at most 64 configurations): propagates c0 over
@@ -275,6 +283,8 @@ int cgpu_batch_energies(cgpu_batch* batch, const double* t, double* energies);
 /* cgpu_observables of every system at t[i]: out[i * (3 + nOSmax) + ...],
  * nOSmax the largest orbital count of the batch (cgpu_batch_sizes). */
 int cgpu_batch_observables(cgpu_batch* batch, const double* t, double* out);
+/* The absorber for every system of the batch (each with its own grid). */
+int cgpu_batch_absorber_setup(cgpu_batch* batch, double onset, double order, int apply_each_step);
 /* Kernels launched per step (all systems); launches so far (reset if nonzero). */
 long cgpu_batch_kernels_per_step(const cgpu_batch* batch);
 /* As cgpu_profile_begin / cgpu_profile_end, for the launches of a batch step. */

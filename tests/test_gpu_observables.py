@@ -109,3 +109,56 @@ def test_restart_files_round_trip(tmp_path):
     assert np.array_equal(e2.download(), st)
     e.close()
     e2.close()
+
+
+def test_absorber_mask_and_per_step_application():
+    from codyfortran_gb300.engine import Engine
+    sp = _helium()
+    onset, order = 12.0, 0.25
+    ea, eb = Engine(sp), Engine(sp)
+    st, orbs, c = _state(sp, ea.x, ea.w, 9, ea.nC)
+    # one application against the mask restated on the host
+    ea.absorber(onset, order)
+    ea.upload(st)
+    ea.absorber_apply()
+    xi = np.abs(ea.x)
+    t = (xi - onset) / (ea.x[-1] - onset)
+    mask = np.where(xi < onset, 1.0, np.cos(0.5 * np.pi * t) ** (1.0 / order))
+    ref = st.copy()
+    ref[ea.nC:] = (orbs * mask[:, None]).ravel(order="F")
+    got = ea.download()
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-14
+    # applied after every step of the step graph == step, apply, step, apply
+    ea.absorber(onset, order, apply_each_step=True)
+    ea.upload(st)
+    ea.propagate_resident(0.0, 0.01, 2, 10, use_metric=True, use_graph=True)
+    eb.absorber(onset, order, apply_each_step=False)
+    eb.upload(st)
+    for k in range(2):
+        eb.propagate_resident(0.01 * k, 0.01, 1, 10, use_metric=True, use_graph=True)
+        eb.absorber_apply()
+    a, b = ea.download(), eb.download()
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-13
+    ea.close()
+    eb.close()
+
+
+def test_tdci_sil_matches_oracle():
+    """TDCI propagation of the CI vector alone by SIL (fixed orbitals, laser on)."""
+    from codyfortran_gb300.engine import Engine
+    sp = _helium()
+    sp.method = "tdci"
+    o, e = Oracle(sp), Engine(sp)
+    orbs = I.mgs_orthonormalize(I.harmonic_orbitals(sp, e.x), e.w)
+    o.tdci_set_orbitals(orbs)
+    e.tdci_set_orbitals(orbs)
+    rng = np.random.default_rng(4)
+    c = rng.normal(size=e.nC) + 1j * rng.normal(size=e.nC)
+    c /= np.linalg.norm(c)
+    a, b, t = c.copy(), c.copy(), 1.0
+    for _ in range(3):
+        a = e.sil(a, t, t + 0.05, 12, which="tdci")
+        b = o.sil(b, t, t + 0.05, 12, which="tdci")
+        t += 0.05
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-12
+    e.close()
