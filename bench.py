@@ -45,6 +45,15 @@ METRIC = "MCTDHF traj-steps/s: mixed-prec batched vs FP64 GPU at ≤1e-8 energy/
 UNIT = "traj-steps/s"
 L2_BYTES = 129 * 1024 * 1024
 ACC_STEPS = 10
+DTYPES = {
+    "fp64": "complex128",
+    "mixed": "mixed (bf16x3 tcgen05 contractions with fp32 accumulation, fp64 rest)",
+    "mixed6": "mixed (bf16x6 tcgen05 contractions with fp32 accumulation, fp64 rest)",
+    "mixed_fx": "mixed (tcgen05 contractions on 5 base-64 digit slices per operand row, exact per-level "
+                "accumulation, fp64 results; fp64 rest)",
+    "mixed_fx6": "mixed (tcgen05 contractions on 6 base-64 digit slices per operand row, exact per-level "
+                 "accumulation, fp64 results; fp64 rest)",
+}
 FAMILIES = ("pair_potentials", "correlation", "h2", "ci_apply", "ci_rdm", "onebody", "lanczos", "rdm_inverse",
             "projectors", "fold", "vector")
 
@@ -207,15 +216,20 @@ def run_reference(args):
     return 0
 
 
-def lanczos_work(systems, K, sil_per_step=2):
-    """Algorithmic bytes and FP64 flops of the Lanczos family in one step: at
-    iteration j the update reads the j basis vectors three times (dots, two
-    Gram-Schmidt passes) and w / v_{j+1} seven times; every basis entry costs
-    one complex multiply-add (8 flops) per pass."""
+def lanczos_work(systems, K, window=0, sil_per_step=2):
+    """Algorithmic bytes and FP64 flops of the Lanczos family in one step.  At
+    iteration j the update forms the dots of w with the nv basis vectors it
+    orthogonalises against (nv = j, or min(j, window)) and ||w||^2 (reads nv + 1
+    vectors and the metric), subtracts the projections and forms the new norm
+    (reads nv + 1 vectors and the metric, writes w) and scales w into v_{j+1}
+    (reads w, writes v_{j+1}): (2 nv + 5) complex and 2 real passes over the
+    state; 16 nv + 13 flops per entry.  The gated second pass does not fire on
+    this workload and is not counted."""
     nS = sum(s.nS for s in systems)
-    passes = sum(3 * j + 7 for j in range(1, K + 1)) * sil_per_step
-    flops = sum(3 * j * 8 + 8 for j in range(1, K + 1)) * sil_per_step * nS
-    return passes * nS * 16.0, float(flops)
+    nvs = [min(j, window) if window > 0 else j for j in range(1, K + 1)]
+    byts = sum(16.0 * (2 * nv + 5) + 16.0 for nv in nvs) * sil_per_step * nS
+    flops = sum(16 * nv + 13 for nv in nvs) * sil_per_step * nS
+    return byts, float(flops)
 
 
 def dense_flops(systems, fam):
@@ -240,10 +254,10 @@ def batch_norms(b, packed):
     return np.array([np.linalg.norm(packed[b.offsets[i]:b.offsets[i] + b.systems[i].nC]) for i in range(len(b))])
 
 
-def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=False, e2e=True, acc_steps=0):
+def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=False, e2e=True, acc_steps=0, window=0):
     from codyfortran_gb300.engine import Batch
     dt, K = cfg["dt"], cfg["krylov"]
-    b = Batch(specs, precision, max_krylov=K)
+    b = Batch(specs, precision, max_krylov=K, krylov_window=window)
     states = [initial_state(sp, s.x, s.w, cfg["seed"] + k) for k, (sp, s) in enumerate(zip(specs, b.systems))]
     host = b.pack(states)
     b.upload(host)
@@ -296,22 +310,46 @@ def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=Fals
     return out
 
 
+def krylov_window(args, precision):
+    """Lanczos re-orthogonalisation window: the reference's full loop for the
+    FP64 form, the three-term recurrence (window 2) for the mixed forms unless
+    --krylov-window says otherwise."""
+    if args.krylov_window is not None:
+        return args.krylov_window
+    return 0 if precision == "fp64" else 2
+
+
+def window_name(window):
+    if window == 0:
+        return "full (every basis vector)"
+    if window == 2:
+        return "three-term recurrence (last 2 basis vectors)"
+    return f"last {window} basis vectors"
+
+
 def run_batch(args):
     rank, world, local = dist_info()
     specs, cfg = workload(args.workload)
     precision = args.precision or "mixed"
     n = len(specs)
+    window = krylov_window(args, precision)
     acc_steps = 0 if args.no_fp64_leg or precision == "fp64" else ACC_STEPS
-    r = run_batch_leg(specs, cfg, precision, args.steps, args.warmup, profile=True, clock=True, acc_steps=acc_steps)
+    r = run_batch_leg(specs, cfg, precision, args.steps, args.warmup, profile=True, clock=True, acc_steps=acc_steps,
+                      window=window)
     ms = barrier_max(r["ms"], world)
     value = world * n * args.steps / (ms / 1e3)
-    # the same batch in the plain FP64 form (short timed region), and the
-    # deviation of the mixed form from it after ACC_STEPS steps from the same states
-    fp64, accuracy = None, None
+    # the same batch in the plain FP64 form with the reference's full Krylov
+    # re-orthogonalisation (short timed region), and the deviation of the mixed
+    # form from it after ACC_STEPS steps from the same states; with a Krylov
+    # window also the FP64 form with that window, to separate the two gains
+    fp64, fp64_win, accuracy = None, None, None
+    fsteps = max(1, min(args.steps, 2))
     if acc_steps:
-        f = run_batch_leg(specs, cfg, "fp64", max(1, min(args.steps, 2)), 1, profile=False, e2e=False,
-                          acc_steps=acc_steps)
-        fp64 = n * max(1, min(args.steps, 2)) / (f["ms"] / 1e3)
+        f = run_batch_leg(specs, cfg, "fp64", fsteps, 1, profile=False, e2e=False, acc_steps=acc_steps)
+        fp64 = n * fsteps / (f["ms"] / 1e3)
+        if window:
+            fw = run_batch_leg(specs, cfg, "fp64", fsteps, 1, profile=False, e2e=False, window=window)
+            fp64_win = n * fsteps / (fw["ms"] / 1e3)
         dA = np.abs(r["acc_energy"] - f["acc_energy"])
         dE = dA / np.abs(f["acc_energy"])
         dN = np.abs(r["acc_norm"] - f["acc_norm"])
@@ -334,7 +372,7 @@ def run_batch(args):
         work = dense_flops(systems, dom) / n_dom
         roof.update(bound="tensor", achieved=work / avg_s / 1e12, peak=bf16, unit="TFLOP/s", work_per_launch=work)
     elif dom == "lanczos":
-        byts, flops = lanczos_work(systems, cfg["krylov"])
+        byts, flops = lanczos_work(systems, cfg["krylov"], window)
         byts /= n_dom
         roof.update(bound="hbm", achieved=byts / avg_s / 1e9, peak=hbm, unit="GB/s", work_per_launch=byts,
                     fp64_tflops=flops / n_dom / avg_s / 1e12)
@@ -346,17 +384,21 @@ def run_batch(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "complex128" if precision == "fp64" else
-                 f"mixed (bf16x{6 if precision == 'mixed6' else 3} tcgen05 contractions with fp32 accumulation, fp64 rest)",
+        "dtype": DTYPES[precision],
         "data": "synthetic (seeded Gaussian orbitals, random normalised CI vectors)",
         "config": {"workload": args.workload, "trajectories": n, "krylov_order": cfg["krylov"], "dt": cfg["dt"],
-                   "precision": precision, "parallelism": f"batch of {n} per GPU, replicas x{world}",
+                   "precision": precision, "krylov_reorthogonalisation": window_name(window),
+                   "parallelism": f"batch of {n} per GPU, replicas x{world}",
                    "n_grid_range": [min(s.nG for s in systems), max(s.nG for s in systems)],
                    "n_determinants_range": [min(s.nC for s in systems), max(s.nC for s in systems)],
                    "l2": f"per-step working set {sum(s.nS for s in systems) * 16 * (cfg['krylov'] + 8) / 1e9:.1f} GB "
                          f"of states and Krylov vectors > L2 ({L2_BYTES / 1e6:.0f} MB): inputs larger than L2, no flush"},
         "fp64_gpu": {"value": fp64, "unit": UNIT, "ratio": (value / fp64) if fp64 else None,
-                     "note": "same batch, plain FP64 form, same GPU"},
+                     "note": "same batch, plain FP64 form with full Krylov re-orthogonalisation (the reference's "
+                             "algorithm), same GPU"},
+        "fp64_gpu_same_krylov": None if fp64_win is None else {
+            "value": fp64_win, "unit": UNIT, "ratio": value / fp64_win,
+            "note": f"same batch, FP64 form with the timed leg's Krylov recurrence ({window_name(window)})"},
         "accuracy_vs_fp64": accuracy,
         "clocks": r["clocks"],
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": r["e2e_bytes"], "d2h_bytes_per_step": r["e2e_bytes"],
@@ -382,7 +424,8 @@ def run_single(args):
     specs, cfg = workload(args.workload)
     sp = specs[0]
     precision = args.precision or "fp64"
-    e = Engine(sp, precision=precision, max_krylov=cfg["krylov"])
+    window = krylov_window(args, precision)
+    e = Engine(sp, precision=precision, max_krylov=cfg["krylov"], krylov_window=window)
     st = initial_state(sp, e.x, e.w, cfg["seed"])
     dt, K = cfg["dt"], cfg["krylov"]
     e.upload(st)
@@ -424,6 +467,8 @@ def run_single(args):
         work, bound = 2.0 * nG * nG * 2 * P, "tensor"
     elif dom in ("correlation", "h2"):
         work, bound = 8.0 * nG * Q * Q, "tensor"
+    elif dom == "lanczos":
+        work, bound = lanczos_work([e], K, window)[0] / max(n_dom, 1), "hbm"
     else:
         work, bound = 16.0 * e.nS * 4, "hbm"
     if bound == "tensor":
@@ -433,10 +478,11 @@ def run_single(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "complex128" if precision == "fp64" else "mixed(bf16 split tcgen05 contractions, fp64 rest)",
+        "dtype": DTYPES[precision],
         "data": "synthetic (seeded Gaussian orbitals, random normalised CI vector)",
         "config": {"workload": args.workload, "n_grid": nG, "n_orbitals": e.nOS, "n_determinants": nC,
-                   "krylov_order": K, "dt": dt, "precision": precision, "parallelism": f"replicas x{world}",
+                   "krylov_order": K, "dt": dt, "precision": precision,
+                   "krylov_reorthogonalisation": window_name(window), "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2, no flush"},
         "clocks": clk.summary(),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": e.nS * 16, "d2h_bytes_per_step": e.nS * 16,
@@ -464,11 +510,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch512", choices=["batch512", "trimer_large", "helium_small"])
-    ap.add_argument("--precision", default=None, choices=["fp64", "mixed", "mixed6"])
+    ap.add_argument("--precision", default=None, choices=list(DTYPES))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-leg", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=25.0)
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one instead of a step graph")
+    ap.add_argument("--krylov-window", type=int, default=None,
+                    help="Gram-Schmidt against the last k Krylov vectors (0: all; default 0 for fp64, 2 otherwise)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -261,6 +261,7 @@ struct cgpu_ctx {
   z_t *state_d = nullptr, *dstate_d = nullptr, *rkInc_d = nullptr, *rkTmp_d = nullptr, *rkStage_d = nullptr;
   z_t *basis_d = nullptr, *lw_d = nullptr, *trial_d = nullptr, *work_d = nullptr;
   int maxKrylov = 0;
+  int krylovWindow = 0;                       // 0: full re-orthogonalisation; k: last k basis vectors
   double* lz_d = nullptr;   // Lanczos scalars: alpha, beta, dots, phi, flags
   double* lz_h = nullptr;   // pinned mirror (trajectory 0)
   // TDCI static data

@@ -364,8 +364,7 @@ void put(cgpu_ctx* c, int b, T* dst0, const std::vector<T>& v) {
 void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
   const cgpu_desc* d0 = &descs[0];
   if (d0->n_body_types < 1 || d0->n_body_types > CODY_MAX_BT) throw std::string("method.mb.nBodyTypes out of range");
-  if (d0->precision != CGPU_PREC_FP64 && d0->precision != CGPU_PREC_MIXED && d0->precision != CGPU_PREC_MIXED_X6)
-    throw std::string("unknown precision");
+  if (d0->precision < CGPU_PREC_FP64 || d0->precision > CGPU_PREC_MIXED_FX6) throw std::string("unknown precision");
   c->nb = nSys;
   c->nBt = d0->n_body_types;
   c->restricted = d0->restricted ? 1 : 0;
@@ -390,13 +389,15 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
     minS = std::min(minS, s.nS);
   }
   for (int b = 0; b < nSys; b++) maxK = std::max(maxK, descs[b].max_krylov);
+  c->krylovWindow = descs[0].krylov_window;
+  for (int b = 0; b < nSys; b++)
+    if (descs[b].krylov_window != c->krylovWindow || descs[b].krylov_window < 0)
+      throw std::string("krylov_window must be >= 0 and the same for every trajectory of a batch");
   c->nGO = nGO;
   ci_build_work(c);
   c->nS = (c->method == CGPU_METHOD_TDCI) ? c->nC : c->nC + nGO;
   c->minS = minS;
   c->maxKrylov = std::max(1, std::min(maxK > 0 ? maxK : 32, 32));
-  // Lanczos reductions: one system spreads 256-entry chunks over up to 4 blocks
-  // per SM; a batch gives each block a 1024-entry chunk of its trajectory.
   // Lanczos reductions: one system spreads 256-entry chunks over up to 4 blocks
   // per SM; a batch gives each trajectory a few blocks of 1024-entry chunks
   // (about 4k blocks in total: few partials, little per-block overhead).

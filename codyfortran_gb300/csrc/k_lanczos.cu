@@ -6,12 +6,16 @@
 //   w = H v_j - beta_{j-1} v_{j-1};  alpha_j = Re<v_j,w>;  w -= alpha_j v_j;
 //   for k = 1..j: w -= <v_k,w> v_k   (modified Gram-Schmidt);  beta_j = ||w||.
 // With the basis orthonormal, the projections it removes are those of H v_j on
-// v_1..v_j; the kernels remove them in two classical Gram-Schmidt passes
-// (each pass one fused reduction), which reproduces the reference's vectors
-// and coefficients to rounding.  Every reduction is deterministic: per-block
+// v_1..v_j; the kernels remove them in a classical Gram-Schmidt pass (one
+// fused reduction) and a second pass when the first one cancelled most of w,
+// which reproduces the reference's vectors and coefficients to rounding.
+// With a window k > 0 the passes run against v_{j-k+1}..v_j only (k = 2: the
+// three-term recurrence, orthogonal to the rest in exact arithmetic).  Every reduction is deterministic: per-block
 // partials in a fixed order, re-summed identically by every consumer block.
 //
 // Device scalar block lz[] (doubles):
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace {
@@ -152,13 +156,13 @@ __global__ void __launch_bounds__(LZ_THREADS) k_mdot(z_t* __restrict__ part, int
 
 // Every block re-sums the dot partials (fixed order) into shared coefficients,
 // subtracts w -= sum_k coef_k V_k and emits the partials of the metric norm^2
-// of the new w.  Block 0 stores the coefficients at lz[LZ_D] (storeDots).
-// Gated as k_mdot.
+// of the new w.  Block 0 stores coefficient k at lz[LZ_D + 2 (dotBase + k)]
+// (dotBase < 0: not stored).  Gated as k_mdot.
 __global__ void __launch_bounds__(LZ_THREADS) k_cgs_pass(z_t* __restrict__ w, const z_t* __restrict__ V, size_t ldv,
                                                           int nVec, const z_t* __restrict__ partIn, int inStride,
                                                           int nBlkIn, z_t* __restrict__ partOut,
                                                           const double* __restrict__ m, TRAJ_ARGS,
-                                                          double* __restrict__ lz, int storeDots, int E,
+                                                          double* __restrict__ lz, int dotBase, int E,
                                                           const z_t* __restrict__ gate0, int gateStride,
                                                           const z_t* __restrict__ gate1) {
   const TrajShape& S = shp[blockIdx.z];
@@ -174,10 +178,10 @@ __global__ void __launch_bounds__(LZ_THREADS) k_cgs_pass(z_t* __restrict__ w, co
   const size_t n = S.nS;
   const int CH = LZ_THREADS * E;
   sum_partials(partIn, nBlkIn, inStride, nVec, coef);
-  if (storeDots && blockIdx.x == 0)
+  if (dotBase >= 0 && blockIdx.x == 0)
     for (int k = threadIdx.x; k < nVec; k += blockDim.x) {
-      lz[LZ_D + 2 * k] = coef[k].x;
-      lz[LZ_D + 2 * k + 1] = coef[k].y;
+      lz[LZ_D + 2 * (dotBase + k)] = coef[k].x;
+      lz[LZ_D + 2 * (dotBase + k) + 1] = coef[k].y;
     }
   double nacc = 0.0;
   for (size_t c0 = (size_t)blockIdx.x * CH; c0 < n; c0 += (size_t)gridDim.x * CH) {
@@ -445,34 +449,38 @@ void launch_lanczos_start(cgpu_ctx* c, const z_t* v) {
   CODY_LAUNCHED(c);
 }
 
-// After lw_d holds H v_j: CGS2 against v_1..v_j, beta_j, v_{j+1}.
+// After lw_d holds H v_j: Gram-Schmidt against v_1..v_j (or the window's last
+// vectors), the gated second pass, beta_j, v_{j+1}.
 void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
   ProfScope prof(c, CGPU_KERNEL_LANCZOS);
   size_t ld = c->nS;
   int nBlk = c->lzBlocks;
-  // p1: pass-1 dots with v_1..v_j and ||w0||^2 (stride j+1); p2: ||w1||^2 after
-  // pass 1; p3, p4: dots and norm of the gated second pass
+  // p1: pass-1 dots with the nv vectors and ||w0||^2 (stride nv+1); p2: ||w1||^2
+  // after pass 1; p3, p4: dots and norm of the gated second pass
   z_t* p1 = c->partial_d;
   z_t* p2 = p1 + (size_t)nBlk * (c->maxKrylov + 1);
   z_t* p3 = p2 + nBlk;
   z_t* p4 = p3 + (size_t)nBlk * (c->maxKrylov + 1);
   if (j > 32) throw std::string("SIL: Krylov order above 32");
-  const int E = c->lzElems, s1 = j + 1;
+  const int base = (c->krylovWindow > 0) ? std::max(0, j - c->krylovWindow) : 0;
+  const int nv = j - base, s1 = nv + 1;
+  const z_t* V = c->basis_d + ld * (size_t)base;
+  const int E = c->lzElems;
   dim3 g = bgrid(c, nBlk);
-  k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p1, s1, c->basis_d, ld, j, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 1,
+  k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p1, s1, V, ld, nv, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 1,
                                           nullptr, 0, nullptr, nBlk);
   CODY_LAUNCHED(c);
-  k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, ld, j, p1, s1, nBlk, p2, c->metric_d, TRAJ_PASS(c),
-                                              c->lz_d, 1, E, nullptr, 0, nullptr);
+  k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, V, ld, nv, p1, s1, nBlk, p2, c->metric_d, TRAJ_PASS(c),
+                                              c->lz_d, base, E, nullptr, 0, nullptr);
   CODY_LAUNCHED(c);
-  k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p3, j, c->basis_d, ld, j, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 0,
-                                          p1 + j, s1, p2, nBlk);
+  k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p3, nv, V, ld, nv, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 0,
+                                          p1 + nv, s1, p2, nBlk);
   CODY_LAUNCHED(c);
-  k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, c->basis_d, ld, j, p3, j, nBlk, p4, c->metric_d, TRAJ_PASS(c),
-                                              c->lz_d, 0, E, p1 + j, s1, p2);
+  k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, V, ld, nv, p3, nv, nBlk, p4, c->metric_d, TRAJ_PASS(c),
+                                              c->lz_d, -1, E, p1 + nv, s1, p2);
   CODY_LAUNCHED(c);
   z_t* vNext = (j < maxDim) ? c->basis_d + ld * (size_t)j : nullptr;
-  k_lz_finish<<<g, LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p2, p4, p1 + j, s1, nBlk, TRAJ_PASS(c), c->lz_d, j,
+  k_lz_finish<<<g, LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p2, p4, p1 + nv, s1, nBlk, TRAJ_PASS(c), c->lz_d, j,
                                                maxDim, 1.0e-14);
   CODY_LAUNCHED(c);
   k_lz_mark_done<<<bgrid(c, 1), 1, 0, c->stream>>>(c->lz_d, j, c->bs);

@@ -14,6 +14,12 @@
 //   sum_(l2,k2) W_(l2k2) R'[(l2,k2), q] = sum_p a_p X_p[q] + b_p Y_p[q],
 //   W_p = a_p + i b_p,  X_p = R1 + R2,  Y_p = i (R1 - R2),
 //   R1 = R'[(l,k), q], R2 = R'[(k,l), q] (0 when l = k).
+//
+// The fixed-point form (precision mixed_fx / mixed_fx6) carries every operand
+// row as L base-64 digit slices under one power of two per row (k_fx.cu) and
+// returns FP64 results whose only error is the operand truncation (~2^-6L of
+// each row's maximum): S and V rows for GEMM1, W rows for GEMM2, R'' rows,
+// W columns for GEMM3.  The row exponents of W come from the GEMM1 epilogue.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -31,6 +37,11 @@ struct MixedBufs {
   int* err = nullptr;
   double* Zd = nullptr;     // (nG, Q) complex
   CUtensorMap mV, mS, mSasB, mW, mWT, mR;  // TMA maps (A operands box 128 rows, B operands box BN rows)
+  // fixed-point form (fxL > 0 slices)
+  int fxL = 0;
+  int *eV = nullptr, *eS = nullptr, *eWr = nullptr, *eWc = nullptr, *eR = nullptr;  // row exponents
+  unsigned *mWr = nullptr, *mWc = nullptr;  // largest biased exponent of |W| per row g / column n
+  double *Wd = nullptr, *Zp = nullptr, *Gd = nullptr;  // FP64 results [split][M][N]
 };
 
 namespace {
@@ -210,7 +221,8 @@ __global__ void k_split_R(__nv_bfloat16* __restrict__ RxB, const z_t* __restrict
 }
 
 // Z[g][q] (complex) = sum_z P2[z][g][2q+s]
-__global__ void k_reduce_Z(z_t* __restrict__ Z, const float* __restrict__ P2, int nSplit, TRAJ_ARGS) {
+template <class PT>
+__global__ void k_reduce_Z(z_t* __restrict__ Z, const PT* __restrict__ P2, int nSplit, TRAJ_ARGS) {
   const TrajShape& T = shp[blockIdx.z];
   const int nG = T.nG, Q = T.nOS * T.nOS;
   Z = bat(Z, bs);
@@ -219,7 +231,7 @@ __global__ void k_reduce_Z(z_t* __restrict__ Z, const float* __restrict__ P2, in
   int g = (int)(e / Q), q = (int)(e % Q);
   double re = 0.0, im = 0.0;
   for (int z = 0; z < nSplit; z++) {
-    const float* r = P2 + ((size_t)z * nG + g) * 2 * Q + 2 * q;
+    const PT* r = P2 + ((size_t)z * nG + g) * 2 * Q + 2 * q;
     re += (double)r[0];
     im += (double)r[1];
   }
@@ -228,7 +240,8 @@ __global__ void k_reduce_Z(z_t* __restrict__ Z, const float* __restrict__ P2, in
 }
 
 // H2s[(i1*n+j1)][(l2*n+k2)] = 1/2 sum_g S_(i1j1) W_(l2k2) from the unordered-pair products.
-__global__ void k_reduce_H2(z_t* __restrict__ H2s, const float* __restrict__ P3, int nSplit,
+template <class PT>
+__global__ void k_reduce_H2(z_t* __restrict__ H2s, const PT* __restrict__ P3, int nSplit,
                             const int* __restrict__ pidx, TRAJ_ARGS) {
   const TrajShape& T = shp[blockIdx.z];
   const int n = T.nOS, nP = T.nPairs;
@@ -247,7 +260,7 @@ __global__ void k_reduce_H2(z_t* __restrict__ H2s, const float* __restrict__ P3,
     int N2 = 2 * nP;
     double rr = 0, ii = 0, ri = 0, ir = 0;
     for (int z = 0; z < nSplit; z++) {
-      const float* G = P3 + (size_t)z * N2 * N2;
+      const PT* G = P3 + (size_t)z * N2 * N2;
       rr += G[(size_t)(2 * p) * N2 + 2 * pp];
       ii += G[(size_t)(2 * p + 1) * N2 + 2 * pp + 1];
       ri += G[(size_t)(2 * p) * N2 + 2 * pp + 1];
@@ -266,6 +279,212 @@ __global__ void k_reduce_H2(z_t* __restrict__ H2s, const float* __restrict__ P3,
 }
 
 
+// ---- fixed-point digit slices -------------------------------------------------
+
+// Signed base-64 digits of x relative to 2^e (|x| < 2^e): X = round(x 2^(6L-e))
+// = sum_i d_i 64^(L-1-i), d_i in [-32, 31] for i > 0, |d_0| <= 64.  Integer
+// operations only.
+template <int L>
+__device__ __forceinline__ void fx_digits(double x, int e, int (&d)[L]) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((u >> 52) & 0x7FF);
+  long long X = 0;
+  if (ex != 0) {
+    const unsigned long long mant = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = 1075 - ex - 6 * L + e;  // >= 53 - 6L > 0 because |x| < 2^e
+    if (sh < 63) X = (long long)((mant + (1ull << (sh - 1))) >> sh);
+    if (u >> 63) X = -X;
+  }
+#pragma unroll
+  for (int i = L - 1; i >= 1; i--) {
+    int t = (int)(X & 63);
+    if (t >= 32) t -= 64;
+    d[i] = t;
+    X = (X - t) >> 6;
+  }
+  d[0] = (int)X;
+}
+
+__device__ __forceinline__ unsigned fx_biased_exp(double v) { return (unsigned)(__double2hiint(v) >> 20) & 0x7FFu; }
+// smallest e with |x| < 2^e for the largest biased exponent m of a row (0: all zero)
+__device__ __forceinline__ int fx_exp(unsigned m) { return m ? (int)m - 1022 : 0; }
+
+template <int L>
+__device__ __forceinline__ void fx_store(__nv_bfloat16* rowBase, size_t pitch, int k, bool valid, double v, int e) {
+  int d[L];
+  if (valid) fx_digits<L>(v, e, d);
+  else
+#pragma unroll
+    for (int l = 0; l < L; l++) d[l] = 0;
+#pragma unroll
+  for (int l = 0; l < L; l++) rowBase[(size_t)l * pitch + k] = __int2bfloat16_rn(d[l]);
+}
+
+__device__ unsigned fx_block_max(unsigned m) {
+  __shared__ unsigned red[32];
+  m = __reduce_max_sync(0xffffffffu, m);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = m;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  unsigned r = 0;
+  for (int i = 0; i < nw; i++) r = max(r, red[i]);
+  return r;
+}
+
+// One block per row: the row's values in dynamic shared memory, the exponent
+// of its maximum, then the L digit planes (zero for K <= k < Kpad).
+template <int L, class F>
+__device__ void fx_row(__nv_bfloat16* rowBase, int* expOut, int K, int Kpad, int pitch, F value) {
+  extern __shared__ double fxbuf[];
+  unsigned m = 0;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    const double v = value(k);
+    fxbuf[k] = v;
+    m = max(m, fx_biased_exp(v));
+  }
+  const int e = fx_exp(fx_block_max(m));
+  if (threadIdx.x == 0) *expOut = e;
+  for (int k = threadIdx.x; k < Kpad; k += blockDim.x) fx_store<L>(rowBase, pitch, k, k < K, k < K ? fxbuf[k] : 0.0, e);
+}
+
+template <int L>
+__global__ void __launch_bounds__(256) k_fx_split_V(__nv_bfloat16* __restrict__ out, int* __restrict__ eV,
+                                                     const double* __restrict__ V, int pitch, TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int g = blockIdx.x, nG = T.nG;
+  if (g >= nG) return;
+  out = bat(out, bs);
+  eV = bat(eV, bs);
+  V = bat(V, bs);
+  const double* row = V + (size_t)g * nG;
+  fx_row<L>(out + (size_t)g * L * pitch, eV + g, nG, T.Kg, pitch, [&](int k) { return row[k]; });
+}
+
+// Row 2p + s of S: (re, im)[conj(phi_l) phi_k w] over the grid (p = (l, k)).
+// Block 0 of a trajectory also clears the W exponent maxima for GEMM1.
+template <int L>
+__global__ void __launch_bounds__(256) k_fx_split_S(__nv_bfloat16* __restrict__ out, int* __restrict__ eS,
+                                                     unsigned* __restrict__ mWr, unsigned* __restrict__ mWc,
+                                                     const z_t* __restrict__ orbs, const double* __restrict__ w,
+                                                     const int* __restrict__ pl, const int* __restrict__ pk, int pitch,
+                                                     TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int row = blockIdx.x, nG = T.nG, nP = T.nPairs;
+  if (row >= 2 * nP) return;
+  out = bat(out, bs);
+  eS = bat(eS, bs);
+  orbs = bat(orbs, bs);
+  w = bat(w, bs);
+  pl = bat(pl, bs);
+  pk = bat(pk, bs);
+  if (row == 0) {
+    mWr = bat(mWr, bs);
+    mWc = bat(mWc, bs);
+    for (int i = threadIdx.x; i < nG; i += blockDim.x) mWr[i] = 0u;
+    for (int i = threadIdx.x; i < 2 * nP; i += blockDim.x) mWc[i] = 0u;
+  }
+  const int p = row >> 1, s = row & 1;
+  const z_t* a = orbs + (size_t)nG * pl[p];
+  const z_t* b = orbs + (size_t)nG * pk[p];
+  fx_row<L>(out + (size_t)row * L * pitch, eS + row, nG, T.Kg, pitch, [&](int g) {
+    const z_t v = zcmul(a[g], b[g]);
+    return (s ? v.y : v.x) * w[g];
+  });
+}
+
+// Row n = 2q + s of R'' (K = 2p + t), as k_split_R.
+template <int L>
+__global__ void k_fx_split_R(__nv_bfloat16* __restrict__ out, int* __restrict__ eR, const z_t* __restrict__ Rp,
+                             const int* __restrict__ pl, const int* __restrict__ pk, int pitch, TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int n = T.nOS, nP = T.nPairs, Q = n * n;
+  const int row = blockIdx.x;
+  if (row >= 2 * Q) return;
+  out = bat(out, bs);
+  eR = bat(eR, bs);
+  Rp = bat(Rp, bs);
+  pl = bat(pl, bs);
+  pk = bat(pk, bs);
+  const int q = row >> 1, s = row & 1;
+  fx_row<L>(out + (size_t)row * L * pitch, eR + row, 2 * nP, T.Kp, pitch, [&](int k) {
+    const int p = k >> 1, t = k & 1;
+    const int l = pl[p], kk = pk[p];
+    const z_t R1 = Rp[(size_t)(l * n + kk) * Q + q];
+    const z_t R2 = (l < kk) ? Rp[(size_t)(kk * n + l) * Q + q] : zmk(0.0, 0.0);
+    const double r1 = s ? (t ? R1.x : R1.y) : (t ? -R1.y : R1.x);
+    const double r2 = s ? (t ? R2.x : R2.y) : (t ? -R2.y : R2.x);
+    return t ? r1 - r2 : r1 + r2;
+  });
+}
+
+// W = sum of the K-split partials (into slot 0) and the exponent maxima of its
+// rows and columns (used when GEMM1 ran with split K).
+__global__ void k_fx_reduce_W(double* __restrict__ Wd, unsigned* __restrict__ mWr, unsigned* __restrict__ mWc,
+                              int nSplit, TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int nG = T.nG, N = 2 * T.nPairs;
+  Wd = bat(Wd, bs);
+  mWr = bat(mWr, bs);
+  mWc = bat(mWc, bs);
+  const size_t tot = (size_t)nG * N;
+  GRID_STRIDE(e, tot) {
+    double v = 0.0;
+    for (int z = 0; z < nSplit; z++) v += Wd[(size_t)z * tot + e];
+    Wd[e] = v;
+    const unsigned ex = fx_biased_exp(v);
+    if (ex) {
+      atomicMax(mWr + e / N, ex);
+      atomicMax(mWc + e % N, ex);
+    }
+  }
+}
+
+// W (FP64 [nG][2P]) to WxA (rows g, K = 2P) and WTxB (rows n, K = nG) digit
+// planes, with the row exponents eWr[g] / eWc[n]; 32 x 32 tiles transposed
+// through shared memory as k_split_W.
+template <int L>
+__global__ void __launch_bounds__(256) k_fx_split_W(__nv_bfloat16* __restrict__ WxA, __nv_bfloat16* __restrict__ WTxB,
+                                                     int* __restrict__ eWr, int* __restrict__ eWc,
+                                                     const double* __restrict__ Wd, const unsigned* __restrict__ mWr,
+                                                     const unsigned* __restrict__ mWc, int pitchP, int pitchG,
+                                                     TRAJ_ARGS) {
+  __shared__ double tile[SW_T][SW_T + 1];
+  const TrajShape& T = shp[blockIdx.z];
+  const int nG = T.nG, N2P = 2 * T.nPairs, KpP = T.Kp, KpG = T.Kg;
+  const int g0 = blockIdx.x * SW_T, n0 = blockIdx.y * SW_T;
+  if (g0 >= KpG || n0 >= KpP) return;
+  WxA = bat(WxA, bs);
+  WTxB = bat(WTxB, bs);
+  eWr = bat(eWr, bs);
+  eWc = bat(eWc, bs);
+  Wd = bat(Wd, bs);
+  mWr = bat(mWr, bs);
+  mWc = bat(mWc, bs);
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  for (int r = ty; r < SW_T; r += 8) {
+    const int g = g0 + r, n = n0 + tx;
+    const bool valid = g < nG && n < N2P;
+    const double v = valid ? Wd[(size_t)g * N2P + n] : 0.0;
+    tile[r][tx] = v;
+    if (g < nG && n < KpP) {
+      const int e = fx_exp(mWr[g]);
+      if (n == 0) eWr[g] = e;
+      fx_store<L>(WxA + (size_t)g * L * pitchP, pitchP, n, valid, v, e);
+    }
+  }
+  __syncthreads();
+  for (int r = ty; r < SW_T; r += 8) {
+    const int n = n0 + r, g = g0 + tx;
+    if (n < N2P && g < KpG) {
+      const int e = fx_exp(mWc[n]);
+      if (g == 0) eWc[n] = e;
+      fx_store<L>(WTxB + (size_t)n * L * pitchG, pitchG, g, g < nG, tile[tx][r], e);
+    }
+  }
+}
+
 size_t take(size_t& off, size_t bytes) {
   size_t o = (off + 255) & ~(size_t)255;
   off = o + std::max<size_t>(bytes, 1);
@@ -280,10 +499,58 @@ size_t mixed_layout(cgpu_ctx* c, char* base, size_t off) {
   if (c->precision == CGPU_PREC_FP64 || !c->hasInteraction) return off;
   if (!c->mixed) c->mixed = new MixedBufs();
   MixedBufs* m = c->mixed;
-  m->terms = c->precision == CGPU_PREC_MIXED_X6 ? 6 : 3;
+  m->fxL = c->precision == CGPU_PREC_MIXED_FX ? 5 : c->precision == CGPU_PREC_MIXED_FX6 ? 6 : 0;
+  m->terms = m->fxL ? m->fxL : c->precision == CGPU_PREC_MIXED_X6 ? 6 : 3;
   int nG = c->nG, nP = c->nPairs, Q = c->nOS * c->nOS, T = m->terms;
   m->KgMax = (nG + 63) / 64 * 64;
   m->KpMax = (2 * nP + 63) / 64 * 64;
+  typedef __nv_bfloat16 bf;
+  if (m->fxL) {
+    const int L = m->fxL;
+    m->bn1 = fx_tile_n(2 * nP, L);
+    m->bn2 = fx_tile_n(2 * Q, L);
+    m->bn3 = fx_tile_n(2 * nP, L);
+    m->s1 = fx_split_count(nG, 2 * nP, m->bn1, m->KgMax / 64, c->nb);
+    m->s2 = fx_split_count(nG, 2 * Q, m->bn2, m->KpMax / 64, c->nb);
+    m->s3 = fx_split_count(2 * nP, 2 * nP, m->bn3, m->KgMax / 64, c->nb);
+    size_t oV = take(off, sizeof(bf) * (size_t)nG * L * m->KgMax);
+    size_t oS = take(off, sizeof(bf) * (size_t)2 * nP * L * m->KgMax);
+    size_t oW = take(off, sizeof(bf) * (size_t)nG * L * m->KpMax);
+    size_t oWT = take(off, sizeof(bf) * (size_t)2 * nP * L * m->KgMax);
+    size_t oR = take(off, sizeof(bf) * (size_t)2 * Q * L * m->KpMax);
+    size_t oWd = take(off, sizeof(double) * (size_t)m->s1 * nG * 2 * nP);
+    size_t oZp = take(off, m->s2 > 1 ? sizeof(double) * (size_t)m->s2 * nG * 2 * Q : 0);
+    size_t oGd = take(off, sizeof(double) * (size_t)m->s3 * 2 * nP * 2 * nP);
+    size_t oE = take(off, sizeof(int));
+    size_t oZ = take(off, sizeof(double) * (size_t)2 * nG * Q);
+    size_t oeV = take(off, sizeof(int) * (size_t)nG);
+    size_t oeS = take(off, sizeof(int) * (size_t)2 * nP);
+    size_t oeWr = take(off, sizeof(int) * (size_t)nG);
+    size_t oeWc = take(off, sizeof(int) * (size_t)2 * nP);
+    size_t oeR = take(off, sizeof(int) * (size_t)2 * Q);
+    size_t omWr = take(off, sizeof(unsigned) * (size_t)nG);
+    size_t omWc = take(off, sizeof(unsigned) * (size_t)2 * nP);
+    if (base) {
+      m->VxB = (bf*)(base + oV);
+      m->SxA = (bf*)(base + oS);
+      m->WxA = (bf*)(base + oW);
+      m->WTxB = (bf*)(base + oWT);
+      m->RxB = (bf*)(base + oR);
+      m->Wd = (double*)(base + oWd);
+      m->Zp = m->s2 > 1 ? (double*)(base + oZp) : nullptr;
+      m->Gd = (double*)(base + oGd);
+      m->err = (int*)(base + oE);
+      m->Zd = (double*)(base + oZ);
+      m->eV = (int*)(base + oeV);
+      m->eS = (int*)(base + oeS);
+      m->eWr = (int*)(base + oeWr);
+      m->eWc = (int*)(base + oeWc);
+      m->eR = (int*)(base + oeR);
+      m->mWr = (unsigned*)(base + omWr);
+      m->mWc = (unsigned*)(base + omWc);
+    }
+    return off;
+  }
   // W = V S: in a batch one N tile of 256 covers all pairs (2P <= 156 for 12
   // orbitals), so the large V operand streams once per trajectory
   m->bn1 = (c->nb > 1 && 2 * nP <= 256) ? 256 : tc_tile_n(2 * nP);
@@ -292,7 +559,6 @@ size_t mixed_layout(cgpu_ctx* c, char* base, size_t off) {
   m->s1 = tc_split_count(nG, 2 * nP, m->bn1, T * m->KgMax / 64, c->nb);
   m->s2 = tc_split_count(nG, 2 * Q, m->bn2, T * m->KpMax / 64, c->nb);
   m->s3 = tc_split_count(2 * nP, 2 * nP, m->bn3, T * m->KgMax / 64, c->nb);
-  typedef __nv_bfloat16 bf;
   size_t oV = take(off, sizeof(bf) * (size_t)nG * T * m->KgMax);
   size_t oS = take(off, sizeof(bf) * (size_t)2 * nP * T * m->KgMax);
   size_t oW = take(off, sizeof(bf) * (size_t)nG * T * m->KpMax);
@@ -329,7 +595,14 @@ void mixed_init(cgpu_ctx* c) {
   if (!m) return;
   int T = m->terms, pG = T * m->KgMax, pP = T * m->KpMax;
   size_t nGK = (size_t)c->nG * m->KgMax;
-  k_split_V<<<bgrid(c, ew_blocks(c, nGK)), 256, 0, c->stream>>>(m->VxB, c->Vint_d, m->KgMax, T, TRAJ_PASS(c));
+  if (m->fxL == 5)
+    k_fx_split_V<5><<<dim3(c->nG, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(m->VxB, m->eV, c->Vint_d,
+                                                                                        m->KgMax, TRAJ_PASS(c));
+  else if (m->fxL == 6)
+    k_fx_split_V<6><<<dim3(c->nG, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(m->VxB, m->eV, c->Vint_d,
+                                                                                        m->KgMax, TRAJ_PASS(c));
+  else
+    k_split_V<<<bgrid(c, ew_blocks(c, nGK)), 256, 0, c->stream>>>(m->VxB, c->Vint_d, m->KgMax, T, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
   int P2 = 2 * c->nPairs, Q2 = 2 * c->nOS * c->nOS;
   m->mV = tc_make_map(c, m->VxB, c->nG, pG, 128);
@@ -348,6 +621,54 @@ int mixed_error(cgpu_ctx* c) {
   return e;
 }
 
+// The fixed-point form of the three contractions (L digit slices).
+template <int L>
+void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
+  MixedBufs* m = c->mixed;
+  const int nG = c->nG, nP = c->nPairs, n = c->nOS, Q = n * n;
+  z_t* Z = (z_t*)m->Zd;
+  {
+    ProfScope prof(c, CGPU_KERNEL_PAIR_POTENTIALS);
+    k_fx_split_S<L><<<dim3(2 * nP, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(
+        m->SxA, m->eS, m->mWr, m->mWc, orbs, c->w_d, c->pairL_d, c->pairK_d, m->KgMax, TRAJ_PASS(c));
+    CODY_LAUNCHED(c);
+    const bool one = m->s1 == 1;
+    fx_gemm(c, L, TC_GEMM_W, m->mV, m->mS, m->bn1, m->Wd, m->eV, m->eS, one ? m->mWr : nullptr,
+            one ? m->mWc : nullptr, m->KgMax, m->s1, nG, 2 * nP, m->err);
+    if (!one) {
+      k_fx_reduce_W<<<bgrid(c, ew_blocks(c, (size_t)nG * 2 * nP)), 256, 0, c->stream>>>(m->Wd, m->mWr, m->mWc, m->s1,
+                                                                                     TRAJ_PASS(c));
+      CODY_LAUNCHED(c);
+    }
+    dim3 gw(ceil_div(m->KgMax, SW_T), ceil_div(m->KpMax, SW_T), c->nb);
+    k_fx_split_W<L><<<gw, 256, 0, c->stream>>>(m->WxA, m->WTxB, m->eWr, m->eWc, m->Wd, m->mWr, m->mWc, m->KpMax,
+                                               m->KgMax, TRAJ_PASS(c));
+    CODY_LAUNCHED(c);
+  }
+  {
+    ProfScope prof(c, CGPU_KERNEL_CORRELATION);
+    k_fx_split_R<L><<<dim3(2 * Q, 1, c->nb), 64, sizeof(double) * m->KpMax, c->stream>>>(
+        m->RxB, m->eR, c->Rp_d, c->pairL_d, c->pairK_d, m->KpMax, TRAJ_PASS(c));
+    CODY_LAUNCHED(c);
+    fx_gemm(c, L, TC_GEMM_Z, m->mW, m->mR, m->bn2, m->s2 > 1 ? m->Zp : m->Zd, m->eWr, m->eR, nullptr, nullptr,
+            m->KpMax, m->s2, nG, 2 * Q, m->err);
+    if (m->s2 > 1) {
+      k_reduce_Z<<<bgrid(c, ew_blocks(c, (size_t)nG * Q)), 256, 0, c->stream>>>(Z, m->Zp, m->s2, TRAJ_PASS(c));
+      CODY_LAUNCHED(c);
+    }
+    launch_corr_epilogue(c, dOrbs, orbs, Z);
+  }
+  if (wantH2) {
+    ProfScope prof(c, CGPU_KERNEL_H2);
+    fx_gemm(c, L, TC_GEMM_H2, m->mSasB, m->mWT, m->bn3, m->Gd, m->eS, m->eWc, nullptr, nullptr, m->KgMax, m->s3,
+            2 * nP, 2 * nP, m->err);
+    k_reduce_H2<<<bgrid(c, ew_blocks(c, (size_t)Q * Q)), 256, 0, c->stream>>>(c->h2s_d, m->Gd, m->s3, c->pidx_d,
+                                                                        TRAJ_PASS(c));
+    CODY_LAUNCHED(c);
+    launch_h2_layout(c);
+  }
+}
+
 // ApplyCorrelationOp in the mixed form: dOrbs += rho^-1 rho2 W phi; h2 (FP64 nO^4) when wantH2.
 void launch_correlation_mixed(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   launch_rdm_inverse(c);
@@ -357,6 +678,8 @@ void launch_correlation_mixed(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int want
   }
   MixedBufs* m = c->mixed;
   int nG = c->nG, nP = c->nPairs, n = c->nOS, Q = n * n, T = m->terms;
+  if (m->fxL == 5) return correlation_fx<5>(c, dOrbs, orbs, wantH2);
+  if (m->fxL == 6) return correlation_fx<6>(c, dOrbs, orbs, wantH2);
   {
     ProfScope prof(c, CGPU_KERNEL_PAIR_POTENTIALS);
     k_split_S<<<bgrid(c, ew_blocks(c, (size_t)2 * nP * m->KgMax)), 256, 0, c->stream>>>(

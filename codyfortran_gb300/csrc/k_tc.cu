@@ -28,85 +28,7 @@
 
 namespace {
 
-constexpr int TC_BM = 128;
-constexpr int TC_BK = 64;  // bf16 elements per 128-byte swizzle row
-constexpr long long TC_WAIT_CYCLES = 4000000000LL;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait: false when the limit expires or another role aborted.
-__device__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abortFlag) {
-  long long t0 = clock64();
-  while (!mbar_test(bar, parity)) {
-    if (*abortFlag) return false;
-    if (clock64() - t0 > TC_WAIT_CYCLES) return false;
-    __nanosleep(32);
-  }
-  return true;
-}
-
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
-                                            int c2) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
-          "r"(smem_u32(dst)),
-      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
-      : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of 1024 bytes.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
-
-__device__ __forceinline__ void umma_bf16(uint32_t tmemD, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                          uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-          tmemD),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-
-#define TMEM_LD_X16(taddr, r)                                                                                  \
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, " \
-               "[%16];"                                                                                        \
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),            \
-                 "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),        \
-                 "=r"(r[14]), "=r"(r[15])                                                                      \
-               : "r"(taddr))
-
-// Per-trajectory sizes of a contraction: M rows of A, N rows of B, K tiles per segment.
-__device__ __forceinline__ void tc_dims(const TrajShape& S, int gemmId, int& M, int& N, int& segTiles) {
-  int P2 = 2 * S.nPairs, Q2 = 2 * S.nOS * S.nOS;
-  if (gemmId == TC_GEMM_W) { M = S.nG; N = P2; segTiles = S.Kg / TC_BK; }
-  else if (gemmId == TC_GEMM_Z) { M = S.nG; N = Q2; segTiles = S.Kp / TC_BK; }
-  else { M = P2; N = P2; segTiles = S.Kg / TC_BK; }
-}
+using namespace tcdev;
 
 // P[traj][z][m][n] = sum_{k in split z} A[m][k] B[n][k]; A rows m0.., B rows n0.., bf16 K-major.
 // blockIdx.z = trajectory * nSplit + split.  K tile i of the trajectory lies in
@@ -235,6 +157,7 @@ __global__ void __launch_bounds__(128, 1)
   // drain TMA copies that were issued but never consumed (only after an abort)
   if (warp == 0 && lane == 0 && abortFlag) {
     volatile int dummy = 0;
+    mbar_wait(&doneBar, 0, &dummy);  // the issued MMAs finish before the tensor memory is freed
     for (int i = consumed; i < issued; i++) {
       int s = i % STAGES, r = i / STAGES;
       mbar_wait(&fullBar[s], r & 1, &dummy);

@@ -20,3 +20,101 @@ CUtensorMap tc_make_map(const cgpu_ctx* c, const __nv_bfloat16* base, int rowsMa
 // segPitch elements each (the valid K of a segment is the trajectory's padded K).
 void tc_gemm(cgpu_ctx* c, int gemmId, const CUtensorMap& ta, const CUtensorMap& tb, int bn, float* P, int terms,
              int segPitch, int nSplit, int Mmax, int Nmax, int* err);
+
+// Fixed-point slice GEMM (k_fx.cu): out[traj][split][M][N] (FP64) = A B^T for
+// operands carried as L digit slices (K segments of segPitch elements) with
+// row exponents expA / expB; maxRow / maxCol (unsplit K only) receive the
+// largest biased exponent of |C| per row / column.
+void fx_gemm(cgpu_ctx* c, int L, int gemmId, const CUtensorMap& ta, const CUtensorMap& tb, int bn, double* out,
+             const int* expA, const int* expB, unsigned* maxRow, unsigned* maxCol, int segPitch, int nSplit, int Mmax,
+             int Nmax, int* err);
+// N-tile width of the fixed-point GEMM for N output columns and L slices (L * BN <= 512 TMEM columns).
+int fx_tile_n(int N, int L);
+// K splits of the fixed-point GEMM: about one wave of 152 SMs, at most 4096 K per split.
+int fx_split_count(int M, int N, int BN, int kTiles, int nb);
+
+// ---- device helpers shared by the tcgen05 kernels (TMA, mbarriers, MMA, TMEM) ----
+namespace tcdev {
+
+constexpr int TC_BM = 128;
+constexpr int TC_BK = 64;  // bf16 elements per 128-byte swizzle row
+constexpr long long TC_WAIT_CYCLES = 4000000000LL;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false when the limit expires or another role aborted.
+__device__ inline bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abortFlag) {
+  long long t0 = clock64();
+  while (!mbar_test(bar, parity)) {
+    if (*abortFlag) return false;
+    if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+    __nanosleep(32);
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
+                                            int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of 1024 bytes.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmemD, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmemD),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+#define TMEM_LD_X16(taddr, r)                                                                                  \
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, " \
+               "[%16];"                                                                                        \
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),            \
+                 "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),        \
+                 "=r"(r[14]), "=r"(r[15])                                                                      \
+               : "r"(taddr))
+
+// Per-trajectory sizes of a contraction: M rows of A, N rows of B, K tiles per segment.
+__device__ __forceinline__ void tc_dims(const TrajShape& S, int gemmId, int& M, int& N, int& segTiles) {
+  int P2 = 2 * S.nPairs, Q2 = 2 * S.nOS * S.nOS;
+  if (gemmId == TC_GEMM_W) { M = S.nG; N = P2; segTiles = S.Kg / TC_BK; }
+  else if (gemmId == TC_GEMM_Z) { M = S.nG; N = Q2; segTiles = S.Kp / TC_BK; }
+  else { M = P2; N = P2; segTiles = S.Kg / TC_BK; }
+}
+
+
+}  // namespace tcdev

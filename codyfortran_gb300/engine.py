@@ -61,6 +61,7 @@ class CgpuDesc(C.Structure):
         ("laser_n_cycles", C.c_double), ("laser_cep", C.c_double), ("laser_t_start", C.c_double),
         ("field_samples", C.POINTER(C.c_double)), ("n_field_samples", C.c_int), ("field_dt", C.c_double),
         ("field_t0", C.c_double), ("method", C.c_int), ("precision", C.c_int), ("max_krylov", C.c_int),
+        ("krylov_window", C.c_int),
     ]
 
 
@@ -102,7 +103,7 @@ def _d(v):
     return C.c_double(float(v))
 
 
-def make_desc(spec: SystemSpec, precision: str = "fp64", max_krylov: int = 32):
+def make_desc(spec: SystemSpec, precision: str = "fp64", max_krylov: int = 32, krylov_window: int = 0):
     d = CgpuDesc()
     d.grid_kind = 0 if spec.grid_kind == "const" else 1
     d.xmin, d.xmax = spec.xmin, spec.xmax
@@ -133,18 +134,19 @@ def make_desc(spec: SystemSpec, precision: str = "fp64", max_krylov: int = 32):
         d.n_field_samples = len(keep)
         d.field_dt, d.field_t0 = L.sample_dt, L.sample_t0
     d.method = 1 if spec.method == "tdci" else 0
-    d.precision = {"fp64": 0, "mixed": 1, "mixed6": 2}[precision]
+    d.precision = {"fp64": 0, "mixed": 1, "mixed6": 2, "mixed_fx": 3, "mixed_fx6": 4}[precision]
     d.max_krylov = max_krylov
+    d.krylov_window = int(krylov_window)
     return d, keep
 
 
 class Engine:
     """The GB300 MCTDHX/TDCI engine for one system (one cgpu_ctx, one CUDA stream)."""
 
-    def __init__(self, spec: SystemSpec, precision: str = "fp64", max_krylov: int = 32):
+    def __init__(self, spec: SystemSpec, precision: str = "fp64", max_krylov: int = 32, krylov_window: int = 0):
         self.lib = load_library()
         self.spec = spec
-        desc, self._keep = make_desc(spec, precision, max_krylov)
+        desc, self._keep = make_desc(spec, precision, max_krylov, krylov_window)
         h = C.c_void_p()
         rc = self.lib.cgpu_ctx_create(C.byref(desc), C.byref(h))
         if rc != 0:
@@ -421,14 +423,14 @@ class Batch:
     of the step covers all systems in one launch, one CUDA-graph launch per
     time step (cgpu_batch_propagate)."""
 
-    def __init__(self, specs, precision: str = "fp64", max_krylov: int = 32):
+    def __init__(self, specs, precision: str = "fp64", max_krylov: int = 32, krylov_window: int = 0):
         self.lib = load_library()
         self.specs = list(specs)
         n = len(self.specs)
         descs = (CgpuDesc * n)()
         self._keep = []
         for i, sp in enumerate(self.specs):
-            d, keep = make_desc(sp, precision, max_krylov)
+            d, keep = make_desc(sp, precision, max_krylov, krylov_window)
             descs[i] = d
             self._keep.append(keep)
         h = C.c_void_p()

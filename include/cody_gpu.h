@@ -52,6 +52,13 @@ extern "C" {
 #define CGPU_PREC_MIXED 1
 /* As CGPU_PREC_MIXED with three-way split operands (hi + mid + lo, six products). */
 #define CGPU_PREC_MIXED_X6 2
+/* Fixed-point split form: every operand row carried as 5 base-64 digit slices under one
+ * power of two per row (30 bits of the row maximum), slice products of one level summed
+ * exactly in their own FP32 tensor-memory accumulator, levels combined in 64-bit integers:
+ * the contractions equal the products of the truncated operands; 15 products. */
+#define CGPU_PREC_MIXED_FX 3
+/* As CGPU_PREC_MIXED_FX with 6 slices (36 bits, 21 products). */
+#define CGPU_PREC_MIXED_FX6 4
 
 /* Time-derivative selectors (the TimeDerivative procedure pointers). */
 #define CGPU_TD_FULL 0   /* Method_TimeDerivative (Mctdhx :101-149)                        */
@@ -93,6 +100,10 @@ typedef struct {
   int method;                    /* CGPU_METHOD_*                                            */
   int precision;                 /* CGPU_PREC_*                                              */
   int max_krylov;                /* largest Krylov dimension the context will be asked for   */
+  int krylov_window;             /* 0: each Lanczos vector is orthogonalised against the whole
+                                    basis (the reference's loop); k > 0: against the last k basis
+                                    vectors only (k = 2: the three-term recurrence); the same for
+                                    every trajectory of a batch                                 */
 } cgpu_desc;
 
 /* ---- context (Fabricate + Setup) ---------------------------------------- */

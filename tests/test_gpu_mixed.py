@@ -1,9 +1,12 @@
-"""Mixed-precision form: tcgen05 split-bf16 contractions against the FP64 oracle.
+"""Mixed-precision forms: tcgen05 split contractions against the FP64 oracle.
 
-Tolerances state the accuracy of the split: bf16x3 (hi + lo operands, three
-products, FP32 accumulation) and bf16x6 (hi + mid + lo, six products).  The
-relative errors measured here are what the form delivers; the propagation
-check compares energy and norm of a mixed trajectory with the FP64 one.
+Tolerances state the accuracy of each form: bf16x3 (hi + lo operands, three
+products, FP32 accumulation), bf16x6 (hi + mid + lo, six products), and the
+fixed-point forms mixed_fx / mixed_fx6 (5 / 6 base-64 digit slices per
+operand row, exact per-level accumulation: only the 30 / 36-bit operand
+truncation remains).  The relative errors measured here are what the forms
+deliver; the propagation check compares energy and norm of a mixed
+trajectory with the FP64 one.
 """
 import numpy as np
 import pytest
@@ -14,7 +17,8 @@ from codyfortran_gb300 import spec as S
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"mixed": 2e-4, "mixed6": 2e-6}
+TOL = {"mixed": 2e-4, "mixed6": 2e-6, "mixed_fx": 1e-7, "mixed_fx6": 1e-9}
+PRECISIONS = ["mixed", "mixed6", "mixed_fx", "mixed_fx6"]
 
 
 def rel(a, b):
@@ -38,7 +42,7 @@ def _state(sp, o, seed):
     return c, orbs, I.pack_state(c, orbs)
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed6"])
+@pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("name", ["helium_restricted", "single_body_type"])
 def test_mixed_correlation_and_nonlin(name, precision):
     from codyfortran_gb300.engine import Engine
@@ -49,13 +53,14 @@ def test_mixed_correlation_and_nonlin(name, precision):
     r1, r2 = o.rdm1(c), o.rdm2(c)
     d_gpu, h2_gpu = e.apply_correlation_op(orbs, r1, r2, 0.0)
     d_orc, h2_orc = o.apply_correlation_op(orbs, r1, r2, 0.0)
+    print(f"{name} {precision}: correlation {rel(d_gpu, d_orc):.3e}, h2 {rel(h2_gpu, h2_orc):.3e}")
     assert rel(d_gpu, d_orc) < TOL[precision]
     assert rel(h2_gpu, h2_orc) < TOL[precision]
     assert rel(e.time_derivative(st, 1.5, "nonlin"), o.time_derivative(st, 1.5, "nonlin")) < TOL[precision]
     e.close()
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed6"])
+@pytest.mark.parametrize("precision", PRECISIONS)
 def test_mixed_nonlin_full_size(precision):
     """2801 points, 16 orbitals (136 pairs), 8008 determinants."""
     from codyfortran_gb300.engine import Engine
@@ -71,7 +76,7 @@ def test_mixed_nonlin_full_size(precision):
     e.close()
 
 
-@pytest.mark.parametrize("precision", ["mixed", "mixed6"])
+@pytest.mark.parametrize("precision", PRECISIONS)
 def test_mixed_trajectory_energy_norm(precision):
     """Energy and norm of a mixed-precision trajectory against the FP64 GPU trajectory."""
     from codyfortran_gb300.engine import Engine
@@ -93,7 +98,7 @@ def test_mixed_trajectory_energy_norm(precision):
     de, dn = abs(em - ef) / abs(ef), abs(nm - nf)
     print(f"{precision}: {n_steps} steps, |dE|/|E| = {de:.3e}, |d norm| = {dn:.3e}")
     # measured on GB300: bf16x3 |dE|/|E| ~ 2e-6, |d norm| ~ 1e-7 over these 200 steps
-    lim = {"mixed": (1e-5, 1e-6), "mixed6": (2e-6, 2e-7)}[precision]
+    lim = {"mixed": (1e-5, 1e-6), "mixed6": (2e-6, 2e-7), "mixed_fx": (1e-8, 1e-9), "mixed_fx6": (1e-9, 1e-10)}[precision]
     assert de < lim[0] and dn < lim[1]
     f.close()
     m.close()
