@@ -361,6 +361,41 @@ void put(cgpu_ctx* c, int b, T* dst0, const std::vector<T>& v) {
   CODY_CUDA(cudaMemcpy((char*)dst0 + (size_t)b * c->bs, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
 }
 
+// Fixed-point form of a batch: when every trajectory has the same dense
+// interaction and its grid is a contiguous, bitwise-equal piece of the largest
+// grid (FEDVR boxes of different length with the same elements), every
+// interaction matrix is a principal block of the largest one; the contraction
+// W = V S then reads one shared set of V slices (resident in L2) at the
+// trajectory's row offset.
+void detect_shared_interaction(cgpu_ctx* c) {
+  c->fxShared = 0;
+  c->fxVRow.assign(c->sys.size(), 0);
+  c->fxKgMax = (c->nG + 63) / 64 * 64;
+  const bool fx = c->precision == CGPU_PREC_MIXED_FX || c->precision == CGPU_PREC_MIXED_FX6;
+  if (!fx || !c->hasInteraction || c->sys.size() < 2) return;
+  int big = 0;
+  for (size_t b = 0; b < c->sys.size(); b++)
+    if (c->sys[b].nG > c->sys[big].nG) big = (int)b;
+  const SysHost& B = c->sys[big];
+  std::vector<int> rows(c->sys.size(), 0);
+  int kgMax = 0;
+  for (size_t b = 0; b < c->sys.size(); b++) {
+    const SysHost& s = c->sys[b];
+    if (s.intToeplitz || B.intToeplitz || s.intS != B.intS || s.intS1 != B.intS1 || s.intS2 != B.intS2 ||
+        s.intDamp != B.intDamp || s.nG < 1)
+      return;
+    auto it = std::lower_bound(B.x.begin(), B.x.end(), s.x[0]);
+    size_t off = (size_t)(it - B.x.begin());
+    if (off + (size_t)s.nG > B.x.size() || std::memcmp(&B.x[off], s.x.data(), sizeof(double) * s.nG) != 0) return;
+    rows[b] = (int)off;
+    kgMax = std::max(kgMax, ((int)off % 64 + s.nG + 63) / 64 * 64);
+  }
+  c->fxShared = 1;
+  c->fxBig = big;
+  c->fxVRow = rows;
+  c->fxKgMax = kgMax;
+}
+
 void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
   const cgpu_desc* d0 = &descs[0];
   if (d0->n_body_types < 1 || d0->n_body_types > CODY_MAX_BT) throw std::string("method.mb.nBodyTypes out of range");
@@ -394,6 +429,7 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
     if (descs[b].krylov_window != c->krylovWindow || descs[b].krylov_window < 0)
       throw std::string("krylov_window must be >= 0 and the same for every trajectory of a batch");
   c->nGO = nGO;
+  detect_shared_interaction(c);
   ci_build_work(c);
   c->nS = (c->method == CGPU_METHOD_TDCI) ? c->nC : c->nC + nGO;
   c->minS = minS;
@@ -467,7 +503,9 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
       t.grpStart[g] = c->restricted ? 0 : s.orbStart[g];
       t.grpSize[g] = c->restricted ? s.nOS : s.nOrbs[g];
     }
-    t.Kg = (s.nG + 63) / 64 * 64;
+    t.vRow = c->fxShared ? c->fxVRow[b] : 0;
+    t.gShift = t.vRow % 64;
+    t.Kg = (t.gShift + s.nG + 63) / 64 * 64;
     t.Kp = (2 * s.nPairs + 63) / 64 * 64;
     t.regEps = s.regEps;
     t.laser = LaserDev{s.laserKind, s.E0, s.omega, s.nCycles, s.cep, s.tStart, s.sampleDt, s.sampleT0,

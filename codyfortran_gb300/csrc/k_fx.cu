@@ -2,30 +2,35 @@
 // of the contractions of ApplyCorrelationOp,
 // src/Method/Mb/OrbBased/S_Method_Mb_OrbBased.f90:647-872).
 //
-// An FP64 operand row x[0..K) is carried as L slices of base-64 digits under
+// An FP64 operand row x[0..K) is carried as L slices of base-2^b digits under
 // one power of two per row:
-//     x[k] ~= 2^e sum_{i<L} d_i[k] 64^-(i+1),   max_k |x[k]| < 2^e,
-//     d_0 in [-64, 64], d_i in [-32, 31] for i > 0 (bf16 holds them exactly),
-// i.e. x rounded to 6L fractional bits of its row maximum.  The product of an
+//     x[k] ~= 2^e sum_{i<L} d_i[k] 2^(-b(i+1)),   max_k |x[k]| < 2^e,
+//     |d_0| <= 2^b, d_i in [-2^(b-1), 2^(b-1)) for i > 0 (bf16 holds them exactly, b <= 8),
+// i.e. x rounded to bL fractional bits of its row maximum.  The product of an
 // A row and a B row splits into levels l = i + j:
-//     C = 2^(ea + eb) sum_l 64^-(l+2) D_l,   D_l = sum_{i+j=l} sum_k a_i[k] b_j[k].
+//     C = 2^(ea + eb) sum_l 2^(-b(l+2)) D_l,   D_l = sum_{i+j=l} sum_k a_i[k] b_j[k].
 // Each level has its own FP32 accumulator in tensor memory (L accumulators of
 // BN columns), fed by the slice products of that level.  A slice product is
-// an integer of magnitude <= 2^12, so D_0 and D_1 stay below 2^24 -- exact in
-// FP32 -- for K <= 4096, and D_2 for K <= 3276; a higher level that passes
-// 2^24 rounds by 2^-24 of a term at least 2^-18 below the result's scale.
-// The epilogue combines the levels in 64-bit integers (Horner in base 64),
-// converts once to FP64 and applies the power-of-two scale, so C is the
-// product of the truncated operands whatever the summation order.  Levels
-// l >= L are not formed; with the operand truncation (2^-(6L+1) of each row
-// maximum) they bound the error at about 2^-6L max|a| max|b| K.
+// an integer of magnitude <= 2^2b, so D_0 and D_1 stay below 2^24 -- exact in
+// FP32 -- for K <= 2^(24-2b) (b = 6: K <= 4096, 7: 1024, 8: 256) and D_2 for
+// K <= 0.8 2^(24-2b); a higher level that passes 2^24 rounds by 2^-24 of a
+// term at least 2^-2b below the result's scale.  The epilogue combines the
+// levels in 64-bit integers (Horner in base 2^b), converts once to FP64 and
+// applies the power-of-two scale, so C is the product of the truncated
+// operands whatever the summation order.  Levels l >= L are not formed; with
+// the operand truncation (2^-(bL+1) of each row maximum) they bound the error
+// at about 2^-bL max|a| max|b| K.
 //
 // Pipeline: one TMA producer thread, one MMA issuer thread, four epilogue
 // warps.  Per 64-wide K block the producer loads the L slices of the B tile
 // into one ring stage and the L slices of the A tile into L stages of a
 // second ring; the issuer runs the L(L+1)/2 slice products of the block from
-// shared memory.  Every wait is bounded: on expiry the kernel sets an error
-// flag, drains its copies, frees its tensor memory and returns.
+// shared memory with the MMA width cut to the trajectory's own N.  The
+// epilogue stages the FP64 tile in shared memory for coalesced stores.  The
+// wide configuration (two B stages, deep A ring) holds one CTA per SM; the
+// compact one (one B stage, L A stages, <= 256 TMEM columns) two.  Every wait
+// is bounded: on expiry the kernel sets an error flag, drains its copies,
+// frees its tensor memory and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -38,21 +43,26 @@ namespace {
 
 using namespace tcdev;
 
-constexpr int FX_NB = 2;  // B ring stages (L slices each)
 constexpr int FX_SMEM_MAX = 232448;
 
-template <int BN, int L>
+template <int BN, int L, int NA_, int NB_>
 struct FxCfg {
   static constexpr int A_BYTES = TC_BM * TC_BK * 2;
   static constexpr int B_BYTES = BN * TC_BK * 2;
   static constexpr int BG_BYTES = L * B_BYTES;
-  static constexpr int NA = std::min(8, (FX_SMEM_MAX - 2048 - FX_NB * BG_BYTES) / A_BYTES);
-  static constexpr int SMEM = NA * A_BYTES + FX_NB * BG_BYTES + 1024;
+  static constexpr int NB = NB_;
+  // NA_ == 0: as many A stages as fit (at most 8)
+  static constexpr int NA = NA_ > 0 ? NA_ : std::min(8, (FX_SMEM_MAX - 2048 - NB * BG_BYTES) / A_BYTES);
+  static constexpr int RING = NA * A_BYTES + NB * BG_BYTES;
+  static constexpr int SMEM = RING + 1024;
+  static constexpr int SP = BN + 1;  // staged output row pitch (doubles)
   static constexpr uint32_t TMEM_COLS = (L * BN) <= 32 ? 32 : (L * BN) <= 64 ? 64 : (L * BN) <= 128 ? 128
                                         : (L * BN) <= 256 ? 256 : 512;
   static_assert(L * BN <= 512, "tensor memory holds 512 columns");
   static_assert(BN % 16 == 0 && BN >= 16, "N tile: multiple of 16");
-  static_assert(NA >= 2, "shared memory");
+  static_assert(NA >= 2 || NA >= L, "A ring");
+  static_assert(SMEM + 2048 <= FX_SMEM_MAX, "shared memory");
+  static_assert(TC_BM * SP * 8 <= RING, "output staging fits the ring");
 };
 
 // 2^e as a double (exact).
@@ -63,18 +73,21 @@ __device__ __forceinline__ double pow2i(int e) {
 
 // out[traj][split][M][N] = C (FP64).  maxRow/maxCol (nSplit == 1 only): the
 // largest biased exponent of |C| per output row / column, by atomicMax.
-template <int BN, int L>
-__global__ void __launch_bounds__(128, 1)
+// aShared: A is one matrix for all trajectories (3D map with one plane); the
+// trajectory's rows start at its vRow and its K range at vRow - gShift.
+template <int BN, int L, int NA_, int NB_>
+__global__ void __launch_bounds__(128)
     k_fx_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, double* __restrict__ out,
               const int* __restrict__ expA, const int* __restrict__ expB, unsigned* __restrict__ maxRow,
-              unsigned* __restrict__ maxCol, TRAJ_ARGS, int gemmId, int segPitch, int nSplit, int* __restrict__ err) {
-  using C = FxCfg<BN, L>;
-  constexpr int NA = C::NA;
+              unsigned* __restrict__ maxCol, TRAJ_ARGS, int gemmId, int segPitchA, int segPitch, int aShared,
+              int nSplit, int digitBits, int* __restrict__ err) {
+  using C = FxCfg<BN, L, NA_, NB_>;
+  constexpr int NA = C::NA, NB = C::NB;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* ringA = smem;
   uint8_t* ringB = smem + NA * C::A_BYTES;
-  __shared__ __align__(8) uint64_t aFull[NA], aEmpty[NA], bFull[FX_NB], bEmpty[FX_NB], doneBar;
+  __shared__ __align__(8) uint64_t aFull[NA], aEmpty[NA], bFull[NB], bEmpty[NB], doneBar;
   __shared__ uint32_t tmemSlot;
   __shared__ volatile int abortFlag;
   __shared__ int consumedA, consumedB;
@@ -85,6 +98,7 @@ __global__ void __launch_bounds__(128, 1)
   tc_dims(shp[traj], gemmId, M, N, segTiles);
   const int n0 = blockIdx.x * BN, m0 = blockIdx.y * TC_BM;
   if (m0 >= M || n0 >= N) return;
+  const int nT = min(BN, (N - n0 + 15) / 16 * 16);  // MMA width for this trajectory's columns
   const int per = (segTiles + nSplit - 1) / nSplit;
   const int kt0 = split * per;
   const int nk = max(0, min(segTiles, kt0 + per) - kt0);
@@ -96,7 +110,11 @@ __global__ void __launch_bounds__(128, 1)
     }
     return;
   }
-  expA = batn(expA, bs, traj);  // blockIdx.z also carries the split: index by trajectory
+  // blockIdx.z also carries the split: index by trajectory
+  const int aRow0 = aShared ? shp[traj].vRow : 0;
+  const int aCol0 = aShared ? shp[traj].vRow - shp[traj].gShift : 0;
+  const int aZ = aShared ? 0 : traj;
+  expA = aShared ? expA + aRow0 : batn(expA, bs, traj);
   expB = batn(expB, bs, traj);
 
   if (threadIdx.x == 0) {
@@ -107,7 +125,7 @@ __global__ void __launch_bounds__(128, 1)
       mbar_init(&aFull[s], 1);
       mbar_init(&aEmpty[s], 1);
     }
-    for (int s = 0; s < FX_NB; s++) {
+    for (int s = 0; s < NB; s++) {
       mbar_init(&bFull[s], 1);
       mbar_init(&bEmpty[s], 1);
     }
@@ -129,7 +147,7 @@ __global__ void __launch_bounds__(128, 1)
   if (warp == 0 && lane == 0) {
     // TMA producer: per K block the L B slices (one stage), then the L A slices
     for (int kb = 0; kb < nk && !abortFlag; kb++) {
-      const int sb = kb % FX_NB, rb = kb / FX_NB;
+      const int sb = kb % NB, rb = kb / NB;
       if (!mbar_wait(&bEmpty[sb], (rb & 1) ^ 1, &abortFlag)) {
         abortFlag = 1;
         atomicExch(err, 11);
@@ -148,18 +166,18 @@ __global__ void __launch_bounds__(128, 1)
           break;
         }
         mbar_expect_tx(&aFull[sa], C::A_BYTES);
-        tma_load_3d(ringA + sa * C::A_BYTES, &tA, &aFull[sa], i * segPitch + x0, m0, traj);
+        tma_load_3d(ringA + sa * C::A_BYTES, &tA, &aFull[sa], i * segPitchA + aCol0 + x0, aRow0 + m0, aZ);
         issuedA = t + 1;
       }
     }
   } else if (warp == 1 && lane == 0) {
-    // MMA issuer: kind::f16, D=F32, A=B=BF16, K-major, N=BN, M=128
-    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+    // MMA issuer: kind::f16, D=F32, A=B=BF16, K-major, N=nT, M=128
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nT >> 3) << 17) |
                            ((uint32_t)(TC_BM >> 4) << 24);
     int ca = 0, kb = 0;
     bool ok = true;
     for (; kb < nk && ok; kb++) {
-      const int sb = kb % FX_NB, rb = kb / FX_NB;
+      const int sb = kb % NB, rb = kb / NB;
       if (!mbar_wait(&bFull[sb], rb & 1, &abortFlag)) {
         abortFlag = 1;
         atomicExch(err, 13);
@@ -197,42 +215,57 @@ __global__ void __launch_bounds__(128, 1)
     umma_commit(&doneBar);
   }
   __syncwarp();
-  bool ok = mbar_wait(&doneBar, 0, &abortFlag);
-  if (!ok) atomicExch(err, 15);
+  const bool waited = mbar_wait(&doneBar, 0, &abortFlag);
+  if (!waited) atomicExch(err, 15);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  __syncwarp();
+  // every MMA has completed and every TMA copy has landed unless a wait gave up
+  const bool good = __syncthreads_and(waited) && !abortFlag;
 
-  // epilogue: warp w owns TMEM lanes [32w, 32w+32) = tile rows
-  const int row = m0 + warp * 32 + lane;
-  const bool rowOk = ok && !abortFlag && row < M;
-  const int ea = rowOk ? expA[row] - 6 * (L + 1) : 0;
-  unsigned rowMaxEx = 0;
+  if (good) {
+    // epilogue: warp w owns TMEM lanes [32w, 32w+32) = tile rows; the FP64
+    // tile goes through shared memory (the operand rings are free now)
+    double* stile = (double*)smem;
+    const int r = warp * 32 + lane, row = m0 + r;
+    const bool rowOk = row < M;
+    const int ea = rowOk ? expA[row] - digitBits * (L + 1) : 0;
+    const long long base = 1LL << digitBits;
+    unsigned rowMaxEx = 0;
 #pragma unroll 1
-  for (int c = 0; c < BN; c += 16) {
-    uint32_t acc[L][16];
+    for (int c = 0; c < nT; c += 16) {
+      uint32_t acc[L][16];
 #pragma unroll
-    for (int l = 0; l < L; l++) TMEM_LD_X16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * BN + c), acc[l]);
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      for (int l = 0; l < L; l++) TMEM_LD_X16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * BN + c), acc[l]);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < 16; j++) {
-      const int col = n0 + c + j;
-      unsigned ex = 0;
-      if (rowOk && col < N) {
-        long long T = 0;
+      for (int j = 0; j < 16; j++) {
+        const int col = n0 + c + j;
+        unsigned ex = 0;
+        double v = 0.0;
+        if (rowOk && col < N) {
+          long long T = 0;
 #pragma unroll
-        for (int l = 0; l < L; l++) T = T * 64 + (long long)__float2int_rn(__uint_as_float(acc[l][j]));
-        const double v = __ll2double_rn(T) * pow2i(ea + expB[col]);
-        Oz[(size_t)row * N + col] = v;
-        ex = (unsigned)(__double2hiint(v) >> 20) & 0x7FFu;
+          for (int l = 0; l < L; l++) T = T * base + (long long)__float2int_rn(__uint_as_float(acc[l][j]));
+          v = __ll2double_rn(T) * pow2i(ea + expB[col]);
+          ex = (unsigned)(__double2hiint(v) >> 20) & 0x7FFu;
+        }
+        stile[r * C::SP + c + j] = v;
+        if (maxCol) {
+          unsigned m = __reduce_max_sync(0xffffffffu, ex);
+          if (lane == 0 && m) atomicMax(batn(maxCol, bs, traj) + col, m);
+        }
+        rowMaxEx = max(rowMaxEx, ex);
       }
-      if (maxCol) {
-        unsigned m = __reduce_max_sync(0xffffffffu, ex);
-        if (lane == 0 && m) atomicMax(batn(maxCol, bs, traj) + col, m);
-      }
-      rowMaxEx = max(rowMaxEx, ex);
+    }
+    if (maxRow && rowOk && rowMaxEx) atomicMax(batn(maxRow, bs, traj) + row, rowMaxEx);
+    __syncthreads();
+    const int nc = min(nT, N - n0);
+    for (int rr = warp; rr < TC_BM; rr += 4) {
+      const int grow = m0 + rr;
+      if (grow >= M) break;
+      double* dst = Oz + (size_t)grow * N + n0;
+      for (int col = lane; col < nc; col += 32) dst[col] = stile[rr * C::SP + col];
     }
   }
-  if (maxRow && rowOk && rowMaxEx) atomicMax(batn(maxRow, bs, traj) + row, rowMaxEx);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   // after an abort: let the issued MMAs finish and drain the TMA copies that
@@ -241,70 +274,86 @@ __global__ void __launch_bounds__(128, 1)
     volatile int dummy = 0;
     mbar_wait(&doneBar, 0, &dummy);
     for (int t = consumedA; t < issuedA; t++) mbar_wait(&aFull[t % NA], (t / NA) & 1, &dummy);
-    for (int t = consumedB; t < issuedB; t++) mbar_wait(&bFull[t % FX_NB], (t / FX_NB) & 1, &dummy);
+    for (int t = consumedB; t < issuedB; t++) mbar_wait(&bFull[t % NB], (t / NB) & 1, &dummy);
   }
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TMEM_COLS) : "memory");
 }
 
-template <int BN, int L>
+template <int BN, int L, int NA_, int NB_>
 void launch_fx_t(cgpu_ctx* c, const CUtensorMap& ta, const CUtensorMap& tb, double* out, const int* expA,
-                 const int* expB, unsigned* maxRow, unsigned* maxCol, int gemmId, int segPitch, int nSplit, int Mmax,
-                 int Nmax, int* err) {
-  using C = FxCfg<BN, L>;
+                 const int* expB, unsigned* maxRow, unsigned* maxCol, int gemmId, int segPitchA, int segPitch,
+                 int aShared, int nSplit, int Mmax, int Nmax, int digitBits, int* err) {
+  using C = FxCfg<BN, L, NA_, NB_>;
   static bool attr = false;
   if (!attr) {
-    CODY_CUDA(cudaFuncSetAttribute(k_fx_gemm<BN, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+    CODY_CUDA(cudaFuncSetAttribute(k_fx_gemm<BN, L, NA_, NB_>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
     attr = true;
   }
   dim3 grid(ceil_div(Nmax, BN), ceil_div(Mmax, TC_BM), (unsigned)(c->nb * nSplit));
-  k_fx_gemm<BN, L><<<grid, 128, C::SMEM, c->stream>>>(ta, tb, out, expA, expB, maxRow, maxCol, TRAJ_PASS(c), gemmId,
-                                                      segPitch, nSplit, err);
+  k_fx_gemm<BN, L, NA_, NB_><<<grid, 128, C::SMEM, c->stream>>>(ta, tb, out, expA, expB, maxRow, maxCol,
+                                                                TRAJ_PASS(c), gemmId, segPitchA, segPitch, aShared,
+                                                                nSplit, digitBits, err);
   CODY_LAUNCHED(c);
 }
 
 }  // namespace
 
-int fx_tile_n(int N, int L) {
-  const int cands[] = {32, 48, 64, 80, 96};
-  int best = 32;
-  long bestCols = -1, bestTiles = 0;
-  for (int bn : cands) {
-    if (bn * L > 512) continue;
-    if (bn != 32 && bn != 64 && bn != 80 && bn != 96) continue;
-    if (L == 6 && bn == 96) continue;
-    long tiles = (N + bn - 1) / bn, cols = tiles * bn;
-    if (bestCols < 0 || cols < bestCols || (cols == bestCols && tiles < bestTiles)) {
-      best = bn;
-      bestCols = cols;
-      bestTiles = tiles;
-    }
-  }
-  return best;
+int fx_digit_bits(int K) { return K <= 256 ? 8 : K <= 1024 ? 7 : 6; }
+
+int fx_slices(int K, int targetBits) {
+  const int b = fx_digit_bits(K);
+  return (targetBits + b - 1) / b;
+}
+
+// Largest N tile of a configuration: L accumulators of BN columns in 512
+// (wide) or 256 (compact) TMEM columns, from the instantiated widths.
+static int fx_max_bn(int L, bool compact) {
+  if (compact) return L == 4 ? 64 : L == 5 ? 32 : 0;
+  return L == 4 ? 128 : L == 5 ? 96 : 80;
+}
+
+bool fx_compact_ok(int L) { return fx_max_bn(L, true) > 0; }
+
+int fx_tile_n(int N, int L, bool compact) {
+  const int widths[] = {32, 64, 80, 96, 128};
+  const int maxBn = fx_max_bn(L, compact);
+  const int tiles = (N + maxBn - 1) / maxBn;
+  const int want = ((N + tiles - 1) / tiles + 15) / 16 * 16;  // balanced tiles
+  for (int w : widths)
+    if (w >= want && w <= maxBn) return w;
+  return maxBn;
 }
 
 int fx_split_count(int M, int N, int BN, int kTiles, int nb) {
   long tiles = (long)((M + TC_BM - 1) / TC_BM) * ((N + BN - 1) / BN) * nb;
   int s = (int)std::max<long>(1, (152 + tiles - 1) / tiles);
   s = std::min(s, std::max(1, kTiles / 2));
-  s = std::max(s, (kTiles + 63) / 64);  // K per split <= 4096: the exact range of the level sums
+  s = std::max(s, (kTiles + 63) / 64);  // K per split <= 4096: the exact range of the level sums at b = 6
   int per = (kTiles + s - 1) / s;
   return (kTiles + per - 1) / per;
 }
 
-void fx_gemm(cgpu_ctx* c, int L, int gemmId, const CUtensorMap& ta, const CUtensorMap& tb, int bn, double* out,
-             const int* expA, const int* expB, unsigned* maxRow, unsigned* maxCol, int segPitch, int nSplit, int Mmax,
-             int Nmax, int* err) {
-  if (segPitch % TC_BK != 0) throw std::string("fx_gemm: segment pitch must be a multiple of 64");
+void fx_gemm(cgpu_ctx* c, int L, int digitBits, bool compact, int gemmId, const CUtensorMap& ta,
+             const CUtensorMap& tb, int bn, double* out, const int* expA, const int* expB, unsigned* maxRow,
+             unsigned* maxCol, int segPitchA, int segPitch, int aShared, int nSplit, int Mmax, int Nmax, int* err) {
+  if (segPitch % TC_BK != 0 || segPitchA % TC_BK != 0)
+    throw std::string("fx_gemm: segment pitch must be a multiple of 64");
   if (nSplit > 1 && (maxRow || maxCol)) throw std::string("fx_gemm: output maxima need an unsplit K");
-#define FX_CASE(BN_, L_)                                                                                          \
-  if (bn == BN_ && L == L_) {                                                                                     \
-    launch_fx_t<BN_, L_>(c, ta, tb, out, expA, expB, maxRow, maxCol, gemmId, segPitch, nSplit, Mmax, Nmax, err); \
-    return;                                                                                                       \
+  if (digitBits < 6 || digitBits > 8 || digitBits * L > 52) throw std::string("fx_gemm: digit width");
+#define FX_CASE(BN_, L_, NA_, NB_, CMP_)                                                                       \
+  if (bn == BN_ && L == L_ && compact == CMP_) {                                                               \
+    launch_fx_t<BN_, L_, NA_, NB_>(c, ta, tb, out, expA, expB, maxRow, maxCol, gemmId, segPitchA, segPitch,   \
+                                   aShared, nSplit, Mmax, Nmax, digitBits, err);                               \
+    return;                                                                                                    \
   }
-  FX_CASE(32, 5) FX_CASE(64, 5) FX_CASE(80, 5) FX_CASE(96, 5)
-  FX_CASE(32, 6) FX_CASE(64, 6) FX_CASE(80, 6)
+  FX_CASE(32, 4, 0, 2, false) FX_CASE(64, 4, 0, 2, false) FX_CASE(80, 4, 0, 2, false) FX_CASE(96, 4, 0, 2, false)
+  FX_CASE(128, 4, 0, 2, false)
+  FX_CASE(32, 5, 0, 2, false) FX_CASE(64, 5, 0, 2, false) FX_CASE(80, 5, 0, 2, false) FX_CASE(96, 5, 0, 2, false)
+  FX_CASE(32, 6, 0, 2, false) FX_CASE(64, 6, 0, 2, false) FX_CASE(80, 6, 0, 2, false)
+  FX_CASE(32, 4, 4, 1, true) FX_CASE(64, 4, 4, 1, true)
+  FX_CASE(32, 5, 5, 1, true)
 #undef FX_CASE
   throw std::string("fx_gemm: unsupported tile");
 }

@@ -16,10 +16,12 @@
 //   R1 = R'[(l,k), q], R2 = R'[(k,l), q] (0 when l = k).
 //
 // The fixed-point form (precision mixed_fx / mixed_fx6) carries every operand
-// row as L base-64 digit slices under one power of two per row (k_fx.cu) and
-// returns FP64 results whose only error is the operand truncation (~2^-6L of
-// each row's maximum): S and V rows for GEMM1, W rows for GEMM2, R'' rows,
-// W columns for GEMM3.  The row exponents of W come from the GEMM1 epilogue.
+// row as L base-2^b digit slices under one power of two per row (k_fx.cu) and
+// returns FP64 results whose only error is the operand truncation (about 30 /
+// 36 bits of each row's maximum): S and V rows for GEMM1, W rows for GEMM2,
+// R'' rows, W columns for GEMM3.  The digit width b follows the contraction
+// length (GEMM1/3: K = nG, GEMM2: K = 2P), the slice count L = ceil(bits / b).
+// The row exponents of W come from the GEMM1 epilogue.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -37,8 +39,16 @@ struct MixedBufs {
   int* err = nullptr;
   double* Zd = nullptr;     // (nG, Q) complex
   CUtensorMap mV, mS, mSasB, mW, mWT, mR;  // TMA maps (A operands box 128 rows, B operands box BN rows)
-  // fixed-point form (fxL > 0 slices)
-  int fxL = 0;
+  // fixed-point form (fxBits > 0): digit width / slices of the K = nG
+  // contractions (GEMM1, GEMM3) and of the K = 2P one (GEMM2)
+  int fxBits = 0, b1 = 0, L1 = 0, b2 = 0, L2 = 0;
+  bool compact2 = false;
+  // one interaction matrix for the batch (cgpu_ctx::fxShared): its slices and row
+  // exponents outside the per-trajectory arena
+  int KgBig = 0;
+  __nv_bfloat16* Vsh = nullptr;
+  int* eVsh = nullptr;
+  CUtensorMap mVsh;
   int *eV = nullptr, *eS = nullptr, *eWr = nullptr, *eWc = nullptr, *eR = nullptr;  // row exponents
   unsigned *mWr = nullptr, *mWc = nullptr;  // largest biased exponent of |W| per row g / column n
   double *Wd = nullptr, *Zp = nullptr, *Gd = nullptr;  // FP64 results [split][M][N]
@@ -281,26 +291,29 @@ __global__ void k_reduce_H2(z_t* __restrict__ H2s, const PT* __restrict__ P3, in
 
 // ---- fixed-point digit slices -------------------------------------------------
 
-// Signed base-64 digits of x relative to 2^e (|x| < 2^e): X = round(x 2^(6L-e))
-// = sum_i d_i 64^(L-1-i), d_i in [-32, 31] for i > 0, |d_0| <= 64.  Integer
-// operations only.
-template <int L>
-__device__ __forceinline__ void fx_digits(double x, int e, int (&d)[L]) {
+constexpr int FX_LMAX = 8;
+
+// Signed base-2^b digits of x relative to 2^e (|x| < 2^e): X = round(x 2^(bL-e))
+// = sum_i d_i 2^(b(L-1-i)), d_i in [-2^(b-1), 2^(b-1)) for i > 0, |d_0| <= 2^b.
+// Integer operations only (bL <= 52).
+__device__ __forceinline__ void fx_digits(double x, int e, int b, int L, int (&d)[FX_LMAX]) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   const int ex = (int)((u >> 52) & 0x7FF);
   long long X = 0;
   if (ex != 0) {
     const unsigned long long mant = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = 1075 - ex - 6 * L + e;  // >= 53 - 6L > 0 because |x| < 2^e
+    const int sh = 1075 - ex - b * L + e;  // >= 53 - bL > 0 because |x| < 2^e
     if (sh < 63) X = (long long)((mant + (1ull << (sh - 1))) >> sh);
     if (u >> 63) X = -X;
   }
+  const long long base = 1LL << b, half = base >> 1, mask = base - 1;
 #pragma unroll
-  for (int i = L - 1; i >= 1; i--) {
-    int t = (int)(X & 63);
-    if (t >= 32) t -= 64;
-    d[i] = t;
-    X = (X - t) >> 6;
+  for (int i = FX_LMAX - 1; i >= 1; i--) {
+    if (i >= L) continue;
+    long long t = X & mask;
+    if (t >= half) t -= base;
+    d[i] = (int)t;
+    X = (X - t) >> b;
   }
   d[0] = (int)X;
 }
@@ -309,15 +322,15 @@ __device__ __forceinline__ unsigned fx_biased_exp(double v) { return (unsigned)(
 // smallest e with |x| < 2^e for the largest biased exponent m of a row (0: all zero)
 __device__ __forceinline__ int fx_exp(unsigned m) { return m ? (int)m - 1022 : 0; }
 
-template <int L>
-__device__ __forceinline__ void fx_store(__nv_bfloat16* rowBase, size_t pitch, int k, bool valid, double v, int e) {
-  int d[L];
-  if (valid) fx_digits<L>(v, e, d);
-  else
+__device__ __forceinline__ void fx_store(__nv_bfloat16* rowBase, size_t pitch, int k, bool valid, double v, int e,
+                                         int b, int L) {
+  int d[FX_LMAX];
 #pragma unroll
-    for (int l = 0; l < L; l++) d[l] = 0;
+  for (int l = 0; l < FX_LMAX; l++) d[l] = 0;
+  if (valid) fx_digits(v, e, b, L, d);
 #pragma unroll
-  for (int l = 0; l < L; l++) rowBase[(size_t)l * pitch + k] = __int2bfloat16_rn(d[l]);
+  for (int l = 0; l < FX_LMAX; l++)
+    if (l < L) rowBase[(size_t)l * pitch + k] = __int2bfloat16_rn(d[l]);
 }
 
 __device__ unsigned fx_block_max(unsigned m) {
@@ -334,9 +347,11 @@ __device__ unsigned fx_block_max(unsigned m) {
 }
 
 // One block per row: the row's values in dynamic shared memory, the exponent
-// of its maximum, then the L digit planes (zero for K <= k < Kpad).
-template <int L, class F>
-__device__ void fx_row(__nv_bfloat16* rowBase, int* expOut, int K, int Kpad, int pitch, F value) {
+// of its maximum, then the L digit planes: value k at column shift + k, zero
+// elsewhere in [0, Kpad).
+template <class F>
+__device__ void fx_row(__nv_bfloat16* rowBase, int* expOut, int K, int Kpad, int pitch, int b, int L, int shift,
+                       F value) {
   extern __shared__ double fxbuf[];
   unsigned m = 0;
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
@@ -346,12 +361,16 @@ __device__ void fx_row(__nv_bfloat16* rowBase, int* expOut, int K, int Kpad, int
   }
   const int e = fx_exp(fx_block_max(m));
   if (threadIdx.x == 0) *expOut = e;
-  for (int k = threadIdx.x; k < Kpad; k += blockDim.x) fx_store<L>(rowBase, pitch, k, k < K, k < K ? fxbuf[k] : 0.0, e);
+  for (int k = threadIdx.x; k < Kpad; k += blockDim.x) {
+    const int src = k - shift;
+    const bool valid = src >= 0 && src < K;
+    fx_store(rowBase, pitch, k, valid, valid ? fxbuf[src] : 0.0, e, b, L);
+  }
 }
 
-template <int L>
 __global__ void __launch_bounds__(256) k_fx_split_V(__nv_bfloat16* __restrict__ out, int* __restrict__ eV,
-                                                     const double* __restrict__ V, int pitch, TRAJ_ARGS) {
+                                                     const double* __restrict__ V, int pitch, int b, int L,
+                                                     TRAJ_ARGS) {
   const TrajShape& T = shp[blockIdx.z];
   const int g = blockIdx.x, nG = T.nG;
   if (g >= nG) return;
@@ -359,17 +378,16 @@ __global__ void __launch_bounds__(256) k_fx_split_V(__nv_bfloat16* __restrict__ 
   eV = bat(eV, bs);
   V = bat(V, bs);
   const double* row = V + (size_t)g * nG;
-  fx_row<L>(out + (size_t)g * L * pitch, eV + g, nG, T.Kg, pitch, [&](int k) { return row[k]; });
+  fx_row(out + (size_t)g * L * pitch, eV + g, nG, T.Kg, pitch, b, L, 0, [&](int k) { return row[k]; });
 }
 
 // Row 2p + s of S: (re, im)[conj(phi_l) phi_k w] over the grid (p = (l, k)).
 // Block 0 of a trajectory also clears the W exponent maxima for GEMM1.
-template <int L>
 __global__ void __launch_bounds__(256) k_fx_split_S(__nv_bfloat16* __restrict__ out, int* __restrict__ eS,
                                                      unsigned* __restrict__ mWr, unsigned* __restrict__ mWc,
                                                      const z_t* __restrict__ orbs, const double* __restrict__ w,
                                                      const int* __restrict__ pl, const int* __restrict__ pk, int pitch,
-                                                     TRAJ_ARGS) {
+                                                     int b, int L, TRAJ_ARGS) {
   const TrajShape& T = shp[blockIdx.z];
   const int row = blockIdx.x, nG = T.nG, nP = T.nPairs;
   if (row >= 2 * nP) return;
@@ -387,17 +405,17 @@ __global__ void __launch_bounds__(256) k_fx_split_S(__nv_bfloat16* __restrict__ 
   }
   const int p = row >> 1, s = row & 1;
   const z_t* a = orbs + (size_t)nG * pl[p];
-  const z_t* b = orbs + (size_t)nG * pk[p];
-  fx_row<L>(out + (size_t)row * L * pitch, eS + row, nG, T.Kg, pitch, [&](int g) {
-    const z_t v = zcmul(a[g], b[g]);
+  const z_t* bo = orbs + (size_t)nG * pk[p];
+  fx_row(out + (size_t)row * L * pitch, eS + row, nG, T.Kg, pitch, b, L, T.gShift, [&](int g) {
+    const z_t v = zcmul(a[g], bo[g]);
     return (s ? v.y : v.x) * w[g];
   });
 }
 
 // Row n = 2q + s of R'' (K = 2p + t), as k_split_R.
-template <int L>
 __global__ void k_fx_split_R(__nv_bfloat16* __restrict__ out, int* __restrict__ eR, const z_t* __restrict__ Rp,
-                             const int* __restrict__ pl, const int* __restrict__ pk, int pitch, TRAJ_ARGS) {
+                             const int* __restrict__ pl, const int* __restrict__ pk, int pitch, int b, int L,
+                             TRAJ_ARGS) {
   const TrajShape& T = shp[blockIdx.z];
   const int n = T.nOS, nP = T.nPairs, Q = n * n;
   const int row = blockIdx.x;
@@ -408,7 +426,7 @@ __global__ void k_fx_split_R(__nv_bfloat16* __restrict__ out, int* __restrict__ 
   pl = bat(pl, bs);
   pk = bat(pk, bs);
   const int q = row >> 1, s = row & 1;
-  fx_row<L>(out + (size_t)row * L * pitch, eR + row, 2 * nP, T.Kp, pitch, [&](int k) {
+  fx_row(out + (size_t)row * L * pitch, eR + row, 2 * nP, T.Kp, pitch, b, L, 0, [&](int k) {
     const int p = k >> 1, t = k & 1;
     const int l = pl[p], kk = pk[p];
     const z_t R1 = Rp[(size_t)(l * n + kk) * Q + q];
@@ -441,15 +459,14 @@ __global__ void k_fx_reduce_W(double* __restrict__ Wd, unsigned* __restrict__ mW
   }
 }
 
-// W (FP64 [nG][2P]) to WxA (rows g, K = 2P) and WTxB (rows n, K = nG) digit
-// planes, with the row exponents eWr[g] / eWc[n]; 32 x 32 tiles transposed
-// through shared memory as k_split_W.
-template <int L>
+// W (FP64 [nG][2P]) to WxA (rows g, K = 2P: b2/L2 digits) and WTxB (rows n,
+// K = nG at columns gShift + g: b1/L1 digits) planes, with the row exponents
+// eWr[g] / eWc[n]; 32 x 32 tiles transposed through shared memory as k_split_W.
 __global__ void __launch_bounds__(256) k_fx_split_W(__nv_bfloat16* __restrict__ WxA, __nv_bfloat16* __restrict__ WTxB,
                                                      int* __restrict__ eWr, int* __restrict__ eWc,
                                                      const double* __restrict__ Wd, const unsigned* __restrict__ mWr,
-                                                     const unsigned* __restrict__ mWc, int pitchP, int pitchG,
-                                                     TRAJ_ARGS) {
+                                                     const unsigned* __restrict__ mWc, int pitchP, int pitchG, int b1,
+                                                     int L1, int b2, int L2, TRAJ_ARGS) {
   __shared__ double tile[SW_T][SW_T + 1];
   const TrajShape& T = shp[blockIdx.z];
   const int nG = T.nG, N2P = 2 * T.nPairs, KpP = T.Kp, KpG = T.Kg;
@@ -471,17 +488,20 @@ __global__ void __launch_bounds__(256) k_fx_split_W(__nv_bfloat16* __restrict__ 
     if (g < nG && n < KpP) {
       const int e = fx_exp(mWr[g]);
       if (n == 0) eWr[g] = e;
-      fx_store<L>(WxA + (size_t)g * L * pitchP, pitchP, n, valid, v, e);
+      fx_store(WxA + (size_t)g * L2 * pitchP, pitchP, n, valid, v, e, b2, L2);
     }
   }
   __syncthreads();
+  const int sh = T.gShift;
   for (int r = ty; r < SW_T; r += 8) {
-    const int n = n0 + r, g = g0 + tx;
-    if (n < N2P && g < KpG) {
+    const int n = n0 + r, g = g0 + tx, col = g + sh;
+    if (n < N2P && col < KpG) {
       const int e = fx_exp(mWc[n]);
       if (g == 0) eWc[n] = e;
-      fx_store<L>(WTxB + (size_t)n * L * pitchG, pitchG, g, g < nG, tile[tx][r], e);
+      fx_store(WTxB + (size_t)n * L1 * pitchG, pitchG, col, g < nG, tile[tx][r], e, b1, L1);
     }
+    if (n < N2P && g0 == 0)  // columns before the shifted grid
+      for (int cz = tx; cz < sh; cz += 32) fx_store(WTxB + (size_t)n * L1 * pitchG, pitchG, cz, false, 0.0, 0, b1, L1);
   }
 }
 
@@ -499,31 +519,39 @@ size_t mixed_layout(cgpu_ctx* c, char* base, size_t off) {
   if (c->precision == CGPU_PREC_FP64 || !c->hasInteraction) return off;
   if (!c->mixed) c->mixed = new MixedBufs();
   MixedBufs* m = c->mixed;
-  m->fxL = c->precision == CGPU_PREC_MIXED_FX ? 5 : c->precision == CGPU_PREC_MIXED_FX6 ? 6 : 0;
-  m->terms = m->fxL ? m->fxL : c->precision == CGPU_PREC_MIXED_X6 ? 6 : 3;
+  m->fxBits = c->precision == CGPU_PREC_MIXED_FX ? 30 : c->precision == CGPU_PREC_MIXED_FX6 ? 36 : 0;
+  m->terms = c->precision == CGPU_PREC_MIXED_X6 ? 6 : 3;
   int nG = c->nG, nP = c->nPairs, Q = c->nOS * c->nOS, T = m->terms;
   m->KgMax = (nG + 63) / 64 * 64;
   m->KpMax = (2 * nP + 63) / 64 * 64;
   typedef __nv_bfloat16 bf;
-  if (m->fxL) {
-    const int L = m->fxL;
-    m->bn1 = fx_tile_n(2 * nP, L);
-    m->bn2 = fx_tile_n(2 * Q, L);
-    m->bn3 = fx_tile_n(2 * nP, L);
+  if (m->fxBits) {
+    m->KgMax = c->fxKgMax;  // includes the K-tile offsets of a shared interaction matrix
+    // digit widths from the longest contraction of the batch (K = nG, K = 2P)
+    m->b1 = fx_digit_bits(nG);
+    m->L1 = fx_slices(nG, m->fxBits);
+    m->b2 = fx_digit_bits(2 * nP);
+    m->L2 = fx_slices(2 * nP, m->fxBits);
+    const int L1 = m->L1, L2 = m->L2;
+    m->compact2 = c->nb > 1 && fx_compact_ok(L2);
+    m->bn1 = fx_tile_n(2 * nP, L1, false);
+    m->bn2 = fx_tile_n(2 * Q, L2, m->compact2);
+    m->bn3 = fx_tile_n(2 * nP, L1, false);
     m->s1 = fx_split_count(nG, 2 * nP, m->bn1, m->KgMax / 64, c->nb);
     m->s2 = fx_split_count(nG, 2 * Q, m->bn2, m->KpMax / 64, c->nb);
     m->s3 = fx_split_count(2 * nP, 2 * nP, m->bn3, m->KgMax / 64, c->nb);
-    size_t oV = take(off, sizeof(bf) * (size_t)nG * L * m->KgMax);
-    size_t oS = take(off, sizeof(bf) * (size_t)2 * nP * L * m->KgMax);
-    size_t oW = take(off, sizeof(bf) * (size_t)nG * L * m->KpMax);
-    size_t oWT = take(off, sizeof(bf) * (size_t)2 * nP * L * m->KgMax);
-    size_t oR = take(off, sizeof(bf) * (size_t)2 * Q * L * m->KpMax);
+    const size_t perTrajV = c->fxShared ? 0 : 1;
+    size_t oV = take(off, perTrajV * sizeof(bf) * (size_t)nG * L1 * m->KgMax);
+    size_t oS = take(off, sizeof(bf) * (size_t)2 * nP * L1 * m->KgMax);
+    size_t oW = take(off, sizeof(bf) * (size_t)nG * L2 * m->KpMax);
+    size_t oWT = take(off, sizeof(bf) * (size_t)2 * nP * L1 * m->KgMax);
+    size_t oR = take(off, sizeof(bf) * (size_t)2 * Q * L2 * m->KpMax);
     size_t oWd = take(off, sizeof(double) * (size_t)m->s1 * nG * 2 * nP);
     size_t oZp = take(off, m->s2 > 1 ? sizeof(double) * (size_t)m->s2 * nG * 2 * Q : 0);
     size_t oGd = take(off, sizeof(double) * (size_t)m->s3 * 2 * nP * 2 * nP);
     size_t oE = take(off, sizeof(int));
     size_t oZ = take(off, sizeof(double) * (size_t)2 * nG * Q);
-    size_t oeV = take(off, sizeof(int) * (size_t)nG);
+    size_t oeV = take(off, perTrajV * sizeof(int) * (size_t)nG);
     size_t oeS = take(off, sizeof(int) * (size_t)2 * nP);
     size_t oeWr = take(off, sizeof(int) * (size_t)nG);
     size_t oeWc = take(off, sizeof(int) * (size_t)2 * nP);
@@ -531,7 +559,7 @@ size_t mixed_layout(cgpu_ctx* c, char* base, size_t off) {
     size_t omWr = take(off, sizeof(unsigned) * (size_t)nG);
     size_t omWc = take(off, sizeof(unsigned) * (size_t)2 * nP);
     if (base) {
-      m->VxB = (bf*)(base + oV);
+      m->VxB = perTrajV ? (bf*)(base + oV) : nullptr;
       m->SxA = (bf*)(base + oS);
       m->WxA = (bf*)(base + oW);
       m->WTxB = (bf*)(base + oWT);
@@ -541,7 +569,7 @@ size_t mixed_layout(cgpu_ctx* c, char* base, size_t off) {
       m->Gd = (double*)(base + oGd);
       m->err = (int*)(base + oE);
       m->Zd = (double*)(base + oZ);
-      m->eV = (int*)(base + oeV);
+      m->eV = perTrajV ? (int*)(base + oeV) : nullptr;
       m->eS = (int*)(base + oeS);
       m->eWr = (int*)(base + oeWr);
       m->eWc = (int*)(base + oeWc);
@@ -585,7 +613,11 @@ size_t mixed_layout(cgpu_ctx* c, char* base, size_t off) {
 }
 
 void mixed_free(cgpu_ctx* c) {
-  delete c->mixed;  // the buffers belong to the arena
+  if (c->mixed) {
+    if (c->mixed->Vsh) cudaFree(c->mixed->Vsh);
+    if (c->mixed->eVsh) cudaFree(c->mixed->eVsh);
+  }
+  delete c->mixed;  // the other buffers belong to the arena
   c->mixed = nullptr;
 }
 
@@ -594,18 +626,30 @@ void mixed_init(cgpu_ctx* c) {
   MixedBufs* m = c->mixed;
   if (!m) return;
   int T = m->terms, pG = T * m->KgMax, pP = T * m->KpMax;
+  if (m->fxBits) {
+    pG = m->L1 * m->KgMax;  // S, V, WT: K = nG slices
+    pP = m->L2 * m->KpMax;  // W, R: K = 2P slices
+  }
   size_t nGK = (size_t)c->nG * m->KgMax;
-  if (m->fxL == 5)
-    k_fx_split_V<5><<<dim3(c->nG, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(m->VxB, m->eV, c->Vint_d,
-                                                                                        m->KgMax, TRAJ_PASS(c));
-  else if (m->fxL == 6)
-    k_fx_split_V<6><<<dim3(c->nG, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(m->VxB, m->eV, c->Vint_d,
-                                                                                        m->KgMax, TRAJ_PASS(c));
+  if (m->fxBits && c->fxShared) {
+    // the largest trajectory's interaction matrix, sliced once for the batch
+    const int big = c->fxBig, nGb = c->sys[big].nG;
+    m->KgBig = (nGb + 63) / 64 * 64;
+    CODY_CUDA(cudaMalloc(&m->Vsh, sizeof(__nv_bfloat16) * (size_t)nGb * m->L1 * m->KgBig));
+    CODY_CUDA(cudaMalloc(&m->eVsh, sizeof(int) * (size_t)nGb));
+    const double* Vb = (const double*)((const char*)c->Vint_d + (size_t)big * c->bs);
+    k_fx_split_V<<<dim3(nGb, 1, 1), 256, sizeof(double) * m->KgBig, c->stream>>>(m->Vsh, m->eVsh, Vb, m->KgBig,
+                                                                              m->b1, m->L1, c->shape_d + big, 0);
+    m->mVsh = tc_make_map_planes(m->Vsh, nGb, m->L1 * m->KgBig, 128, 1, 0);
+  } else if (m->fxBits)
+    k_fx_split_V<<<dim3(c->nG, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(m->VxB, m->eV, c->Vint_d,
+                                                                                     m->KgMax, m->b1, m->L1,
+                                                                                     TRAJ_PASS(c));
   else
     k_split_V<<<bgrid(c, ew_blocks(c, nGK)), 256, 0, c->stream>>>(m->VxB, c->Vint_d, m->KgMax, T, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
   int P2 = 2 * c->nPairs, Q2 = 2 * c->nOS * c->nOS;
-  m->mV = tc_make_map(c, m->VxB, c->nG, pG, 128);
+  if (m->VxB) m->mV = tc_make_map(c, m->VxB, c->nG, pG, 128);
   m->mS = tc_make_map(c, m->SxA, P2, pG, m->bn1);
   m->mW = tc_make_map(c, m->WxA, c->nG, pP, 128);
   m->mR = tc_make_map(c, m->RxB, Q2, pP, m->bn2);
@@ -621,37 +665,40 @@ int mixed_error(cgpu_ctx* c) {
   return e;
 }
 
-// The fixed-point form of the three contractions (L digit slices).
-template <int L>
+// The fixed-point form of the three contractions.
 void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   MixedBufs* m = c->mixed;
   const int nG = c->nG, nP = c->nPairs, n = c->nOS, Q = n * n;
   z_t* Z = (z_t*)m->Zd;
   {
     ProfScope prof(c, CGPU_KERNEL_PAIR_POTENTIALS);
-    k_fx_split_S<L><<<dim3(2 * nP, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(
-        m->SxA, m->eS, m->mWr, m->mWc, orbs, c->w_d, c->pairL_d, c->pairK_d, m->KgMax, TRAJ_PASS(c));
+    k_fx_split_S<<<dim3(2 * nP, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(
+        m->SxA, m->eS, m->mWr, m->mWc, orbs, c->w_d, c->pairL_d, c->pairK_d, m->KgMax, m->b1, m->L1, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
     const bool one = m->s1 == 1;
-    fx_gemm(c, L, TC_GEMM_W, m->mV, m->mS, m->bn1, m->Wd, m->eV, m->eS, one ? m->mWr : nullptr,
-            one ? m->mWc : nullptr, m->KgMax, m->s1, nG, 2 * nP, m->err);
+    if (c->fxShared)
+      fx_gemm(c, m->L1, m->b1, false, TC_GEMM_W, m->mVsh, m->mS, m->bn1, m->Wd, m->eVsh, m->eS,
+              one ? m->mWr : nullptr, one ? m->mWc : nullptr, m->KgBig, m->KgMax, 1, m->s1, nG, 2 * nP, m->err);
+    else
+      fx_gemm(c, m->L1, m->b1, false, TC_GEMM_W, m->mV, m->mS, m->bn1, m->Wd, m->eV, m->eS, one ? m->mWr : nullptr,
+              one ? m->mWc : nullptr, m->KgMax, m->KgMax, 0, m->s1, nG, 2 * nP, m->err);
     if (!one) {
       k_fx_reduce_W<<<bgrid(c, ew_blocks(c, (size_t)nG * 2 * nP)), 256, 0, c->stream>>>(m->Wd, m->mWr, m->mWc, m->s1,
                                                                                      TRAJ_PASS(c));
       CODY_LAUNCHED(c);
     }
     dim3 gw(ceil_div(m->KgMax, SW_T), ceil_div(m->KpMax, SW_T), c->nb);
-    k_fx_split_W<L><<<gw, 256, 0, c->stream>>>(m->WxA, m->WTxB, m->eWr, m->eWc, m->Wd, m->mWr, m->mWc, m->KpMax,
-                                               m->KgMax, TRAJ_PASS(c));
+    k_fx_split_W<<<gw, 256, 0, c->stream>>>(m->WxA, m->WTxB, m->eWr, m->eWc, m->Wd, m->mWr, m->mWc, m->KpMax,
+                                            m->KgMax, m->b1, m->L1, m->b2, m->L2, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
   }
   {
     ProfScope prof(c, CGPU_KERNEL_CORRELATION);
-    k_fx_split_R<L><<<dim3(2 * Q, 1, c->nb), 64, sizeof(double) * m->KpMax, c->stream>>>(
-        m->RxB, m->eR, c->Rp_d, c->pairL_d, c->pairK_d, m->KpMax, TRAJ_PASS(c));
+    k_fx_split_R<<<dim3(2 * Q, 1, c->nb), 64, sizeof(double) * m->KpMax, c->stream>>>(
+        m->RxB, m->eR, c->Rp_d, c->pairL_d, c->pairK_d, m->KpMax, m->b2, m->L2, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
-    fx_gemm(c, L, TC_GEMM_Z, m->mW, m->mR, m->bn2, m->s2 > 1 ? m->Zp : m->Zd, m->eWr, m->eR, nullptr, nullptr,
-            m->KpMax, m->s2, nG, 2 * Q, m->err);
+    fx_gemm(c, m->L2, m->b2, m->compact2, TC_GEMM_Z, m->mW, m->mR, m->bn2, m->s2 > 1 ? m->Zp : m->Zd, m->eWr, m->eR,
+            nullptr, nullptr, m->KpMax, m->KpMax, 0, m->s2, nG, 2 * Q, m->err);
     if (m->s2 > 1) {
       k_reduce_Z<<<bgrid(c, ew_blocks(c, (size_t)nG * Q)), 256, 0, c->stream>>>(Z, m->Zp, m->s2, TRAJ_PASS(c));
       CODY_LAUNCHED(c);
@@ -660,8 +707,8 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   }
   if (wantH2) {
     ProfScope prof(c, CGPU_KERNEL_H2);
-    fx_gemm(c, L, TC_GEMM_H2, m->mSasB, m->mWT, m->bn3, m->Gd, m->eS, m->eWc, nullptr, nullptr, m->KgMax, m->s3,
-            2 * nP, 2 * nP, m->err);
+    fx_gemm(c, m->L1, m->b1, false, TC_GEMM_H2, m->mSasB, m->mWT, m->bn3, m->Gd, m->eS, m->eWc, nullptr, nullptr,
+            m->KgMax, m->KgMax, 0, m->s3, 2 * nP, 2 * nP, m->err);
     k_reduce_H2<<<bgrid(c, ew_blocks(c, (size_t)Q * Q)), 256, 0, c->stream>>>(c->h2s_d, m->Gd, m->s3, c->pidx_d,
                                                                         TRAJ_PASS(c));
     CODY_LAUNCHED(c);
@@ -678,8 +725,7 @@ void launch_correlation_mixed(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int want
   }
   MixedBufs* m = c->mixed;
   int nG = c->nG, nP = c->nPairs, n = c->nOS, Q = n * n, T = m->terms;
-  if (m->fxL == 5) return correlation_fx<5>(c, dOrbs, orbs, wantH2);
-  if (m->fxL == 6) return correlation_fx<6>(c, dOrbs, orbs, wantH2);
+  if (m->fxBits) return correlation_fx(c, dOrbs, orbs, wantH2);
   {
     ProfScope prof(c, CGPU_KERNEL_PAIR_POTENTIALS);
     k_split_S<<<bgrid(c, ew_blocks(c, (size_t)2 * nP * m->KgMax)), 256, 0, c->stream>>>(

@@ -215,13 +215,20 @@ int tc_split_count(int M, int N, int BN, int kTiles, int nb) {
 
 // 3D bf16 tensor [nb][rowsMax][pitch] (pitch contiguous, multiple of 64, trajectories bs bytes apart).
 CUtensorMap tc_make_map(const cgpu_ctx* c, const __nv_bfloat16* base, int rowsMax, int pitch, int boxRows) {
+  return tc_make_map_planes(base, rowsMax, pitch, boxRows, c->nb, c->bs);
+}
+
+CUtensorMap tc_make_map_planes(const __nv_bfloat16* base, int rowsMax, int pitch, int boxRows, int planes,
+                               size_t planeBytes) {
   ensure_encode();
-  if ((uintptr_t)base % 16 != 0 || pitch % TC_BK != 0 || c->bs % 16 != 0)
+  if (planes > 1 && planeBytes % 16 != 0) throw std::string("tensor map: bad alignment");
+  if (planes == 1) planeBytes = (size_t)pitch * 2 * (size_t)rowsMax;
+  if ((uintptr_t)base % 16 != 0 || pitch % TC_BK != 0 || planeBytes % 16 != 0)
     throw std::string("tensor map: bad alignment");
   CUtensorMap m;
   std::memset(&m, 0, sizeof(m));
-  cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)rowsMax, (cuuint64_t)c->nb};
-  cuuint64_t strides[2] = {(cuuint64_t)pitch * 2, (cuuint64_t)c->bs};
+  cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)rowsMax, (cuuint64_t)planes};
+  cuuint64_t strides[2] = {(cuuint64_t)pitch * 2, (cuuint64_t)planeBytes};
   cuuint32_t box[3] = {(cuuint32_t)TC_BK, (cuuint32_t)boxRows, 1};
   cuuint32_t es[3] = {1, 1, 1};
   CUresult r = g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(base), dims, strides, box,

@@ -22,14 +22,26 @@ void tc_gemm(cgpu_ctx* c, int gemmId, const CUtensorMap& ta, const CUtensorMap& 
              int segPitch, int nSplit, int Mmax, int Nmax, int* err);
 
 // Fixed-point slice GEMM (k_fx.cu): out[traj][split][M][N] (FP64) = A B^T for
-// operands carried as L digit slices (K segments of segPitch elements) with
-// row exponents expA / expB; maxRow / maxCol (unsplit K only) receive the
-// largest biased exponent of |C| per row / column.
-void fx_gemm(cgpu_ctx* c, int L, int gemmId, const CUtensorMap& ta, const CUtensorMap& tb, int bn, double* out,
-             const int* expA, const int* expB, unsigned* maxRow, unsigned* maxCol, int segPitch, int nSplit, int Mmax,
-             int Nmax, int* err);
-// N-tile width of the fixed-point GEMM for N output columns and L slices (L * BN <= 512 TMEM columns).
-int fx_tile_n(int N, int L);
+// operands carried as L base-2^digitBits digit slices (K segments of
+// segPitchA / segPitch elements) with row exponents expA / expB; maxRow /
+// maxCol (unsplit K only) receive the largest biased exponent of |C| per row /
+// column.  compact: the two-CTAs-per-SM configuration (small K).  aShared: A
+// is one matrix shared by the trajectories, read at each trajectory's vRow.
+void fx_gemm(cgpu_ctx* c, int L, int digitBits, bool compact, int gemmId, const CUtensorMap& ta,
+             const CUtensorMap& tb, int bn, double* out, const int* expA, const int* expB, unsigned* maxRow,
+             unsigned* maxCol, int segPitchA, int segPitch, int aShared, int nSplit, int Mmax, int Nmax, int* err);
+// 3D TMA map over an explicit [planes][rowsMax][pitch] bf16 tensor (planes planeBytes apart).
+CUtensorMap tc_make_map_planes(const __nv_bfloat16* base, int rowsMax, int pitch, int boxRows, int planes,
+                               size_t planeBytes);
+// Digit width for a contraction of length K: 8 bits up to 256, 7 up to 1024, else 6
+// (the level sums of the two leading levels stay exact in FP32).
+int fx_digit_bits(int K);
+// Slices that carry targetBits fractional bits at that width.
+int fx_slices(int K, int targetBits);
+// N-tile width for N output columns and L slices (wide: L * BN <= 512, compact: <= 256).
+int fx_tile_n(int N, int L, bool compact);
+// Whether a compact configuration exists for L slices.
+bool fx_compact_ok(int L);
 // K splits of the fixed-point GEMM: about one wave of 152 SMs, at most 4096 K per split.
 int fx_split_count(int M, int N, int BN, int kTiles, int nb);
 

@@ -1,6 +1,6 @@
 """Advance a benchmark workload by a few steps on the GPU (for profilers).
 
-    python -m codyfortran_gb300.run_steps --workload batch512 --precision mixed --steps 1 [--trajectories N]
+    python -m codyfortran_gb300.run_steps --workload batch512 --precision mixed_fx --steps 1 [--trajectories N]
 
 Builds the workload (the 512-trajectory batch, or a prefix of it, or the
 trimer), uploads seeded initial states and propagates --steps Strang steps
@@ -26,10 +26,13 @@ def main():
 
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="batch512", choices=["batch512", "trimer_large"])
-    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed", "mixed6", "mixed_fx", "mixed_fx6"])
+    ap.add_argument("--precision", default="mixed_fx", choices=["fp64", "mixed", "mixed6", "mixed_fx", "mixed_fx6"])
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--trajectories", type=int, default=512)
+    ap.add_argument("--krylov-window", type=int, default=None,
+                    help="Gram-Schmidt window of the Lanczos recurrence (default: 0 for fp64, 2 for mixed forms)")
     args = ap.parse_args()
+    window = args.krylov_window if args.krylov_window is not None else (0 if args.precision == "fp64" else 2)
 
     def state(sp, x, w, seed):
         rng = np.random.default_rng(seed)
@@ -39,7 +42,7 @@ def main():
 
     if args.workload == "batch512":
         specs = S.batch_trajectory_specs(512, 1234)[: args.trajectories]
-        b = Batch(specs, args.precision, max_krylov=12)
+        b = Batch(specs, args.precision, max_krylov=12, krylov_window=window)
         b.upload([state(sp, s.x, s.w, 1234 + k) for k, (sp, s) in enumerate(zip(specs, b.systems))])
         print("set-up launches", b.launch_count(), flush=True)
         ms = b.propagate(0.0, 0.02, args.steps, 12)
@@ -47,7 +50,7 @@ def main():
         b.close()
     else:
         sp = S.cfg_trimer_large()
-        e = Engine(sp, args.precision, max_krylov=16)
+        e = Engine(sp, args.precision, max_krylov=16, krylov_window=window)
         e.upload(state(sp, e.x, e.w, 7))
         print("set-up launches", e.launch_count(), flush=True)
         ms = e.propagate_resident_timed(0.0, 0.02, args.steps, 16, use_metric=True, use_graph=True)

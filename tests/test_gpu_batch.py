@@ -43,8 +43,11 @@ def _states(engines, seed):
 # FP64: the batch sums its reductions over other block counts than a single
 # system, so agreement is to rounding.  Mixed: the split-K partitions of the
 # FP32-accumulated contractions differ too, so agreement is to the mixed form's
-# own accuracy.
-@pytest.mark.parametrize("precision,tol,etol", [("fp64", 1e-12, 1e-12), ("mixed", 2e-5, 1e-6)])
+# own accuracy.  mixed_fx: the batch's digit width follows its longest grid
+# (6-bit digits) while a small system alone uses 8-bit ones, so agreement is to
+# the fixed-point form's truncation.
+@pytest.mark.parametrize("precision,tol,etol", [("fp64", 1e-12, 1e-12), ("mixed", 2e-5, 1e-6),
+                                                 ("mixed_fx", 1e-8, 1e-9)])
 def test_batch_matches_individual_contexts(precision, tol, etol):
     from codyfortran_gb300.engine import Batch, Engine
     specs = S.batch_trajectory_specs(512, 1234)[:3] + [_small_helium(), _two_per_spin()]
@@ -118,3 +121,56 @@ def test_krylov_window_rejects_negative():
     from codyfortran_gb300.engine import Batch, CodyError
     with pytest.raises(CodyError):
         Batch([_small_helium()], "fp64", krylov_window=-1)
+
+
+def test_mixed_fx_batch_without_shared_interaction():
+    """Systems whose interaction matrices are not blocks of one matrix (another
+    softening) keep one interaction matrix per trajectory."""
+    from codyfortran_gb300.engine import Batch, Engine
+    other = _small_helium()
+    other.int_s1 = 0.7
+    specs = [_small_helium(), other, _two_per_spin()]
+    b = Batch(specs, "mixed_fx", max_krylov=12)
+    st = _states(b.systems, 31)
+    b.upload(st)
+    t0 = np.array([0.0, 1.0, 2.0])
+    b.propagate(t0, 0.02, 3, 12)
+    got = b.download()
+    for k, sp in enumerate(specs):
+        e = Engine(sp, "mixed_fx", max_krylov=12)
+        e.upload(st[k])
+        e.propagate_resident(t0[k], 0.02, 3, 12, use_metric=True, use_graph=True)
+        ref = e.download()
+        e.close()
+        assert rel(got[k], ref) <= 1e-10, (k, rel(got[k], ref))
+    b.close()
+
+
+def test_mixed_fx_shared_interaction_matches_per_trajectory():
+    """These grids nest (FEDVR elements of width 2 on boxes of different length),
+    so the batch reads one shared interaction matrix at each trajectory's row
+    offset.  Adding a system with another softening switches the batch to one
+    matrix per trajectory with the same digit widths: the fixed-point
+    contractions are exact sums of the same digits, so both batches agree to
+    the rounding of their FP64 parts."""
+    from codyfortran_gb300.engine import Batch
+    specs = S.batch_trajectory_specs(512, 1234)[:3] + [_small_helium(), _two_per_spin()]
+    other = _small_helium()
+    other.int_s1 = 0.7
+    shared = Batch(specs, "mixed_fx", max_krylov=12, krylov_window=2)
+    single = Batch(specs + [other], "mixed_fx", max_krylov=12, krylov_window=2)
+    st = _states(shared.systems, 41)
+    st_other = _states(single.systems[-1:], 99)
+    shared.upload(st)
+    single.upload(st + st_other)
+    t0 = np.array([0.0, 3.0, 7.5, 1.0, 0.25])
+    shared.propagate(t0, 0.02, 4, 12)
+    single.propagate(np.append(t0, 0.5), 0.02, 4, 12)
+    a, b = shared.download(), single.download()
+    Ea = shared.energies(t0 + 0.08)
+    Eb = single.energies(np.append(t0, 0.5) + 0.08)
+    for k in range(len(specs)):
+        assert rel(a[k], b[k]) < 1e-12, (k, rel(a[k], b[k]))
+        assert abs(Ea[k] - Eb[k]) <= 1e-12 * abs(Eb[k]), (k, Ea[k], Eb[k])
+    shared.close()
+    single.close()
