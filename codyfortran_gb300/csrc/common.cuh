@@ -146,8 +146,10 @@ struct TrajShape {
   int nGroups;               // (1-P) projector groups: one when restricted, else one per body type
   int grpStart[CODY_MAX_BT], grpSize[CODY_MAX_BT];
   int Kg, Kp;                // mixed form: K of the grid / pair contractions padded to 64 (Kg includes gShift)
-  int vRow, gShift;          // fixed-point form with a shared interaction matrix: first grid point of this
-                             // trajectory in the largest grid, and its offset within a 64-wide K tile
+  int vRow, gShift;          // fixed-point form with shared interaction matrices: first grid point of this
+                             // trajectory in its root grid, and its offset within a 64-wide K tile
+  int vRoot, vExp;           // the root grid (plane of the shared slices) and the offset of the
+                             // trajectory's first row in the shared row-exponent array
   double regEps;
   LaserDev laser;
   CiView view;
@@ -264,10 +266,10 @@ struct cgpu_ctx {
   z_t *basis_d = nullptr, *lw_d = nullptr, *trial_d = nullptr, *work_d = nullptr;
   int maxKrylov = 0;
   int krylovWindow = 0;                       // 0: full re-orthogonalisation; k: last k basis vectors
-  // fixed-point form: every trajectory's grid a contiguous piece of the largest one (same interaction):
-  // one shared interaction matrix, rows/columns from fxVRow
-  int fxShared = 0, fxBig = 0, fxKgMax = 0;
-  std::vector<int> fxVRow;
+  // fixed-point form: every trajectory's grid a contiguous piece of one of a few root grids (same
+  // interaction): one shared interaction matrix per root, rows/columns from fxVRow
+  int fxShared = 0, fxKgMax = 0;
+  std::vector<int> fxVRow, fxVRoot, fxRoots;  // per trajectory: row offset, root index; per root: trajectory
   double* lz_d = nullptr;   // Lanczos scalars: alpha, beta, dots, phi, flags
   double* lz_h = nullptr;   // pinned mirror (trajectory 0)
   // TDCI static data

@@ -362,37 +362,56 @@ void put(cgpu_ctx* c, int b, T* dst0, const std::vector<T>& v) {
 }
 
 // Fixed-point form of a batch: when every trajectory has the same dense
-// interaction and its grid is a contiguous, bitwise-equal piece of the largest
-// grid (FEDVR boxes of different length with the same elements), every
-// interaction matrix is a principal block of the largest one; the contraction
-// W = V S then reads one shared set of V slices (resident in L2) at the
-// trajectory's row offset.
+// interaction and its grid is a contiguous, bitwise-equal piece of one of a
+// few root grids (FEDVR boxes of different length with the same elements: the
+// grids with an even and with an odd element count on [-n, n] form two
+// families), every interaction matrix is a principal block of its root's; the
+// contraction W = V S then reads one shared set of V slices per root
+// (resident in L2) at the trajectory's row offset.
+constexpr int FX_MAX_ROOTS = 8;
 void detect_shared_interaction(cgpu_ctx* c) {
+  const size_t n = c->sys.size();
   c->fxShared = 0;
-  c->fxVRow.assign(c->sys.size(), 0);
+  c->fxVRow.assign(n, 0);
+  c->fxVRoot.assign(n, 0);
+  c->fxRoots.clear();
   c->fxKgMax = (c->nG + 63) / 64 * 64;
   const bool fx = c->precision == CGPU_PREC_MIXED_FX || c->precision == CGPU_PREC_MIXED_FX6;
-  if (!fx || !c->hasInteraction || c->sys.size() < 2) return;
-  int big = 0;
-  for (size_t b = 0; b < c->sys.size(); b++)
-    if (c->sys[b].nG > c->sys[big].nG) big = (int)b;
-  const SysHost& B = c->sys[big];
-  std::vector<int> rows(c->sys.size(), 0);
+  if (!fx || !c->hasInteraction || n < 2) return;
+  std::vector<int> order(n);
+  for (size_t b = 0; b < n; b++) order[b] = (int)b;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return c->sys[a].nG > c->sys[b].nG; });
+  const SysHost& S0 = c->sys[order[0]];
+  std::vector<int> roots, rows(n, 0), rootOf(n, 0);
   int kgMax = 0;
-  for (size_t b = 0; b < c->sys.size(); b++) {
+  for (int b : order) {
     const SysHost& s = c->sys[b];
-    if (s.intToeplitz || B.intToeplitz || s.intS != B.intS || s.intS1 != B.intS1 || s.intS2 != B.intS2 ||
-        s.intDamp != B.intDamp || s.nG < 1)
+    if (s.intToeplitz || s.intS != S0.intS || s.intS1 != S0.intS1 || s.intS2 != S0.intS2 ||
+        s.intDamp != S0.intDamp || s.nG < 1)
       return;
-    auto it = std::lower_bound(B.x.begin(), B.x.end(), s.x[0]);
-    size_t off = (size_t)(it - B.x.begin());
-    if (off + (size_t)s.nG > B.x.size() || std::memcmp(&B.x[off], s.x.data(), sizeof(double) * s.nG) != 0) return;
-    rows[b] = (int)off;
-    kgMax = std::max(kgMax, ((int)off % 64 + s.nG + 63) / 64 * 64);
+    int found = -1;
+    for (size_t r = 0; r < roots.size() && found < 0; r++) {
+      const SysHost& B = c->sys[roots[r]];
+      auto it = std::lower_bound(B.x.begin(), B.x.end(), s.x[0]);
+      size_t off = (size_t)(it - B.x.begin());
+      if (off + (size_t)s.nG <= B.x.size() && std::memcmp(&B.x[off], s.x.data(), sizeof(double) * s.nG) == 0) {
+        found = (int)r;
+        rows[b] = (int)off;
+      }
+    }
+    if (found < 0) {  // a new root: the largest grid of its family
+      if ((int)roots.size() == FX_MAX_ROOTS) return;
+      found = (int)roots.size();
+      roots.push_back(b);
+      rows[b] = 0;
+    }
+    rootOf[b] = found;
+    kgMax = std::max(kgMax, (rows[b] % 64 + s.nG + 63) / 64 * 64);
   }
   c->fxShared = 1;
-  c->fxBig = big;
+  c->fxRoots = roots;
   c->fxVRow = rows;
+  c->fxVRoot = rootOf;
   c->fxKgMax = kgMax;
 }
 
@@ -505,6 +524,8 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
     }
     t.vRow = c->fxShared ? c->fxVRow[b] : 0;
     t.gShift = t.vRow % 64;
+    t.vRoot = c->fxShared ? c->fxVRoot[b] : 0;
+    t.vExp = t.vRoot * c->nG + t.vRow;  // shared row exponents: [root][c->nG]
     t.Kg = (t.gShift + s.nG + 63) / 64 * 64;
     t.Kp = (2 * s.nPairs + 63) / 64 * 64;
     t.regEps = s.regEps;
@@ -1602,6 +1623,10 @@ int cgpu_batch_observables(cgpu_batch* b, const double* t, double* out) {
 long cgpu_batch_kernels_per_step(const cgpu_batch* b) { return (b && b->c) ? b->c->graphKernels : 0; }
 
 long cgpu_batch_launch_count(cgpu_batch* b, int reset) { return (b && b->c) ? cgpu_launch_count(b->c, reset) : -1; }
+
+int cgpu_batch_shared_interactions(const cgpu_batch* b) {
+  return (b && b->c && b->c->fxShared) ? (int)b->c->fxRoots.size() : 0;
+}
 
 int cgpu_batch_profile_begin(cgpu_batch* b, int kernel) {
   if (!b || !b->c) return fail(nullptr, "null batch", CGPU_ERR_ARG);

@@ -23,8 +23,8 @@
 //
 // Pipeline: one TMA producer thread, one MMA issuer thread, four epilogue
 // warps.  Per 64-wide K block the producer loads the L slices of the B tile
-// into one ring stage and the L slices of the A tile into L stages of a
-// second ring; the issuer runs the L(L+1)/2 slice products of the block from
+// (in 16-row boxes, only the rows of the trajectory's own columns) into one
+// ring stage and the L slices of the A tile into L stages of a second ring; the issuer runs the L(L+1)/2 slice products of the block from
 // shared memory with the MMA width cut to the trajectory's own N.  The
 // epilogue stages the FP64 tile in shared memory for coalesced stores.  The
 // wide configuration (two B stages, deep A ring) holds one CTA per SM; the
@@ -65,16 +65,39 @@ struct FxCfg {
   static_assert(TC_BM * SP * 8 <= RING, "output staging fits the ring");
 };
 
-// 2^e as a double (exact).
-__device__ __forceinline__ double pow2i(int e) {
-  if (e >= -1022 && e <= 1023) return __longlong_as_double((long long)(e + 1023) << 52);
-  return ldexp(1.0, e);
+// T 2^e as a double by integer operations (the FP64 pipes are the scarce
+// resource): round-to-nearest-even when |T| needs more than 53 bits; results
+// outside the normal range go through ldexp.
+__device__ __forceinline__ double ll_scaled(long long T, int e) {
+  if (T == 0) return 0.0;
+  const unsigned long long sign = T < 0 ? 0x8000000000000000ull : 0ull;
+  unsigned long long a = T < 0 ? (unsigned long long)(-T) : (unsigned long long)T;
+  const int msb = 63 - __clzll((long long)a);
+  int ee;  // value = a 2^ee with a in [2^52, 2^53)
+  if (msb > 52) {
+    const int sh = msb - 52;
+    const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    a >>= sh;
+    if (rem > half || (rem == half && (a & 1ull))) a++;
+    ee = e + sh;
+    if (a >> 53) {
+      a >>= 1;
+      ee++;
+    }
+  } else {
+    a <<= (52 - msb);
+    ee = e - (52 - msb);
+  }
+  const int be = ee + 52 + 1023;
+  if (be <= 0 || be >= 2047) return ldexp((double)T, e);
+  return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | (a & 0xFFFFFFFFFFFFFull)));
 }
 
 // out[traj][split][M][N] = C (FP64).  maxRow/maxCol (nSplit == 1 only): the
 // largest biased exponent of |C| per output row / column, by atomicMax.
-// aShared: A is one matrix for all trajectories (3D map with one plane); the
-// trajectory's rows start at its vRow and its K range at vRow - gShift.
+// aShared: A is shared by the trajectories (3D map with one plane per root
+// grid); the trajectory's rows start at vRow of plane vRoot, its K range at
+// vRow - gShift, its row exponents at expA[vExp].
 template <int BN, int L, int NA_, int NB_>
 __global__ void __launch_bounds__(128)
     k_fx_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, double* __restrict__ out,
@@ -113,8 +136,8 @@ __global__ void __launch_bounds__(128)
   // blockIdx.z also carries the split: index by trajectory
   const int aRow0 = aShared ? shp[traj].vRow : 0;
   const int aCol0 = aShared ? shp[traj].vRow - shp[traj].gShift : 0;
-  const int aZ = aShared ? 0 : traj;
-  expA = aShared ? expA + aRow0 : batn(expA, bs, traj);
+  const int aZ = aShared ? shp[traj].vRoot : traj;
+  expA = aShared ? expA + shp[traj].vExp : batn(expA, bs, traj);
   expB = batn(expB, bs, traj);
 
   if (threadIdx.x == 0) {
@@ -154,9 +177,11 @@ __global__ void __launch_bounds__(128)
         break;
       }
       const int x0 = (kt0 + kb) * TC_BK;
-      mbar_expect_tx(&bFull[sb], C::BG_BYTES);
+      mbar_expect_tx(&bFull[sb], (uint32_t)(L * nT * TC_BK * 2));
       for (int j = 0; j < L; j++)
-        tma_load_3d(ringB + sb * C::BG_BYTES + j * C::B_BYTES, &tB, &bFull[sb], j * segPitch + x0, n0, traj);
+        for (int r = 0; r < nT; r += 16)
+          tma_load_3d(ringB + sb * C::BG_BYTES + j * C::B_BYTES + r * TC_BK * 2, &tB, &bFull[sb],
+                      j * segPitch + x0, n0 + r, traj);
       issuedB = kb + 1;
       for (int i = 0; i < L; i++) {
         const int t = kb * L + i, sa = t % NA, ra = t / NA;
@@ -174,6 +199,9 @@ __global__ void __launch_bounds__(128)
     // MMA issuer: kind::f16, D=F32, A=B=BF16, K-major, N=nT, M=128
     const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nT >> 3) << 17) |
                            ((uint32_t)(TC_BM >> 4) << 24);
+    // descriptors advance by address / 16: +2 per 16-wide K step, +B_BYTES/16 per B slice
+    const uint64_t bdesc0 = sw128_desc(smem_u32(ringB));
+    const uint64_t adesc0 = sw128_desc(smem_u32(ringA));
     int ca = 0, kb = 0;
     bool ok = true;
     for (; kb < nk && ok; kb++) {
@@ -185,7 +213,8 @@ __global__ void __launch_bounds__(128)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t bBase = smem_u32(ringB + sb * C::BG_BYTES);
+      const uint64_t bd = bdesc0 + (uint64_t)((sb * C::BG_BYTES) >> 4);
+#pragma unroll
       for (int i = 0; i < L; i++) {
         const int sa = ca % NA, ra = ca / NA;
         if (!mbar_wait(&aFull[sa], ra & 1, &abortFlag)) {
@@ -195,15 +224,14 @@ __global__ void __launch_bounds__(128)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t a = smem_u32(ringA + sa * C::A_BYTES);
+        const uint64_t ad = adesc0 + (uint64_t)((sa * C::A_BYTES) >> 4);
 #pragma unroll
-        for (int j = 0; j < L; j++) {
-          if (j >= L - i) break;
-          const uint32_t b = bBase + j * C::B_BYTES;
+        for (int j = 0; j < L - i; j++) {
           const uint32_t d = tmem + (uint32_t)((i + j) * BN);
+          const uint64_t bdj = bd + (uint64_t)((j * C::B_BYTES) >> 4);
 #pragma unroll
           for (int k = 0; k < TC_BK / 16; k++)
-            umma_bf16(d, sw128_desc(a + k * 32), sw128_desc(b + k * 32), idesc, (kb > 0 || i > 0 || k > 0) ? 1u : 0u);
+            umma_bf16(d, ad + 2 * k, bdj + 2 * k, idesc, (kb > 0 || i > 0 || k > 0) ? 1u : 0u);
         }
         umma_commit(&aEmpty[sa]);
         ca++;
@@ -245,7 +273,7 @@ __global__ void __launch_bounds__(128)
           long long T = 0;
 #pragma unroll
           for (int l = 0; l < L; l++) T = T * base + (long long)__float2int_rn(__uint_as_float(acc[l][j]));
-          v = __ll2double_rn(T) * pow2i(ea + expB[col]);
+          v = ll_scaled(T, ea + expB[col]);
           ex = (unsigned)(__double2hiint(v) >> 20) & 0x7FFu;
         }
         stile[r * C::SP + c + j] = v;

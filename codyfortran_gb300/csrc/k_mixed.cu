@@ -43,8 +43,8 @@ struct MixedBufs {
   // contractions (GEMM1, GEMM3) and of the K = 2P one (GEMM2)
   int fxBits = 0, b1 = 0, L1 = 0, b2 = 0, L2 = 0;
   bool compact2 = false;
-  // one interaction matrix for the batch (cgpu_ctx::fxShared): its slices and row
-  // exponents outside the per-trajectory arena
+  // one interaction matrix per root grid (cgpu_ctx::fxShared): slices [root][c->nG][L1 KgBig]
+  // and row exponents [root][c->nG], outside the per-trajectory arena
   int KgBig = 0;
   __nv_bfloat16* Vsh = nullptr;
   int* eVsh = nullptr;
@@ -632,15 +632,21 @@ void mixed_init(cgpu_ctx* c) {
   }
   size_t nGK = (size_t)c->nG * m->KgMax;
   if (m->fxBits && c->fxShared) {
-    // the largest trajectory's interaction matrix, sliced once for the batch
-    const int big = c->fxBig, nGb = c->sys[big].nG;
-    m->KgBig = (nGb + 63) / 64 * 64;
-    CODY_CUDA(cudaMalloc(&m->Vsh, sizeof(__nv_bfloat16) * (size_t)nGb * m->L1 * m->KgBig));
-    CODY_CUDA(cudaMalloc(&m->eVsh, sizeof(int) * (size_t)nGb));
-    const double* Vb = (const double*)((const char*)c->Vint_d + (size_t)big * c->bs);
-    k_fx_split_V<<<dim3(nGb, 1, 1), 256, sizeof(double) * m->KgBig, c->stream>>>(m->Vsh, m->eVsh, Vb, m->KgBig,
-                                                                              m->b1, m->L1, c->shape_d + big, 0);
-    m->mVsh = tc_make_map_planes(m->Vsh, nGb, m->L1 * m->KgBig, 128, 1, 0);
+    // each root trajectory's interaction matrix, sliced once for the batch
+    const int nR = (int)c->fxRoots.size();
+    m->KgBig = (c->nG + 63) / 64 * 64;
+    const size_t plane = (size_t)c->nG * m->L1 * m->KgBig;  // elements per root
+    CODY_CUDA(cudaMalloc(&m->Vsh, sizeof(__nv_bfloat16) * plane * nR));
+    CODY_CUDA(cudaMalloc(&m->eVsh, sizeof(int) * (size_t)c->nG * nR));
+    CODY_CUDA(cudaMemsetAsync(m->Vsh, 0, sizeof(__nv_bfloat16) * plane * nR, c->stream));
+    for (int r = 0; r < nR; r++) {
+      const int root = c->fxRoots[r], nGb = c->sys[root].nG;
+      const double* Vb = (const double*)((const char*)c->Vint_d + (size_t)root * c->bs);
+      k_fx_split_V<<<dim3(nGb, 1, 1), 256, sizeof(double) * m->KgBig, c->stream>>>(
+          m->Vsh + plane * r, m->eVsh + (size_t)c->nG * r, Vb, m->KgBig, m->b1, m->L1, c->shape_d + root, 0);
+      CODY_LAUNCHED(c);
+    }
+    m->mVsh = tc_make_map_planes(m->Vsh, c->nG, m->L1 * m->KgBig, 128, nR, sizeof(__nv_bfloat16) * plane);
   } else if (m->fxBits)
     k_fx_split_V<<<dim3(c->nG, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(m->VxB, m->eV, c->Vint_d,
                                                                                      m->KgMax, m->b1, m->L1,
@@ -650,11 +656,12 @@ void mixed_init(cgpu_ctx* c) {
   CODY_LAUNCHED(c);
   int P2 = 2 * c->nPairs, Q2 = 2 * c->nOS * c->nOS;
   if (m->VxB) m->mV = tc_make_map(c, m->VxB, c->nG, pG, 128);
-  m->mS = tc_make_map(c, m->SxA, P2, pG, m->bn1);
+  // the fixed-point GEMM loads its B operands in 16-row boxes
+  m->mS = tc_make_map(c, m->SxA, P2, pG, m->fxBits ? 16 : m->bn1);
   m->mW = tc_make_map(c, m->WxA, c->nG, pP, 128);
-  m->mR = tc_make_map(c, m->RxB, Q2, pP, m->bn2);
+  m->mR = tc_make_map(c, m->RxB, Q2, pP, m->fxBits ? 16 : m->bn2);
   m->mSasB = tc_make_map(c, m->SxA, P2, pG, 128);
-  m->mWT = tc_make_map(c, m->WTxB, P2, pG, m->bn3);
+  m->mWT = tc_make_map(c, m->WTxB, P2, pG, m->fxBits ? 16 : m->bn3);
   CODY_CUDA(cudaStreamSynchronize(c->stream));
 }
 

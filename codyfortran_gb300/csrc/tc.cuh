@@ -21,7 +21,8 @@ CUtensorMap tc_make_map(const cgpu_ctx* c, const __nv_bfloat16* base, int rowsMa
 void tc_gemm(cgpu_ctx* c, int gemmId, const CUtensorMap& ta, const CUtensorMap& tb, int bn, float* P, int terms,
              int segPitch, int nSplit, int Mmax, int Nmax, int* err);
 
-// Fixed-point slice GEMM (k_fx.cu): out[traj][split][M][N] (FP64) = A B^T for
+// Fixed-point slice GEMM (k_fx.cu): out[traj][split][M][N] (FP64) = A B^T (the
+// B map with 16-row boxes, the A map with 128-row boxes) for
 // operands carried as L base-2^digitBits digit slices (K segments of
 // segPitchA / segPitch elements) with row exponents expA / expB; maxRow /
 // maxCol (unsplit K only) receive the largest biased exponent of |C| per row /
@@ -72,13 +73,25 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+// mbarrier.try_wait: suspends the thread in hardware for a bounded, implementation-defined
+// time while the phase is incomplete; true once it completed.
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 // Bounded wait: false when the limit expires or another role aborted.
 __device__ inline bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abortFlag) {
+  if (mbar_try(bar, parity)) return true;
   long long t0 = clock64();
-  while (!mbar_test(bar, parity)) {
+  while (!mbar_try(bar, parity)) {
     if (*abortFlag) return false;
     if (clock64() - t0 > TC_WAIT_CYCLES) return false;
-    __nanosleep(32);
   }
   return true;
 }

@@ -34,7 +34,7 @@ EXPORTED = [
     "cgpu_profile_begin", "cgpu_profile_end", "cgpu_weighted_gram_noalloc",
     "cgpu_batch_create", "cgpu_batch_destroy", "cgpu_batch_size", "cgpu_batch_sizes", "cgpu_batch_grid",
     "cgpu_batch_upload", "cgpu_batch_download", "cgpu_batch_propagate", "cgpu_batch_energies",
-    "cgpu_batch_kernels_per_step", "cgpu_batch_launch_count", "cgpu_batch_profile_begin", "cgpu_batch_profile_end",
+    "cgpu_batch_kernels_per_step", "cgpu_batch_launch_count", "cgpu_batch_shared_interactions", "cgpu_batch_profile_begin", "cgpu_batch_profile_end",
     "cgpu_tdci_adjoint", "cgpu_observables", "cgpu_relax", "cgpu_batch_observables", "cgpu_save_restart",
     "cgpu_load_restart", "cgpu_absorber_setup", "cgpu_absorber_apply", "cgpu_batch_absorber_setup",
 ]
@@ -89,6 +89,8 @@ def load_library(path: str = LIB_PATH):
     lib.cgpu_batch_kernels_per_step.argtypes = [C.c_void_p]
     lib.cgpu_batch_launch_count.restype = C.c_long
     lib.cgpu_batch_launch_count.argtypes = [C.c_void_p, C.c_int]
+    lib.cgpu_batch_shared_interactions.restype = C.c_int
+    lib.cgpu_batch_shared_interactions.argtypes = [C.c_void_p]
     lib.cgpu_save_restart.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
     lib.cgpu_load_restart.argtypes = [C.c_void_p, C.c_char_p]
     _lib = lib
@@ -506,6 +508,10 @@ class Batch:
         e = np.zeros(len(self))
         self._check(self.lib.cgpu_batch_energies(self.h, _p(tt), _p(e)))
         return e
+
+    def shared_interactions(self):
+        """Number of interaction matrices shared by the batch (fixed-point form), 0 if none."""
+        return self.lib.cgpu_batch_shared_interactions(self.h)
 
     def kernels_per_step(self):
         return self.lib.cgpu_batch_kernels_per_step(self.h)

@@ -302,6 +302,9 @@ long cgpu_batch_kernels_per_step(const cgpu_batch* batch);
 int cgpu_batch_profile_begin(cgpu_batch* batch, int kernel);
 int cgpu_batch_profile_end(cgpu_batch* batch, long* launches, double* total_ms);
 long cgpu_batch_launch_count(cgpu_batch* batch, int reset);
+/* Fixed-point form: the number of shared interaction matrices (root grids in which every
+ * trajectory's grid is a contiguous piece), 0 when each trajectory keeps its own. */
+int cgpu_batch_shared_interactions(const cgpu_batch* batch);
 
 /* ---- no-allocation variant ---------------------------------------------- */
 /* No counterpart in the reference.  Weighted Gram matrix of two orbital sets,

@@ -159,6 +159,7 @@ def test_mixed_fx_shared_interaction_matches_per_trajectory():
     other.int_s1 = 0.7
     shared = Batch(specs, "mixed_fx", max_krylov=12, krylov_window=2)
     single = Batch(specs + [other], "mixed_fx", max_krylov=12, krylov_window=2)
+    assert shared.shared_interactions() >= 1 and single.shared_interactions() == 0
     st = _states(shared.systems, 41)
     st_other = _states(single.systems[-1:], 99)
     shared.upload(st)
