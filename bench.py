@@ -226,12 +226,19 @@ def lanczos_work(systems, K, window=0, sil_per_step=2):
     vectors and the metric), subtracts the projections and forms the new norm
     (reads nv + 1 vectors and the metric, writes w) and scales w into v_{j+1}
     (reads w, writes v_{j+1}): (2 nv + 5) complex and 2 real passes over the
-    state; 16 nv + 13 flops per entry.  The gated second pass does not fire on
-    this workload and is not counted."""
+    state; 16 nv + 13 flops per entry.  The three-term recurrence (window 1)
+    reads v_{j-1}, v_j, w twice (one real dot and ||w||^2, then the update with
+    the new norm), writes w, then scales: 8 complex and 2 real passes, 28 flops
+    per entry.  The gated second pass does not fire on this workload and is not
+    counted."""
     nS = sum(s.nS for s in systems)
-    nvs = [min(j, window) if window > 0 else j for j in range(1, K + 1)]
-    byts = sum(16.0 * (2 * nv + 5) + 16.0 for nv in nvs) * sil_per_step * nS
-    flops = sum(16 * nv + 13 for nv in nvs) * sil_per_step * nS
+    if window == 1:
+        per = [(16.0 * 8 + 16.0, 28) for _ in range(1, K + 1)]
+    else:
+        nvs = [min(j, window) if window > 0 else j for j in range(1, K + 1)]
+        per = [(16.0 * (2 * nv + 5) + 16.0, 16 * nv + 13) for nv in nvs]
+    byts = sum(b for b, _ in per) * sil_per_step * nS
+    flops = sum(f for _, f in per) * sil_per_step * nS
     return byts, float(flops)
 
 
@@ -315,19 +322,19 @@ def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=Fals
 
 def krylov_window(args, precision):
     """Lanczos re-orthogonalisation window: the reference's full loop for the
-    FP64 form, the three-term recurrence (window 2) for the mixed forms unless
+    FP64 form, the three-term recurrence (window 1) for the mixed forms unless
     --krylov-window says otherwise."""
     if args.krylov_window is not None:
         return args.krylov_window
-    return 0 if precision == "fp64" else 2
+    return 0 if precision == "fp64" else 1
 
 
 def window_name(window):
     if window == 0:
         return "full (every basis vector)"
-    if window == 2:
-        return "three-term recurrence (last 2 basis vectors)"
-    return f"last {window} basis vectors"
+    if window == 1:
+        return "three-term recurrence"
+    return f"Gram-Schmidt against the last {window} basis vectors"
 
 
 def run_batch(args):
@@ -523,7 +530,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=25.0)
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one instead of a step graph")
     ap.add_argument("--krylov-window", type=int, default=None,
-                    help="Gram-Schmidt against the last k Krylov vectors (0: all; default 0 for fp64, 2 otherwise)")
+                    help="0: Gram-Schmidt against all Krylov vectors; 1: three-term recurrence; k > 1: against the "
+                         "last k (default 0 for fp64, 1 otherwise)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

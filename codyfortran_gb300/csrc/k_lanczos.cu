@@ -9,8 +9,11 @@
 // v_1..v_j; the kernels remove them in a classical Gram-Schmidt pass (one
 // fused reduction) and a second pass when the first one cancelled most of w,
 // which reproduces the reference's vectors and coefficients to rounding.
-// With a window k > 0 the passes run against v_{j-k+1}..v_j only (k = 2: the
-// three-term recurrence, orthogonal to the rest in exact arithmetic).  Every reduction is deterministic: per-block
+// With a window k > 1 the passes run against v_{j-k+1}..v_j only (orthogonal
+// to the rest in exact arithmetic).  k = 1 is the three-term recurrence
+// proper: w = H v_j - beta_{j-1} v_{j-1}, alpha_j = Re<v_j, w>_m,
+// w -= alpha_j v_j, with beta_{j-1} known from the previous iteration (no dot
+// with v_{j-1}; about 30% fewer FP64 operations per entry than k = 2).  Every reduction is deterministic: per-block
 // partials in a fixed order, re-summed identically by every consumer block.
 //
 // Device scalar block lz[] (doubles):
@@ -434,6 +437,87 @@ __global__ void k_norm_partial(z_t* __restrict__ part, const z_t* __restrict__ v
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
+// Three-term recurrence, pass 1: part[blk*2] = sum m Re(conj(v_j) w'),
+// part[blk*2+1] = sum m |w'|^2, w' = w - beta_{j-1} v_{j-1} (formed on the fly).
+__global__ void __launch_bounds__(LZ_THREADS) k_lz3_dot(z_t* __restrict__ part, const z_t* __restrict__ vPrev,
+                                                         const z_t* __restrict__ vCur, const z_t* __restrict__ w,
+                                                         const double* __restrict__ m, TRAJ_ARGS,
+                                                         const double* __restrict__ lz, int j) {
+  const TrajShape& S = shp[blockIdx.z];
+  lz = bat(lz, bs);
+  if (lz[LZ_DONE] != 0.0) return;
+  vCur = bat(vCur, bs);
+  w = bat(w, bs);
+  m = bat(m, bs);
+  const double beta = (j > 1) ? lz[LZ_BETA + j - 2] : 0.0;
+  vPrev = (j > 1) ? bat(vPrev, bs) : nullptr;
+  const size_t n = S.nS;
+  double a = 0.0, q = 0.0;
+  for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = vidx(S, l);
+    z_t x = w[i];
+    if (vPrev) {
+      const z_t p = vPrev[i];
+      x.x = fma(-beta, p.x, x.x);
+      x.y = fma(-beta, p.y, x.y);
+    }
+    const z_t v = vCur[i];
+    const double mi = m[i];
+    a = fma(mi, fma(v.x, x.x, v.y * x.y), a);
+    q = fma(mi, fma(x.x, x.x, x.y * x.y), q);
+  }
+  const z_t t = block_sum2(zmk(a, q));
+  if (threadIdx.x == 0) {
+    part[(size_t)blockIdx.x * 2] = zmk(t.x, 0.0);
+    part[(size_t)blockIdx.x * 2 + 1] = zmk(t.y, 0.0);
+  }
+}
+
+// Three-term recurrence, pass 2: alpha_j from the pass-1 partials (stored at
+// lz[LZ_D + 2 (j-1)] for k_lz_finish), w <- w - beta_{j-1} v_{j-1} - alpha_j v_j,
+// partials of the new ||w||_m^2.
+__global__ void __launch_bounds__(LZ_THREADS) k_lz3_update(z_t* __restrict__ w, const z_t* __restrict__ vPrev,
+                                                            const z_t* __restrict__ vCur, const z_t* __restrict__ partIn,
+                                                            int nBlkIn, z_t* __restrict__ partOut,
+                                                            const double* __restrict__ m, TRAJ_ARGS,
+                                                            double* __restrict__ lz, int j) {
+  const TrajShape& S = shp[blockIdx.z];
+  lz = bat(lz, bs);
+  if (lz[LZ_DONE] != 0.0) return;
+  w = bat(w, bs);
+  vCur = bat(vCur, bs);
+  partIn = bat(partIn, bs);
+  partOut = bat(partOut, bs);
+  m = bat(m, bs);
+  const double beta = (j > 1) ? lz[LZ_BETA + j - 2] : 0.0;
+  vPrev = (j > 1) ? bat(vPrev, bs) : nullptr;
+  __shared__ z_t al[1];
+  sum_partials(partIn, nBlkIn, 2, 1, al);
+  const double alpha = al[0].x;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    lz[LZ_D + 2 * (j - 1)] = alpha;
+    lz[LZ_D + 2 * (j - 1) + 1] = 0.0;
+  }
+  const size_t n = S.nS;
+  double q = 0.0;
+  for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = vidx(S, l);
+    z_t x = w[i];
+    if (vPrev) {
+      const z_t p = vPrev[i];
+      x.x = fma(-beta, p.x, x.x);
+      x.y = fma(-beta, p.y, x.y);
+    }
+    const z_t v = vCur[i];
+    x.x = fma(-alpha, v.x, x.x);
+    x.y = fma(-alpha, v.y, x.y);
+    w[i] = x;
+    q = fma(m[i], fma(x.x, x.x, x.y * x.y), q);
+  }
+  const z_t t = block_sum2(zmk(q, 0.0));
+  if (threadIdx.x == 0) partOut[blockIdx.x] = t;
+}
+
 }  // namespace
 
 size_t lanczos_partial_need(const cgpu_ctx* c) { return (size_t)c->lzBlocks * (2 * (c->maxKrylov + 1) + 2); }
@@ -462,6 +546,31 @@ void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
   z_t* p3 = p2 + nBlk;
   z_t* p4 = p3 + (size_t)nBlk * (c->maxKrylov + 1);
   if (j > 32) throw std::string("SIL: Krylov order above 32");
+  if (c->krylovWindow == 1) {
+    // three-term recurrence; the gated second pass re-orthogonalises against v_j
+    const z_t* vCur = c->basis_d + ld * (size_t)(j - 1);
+    const z_t* vPrev = (j > 1) ? c->basis_d + ld * (size_t)(j - 2) : nullptr;
+    dim3 g = bgrid(c, nBlk);
+    const int E = c->lzElems;
+    k_lz3_dot<<<g, LZ_THREADS, 0, c->stream>>>(p1, vPrev, vCur, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, j);
+    CODY_LAUNCHED(c);
+    k_lz3_update<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, vPrev, vCur, p1, nBlk, p2, c->metric_d, TRAJ_PASS(c),
+                                                  c->lz_d, j);
+    CODY_LAUNCHED(c);
+    k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p3, 1, vCur, ld, 1, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 0,
+                                            p1 + 1, 2, p2, nBlk);
+    CODY_LAUNCHED(c);
+    k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, vCur, ld, 1, p3, 1, nBlk, p4, c->metric_d, TRAJ_PASS(c),
+                                                c->lz_d, -1, E, p1 + 1, 2, p2);
+    CODY_LAUNCHED(c);
+    z_t* vNext = (j < maxDim) ? c->basis_d + ld * (size_t)j : nullptr;
+    k_lz_finish<<<g, LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p2, p4, p1 + 1, 2, nBlk, TRAJ_PASS(c), c->lz_d, j,
+                                                 maxDim, 1.0e-14);
+    CODY_LAUNCHED(c);
+    k_lz_mark_done<<<bgrid(c, 1), 1, 0, c->stream>>>(c->lz_d, j, c->bs);
+    CODY_LAUNCHED(c);
+    return;
+  }
   const int base = (c->krylovWindow > 0) ? std::max(0, j - c->krylovWindow) : 0;
   const int nv = j - base, s1 = nv + 1;
   const z_t* V = c->basis_d + ld * (size_t)base;

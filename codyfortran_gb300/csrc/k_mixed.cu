@@ -295,7 +295,7 @@ constexpr int FX_LMAX = 8;
 
 // Signed base-2^b digits of x relative to 2^e (|x| < 2^e): X = round(x 2^(bL-e))
 // = sum_i d_i 2^(b(L-1-i)), d_i in [-2^(b-1), 2^(b-1)) for i > 0, |d_0| <= 2^b.
-// Integer operations only (bL <= 52).
+// Integer operations only (bL <= 52); 32-bit arithmetic when bL <= 30.
 __device__ __forceinline__ void fx_digits(double x, int e, int b, int L, int (&d)[FX_LMAX]) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   const int ex = (int)((u >> 52) & 0x7FF);
@@ -305,6 +305,20 @@ __device__ __forceinline__ void fx_digits(double x, int e, int b, int L, int (&d
     const int sh = 1075 - ex - b * L + e;  // >= 53 - bL > 0 because |x| < 2^e
     if (sh < 63) X = (long long)((mant + (1ull << (sh - 1))) >> sh);
     if (u >> 63) X = -X;
+  }
+  if (b * L <= 30) {  // |X| <= 2^30
+    int Y = (int)X;
+    const int base = 1 << b, half = base >> 1, mask = base - 1;
+#pragma unroll
+    for (int i = FX_LMAX - 1; i >= 1; i--) {
+      if (i >= L) continue;
+      int t = Y & mask;
+      if (t >= half) t -= base;
+      d[i] = t;
+      Y = (Y - t) >> b;
+    }
+    d[0] = Y;
+    return;
   }
   const long long base = 1LL << b, half = base >> 1, mask = base - 1;
 #pragma unroll
@@ -316,6 +330,14 @@ __device__ __forceinline__ void fx_digits(double x, int e, int b, int L, int (&d
     X = (X - t) >> b;
   }
   d[0] = (int)X;
+}
+
+// bf16 of an integer |d| <= 256 without a conversion instruction: the FP32
+// magic-number sum 1.5 2^23 + d is exact, subtracting 1.5 2^23 leaves d as an
+// FP32 with at most 9 significant bits, whose upper half is its bf16.
+__device__ __forceinline__ __nv_bfloat16 fx_bf16(int d) {
+  const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
+  return __ushort_as_bfloat16((unsigned short)(__float_as_uint(f) >> 16));
 }
 
 __device__ __forceinline__ unsigned fx_biased_exp(double v) { return (unsigned)(__double2hiint(v) >> 20) & 0x7FFu; }
@@ -330,7 +352,7 @@ __device__ __forceinline__ void fx_store(__nv_bfloat16* rowBase, size_t pitch, i
   if (valid) fx_digits(v, e, b, L, d);
 #pragma unroll
   for (int l = 0; l < FX_LMAX; l++)
-    if (l < L) rowBase[(size_t)l * pitch + k] = __int2bfloat16_rn(d[l]);
+    if (l < L) rowBase[(size_t)l * pitch + k] = fx_bf16(d[l]);
 }
 
 __device__ unsigned fx_block_max(unsigned m) {

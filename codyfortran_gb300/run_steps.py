@@ -30,9 +30,9 @@ def main():
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--trajectories", type=int, default=512)
     ap.add_argument("--krylov-window", type=int, default=None,
-                    help="Gram-Schmidt window of the Lanczos recurrence (default: 0 for fp64, 2 for mixed forms)")
+                    help="Lanczos re-orthogonalisation window (default: 0 for fp64, 1 = three-term recurrence for mixed forms)")
     args = ap.parse_args()
-    window = args.krylov_window if args.krylov_window is not None else (0 if args.precision == "fp64" else 2)
+    window = args.krylov_window if args.krylov_window is not None else (0 if args.precision == "fp64" else 1)
 
     def state(sp, x, w, seed):
         rng = np.random.default_rng(seed)

@@ -101,9 +101,10 @@ typedef struct {
   int precision;                 /* CGPU_PREC_*                                              */
   int max_krylov;                /* largest Krylov dimension the context will be asked for   */
   int krylov_window;             /* 0: each Lanczos vector is orthogonalised against the whole
-                                    basis (the reference's loop); k > 0: against the last k basis
-                                    vectors only (k = 2: the three-term recurrence); the same for
-                                    every trajectory of a batch                                 */
+                                    basis (the reference's loop); 1: the three-term recurrence
+                                    (w = H v_j - beta v_{j-1} - alpha v_j); k > 1: Gram-Schmidt
+                                    against the last k basis vectors; the same for every
+                                    trajectory of a batch                                       */
 } cgpu_desc;
 
 /* ---- context (Fabricate + Setup) ---------------------------------------- */
