@@ -44,6 +44,93 @@ __device__ __forceinline__ z_t zsign(z_t a, bool neg) {
   return make_double2(__longlong_as_double(__double_as_longlong(a.x) ^ m),
                       __longlong_as_double(__double_as_longlong(a.y) ^ m));
 }
+
+// ---- double-float arithmetic (a value as an unevaluated sum hi + lo of two
+// FP32 numbers, about 47 bits): the mixed forms' CI arithmetic, where FP64
+// issue (two FMA per cycle per SM) is the bound and FP32 runs 64 times faster.
+// A complex value is float4 {re.hi, re.lo, im.hi, im.lo} (16 bytes, as z_t).
+
+// x as hi + lo by integer operations: hi = the leading 24 bits (truncated),
+// lo = the next 29 bits rounded down to 24; |x| < 2^-100 becomes 0.
+__device__ __forceinline__ float2 df_split(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
+  const int e = (int)((u >> 52) & 0x7FF) - 1023;
+  if (e < -100) return make_float2(0.0f, 0.0f);
+  if (e > 127) return make_float2(__int_as_float((int)(sign | 0x7F800000u)), 0.0f);
+  const float hi = __int_as_float((int)(sign | ((unsigned)(e + 127) << 23) | (unsigned)((u >> 29) & 0x7FFFFF)));
+  const unsigned r = (unsigned)(u & 0x1FFFFFFF);  // value r 2^(e-52)
+  if (r == 0) return make_float2(hi, 0.0f);
+  const int msb = 31 - __clz(r);
+  const int elo = e - 52 + msb;
+  if (elo < -126) return make_float2(hi, 0.0f);
+  const unsigned mlo = (msb >= 23) ? ((r >> (msb - 23)) & 0x7FFFFF) : ((r << (23 - msb)) & 0x7FFFFF);
+  return make_float2(hi, __int_as_float((int)(sign | ((unsigned)(elo + 127) << 23) | mlo)));
+}
+
+__device__ __forceinline__ float4 zdf_from(z_t z) {
+  const float2 r = df_split(z.x), i = df_split(z.y);
+  return make_float4(r.x, r.y, i.x, i.y);
+}
+
+// (s, c) += p + q with an exact FP32 two-sum of s + p; the rounding errors and
+// q accumulate in c.
+__device__ __forceinline__ void df_acc(float& s, float& c, float p, float q) {
+  const float t = s + p;
+  const float bp = t - s;
+  const float err = (s - (t - bp)) + (p - bp);
+  s = t;
+  c += err + q;
+}
+
+// acc += h * x for complex double-float h, x; x negated when neg (sign bits).
+struct zdf_acc {
+  float rs, rc, is, ic;
+};
+__device__ __forceinline__ void zdf_fma(zdf_acc& a, float4 h, float4 x, bool neg) {
+  if (neg) {
+    x.x = -x.x;
+    x.y = -x.y;
+    x.z = -x.z;
+    x.w = -x.w;
+  }
+  // products a b of double-floats: p = a1 b1 exactly as p + e, plus the cross terms
+  float p, e;
+  p = h.x * x.x;
+  e = fmaf(h.x, x.x, -p);
+  e = fmaf(h.x, x.y, e);
+  e = fmaf(h.y, x.x, e);
+  df_acc(a.rs, a.rc, p, e);  // + hr xr
+  p = h.z * x.z;
+  e = fmaf(h.z, x.z, -p);
+  e = fmaf(h.z, x.w, e);
+  e = fmaf(h.w, x.z, e);
+  df_acc(a.rs, a.rc, -p, -e);  // - hi xi
+  p = h.x * x.z;
+  e = fmaf(h.x, x.z, -p);
+  e = fmaf(h.x, x.w, e);
+  e = fmaf(h.y, x.z, e);
+  df_acc(a.is, a.ic, p, e);  // + hr xi
+  p = h.z * x.x;
+  e = fmaf(h.z, x.x, -p);
+  e = fmaf(h.z, x.y, e);
+  e = fmaf(h.w, x.x, e);
+  df_acc(a.is, a.ic, p, e);  // + hi xr
+}
+
+__device__ __forceinline__ zdf_acc zdf_warp_sum(zdf_acc a) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const float rs = __shfl_xor_sync(0xffffffffu, a.rs, o), rc = __shfl_xor_sync(0xffffffffu, a.rc, o);
+    const float is = __shfl_xor_sync(0xffffffffu, a.is, o), ic = __shfl_xor_sync(0xffffffffu, a.ic, o);
+    df_acc(a.rs, a.rc, rs, rc);
+    df_acc(a.is, a.ic, is, ic);
+  }
+  return a;
+}
+
+__device__ __forceinline__ z_t zdf_to_z(const zdf_acc& a) {
+  return zmk((double)a.rs + (double)a.rc, (double)a.is + (double)a.ic);
+}
 // a += conj(b) * c
 __host__ __device__ __forceinline__ void zcfma(z_t& a, z_t b, z_t c) {
   a.x = fma(b.x, c.x, fma(b.y, c.y, a.x));
@@ -242,6 +329,9 @@ struct cgpu_ctx {
   int *pairL_d = nullptr, *pairK_d = nullptr, *pidx_d = nullptr;
   // CI
   z_t *h1Lin_d = nullptr, *h2Lin_d = nullptr, *rdm1Lin_d = nullptr, *rdm2Lin_d = nullptr;
+  // fixed-point forms: the CI apply in double-float arithmetic, from double-float copies of h1Lin / h2Lin
+  int ciDf = 0;
+  float4 *h1Df_d = nullptr, *h2Df_d = nullptr;
   z_t *rdm1_d = nullptr, *rdm2_d = nullptr, *h1_d = nullptr, *h2_d = nullptr;
   // mean-field
   z_t *S_d = nullptr, *W_d = nullptr;         // (nG, nPairs) row-major by grid point

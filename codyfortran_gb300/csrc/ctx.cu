@@ -322,6 +322,14 @@ size_t layout(cgpu_ctx* c, char* base) {
   Z(c->h1Lin_d, nO2 + 1);
   Z(c->rdm1Lin_d, nO2 + 1);
   Z(c->h2Lin_d, nO4 + 1);
+  if (c->ciDf) {
+    size_t o1 = take(off, sizeof(float4) * (nO2 + 1));
+    size_t o2 = take(off, sizeof(float4) * (nO4 + 1));
+    if (base) {
+      c->h1Df_d = (float4*)(base + o1);
+      c->h2Df_d = (float4*)(base + o2);
+    }
+  }
   Z(c->rdm2Lin_d, nO4 + 1);
   Z(c->rdm1_d, nO2);
   Z(c->h1_d, nO2);
@@ -424,6 +432,7 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
   c->restricted = d0->restricted ? 1 : 0;
   c->method = d0->method;
   c->precision = d0->precision;
+  c->ciDf = (c->precision == CGPU_PREC_MIXED_FX || c->precision == CGPU_PREC_MIXED_FX6) ? 1 : 0;
   c->hasInteraction = d0->has_interaction ? 1 : 0;
   CODY_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   c->sys.resize(nSys);

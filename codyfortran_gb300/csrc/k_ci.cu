@@ -219,6 +219,91 @@ __global__ void k_ci_apply(const z_t* __restrict__ C0, z_t* __restrict__ dC0, co
   }
 }
 
+// H.C in double-float arithmetic (the fixed-point forms): the same traversal as
+// k_ci_apply with C staged in shared memory as double-floats, the integrals read
+// from their double-float copies and every term an FP32 error-free product
+// with two-sum accumulation (~47 bits); one conversion to FP64 per configuration.
+__global__ void k_ci_apply_df(const z_t* __restrict__ C0, z_t* __restrict__ dC0, const float4* __restrict__ h1Df0,
+                              const float4* __restrict__ h2Df0, TRAJ_ARGS, const CiWork* __restrict__ work, int useH1,
+                              int useH2) {
+  extern __shared__ float4 cdf[];
+  const CiWork wk = work[blockIdx.x];
+  const int tb = wk.traj;
+  const CiView& v = shp[tb].view;
+  const z_t* Cg = batn(C0, bs, tb);
+  for (int i = threadIdx.x; i < v.nC; i += blockDim.x) cdf[i] = zdf_from(Cg[i]);
+  __syncthreads();
+  const float4* C = cdf;
+  z_t* dC = batn(dC0, bs, tb);
+  const float4* h1 = batn(h1Df0, bs, tb);
+  const float4* h2 = batn(h2Df0, bs, tb);
+  const int lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  for (int warp = wk.t0 + (threadIdx.x >> 5); warp < wk.t1; warp += nw) {
+    int I = warp + 1;
+    int conf[CODY_MAX_BT];
+    conf_from_index(v, I, conf);
+    zdf_acc acc = {0.0f, 0.0f, 0.0f, 0.0f};
+    int nO2 = v.nO * v.nO;
+    for (int b = 0; b < v.nBt; b++) {
+      int c = conf[b];
+      int st = v.stride[b];
+      if (useH1) {
+        int n = v.sN[b][c - 1];
+        size_t col = (size_t)v.maxS[b] * (c - 1);
+        for (int k = lane; k < n; k += 32) {
+          int oc = v.sCode[b][col + k];
+          int jG = I + (v.sExc[b][col + k] - c) * st;
+          zdf_fma(acc, h1[oc], C[jG - 1], v.sFac[b][col + k] < 0);
+        }
+      }
+      if (useH2) {
+        int n = v.dN[b][c - 1];
+        size_t col = (size_t)v.maxD[b] * (c - 1);
+        for (int k = lane; k < n; k += 32) {
+          int oc = v.dCode[b][col + k];
+          int jG = I + (v.dExc[b][col + k] - c) * st;
+          zdf_fma(acc, h2[oc], C[jG - 1], v.dFac[b][col + k] < 0);
+        }
+        int n1 = v.sN[b][c - 1];
+        size_t col1 = (size_t)v.maxS[b] * (c - 1);
+        for (int b2 = b + 1; b2 < v.nBt; b2++) {
+          int c2 = conf[b2];
+          int n2 = v.sN[b2][c2 - 1];
+          size_t col2 = (size_t)v.maxS[b2] * (c2 - 1);
+          int st2 = v.stride[b2];
+          for (int k2b = 0; k2b < n2; k2b += 32) {
+            int k2 = k2b + lane;
+            bool has2 = k2 < n2;
+            int oc2 = has2 ? v.sCode[b2][col2 + k2] : 0;
+            int d2 = has2 ? (v.sExc[b2][col2 + k2] - c2) * st2 : 0;
+            int f2 = has2 ? v.sFac[b2][col2 + k2] : 0;
+            for (int k1b = 0; k1b < n1; k1b += 32) {
+              int k1 = k1b + lane;
+              int oc1 = 0, d1 = 0, f1 = 0;
+              if (k1 < n1) {
+                oc1 = v.sCode[b][col1 + k1];
+                d1 = (v.sExc[b][col1 + k1] - c) * st;
+                f1 = v.sFac[b][col1 + k1];
+              }
+              int cnt = min(32, n1 - k1b);
+#pragma unroll 4
+              for (int u = 0; u < cnt; u++) {
+                int o1 = __shfl_sync(0xffffffffu, oc1, u);
+                int e1 = __shfl_sync(0xffffffffu, d1, u);
+                int g1 = __shfl_sync(0xffffffffu, f1, u);
+                if (has2) zdf_fma(acc, h2[(o1 - 1) * nO2 + oc2], C[I - 1 + e1 + d2], g1 * f2 < 0);
+              }
+            }
+          }
+        }
+      }
+    }
+    acc = zdf_warp_sum(acc);
+    if (lane == 0) dC[warp] = zadd(dC[warp], zdf_to_z(acc));
+  }
+}
+
 // Configuration index (0-based) of the body types other than b1 and b2 (b2 < 0:
 // only b1 excluded), from r in mixed radix over those body types.
 __device__ __forceinline__ int rest_base(const CiView& v, int r, int b1, int b2) {
@@ -323,13 +408,16 @@ __global__ void k_ci_rdm_pairs(const z_t* __restrict__ C0, z_t* __restrict__ r2L
 }
 
 // FillH1Lin: h1Lin((i1-1)*nO + j1) = h1(i1, j1)
-__global__ void k_fold_h1(z_t* __restrict__ h1Lin, const z_t* __restrict__ h1, TRAJ_ARGS) {
+__global__ void k_fold_h1(z_t* __restrict__ h1Lin, float4* __restrict__ h1Df, const z_t* __restrict__ h1,
+                          TRAJ_ARGS) {
   const int nO = shp[blockIdx.z].nO;
   h1Lin = bat(h1Lin, bs);
+  h1Df = bat(h1Df, bs);
   h1 = bat(h1, bs);
   GRID_STRIDE(e, nO * nO) {
     int i1 = (int)(e % nO), j1 = (int)(e / nO);  // 0-based
     h1Lin[i1 * nO + j1 + 1] = h1[e];
+    if (h1Df) h1Df[i1 * nO + j1 + 1] = zdf_from(h1[e]);
   }
 }
 
@@ -341,11 +429,12 @@ __device__ __forceinline__ bool bt_rule_ok(const int* btOf, int i1, int i2, int 
 }
 
 // FillH2Lin (fermions; inter-body-type pairs use the same antisymmetric form)
-__global__ void k_fold_h2(z_t* __restrict__ h2Lin, const z_t* __restrict__ h2, const int* __restrict__ btOf,
-                          TRAJ_ARGS) {
+__global__ void k_fold_h2(z_t* __restrict__ h2Lin, float4* __restrict__ h2Df, const z_t* __restrict__ h2,
+                          const int* __restrict__ btOf, TRAJ_ARGS) {
   const int nO = shp[blockIdx.z].nO;
   size_t n4 = (size_t)nO * nO * nO * nO;
   h2Lin = bat(h2Lin, bs);
+  h2Df = bat(h2Df, bs);
   h2 = bat(h2, bs);
   btOf = bat(btOf, bs);
   GRID_STRIDE(e, n4) {
@@ -358,6 +447,7 @@ __global__ void k_fold_h2(z_t* __restrict__ h2Lin, const z_t* __restrict__ h2, c
       v = zadd(zsub(zsub(H(i1, i2, j1, j2), H(i1, i2, j2, j1)), H(i2, i1, j1, j2)), H(i2, i1, j2, j1));
     }
     h2Lin[e + 1] = v;
+    if (h2Df) h2Df[e + 1] = zdf_from(v);
   }
 }
 
@@ -621,6 +711,7 @@ void ci_build_work(cgpu_ctx* c) {
   c->ciSmem = need <= 72 * 1024 ? (int)need : 0;  // leaves room for three blocks per SM
   if (c->ciSmem > 48 * 1024) {
     CODY_CUDA(cudaFuncSetAttribute(k_ci_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
+    CODY_CUDA(cudaFuncSetAttribute(k_ci_apply_df, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
     CODY_CUDA(cudaFuncSetAttribute(k_ci_rdm_codes, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
     CODY_CUDA(cudaFuncSetAttribute(k_ci_rdm_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
   }
@@ -628,8 +719,12 @@ void ci_build_work(cgpu_ctx* c) {
 
 void launch_ci_apply(cgpu_ctx* c, const z_t* C, z_t* dC, int useH1, int useH2) {
   ProfScope prof(c, CGPU_KERNEL_CI_APPLY);
-  k_ci_apply<<<c->nApplyWork, 256, c->ciSmem, c->stream>>>(C, dC, c->h1Lin_d, c->h2Lin_d, TRAJ_PASS(c), c->applyWork_d,
-                                                          c->ciSmem > 0, useH1, useH2);
+  if (c->ciDf && c->ciSmem > 0)
+    k_ci_apply_df<<<c->nApplyWork, 256, c->ciSmem, c->stream>>>(C, dC, c->h1Df_d, c->h2Df_d, TRAJ_PASS(c),
+                                                               c->applyWork_d, useH1, useH2);
+  else
+    k_ci_apply<<<c->nApplyWork, 256, c->ciSmem, c->stream>>>(C, dC, c->h1Lin_d, c->h2Lin_d, TRAJ_PASS(c),
+                                                            c->applyWork_d, c->ciSmem > 0, useH1, useH2);
   CODY_LAUNCHED(c);
 }
 
@@ -661,13 +756,15 @@ void launch_ci_rdm(cgpu_ctx* c, const z_t* C, int want1, int want2) {
 void launch_fold_h1(cgpu_ctx* c) {
   ProfScope prof(c, CGPU_KERNEL_FOLD);
   size_t n2 = (size_t)c->nO * c->nO;
-  k_fold_h1<<<bgrid(c, ew_blocks(c, n2)), 256, 0, c->stream>>>(c->h1Lin_d, c->h1_d, TRAJ_PASS(c));
+  k_fold_h1<<<bgrid(c, ew_blocks(c, n2)), 256, 0, c->stream>>>(c->h1Lin_d, c->ciDf ? c->h1Df_d : nullptr, c->h1_d,
+                                                               TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
 void launch_fold_h2(cgpu_ctx* c) {
   ProfScope prof(c, CGPU_KERNEL_FOLD);
   size_t n4 = (size_t)c->nO * c->nO * c->nO * c->nO;
-  k_fold_h2<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(c->h2Lin_d, c->h2_d, c->btOfOrb_d, TRAJ_PASS(c));
+  k_fold_h2<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(c->h2Lin_d, c->ciDf ? c->h2Df_d : nullptr, c->h2_d,
+                                                               c->btOfOrb_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
