@@ -118,6 +118,13 @@ __device__ __forceinline__ void zdf_fma(zdf_acc& a, float4 h, float4 x, bool neg
   df_acc(a.is, a.ic, p, e);  // + hi xr
 }
 
+// acc += conj(h) * x for complex double-floats; x negated when neg.
+__device__ __forceinline__ void zdf_cfma(zdf_acc& a, float4 h, float4 x, bool neg) {
+  h.z = -h.z;
+  h.w = -h.w;
+  zdf_fma(a, h, x, neg);
+}
+
 __device__ __forceinline__ zdf_acc zdf_warp_sum(zdf_acc a) {
   for (int o = 16; o > 0; o >>= 1) {
     const float rs = __shfl_xor_sync(0xffffffffu, a.rs, o), rc = __shfl_xor_sync(0xffffffffu, a.rc, o);

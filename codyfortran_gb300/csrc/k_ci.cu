@@ -407,6 +407,98 @@ __global__ void k_ci_rdm_pairs(const z_t* __restrict__ C0, z_t* __restrict__ r2L
   }
 }
 
+// The RDM gathers in double-float arithmetic (the fixed-point forms): as
+// k_ci_rdm_codes / k_ci_rdm_pairs with C staged as double-floats and every
+// product conj(C_J) C_I an FP32 error-free product with two-sum accumulation.
+__global__ void k_ci_rdm_codes_df(const z_t* __restrict__ C0, z_t* __restrict__ r1Lin0, z_t* __restrict__ r2Lin0,
+                                  TRAJ_ARGS, const CiWork* __restrict__ work, int want1, int want2) {
+  extern __shared__ float4 cdf[];
+  const CiWork wk = work[blockIdx.x];
+  const int tb = wk.traj;
+  const CiView& v = shp[tb].view;
+  const z_t* Cg = batn(C0, bs, tb);
+  for (int i = threadIdx.x; i < v.nC; i += blockDim.x) cdf[i] = zdf_from(Cg[i]);
+  __syncthreads();
+  const float4* C = cdf;
+  z_t* r1Lin = batn(r1Lin0, bs, tb);
+  z_t* r2Lin = batn(r2Lin0, bs, tb);
+  int nS = 0;
+  for (int b = 0; b < v.nBt; b++) nS += v.nSc[b];
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int task = wk.t0 + (threadIdx.x >> 5); task < wk.t1; task += nw) {
+    int q = task;
+    const int kind = q < nS ? 0 : 1;
+    if (kind == 1) q -= nS;
+    if ((kind == 0 && !want1) || (kind == 1 && !want2)) continue;
+    int b = 0;
+    const int* cnt = kind == 0 ? v.nSc : v.nDc;
+    while (q >= cnt[b]) q -= cnt[b++];
+    const int* start = kind == 0 ? v.sxStart[b] : v.dxStart[b];
+    const int* src = kind == 0 ? v.sxSrc[b] : v.dxSrc[b];
+    const int* dst = kind == 0 ? v.sxDst[b] : v.dxDst[b];
+    const int8_t* fac = kind == 0 ? v.sxFac[b] : v.dxFac[b];
+    const int e0 = start[q], e1 = start[q + 1];
+    const int nRest = v.nC / v.nConf[b], st = v.stride[b];
+    zdf_acc acc = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (nRest == 1) {
+      for (int e = e0 + lane; e < e1; e += 32) zdf_cfma(acc, C[dst[e] * st], C[src[e] * st], fac[e] < 0);
+    } else {
+      for (int t = lane; t < (e1 - e0) * nRest; t += 32) {
+        int e = e0 + t / nRest, r = t % nRest;
+        int base = rest_base(v, r, b, -1);
+        zdf_cfma(acc, C[base + dst[e] * st], C[base + src[e] * st], fac[e] < 0);
+      }
+    }
+    acc = zdf_warp_sum(acc);
+    if (lane == 0) (kind == 0 ? r1Lin : r2Lin)[kind == 0 ? v.sxCode[b][q] : v.dxCode[b][q]] = zdf_to_z(acc);
+  }
+}
+
+__global__ void k_ci_rdm_pairs_df(const z_t* __restrict__ C0, z_t* __restrict__ r2Lin0, TRAJ_ARGS,
+                                  const CiWork* __restrict__ work) {
+  extern __shared__ float4 cdf[];
+  const CiWork wk = work[blockIdx.x];
+  const int tb = wk.traj;
+  const CiView& v = shp[tb].view;
+  const z_t* Cg = batn(C0, bs, tb);
+  for (int i = threadIdx.x; i < v.nC; i += blockDim.x) cdf[i] = zdf_from(Cg[i]);
+  __syncthreads();
+  const float4* C = cdf;
+  z_t* r2Lin = batn(r2Lin0, bs, tb);
+  const int nO2 = v.nO * v.nO;
+  for (int task = wk.t0 + threadIdx.x; task < wk.t1; task += blockDim.x) {
+    int q = task, b1 = 0, b2 = 1;
+    for (;;) {
+      int seg = v.nSc[b1] * v.nSc[b2];
+      if (q < seg) break;
+      q -= seg;
+      if (++b2 >= v.nBt) { b1++; b2 = b1 + 1; }
+    }
+    int q1 = q / v.nSc[b2], q2 = q % v.nSc[b2];
+    int s1 = v.sxStart[b1][q1], n1 = v.sxStart[b1][q1 + 1] - s1;
+    int s2 = v.sxStart[b2][q2], n2 = v.sxStart[b2][q2 + 1] - s2;
+    int st1 = v.stride[b1], st2 = v.stride[b2];
+    int nRest = v.nC / (v.nConf[b1] * v.nConf[b2]);
+    const int *src1 = v.sxSrc[b1], *dst1 = v.sxDst[b1], *src2 = v.sxSrc[b2], *dst2 = v.sxDst[b2];
+    const int8_t *fac1 = v.sxFac[b1], *fac2 = v.sxFac[b2];
+    zdf_acc acc = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int e1 = s1; e1 < s1 + n1; e1++) {
+      int i1 = src1[e1] * st1, j1 = dst1[e1] * st1;
+      bool g1 = fac1[e1] < 0;
+#pragma unroll 4
+      for (int e2 = s2; e2 < s2 + n2; e2++) {
+        int i2 = src2[e2] * st2, j2 = dst2[e2] * st2;
+        bool neg = g1 != (fac2[e2] < 0);
+        for (int r = 0; r < nRest; r++) {
+          int base = nRest == 1 ? 0 : rest_base(v, r, b1, b2);
+          zdf_cfma(acc, C[base + j1 + j2], C[base + i1 + i2], neg);
+        }
+      }
+    }
+    r2Lin[(v.sxCode[b1][q1] - 1) * nO2 + v.sxCode[b2][q2]] = zdf_to_z(acc);
+  }
+}
+
 // FillH1Lin: h1Lin((i1-1)*nO + j1) = h1(i1, j1)
 __global__ void k_fold_h1(z_t* __restrict__ h1Lin, float4* __restrict__ h1Df, const z_t* __restrict__ h1,
                           TRAJ_ARGS) {
@@ -712,6 +804,8 @@ void ci_build_work(cgpu_ctx* c) {
   if (c->ciSmem > 48 * 1024) {
     CODY_CUDA(cudaFuncSetAttribute(k_ci_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
     CODY_CUDA(cudaFuncSetAttribute(k_ci_apply_df, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
+    CODY_CUDA(cudaFuncSetAttribute(k_ci_rdm_codes_df, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
+    CODY_CUDA(cudaFuncSetAttribute(k_ci_rdm_pairs_df, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
     CODY_CUDA(cudaFuncSetAttribute(k_ci_rdm_codes, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
     CODY_CUDA(cudaFuncSetAttribute(k_ci_rdm_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, c->ciSmem));
   }
@@ -732,14 +826,22 @@ void launch_ci_rdm(cgpu_ctx* c, const z_t* C, int want1, int want2) {
   ProfScope prof(c, CGPU_KERNEL_CI_RDM);
   size_t n2 = (size_t)c->nO * c->nO, n4 = n2 * n2;
   // every code present is written; the other entries of the Lin arrays stay zero
+  const bool df = c->ciDf && c->ciSmem > 0;
   if (c->nRdmWork > 0) {
-    k_ci_rdm_codes<<<c->nRdmWork, 256, c->ciSmem, c->stream>>>(C, c->rdm1Lin_d, c->rdm2Lin_d, TRAJ_PASS(c),
-                                                               c->rdmWork_d, c->ciSmem > 0, want1, want2);
+    if (df)
+      k_ci_rdm_codes_df<<<c->nRdmWork, 256, c->ciSmem, c->stream>>>(C, c->rdm1Lin_d, c->rdm2Lin_d, TRAJ_PASS(c),
+                                                                    c->rdmWork_d, want1, want2);
+    else
+      k_ci_rdm_codes<<<c->nRdmWork, 256, c->ciSmem, c->stream>>>(C, c->rdm1Lin_d, c->rdm2Lin_d, TRAJ_PASS(c),
+                                                                 c->rdmWork_d, c->ciSmem > 0, want1, want2);
     CODY_LAUNCHED(c);
   }
   if (want2 && c->nPairWork > 0) {
-    k_ci_rdm_pairs<<<c->nPairWork, 128, c->ciSmem, c->stream>>>(C, c->rdm2Lin_d, TRAJ_PASS(c), c->pairWork_d,
-                                                                c->ciSmem > 0);
+    if (df)
+      k_ci_rdm_pairs_df<<<c->nPairWork, 128, c->ciSmem, c->stream>>>(C, c->rdm2Lin_d, TRAJ_PASS(c), c->pairWork_d);
+    else
+      k_ci_rdm_pairs<<<c->nPairWork, 128, c->ciSmem, c->stream>>>(C, c->rdm2Lin_d, TRAJ_PASS(c), c->pairWork_d,
+                                                                  c->ciSmem > 0);
     CODY_LAUNCHED(c);
   }
   if (want1) {
