@@ -135,8 +135,28 @@ __device__ __forceinline__ zdf_acc zdf_warp_sum(zdf_acc a) {
   return a;
 }
 
+// An FP32 value as FP64 by integer operations (exact; zero and FP32
+// subnormals, below 2^-126, give 0).
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xFFu;
+  if (e == 0) return 0.0;
+  const unsigned long long be = (e == 0xFFu) ? 0x7FFull : (unsigned long long)(e - 127 + 1023);
+  return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) | (be << 52) |
+                                          ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+
 __device__ __forceinline__ z_t zdf_to_z(const zdf_acc& a) {
-  return zmk((double)a.rs + (double)a.rc, (double)a.is + (double)a.ic);
+  return zmk(f2d_exact(a.rs) + f2d_exact(a.rc), f2d_exact(a.is) + f2d_exact(a.ic));
+}
+
+// (s, c) += a * b for double-floats a, b (error-free FP32 product plus cross terms).
+__device__ __forceinline__ void df_mul_acc(float& s, float& c, float a1, float a2, float b1, float b2) {
+  const float p = a1 * b1;
+  float e = fmaf(a1, b1, -p);
+  e = fmaf(a1, b2, e);
+  e = fmaf(a2, b1, e);
+  df_acc(s, c, p, e);
 }
 // a += conj(b) * c
 __host__ __device__ __forceinline__ void zcfma(z_t& a, z_t b, z_t c) {
@@ -339,6 +359,7 @@ struct cgpu_ctx {
   // fixed-point forms: the CI apply in double-float arithmetic, from double-float copies of h1Lin / h2Lin
   int ciDf = 0;
   float4 *h1Df_d = nullptr, *h2Df_d = nullptr;
+  float2* Tdf_d = nullptr;  // double-float copy of the kinetic band (static)
   z_t *rdm1_d = nullptr, *rdm2_d = nullptr, *h1_d = nullptr, *h2_d = nullptr;
   // mean-field
   z_t *S_d = nullptr, *W_d = nullptr;         // (nG, nPairs) row-major by grid point

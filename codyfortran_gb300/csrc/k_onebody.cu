@@ -103,6 +103,59 @@ __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, c
   out[o] = r;
 }
 
+// The one-body apply in double-float arithmetic (the fixed-point forms): the
+// orbital tile staged as double-floats, the static double-float band, every
+// product error-free in FP32 with two-sum accumulation; the potential V0 + E x
+// formed in FP64 (one FMA) and split.
+__global__ void k_onebody_df(z_t* __restrict__ out, const z_t* __restrict__ orbs, const float2* __restrict__ Tdf,
+                             const double* __restrict__ V0, const double* __restrict__ x,
+                             const int* __restrict__ btOf, TRAJ_ARGS, const double* __restrict__ Efield, z_t alpha,
+                             int accumulate) {
+  extern __shared__ float4 shf[];
+  const TrajShape& S = shp[blockIdx.z];
+  const int nG = S.nG, band = S.band;
+  int i = blockIdx.y;
+  int g0 = blockIdx.x * OB_THREADS;
+  if (i >= S.nOS || g0 >= nG) return;
+  out = bat(out, bs);
+  orbs = bat(orbs, bs);
+  Tdf = bat(Tdf, bs);
+  V0 = bat(V0, bs);
+  x = bat(x, bs);
+  btOf = bat(btOf, bs);
+  const double E = *bat(Efield, bs);
+  const z_t* f = orbs + (size_t)nG * i;
+  int nTile = OB_THREADS + 2 * band;
+  for (int t = threadIdx.x; t < nTile; t += OB_THREADS) {
+    int g = g0 - band + t;
+    shf[t] = (g >= 0 && g < nG) ? zdf_from(f[g]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+  __syncthreads();
+  int g = g0 + threadIdx.x;
+  if (g >= nG) return;
+  int bt = S.restricted ? 0 : btOf[i];
+  int nd = 2 * band + 1;
+  const float2* Tb = Tdf + (size_t)bt * nd * nG;
+  zdf_acc acc = {0.0f, 0.0f, 0.0f, 0.0f};
+  for (int d = 0; d < nd; d++) {
+    const float2 cf = Tb[(size_t)d * nG + g];
+    const float4 v = shf[threadIdx.x + d];
+    df_mul_acc(acc.rs, acc.rc, cf.x, cf.y, v.x, v.y);
+    df_mul_acc(acc.is, acc.ic, cf.x, cf.y, v.z, v.w);
+  }
+  if (S.hasPot) {
+    const float2 pd = df_split(fma(E, x[g], V0[g]));
+    const float4 v = shf[threadIdx.x + band];
+    df_mul_acc(acc.rs, acc.rc, pd.x, pd.y, v.x, v.y);
+    df_mul_acc(acc.is, acc.ic, pd.x, pd.y, v.z, v.w);
+  }
+  const z_t a = zdf_to_z(acc);
+  z_t r = (alpha.x == 1.0 && alpha.y == 0.0) ? a : (alpha.x == 0.0 && alpha.y == -1.0) ? zmi(a) : zmul(alpha, a);
+  size_t o = (size_t)nG * i + g;
+  if (accumulate) r = zadd(out[o], r);
+  out[o] = r;
+}
+
 // Column range of a Gram / projector call: group < 0 = all stored orbitals,
 // otherwise projector group `group` (false when the trajectory has none).
 __device__ __forceinline__ bool gram_cols(const TrajShape& S, int group, int& c0, int& n) {
@@ -522,6 +575,62 @@ void check_partial(const cgpu_ctx* c, size_t need) {
 }
 
 // grid/launch of the two-kernel Gram: G (n x n) = scale * A^H W B over the group's columns
+// The weighted Gram partials in double-float arithmetic (the fixed-point forms):
+// the chunk of A and w B staged as double-floats, every term conj(a) b an
+// error-free FP32 product with two-sum accumulation, FP64 partials out.
+__global__ void k_gram_partial_df(z_t* __restrict__ part, const z_t* __restrict__ A, const z_t* __restrict__ B,
+                                  const double* __restrict__ w, TRAJ_ARGS, int group, int chunk) {
+  extern __shared__ float4 shg[];
+  const TrajShape& S = shp[blockIdx.z];
+  int c0, n;
+  if (!gram_cols(S, group, c0, n)) return;
+  const int nG = S.nG;
+  part = bat(part, bs);
+  A = bat(A, bs);
+  B = bat(B, bs);
+  w = bat(w, bs);
+  float4* sa = shg;              // chunk x n
+  float4* sb = shg + chunk * n;  // chunk x n
+  int nn = n * n;
+  zdf_acc acc[GR_PER_THREAD];
+  for (int q = 0; q < GR_PER_THREAD; q++) acc[q] = {0.0f, 0.0f, 0.0f, 0.0f};
+  for (int r0 = blockIdx.x * chunk; r0 < nG; r0 += gridDim.x * chunk) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < chunk * n; t += blockDim.x) {
+      int col = t / chunk, r = t % chunk;
+      int g = r0 + r;
+      float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a;
+      if (g < nG) {
+        a = zdf_from(A[(size_t)nG * (c0 + col) + g]);
+        const float4 bb = zdf_from(B[(size_t)nG * (c0 + col) + g]);
+        const float2 wg = df_split(w[g]);
+        zdf_acc t2 = {0.0f, 0.0f, 0.0f, 0.0f};
+        df_mul_acc(t2.rs, t2.rc, wg.x, wg.y, bb.x, bb.y);
+        df_mul_acc(t2.is, t2.ic, wg.x, wg.y, bb.z, bb.w);
+        b = make_float4(t2.rs, t2.rc, t2.is, t2.ic);
+      }
+      sa[r * n + col] = a;
+      sb[r * n + col] = b;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < GR_PER_THREAD; q++) {
+      int e = threadIdx.x + q * blockDim.x;
+      if (e >= nn) break;
+      int ii = e % n, jj = e / n;
+      zdf_acc s = acc[q];
+      for (int r = 0; r < chunk; r++) zdf_cfma(s, sa[r * n + ii], sb[r * n + jj], false);
+      acc[q] = s;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < GR_PER_THREAD; q++) {
+    int e = threadIdx.x + q * blockDim.x;
+    if (e >= nn) break;
+    part[(size_t)blockIdx.x * nn + e] = zdf_to_z(acc[q]);
+  }
+}
+
 void launch_gram(cgpu_ctx* c, z_t* G, const z_t* A, const z_t* B, int group, int nMax, double scale) {
   int chunk = gram_chunk(nMax);
   int nBlk = gram_blocks(c, chunk);
@@ -529,7 +638,12 @@ void launch_gram(cgpu_ctx* c, z_t* G, const z_t* A, const z_t* B, int group, int
   size_t sh = 2 * sizeof(z_t) * chunk * nMax;
   int threads = 256;
   if (nMax * nMax > GR_PER_THREAD * threads) throw std::string("launch_gram: more than 64 orbitals");
-  k_gram_partial<<<bgrid(c, nBlk), threads, sh, c->stream>>>(c->partial_d, A, B, c->w_d, TRAJ_PASS(c), group, chunk);
+  if (c->ciDf)
+    k_gram_partial_df<<<bgrid(c, nBlk), threads, sh, c->stream>>>(c->partial_d, A, B, c->w_d, TRAJ_PASS(c), group,
+                                                                  chunk);
+  else
+    k_gram_partial<<<bgrid(c, nBlk), threads, sh, c->stream>>>(c->partial_d, A, B, c->w_d, TRAJ_PASS(c), group,
+                                                               chunk);
   CODY_LAUNCHED(c);
   k_gram_final<<<bgrid(c, ceil_div((size_t)nMax * nMax * 32, 256)), 256, 0, c->stream>>>(G, c->partial_d, nBlk,
                                                                                          TRAJ_PASS(c), group, scale);
@@ -559,8 +673,12 @@ void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha,
   double* E = c->scal_d + CODY_SCAL_FIELD;
   k_field<<<bgrid(c, 1), 1, 0, c->stream>>>(E, TRAJ_PASS(c), base, off);
   CODY_LAUNCHED(c);
-  k_onebody<<<grid, OB_THREADS, sh, c->stream>>>(out, orbs, c->T_d, c->V0_d, c->x_d, c->btOfOrb_d, TRAJ_PASS(c), E,
-                                                 alpha, accumulate);
+  if (c->Tdf_d)
+    k_onebody_df<<<grid, OB_THREADS, sh, c->stream>>>(out, orbs, c->Tdf_d, c->V0_d, c->x_d, c->btOfOrb_d,
+                                                      TRAJ_PASS(c), E, alpha, accumulate);
+  else
+    k_onebody<<<grid, OB_THREADS, sh, c->stream>>>(out, orbs, c->T_d, c->V0_d, c->x_d, c->btOfOrb_d, TRAJ_PASS(c), E,
+                                                   alpha, accumulate);
   CODY_LAUNCHED(c);
 }
 
