@@ -45,6 +45,52 @@ __device__ __forceinline__ z_t zsign(z_t a, bool neg) {
                       __longlong_as_double(__double_as_longlong(a.y) ^ m));
 }
 
+// ---- element formulas shared by the nO^4 layout kernels and their fused forms
+
+// Body-type rule of FillH2Lin / FillRdm2FromRdm2Lin.
+__device__ __forceinline__ bool bt_rule_ok(const int* btOf, int i1, int i2, int j1, int j2) {
+  int bi1 = btOf[i1], bi2 = btOf[i2], bj1 = btOf[j1], bj2 = btOf[j2];
+  if (bi1 == bi2 && bj1 != bj2) return false;
+  if (bi1 != bi2 && bj1 == bj2) return false;
+  return true;
+}
+
+// rdm2(a, b, c, d) (index a + n (b + n (c + n d))) from rdm2Lin (FillRdm2FromRdm2Lin).
+__device__ __forceinline__ z_t rdm2_from_lin(const z_t* __restrict__ lin, const int* __restrict__ btOf, size_t n, int a,
+                                             int b, int c, int d) {
+  auto L = [&](int i1, int j1, int i2, int j2) { return lin[(((size_t)i1 * n + j1) * n + i2) * n + j2 + 1]; };
+  z_t s = make_double2(0.0, 0.0);
+  if (a <= b && c <= d && bt_rule_ok(btOf, a, b, c, d)) s = zadd(s, L(a, c, b, d));
+  if (b <= a && c <= d && bt_rule_ok(btOf, b, a, c, d)) s = zsub(s, L(b, c, a, d));
+  if (a <= b && d <= c && bt_rule_ok(btOf, a, b, d, c)) s = zsub(s, L(a, d, b, c));
+  if (b <= a && d <= c && bt_rule_ok(btOf, b, a, d, c)) s = zadd(s, L(b, d, a, c));
+  return s;
+}
+
+// h2(i1, l2, j1, k2) (index i1 + N (l2 + N (j1 + N k2))) from the spatial H2s.
+__device__ __forceinline__ z_t h2_from_h2s(const z_t* __restrict__ H2s, const int* __restrict__ btOf, int restricted,
+                                           int n, int i1, int l2, int j1, int k2) {
+  if (restricted) {
+    int s1 = i1 / n, s2 = l2 / n, s3 = j1 / n, s4 = k2 / n;
+    if (s1 == s3 && s2 == s4) {
+      int a = i1 % n, b = l2 % n, c = j1 % n, d = k2 % n;
+      return H2s[(size_t)(a * n + c) * n * n + (b * n + d)];
+    }
+    return make_double2(0.0, 0.0);
+  }
+  if (btOf[i1] == btOf[j1] && btOf[l2] == btOf[k2]) return H2s[(size_t)(i1 * n + j1) * n * n + (l2 * n + k2)];
+  return make_double2(0.0, 0.0);
+}
+
+// h2Lin(orbCode) (FillH2Lin, fermions) with H(a, b, c, d) = h2(a, b, c, d).
+template <class H>
+__device__ __forceinline__ z_t h2lin_value(const int* __restrict__ btOf, int i1, int j1, int i2, int j2, H h) {
+  z_t v = make_double2(0.0, 0.0);
+  if (i1 <= i2 && j1 <= j2 && bt_rule_ok(btOf, i1, i2, j1, j2) && i1 != i2 && j1 != j2)
+    v = zadd(zsub(zsub(h(i1, i2, j1, j2), h(i1, i2, j2, j1)), h(i2, i1, j1, j2)), h(i2, i1, j2, j1));
+  return v;
+}
+
 // ---- double-float arithmetic (a value as an unevaluated sum hi + lo of two
 // FP32 numbers, about 47 bits): the mixed forms' CI arithmetic, where FP64
 // issue (two FMA per cycle per SM) is the bound and FP32 runs 64 times faster.
@@ -358,6 +404,9 @@ struct cgpu_ctx {
   z_t *h1Lin_d = nullptr, *h2Lin_d = nullptr, *rdm1Lin_d = nullptr, *rdm2Lin_d = nullptr;
   // fixed-point forms: the CI apply in double-float arithmetic, from double-float copies of h1Lin / h2Lin
   int ciDf = 0;
+  // inside the NonLin time derivative: r2s from rdm2Lin and h2Lin from h2s
+  // directly (the nO^4 rdm2 / h2 tensors are not formed)
+  int fuseLayouts = 0;
   float4 *h1Df_d = nullptr, *h2Df_d = nullptr;
   float2* Tdf_d = nullptr;  // double-float copy of the kinetic band (static)
   z_t *rdm1_d = nullptr, *rdm2_d = nullptr, *h1_d = nullptr, *h2_d = nullptr;

@@ -641,6 +641,13 @@ void td_device(cgpu_ctx* c, int which, z_t* out, const z_t* in, double t, z_t po
     return;
   }
   if (which != CGPU_TD_FULL && which != CGPU_TD_NONLIN) throw std::string("unknown time-derivative selector");
+  // the nO^4 rdm2 / h2 tensors are not needed inside the derivative
+  struct FuseScope {
+    cgpu_ctx* c;
+    int prev;
+    explicit FuseScope(cgpu_ctx* cc) : c(cc), prev(cc->fuseLayouts) { c->fuseLayouts = 1; }
+    ~FuseScope() { c->fuseLayouts = prev; }
+  } fuse(c);
   launch_ci_rdm(c, C, 1, 1);
   if (which == CGPU_TD_FULL) {
     launch_onebody(c, dOrbs, orbs, t, zmk(1.0, 0.0), 0);

@@ -513,13 +513,6 @@ __global__ void k_fold_h1(z_t* __restrict__ h1Lin, float4* __restrict__ h1Df, co
   }
 }
 
-__device__ __forceinline__ bool bt_rule_ok(const int* btOf, int i1, int i2, int j1, int j2) {
-  int bi1 = btOf[i1], bi2 = btOf[i2], bj1 = btOf[j1], bj2 = btOf[j2];
-  if (bi1 == bi2 && bj1 != bj2) return false;
-  if (bi1 != bi2 && bj1 == bj2) return false;
-  return true;
-}
-
 // FillH2Lin (fermions; inter-body-type pairs use the same antisymmetric form)
 __global__ void k_fold_h2(z_t* __restrict__ h2Lin, float4* __restrict__ h2Df, const z_t* __restrict__ h2,
                           const int* __restrict__ btOf, TRAJ_ARGS) {
@@ -532,13 +525,32 @@ __global__ void k_fold_h2(z_t* __restrict__ h2Lin, float4* __restrict__ h2Df, co
   GRID_STRIDE(e, n4) {
     // e = orbCode - 1 with orbCode = (((i1-1) nO + j1 - 1) nO + i2 - 1) nO + j2
     int j2 = (int)(e % nO), i2 = (int)((e / nO) % nO), j1 = (int)((e / nO / nO) % nO), i1 = (int)(e / nO / nO / nO);
-    z_t v = zmk(0.0, 0.0);
-    if (i1 <= i2 && j1 <= j2 && bt_rule_ok(btOf, i1, i2, j1, j2) && i1 != i2 && j1 != j2) {
-      size_t n = nO;
-      auto H = [&](int a, int b, int c, int d) { return h2[a + n * (b + n * (c + n * d))]; };
-      v = zadd(zsub(zsub(H(i1, i2, j1, j2), H(i1, i2, j2, j1)), H(i2, i1, j1, j2)), H(i2, i1, j2, j1));
-    }
+    const size_t n = nO;
+    const z_t v = h2lin_value(btOf, i1, j1, i2, j2,
+                              [&](int a, int b, int c, int d) { return h2[a + n * (b + n * (c + n * d))]; });
     h2Lin[e + 1] = v;
+    if (h2Df) h2Df[e + 1] = zdf_from(v);
+  }
+}
+
+// FillH2Lin straight from the spatial H2s (inside the NonLin derivative: the
+// nO^4 h2 is not formed); the same values as k_h2_layout + k_fold_h2.  h2Lin
+// (FP64) is written when non-null, h2Df when non-null.
+__global__ void k_fold_h2s(z_t* __restrict__ h2Lin, float4* __restrict__ h2Df, const z_t* __restrict__ H2s,
+                           const int* __restrict__ btOf, TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int nO = T.nO, n = T.nOS, restricted = T.restricted;
+  size_t n4 = (size_t)nO * nO * nO * nO;
+  h2Lin = bat(h2Lin, bs);
+  h2Df = bat(h2Df, bs);
+  H2s = bat(H2s, bs);
+  btOf = bat(btOf, bs);
+  GRID_STRIDE(e, n4) {
+    int j2 = (int)(e % nO), i2 = (int)((e / nO) % nO), j1 = (int)((e / nO / nO) % nO), i1 = (int)(e / nO / nO / nO);
+    const z_t v = h2lin_value(btOf, i1, j1, i2, j2, [&](int a, int b, int c, int d) {
+      return h2_from_h2s(H2s, btOf, restricted, n, a, b, c, d);
+    });
+    if (h2Lin) h2Lin[e + 1] = v;
     if (h2Df) h2Df[e + 1] = zdf_from(v);
   }
 }
@@ -563,13 +575,7 @@ __global__ void k_unfold_rdm2(z_t* __restrict__ rdm2, const z_t* __restrict__ li
   btOf = bat(btOf, bs);
   GRID_STRIDE(e, n * n * n * n) {
     int a = (int)(e % n), b = (int)((e / n) % n), c = (int)((e / n / n) % n), d = (int)(e / n / n / n);
-    auto L = [&](int i1, int j1, int i2, int j2) { return lin[(((size_t)i1 * n + j1) * n + i2) * n + j2 + 1]; };
-    z_t s = zmk(0.0, 0.0);
-    if (a <= b && c <= d && bt_rule_ok(btOf, a, b, c, d)) s = zadd(s, L(a, c, b, d));
-    if (b <= a && c <= d && bt_rule_ok(btOf, b, a, c, d)) s = zsub(s, L(b, c, a, d));
-    if (a <= b && d <= c && bt_rule_ok(btOf, a, b, d, c)) s = zsub(s, L(a, d, b, c));
-    if (b <= a && d <= c && bt_rule_ok(btOf, b, a, d, c)) s = zadd(s, L(b, d, a, c));
-    rdm2[e] = s;
+    rdm2[e] = rdm2_from_lin(lin, btOf, n, a, b, c, d);
   }
 }
 
@@ -848,7 +854,7 @@ void launch_ci_rdm(cgpu_ctx* c, const z_t* C, int want1, int want2) {
     k_unfold_rdm1<<<bgrid(c, ew_blocks(c, n2)), 256, 0, c->stream>>>(c->rdm1_d, c->rdm1Lin_d, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
   }
-  if (want2) {
+  if (want2 && !c->fuseLayouts) {
     k_unfold_rdm2<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(c->rdm2_d, c->rdm2Lin_d, c->btOfOrb_d,
                                                                        TRAJ_PASS(c));
     CODY_LAUNCHED(c);
@@ -866,7 +872,15 @@ void launch_fold_h1(cgpu_ctx* c) {
 void launch_fold_h2(cgpu_ctx* c) {
   ProfScope prof(c, CGPU_KERNEL_FOLD);
   size_t n4 = (size_t)c->nO * c->nO * c->nO * c->nO;
-  k_fold_h2<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(c->h2Lin_d, c->ciDf ? c->h2Df_d : nullptr, c->h2_d,
-                                                               c->btOfOrb_d, TRAJ_PASS(c));
+  if (c->fuseLayouts) {
+    // h2Lin from the spatial H2s; the FP64 copy only when the FP64 CI apply reads it
+    const bool dfOnly = c->ciDf && c->ciSmem > 0;
+    k_fold_h2s<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(dfOnly ? nullptr : c->h2Lin_d,
+                                                                  c->ciDf ? c->h2Df_d : nullptr, c->h2s_d,
+                                                                  c->btOfOrb_d, TRAJ_PASS(c));
+  } else {
+    k_fold_h2<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(c->h2Lin_d, c->ciDf ? c->h2Df_d : nullptr, c->h2_d,
+                                                                 c->btOfOrb_d, TRAJ_PASS(c));
+  }
   CODY_LAUNCHED(c);
 }

@@ -101,17 +101,7 @@ __global__ void k_h2_layout(z_t* __restrict__ h2, const z_t* __restrict__ H2s, c
   btOf = bat(btOf, bs);
   GRID_STRIDE(e, N * N * N * N) {
     int i1 = (int)(e % N), l2 = (int)((e / N) % N), j1 = (int)((e / N / N) % N), k2 = (int)(e / N / N / N);
-    z_t v = zmk(0.0, 0.0);
-    if (T.restricted) {
-      int s1 = i1 / n, s2 = l2 / n, s3 = j1 / n, s4 = k2 / n;
-      if (s1 == s3 && s2 == s4) {
-        int a = i1 % n, b = l2 % n, c = j1 % n, d = k2 % n;
-        v = H2s[(size_t)(a * n + c) * n * n + (b * n + d)];
-      }
-    } else {
-      if (btOf[i1] == btOf[j1] && btOf[l2] == btOf[k2]) v = H2s[(size_t)(i1 * n + j1) * n * n + (l2 * n + k2)];
-    }
-    h2[e] = v;
+    h2[e] = h2_from_h2s(H2s, btOf, T.restricted, n, i1, l2, j1, k2);
   }
 }
 
@@ -471,6 +461,31 @@ __global__ void k_build_r2s(z_t* __restrict__ r2s, const z_t* __restrict__ rdm2,
   }
 }
 
+// As k_build_r2s with the rdm2 entries formed from rdm2Lin (inside the NonLin
+// derivative the nO^4 rdm2 is not formed); the same values.
+__global__ void k_build_r2s_lin(z_t* __restrict__ r2s, const z_t* __restrict__ lin, const int* __restrict__ btOf,
+                                TRAJ_ARGS) {
+  const TrajShape& T = shp[blockIdx.z];
+  const int n = T.nOS, restricted = T.restricted;
+  size_t Q = (size_t)n * n;
+  r2s = bat(r2s, bs);
+  lin = bat(lin, bs);
+  btOf = bat(btOf, bs);
+  const size_t N = T.nO;
+  auto R2 = [&](int a, int b, int c, int d) { return rdm2_from_lin(lin, btOf, N, a, b, c, d); };
+  GRID_STRIDE(e, Q * Q) {
+    int row = (int)(e / Q), col = (int)(e % Q);
+    int l2 = row / n, k2 = row % n, k1 = col / n, k = col % n;
+    z_t r = zmk(0.0, 0.0);
+    if (restricted)
+      r = zadd(zadd(zadd(R2(k1, k2, k, l2), R2(n + k1, k2, n + k, l2)), R2(k1, n + k2, k, n + l2)),
+               R2(n + k1, n + k2, n + k, n + l2));
+    else if (btOf[l2] == btOf[k2] && btOf[k1] == btOf[k])
+      r = R2(k1, k2, k, l2);
+    r2s[e] = r;
+  }
+}
+
 // R'[(l2*n+k2)][(k1*n+j)] = sum_k r2s[(l2,k2)][(k1,k)] Mreg(k,j), masked by body types.
 __global__ void k_build_R(z_t* __restrict__ Rp, const z_t* __restrict__ r2s, const z_t* __restrict__ Mreg,
                           const int* __restrict__ btOf, TRAJ_ARGS) {
@@ -583,7 +598,12 @@ void launch_rdm_inverse(cgpu_ctx* c) {
                                                         c->scal_d + CODY_SCAL_OCC, TRAJ_PASS(c));
   CODY_LAUNCHED(c);
   size_t Q = (size_t)n * n;
-  k_build_r2s<<<bgrid(c, ew_blocks(c, Q * Q)), 256, 0, c->stream>>>(c->r2s_d, c->rdm2_d, c->btOfOrb_d, TRAJ_PASS(c));
+  if (c->fuseLayouts)
+    k_build_r2s_lin<<<bgrid(c, ew_blocks(c, Q * Q)), 256, 0, c->stream>>>(c->r2s_d, c->rdm2Lin_d, c->btOfOrb_d,
+                                                                         TRAJ_PASS(c));
+  else
+    k_build_r2s<<<bgrid(c, ew_blocks(c, Q * Q)), 256, 0, c->stream>>>(c->r2s_d, c->rdm2_d, c->btOfOrb_d,
+                                                                     TRAJ_PASS(c));
   CODY_LAUNCHED(c);
   k_build_R<<<bgrid(c, ew_blocks(c, Q * Q)), 256, 0, c->stream>>>(c->Rp_d, c->r2s_d, c->Mreg_d, c->btOfOrb_d,
                                                                     TRAJ_PASS(c));
@@ -595,7 +615,10 @@ void launch_rdm_inverse(cgpu_ctx* c) {
 void launch_correlation(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   launch_rdm_inverse(c);
   if (!c->hasInteraction) {
-    if (wantH2) batch_zero(c, c->h2_d, sizeof(z_t) * (size_t)c->nO * c->nO * c->nO * c->nO);
+    if (wantH2) {
+      batch_zero(c, c->h2_d, sizeof(z_t) * (size_t)c->nO * c->nO * c->nO * c->nO);
+      batch_zero(c, c->h2s_d, sizeof(z_t) * (size_t)c->nOS * c->nOS * c->nOS * c->nOS);
+    }
     return;
   }
   launch_pair_potentials(c, orbs);
@@ -629,6 +652,7 @@ void launch_corr_epilogue(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, const z_t* Z
 }
 
 void launch_h2_layout(cgpu_ctx* c) {
+  if (c->fuseLayouts) return;  // launch_fold_h2 reads H2s directly
   size_t n4 = (size_t)c->nO * c->nO * c->nO * c->nO;
   k_h2_layout<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(c->h2_d, c->h2s_d, c->btOfOrb_d, TRAJ_PASS(c));
   CODY_LAUNCHED(c);

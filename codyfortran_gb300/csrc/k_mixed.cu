@@ -749,7 +749,10 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
 void launch_correlation_mixed(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   launch_rdm_inverse(c);
   if (!c->hasInteraction) {
-    if (wantH2) batch_zero(c, c->h2_d, sizeof(z_t) * (size_t)c->nO * c->nO * c->nO * c->nO);
+    if (wantH2) {
+      batch_zero(c, c->h2_d, sizeof(z_t) * (size_t)c->nO * c->nO * c->nO * c->nO);
+      batch_zero(c, c->h2s_d, sizeof(z_t) * (size_t)c->nOS * c->nOS * c->nOS * c->nOS);
+    }
     return;
   }
   MixedBufs* m = c->mixed;
