@@ -407,6 +407,7 @@ struct cgpu_ctx {
   // inside the NonLin time derivative: r2s from rdm2Lin and h2Lin from h2s
   // directly (the nO^4 rdm2 / h2 tensors are not formed)
   int fuseLayouts = 0;
+  int numSms = 148;  // streaming multiprocessors of the device
   float4 *h1Df_d = nullptr, *h2Df_d = nullptr;
   float2* Tdf_d = nullptr;  // double-float copy of the kinetic band (static)
   z_t *rdm1_d = nullptr, *rdm2_d = nullptr, *h1_d = nullptr, *h2_d = nullptr;

@@ -464,6 +464,11 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
   c->ciDf = (c->precision == CGPU_PREC_MIXED_FX || c->precision == CGPU_PREC_MIXED_FX6) ? 1 : 0;
   c->hasInteraction = d0->has_interaction ? 1 : 0;
   CODY_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  {
+    int dev = 0;
+    CODY_CUDA(cudaGetDevice(&dev));
+    CODY_CUDA(cudaDeviceGetAttribute(&c->numSms, cudaDevAttrMultiProcessorCount, dev));
+  }
   c->sys.resize(nSys);
   for (int b = 0; b < nSys; b++) build_system(c, c->sys[b], &descs[b]);
   // maxima over the systems

@@ -93,57 +93,43 @@ __device__ __forceinline__ double ll_scaled(long long T, int e) {
   return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | (a & 0xFFFFFFFFFFFFFull)));
 }
 
-// out[traj][split][M][N] = C (FP64).  maxRow/maxCol (nSplit == 1 only): the
-// largest biased exponent of |C| per output row / column, by atomicMax.
+// One work item of a persistent CTA: trajectory, first output row, first
+// output column, K split.
+struct FxTile {
+  int traj, m0, n0, split;
+};
+
+// out[traj][split][M][N] = C (FP64) over the tile list; a persistent CTA takes
+// tiles blockIdx.x, blockIdx.x + gridDim.x, ...  Warps 0-3: epilogue (TMEM lanes
+// 32w..32w+31); warp 4: TMA producer; warp 5: MMA issuer.  The rings and their
+// phases run on across tiles; the accumulator hand-off uses accFull (MMA ->
+// epilogue) and accEmpty (epilogue -> MMA), so the producer loads the next
+// tile while the epilogue drains the current one.  maxRow/maxCol (nSplit == 1
+// only): the largest biased exponent of |C| per output row / column.
 // aShared: A is shared by the trajectories (3D map with one plane per root
 // grid); the trajectory's rows start at vRow of plane vRoot, its K range at
 // vRow - gShift, its row exponents at expA[vExp].
 template <int BN, int L, int NA_, int NB_>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(192)
     k_fx_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, double* __restrict__ out,
               const int* __restrict__ expA, const int* __restrict__ expB, unsigned* __restrict__ maxRow,
               unsigned* __restrict__ maxCol, TRAJ_ARGS, int gemmId, int segPitchA, int segPitch, int aShared,
-              int nSplit, int digitBits, int* __restrict__ err) {
+              int nSplit, int digitBits, const FxTile* __restrict__ tiles, int nTiles, int* __restrict__ err) {
   using C = FxCfg<BN, L, NA_, NB_>;
   constexpr int NA = C::NA, NB = C::NB;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* ringA = smem;
   uint8_t* ringB = smem + NA * C::A_BYTES;
-  __shared__ __align__(8) uint64_t aFull[NA], aEmpty[NA], bFull[NB], bEmpty[NB], doneBar;
+  __shared__ __align__(8) uint64_t aFull[NA], aEmpty[NA], bFull[NB], bEmpty[NB], accFull, accEmpty, finalBar;
   __shared__ uint32_t tmemSlot;
   __shared__ volatile int abortFlag;
-  __shared__ int consumedA, consumedB;
+  __shared__ int consumedA, consumedB, issuedA, issuedB;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int traj = blockIdx.z / nSplit, split = blockIdx.z % nSplit;
-  int M, N, segTiles;
-  tc_dims(shp[traj], gemmId, M, N, segTiles);
-  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * TC_BM;
-  if (m0 >= M || n0 >= N) return;
-  const int nT = min(BN, (N - n0 + 15) / 16 * 16);  // MMA width for this trajectory's columns
-  const int per = (segTiles + nSplit - 1) / nSplit;
-  const int kt0 = split * per;
-  const int nk = max(0, min(segTiles, kt0 + per) - kt0);
-  double* Oz = batn(out, bs, traj) + (size_t)split * (size_t)M * N;
-  if (nk == 0) {
-    for (int e = threadIdx.x; e < TC_BM * BN; e += blockDim.x) {
-      int r = m0 + e / BN, col = n0 + e % BN;
-      if (r < M && col < N) Oz[(size_t)r * N + col] = 0.0;
-    }
-    return;
-  }
-  // blockIdx.z also carries the split: index by trajectory
-  const int aRow0 = aShared ? shp[traj].vRow : 0;
-  const int aCol0 = aShared ? shp[traj].vRow - shp[traj].gShift : 0;
-  const int aZ = aShared ? shp[traj].vRoot : traj;
-  expA = aShared ? expA + shp[traj].vExp : batn(expA, bs, traj);
-  expB = batn(expB, bs, traj);
-
   if (threadIdx.x == 0) {
     abortFlag = 0;
-    consumedA = 0;
-    consumedB = 0;
+    consumedA = consumedB = issuedA = issuedB = 0;
     for (int s = 0; s < NA; s++) {
       mbar_init(&aFull[s], 1);
       mbar_init(&aEmpty[s], 1);
@@ -152,7 +138,9 @@ __global__ void __launch_bounds__(128)
       mbar_init(&bFull[s], 1);
       mbar_init(&bEmpty[s], 1);
     }
-    mbar_init(&doneBar, 1);
+    mbar_init(&accFull, 1);
+    mbar_init(&accEmpty, 4);
+    mbar_init(&finalBar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -166,144 +154,200 @@ __global__ void __launch_bounds__(128)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmemSlot;
 
-  int issuedA = 0, issuedB = 0;
-  if (warp == 0 && lane == 0) {
-    // TMA producer: per K block the L B slices (one stage), then the L A slices
-    for (int kb = 0; kb < nk && !abortFlag; kb++) {
-      const int sb = kb % NB, rb = kb / NB;
-      if (!mbar_wait(&bEmpty[sb], (rb & 1) ^ 1, &abortFlag)) {
-        abortFlag = 1;
-        atomicExch(err, 11);
-        break;
-      }
-      const int x0 = (kt0 + kb) * TC_BK;
-      mbar_expect_tx(&bFull[sb], (uint32_t)(L * nT * TC_BK * 2));
-      for (int j = 0; j < L; j++)
-        for (int r = 0; r < nT; r += 16)
-          tma_load_3d(ringB + sb * C::BG_BYTES + j * C::B_BYTES + r * TC_BK * 2, &tB, &bFull[sb],
-                      j * segPitch + x0, n0 + r, traj);
-      issuedB = kb + 1;
-      for (int i = 0; i < L; i++) {
-        const int t = kb * L + i, sa = t % NA, ra = t / NA;
-        if (!mbar_wait(&aEmpty[sa], (ra & 1) ^ 1, &abortFlag)) {
-          abortFlag = 1;
-          atomicExch(err, 12);
-          break;
+  // per-tile geometry (every role derives the same values)
+  auto geometry = [&](const FxTile& tl, int& M, int& N, int& nT, int& kt0, int& nk) {
+    int segTiles;
+    tc_dims(shp[tl.traj], gemmId, M, N, segTiles);
+    nT = min(BN, (N - tl.n0 + 15) / 16 * 16);
+    const int per = (segTiles + nSplit - 1) / nSplit;
+    kt0 = tl.split * per;
+    nk = max(0, min(segTiles, kt0 + per) - kt0);
+  };
+
+  if (warp == 4) {
+    if (lane == 0) {
+      // TMA producer: per K block the L B slices (16-row boxes of the tile's rows), then the L A slices
+      int ta = 0, tb = 0;
+      for (int t = blockIdx.x; t < nTiles && !abortFlag; t += gridDim.x) {
+        const FxTile tl = tiles[t];
+        int M, N, nT, kt0, nk;
+        geometry(tl, M, N, nT, kt0, nk);
+        const TrajShape& T = shp[tl.traj];
+        const int aRow0 = aShared ? T.vRow : 0, aCol0 = aShared ? T.vRow - T.gShift : 0;
+        const int aZ = aShared ? T.vRoot : tl.traj;
+        for (int kb = 0; kb < nk && !abortFlag; kb++) {
+          const int sb = tb % NB, rb = tb / NB;
+          if (!mbar_wait(&bEmpty[sb], (rb & 1) ^ 1, &abortFlag)) {
+            abortFlag = 1;
+            atomicExch(err, 11);
+            break;
+          }
+          const int x0 = (kt0 + kb) * TC_BK;
+          mbar_expect_tx(&bFull[sb], (uint32_t)(L * nT * TC_BK * 2));
+          for (int j = 0; j < L; j++)
+            for (int r = 0; r < nT; r += 16)
+              tma_load_3d(ringB + sb * C::BG_BYTES + j * C::B_BYTES + r * TC_BK * 2, &tB, &bFull[sb],
+                          j * segPitch + x0, tl.n0 + r, tl.traj);
+          tb++;
+          issuedB = tb;
+          for (int i = 0; i < L; i++) {
+            const int sa = ta % NA, ra = ta / NA;
+            if (!mbar_wait(&aEmpty[sa], (ra & 1) ^ 1, &abortFlag)) {
+              abortFlag = 1;
+              atomicExch(err, 12);
+              break;
+            }
+            mbar_expect_tx(&aFull[sa], C::A_BYTES);
+            tma_load_3d(ringA + sa * C::A_BYTES, &tA, &aFull[sa], i * segPitchA + aCol0 + x0, aRow0 + tl.m0, aZ);
+            ta++;
+            issuedA = ta;
+          }
         }
-        mbar_expect_tx(&aFull[sa], C::A_BYTES);
-        tma_load_3d(ringA + sa * C::A_BYTES, &tA, &aFull[sa], i * segPitchA + aCol0 + x0, aRow0 + m0, aZ);
-        issuedA = t + 1;
       }
     }
-  } else if (warp == 1 && lane == 0) {
-    // MMA issuer: kind::f16, D=F32, A=B=BF16, K-major, N=nT, M=128
-    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nT >> 3) << 17) |
-                           ((uint32_t)(TC_BM >> 4) << 24);
-    // descriptors advance by address / 16: +2 per 16-wide K step, +B_BYTES/16 per B slice
-    const uint64_t bdesc0 = sw128_desc(smem_u32(ringB));
-    const uint64_t adesc0 = sw128_desc(smem_u32(ringA));
-    int ca = 0, kb = 0;
-    bool ok = true;
-    for (; kb < nk && ok; kb++) {
-      const int sb = kb % NB, rb = kb / NB;
-      if (!mbar_wait(&bFull[sb], rb & 1, &abortFlag)) {
-        abortFlag = 1;
-        atomicExch(err, 13);
-        ok = false;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint64_t bd = bdesc0 + (uint64_t)((sb * C::BG_BYTES) >> 4);
-#pragma unroll
-      for (int i = 0; i < L; i++) {
-        const int sa = ca % NA, ra = ca / NA;
-        if (!mbar_wait(&aFull[sa], ra & 1, &abortFlag)) {
+  } else if (warp == 5) {
+    if (lane == 0) {
+      // MMA issuer: kind::f16, D=F32, A=B=BF16, K-major, M=128; descriptors
+      // advance by address / 16: +2 per 16-wide K step, +B_BYTES/16 per B slice
+      const uint64_t bdesc0 = sw128_desc(smem_u32(ringB));
+      const uint64_t adesc0 = sw128_desc(smem_u32(ringA));
+      int ca = 0, cb = 0, ph = 0;  // ph: accumulator phases (tiles with K work)
+      for (int t = blockIdx.x; t < nTiles && !abortFlag; t += gridDim.x) {
+        const FxTile tl = tiles[t];
+        int M, N, nT, kt0, nk;
+        geometry(tl, M, N, nT, kt0, nk);
+        if (nk == 0) continue;  // the epilogue writes the empty split's zeros
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nT >> 3) << 17) |
+                               ((uint32_t)(TC_BM >> 4) << 24);
+        if (ph > 0 && !mbar_wait(&accEmpty, (ph - 1) & 1, &abortFlag)) {  // the epilogue drained TMEM
           abortFlag = 1;
-          atomicExch(err, 14);
-          ok = false;
+          atomicExch(err, 16);
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint64_t ad = adesc0 + (uint64_t)((sa * C::A_BYTES) >> 4);
+        bool ok = true;
+        for (int kb = 0; kb < nk && ok; kb++) {
+          const int sb = cb % NB, rb = cb / NB;
+          if (!mbar_wait(&bFull[sb], rb & 1, &abortFlag)) {
+            abortFlag = 1;
+            atomicExch(err, 13);
+            ok = false;
+            break;
+          }
+          cb++;
+          consumedB = cb;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint64_t bd = bdesc0 + (uint64_t)((sb * C::BG_BYTES) >> 4);
 #pragma unroll
-        for (int j = 0; j < L - i; j++) {
-          const uint32_t d = tmem + (uint32_t)((i + j) * BN);
-          const uint64_t bdj = bd + (uint64_t)((j * C::B_BYTES) >> 4);
+          for (int i = 0; i < L; i++) {
+            const int sa = ca % NA, ra = ca / NA;
+            if (!mbar_wait(&aFull[sa], ra & 1, &abortFlag)) {
+              abortFlag = 1;
+              atomicExch(err, 14);
+              ok = false;
+              break;
+            }
+            ca++;
+            consumedA = ca;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint64_t ad = adesc0 + (uint64_t)((sa * C::A_BYTES) >> 4);
 #pragma unroll
-          for (int k = 0; k < TC_BK / 16; k++)
-            umma_bf16(d, ad + 2 * k, bdj + 2 * k, idesc, (kb > 0 || i > 0 || k > 0) ? 1u : 0u);
+            for (int j = 0; j < L - i; j++) {
+              const uint32_t d = tmem + (uint32_t)((i + j) * BN);
+              const uint64_t bdj = bd + (uint64_t)((j * C::B_BYTES) >> 4);
+#pragma unroll
+              for (int k = 0; k < TC_BK / 16; k++)
+                umma_bf16(d, ad + 2 * k, bdj + 2 * k, idesc, (kb > 0 || i > 0 || k > 0) ? 1u : 0u);
+            }
+            umma_commit(&aEmpty[sa]);
+          }
+          if (ok) umma_commit(&bEmpty[sb]);
         }
-        umma_commit(&aEmpty[sa]);
-        ca++;
+        if (!ok) break;
+        umma_commit(&accFull);
+        ph++;
       }
-      if (ok) umma_commit(&bEmpty[sb]);
+      umma_commit(&finalBar);  // arrives when every issued MMA has completed
     }
-    consumedA = ca;
-    consumedB = kb;  // B stages whose full barrier the issuer passed
-    umma_commit(&doneBar);
-  }
-  __syncwarp();
-  const bool waited = mbar_wait(&doneBar, 0, &abortFlag);
-  if (!waited) atomicExch(err, 15);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  // every MMA has completed and every TMA copy has landed unless a wait gave up
-  const bool good = __syncthreads_and(waited) && !abortFlag;
-
-  if (good) {
-    // epilogue: warp w owns TMEM lanes [32w, 32w+32) = tile rows; the FP64
-    // tile goes through shared memory (the operand rings are free now)
-    double* stile = (double*)smem;
-    const int r = warp * 32 + lane, row = m0 + r;
-    const bool rowOk = row < M;
-    const int ea = rowOk ? expA[row] - digitBits * (L + 1) : 0;
+  } else {
+    // epilogue: warp w owns TMEM lanes [32w, 32w+32) = tile rows
     const long long base = 1LL << digitBits;
-    unsigned rowMaxEx = 0;
-#pragma unroll 1
-    for (int c = 0; c < nT; c += 16) {
-      uint32_t acc[L][16];
-#pragma unroll
-      for (int l = 0; l < L; l++) TMEM_LD_X16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * BN + c), acc[l]);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-      for (int j = 0; j < 16; j++) {
-        const int col = n0 + c + j;
-        unsigned ex = 0;
-        double v = 0.0;
-        if (rowOk && col < N) {
-          long long T = 0;
-#pragma unroll
-          for (int l = 0; l < L; l++) T = T * base + (long long)__float2int_rn(__uint_as_float(acc[l][j]));
-          v = ll_scaled(T, ea + expB[col]);
-          ex = (unsigned)(__double2hiint(v) >> 20) & 0x7FFu;
-        }
-        stile[r * C::SP + c + j] = v;
-        if (maxCol) {
-          unsigned m = __reduce_max_sync(0xffffffffu, ex);
-          if (lane == 0 && m) atomicMax(batn(maxCol, bs, traj) + col, m);
-        }
-        rowMaxEx = max(rowMaxEx, ex);
+    int ph = 0;
+    for (int t = blockIdx.x; t < nTiles; t += gridDim.x) {
+      const FxTile tl = tiles[t];
+      int M, N, nT, kt0, nk;
+      geometry(tl, M, N, nT, kt0, nk);
+      double* Oz = batn(out, bs, tl.traj) + (size_t)tl.split * (size_t)M * N;
+      const int r = warp * 32 + lane, row = tl.m0 + r;
+      const bool rowOk = row < M;
+      if (nk == 0) {  // empty split: its partial is zero
+        if (rowOk)
+          for (int col = tl.n0; col < min(N, tl.n0 + BN); col++) Oz[(size_t)row * N + col] = 0.0;
+        continue;
       }
+      const bool waited = mbar_wait(&accFull, ph & 1, &abortFlag);
+      if (__any_sync(0xffffffffu, !waited)) {
+        if (lane == 0) atomicExch(err, 15);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const TrajShape& T = shp[tl.traj];
+      const int* eA = aShared ? expA + T.vExp : batn(expA, bs, tl.traj);
+      const int* eB = batn(expB, bs, tl.traj);
+      const int ea = rowOk ? eA[row] - digitBits * (L + 1) : 0;
+      unsigned rowMaxEx = 0;
+#pragma unroll 1
+      for (int c = 0; c < nT; c += 16) {
+        uint32_t acc[L][16];
+#pragma unroll
+        for (int l = 0; l < L; l++)
+          TMEM_LD_X16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * BN + c), acc[l]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        double v[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const int col = tl.n0 + c + j;
+          unsigned ex = 0;
+          v[j] = 0.0;
+          if (rowOk && col < N) {
+            long long Tv = 0;
+#pragma unroll
+            for (int l = 0; l < L; l++) Tv = Tv * base + (long long)__float2int_rn(__uint_as_float(acc[l][j]));
+            v[j] = ll_scaled(Tv, ea + eB[col]);
+            ex = (unsigned)(__double2hiint(v[j]) >> 20) & 0x7FFu;
+          }
+          if (maxCol) {
+            unsigned m = __reduce_max_sync(0xffffffffu, ex);
+            if (lane == 0 && m) atomicMax(batn(maxCol, bs, tl.traj) + col, m);
+          }
+          rowMaxEx = max(rowMaxEx, ex);
+        }
+        if (rowOk) {
+          double* dst = Oz + (size_t)row * N + tl.n0 + c;
+#pragma unroll
+          for (int j = 0; j < 16; j += 2)
+            if (tl.n0 + c + j < N) *reinterpret_cast<double2*>(dst + j) = make_double2(v[j], v[j + 1]);
+        }
+      }
+      if (maxRow && rowOk && rowMaxEx) atomicMax(batn(maxRow, bs, tl.traj) + row, rowMaxEx);
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&accEmpty);
+      ph++;
     }
-    if (maxRow && rowOk && rowMaxEx) atomicMax(batn(maxRow, bs, traj) + row, rowMaxEx);
-    __syncthreads();
-    const int nc = min(nT, N - n0);
-    for (int rr = warp; rr < TC_BM; rr += 4) {
-      const int grow = m0 + rr;
-      if (grow >= M) break;
-      double* dst = Oz + (size_t)grow * N + n0;
-      for (int col = lane; col < nc; col += 32) dst[col] = stile[rr * C::SP + col];
+  }
+  __syncthreads();
+  // every issued MMA has completed before the tensor memory is freed; after an
+  // abort also the TMA copies that were issued but never consumed (bounded waits)
+  if (warp == 4 && lane == 0) {
+    volatile int dummy = 0;
+    mbar_wait(&finalBar, 0, &dummy);
+    if (abortFlag) {
+      for (int t = consumedA; t < issuedA; t++) mbar_wait(&aFull[t % NA], (t / NA) & 1, &dummy);
+      for (int t = consumedB; t < issuedB; t++) mbar_wait(&bFull[t % NB], (t / NB) & 1, &dummy);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  // after an abort: let the issued MMAs finish and drain the TMA copies that
-  // were issued but never consumed (bounded waits)
-  if (warp == 0 && lane == 0 && abortFlag) {
-    volatile int dummy = 0;
-    mbar_wait(&doneBar, 0, &dummy);
-    for (int t = consumedA; t < issuedA; t++) mbar_wait(&aFull[t % NA], (t / NA) & 1, &dummy);
-    for (int t = consumedB; t < issuedB; t++) mbar_wait(&bFull[t % NB], (t / NB) & 1, &dummy);
-  }
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TMEM_COLS) : "memory");
@@ -312,17 +356,18 @@ __global__ void __launch_bounds__(128)
 template <int BN, int L, int NA_, int NB_>
 void launch_fx_t(cgpu_ctx* c, const CUtensorMap& ta, const CUtensorMap& tb, double* out, const int* expA,
                  const int* expB, unsigned* maxRow, unsigned* maxCol, int gemmId, int segPitchA, int segPitch,
-                 int aShared, int nSplit, int Mmax, int Nmax, int digitBits, int* err) {
+                 int aShared, int nSplit, int digitBits, const FxTile* tiles, int nTiles, int ctasPerSm, int* err) {
   using C = FxCfg<BN, L, NA_, NB_>;
   static bool attr = false;
   if (!attr) {
     CODY_CUDA(cudaFuncSetAttribute(k_fx_gemm<BN, L, NA_, NB_>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
     attr = true;
   }
-  dim3 grid(ceil_div(Nmax, BN), ceil_div(Mmax, TC_BM), (unsigned)(c->nb * nSplit));
-  k_fx_gemm<BN, L, NA_, NB_><<<grid, 128, C::SMEM, c->stream>>>(ta, tb, out, expA, expB, maxRow, maxCol,
-                                                                TRAJ_PASS(c), gemmId, segPitchA, segPitch, aShared,
-                                                                nSplit, digitBits, err);
+  if (nTiles <= 0) return;
+  const int grid = std::min(nTiles, c->numSms * ctasPerSm);
+  k_fx_gemm<BN, L, NA_, NB_><<<grid, 192, C::SMEM, c->stream>>>(ta, tb, out, expA, expB, maxRow, maxCol, TRAJ_PASS(c),
+                                                                gemmId, segPitchA, segPitch, aShared, nSplit,
+                                                                digitBits, tiles, nTiles, err);
   CODY_LAUNCHED(c);
 }
 
@@ -363,18 +408,39 @@ int fx_split_count(int M, int N, int BN, int kTiles, int nb) {
   return (kTiles + per - 1) / per;
 }
 
+void* fx_build_tiles(cgpu_ctx* c, int gemmId, int bn, int nSplit, int* nTiles) {
+  std::vector<FxTile> v;
+  for (int b = 0; b < c->nb; b++) {
+    const TrajShape& S = c->shape_h[b];
+    int P2 = 2 * S.nPairs, Q2 = 2 * S.nOS * S.nOS, M, N;
+    if (gemmId == TC_GEMM_W) { M = S.nG; N = P2; }
+    else if (gemmId == TC_GEMM_Z) { M = S.nG; N = Q2; }
+    else { M = P2; N = P2; }
+    for (int m0 = 0; m0 < M; m0 += TC_BM)
+      for (int n0 = 0; n0 < N; n0 += bn)
+        for (int z = 0; z < nSplit; z++) v.push_back(FxTile{b, m0, n0, z});
+  }
+  *nTiles = (int)v.size();
+  void* d = nullptr;
+  CODY_CUDA(cudaMalloc(&d, sizeof(FxTile) * std::max<size_t>(v.size(), 1)));
+  if (!v.empty()) CODY_CUDA(cudaMemcpy(d, v.data(), sizeof(FxTile) * v.size(), cudaMemcpyHostToDevice));
+  return d;
+}
+
 void fx_gemm(cgpu_ctx* c, int L, int digitBits, bool compact, int gemmId, const CUtensorMap& ta,
              const CUtensorMap& tb, int bn, double* out, const int* expA, const int* expB, unsigned* maxRow,
-             unsigned* maxCol, int segPitchA, int segPitch, int aShared, int nSplit, int Mmax, int Nmax, int* err) {
+             unsigned* maxCol, int segPitchA, int segPitch, int aShared, int nSplit, const void* tiles, int nTiles,
+             int* err) {
   if (segPitch % TC_BK != 0 || segPitchA % TC_BK != 0)
     throw std::string("fx_gemm: segment pitch must be a multiple of 64");
   if (nSplit > 1 && (maxRow || maxCol)) throw std::string("fx_gemm: output maxima need an unsplit K");
   if (digitBits < 6 || digitBits > 8 || digitBits * L > 52) throw std::string("fx_gemm: digit width");
-#define FX_CASE(BN_, L_, NA_, NB_, CMP_)                                                                       \
-  if (bn == BN_ && L == L_ && compact == CMP_) {                                                               \
-    launch_fx_t<BN_, L_, NA_, NB_>(c, ta, tb, out, expA, expB, maxRow, maxCol, gemmId, segPitchA, segPitch,   \
-                                   aShared, nSplit, Mmax, Nmax, digitBits, err);                               \
-    return;                                                                                                    \
+  const FxTile* tl = (const FxTile*)tiles;
+#define FX_CASE(BN_, L_, NA_, NB_, CMP_)                                                                        \
+  if (bn == BN_ && L == L_ && compact == CMP_) {                                                                \
+    launch_fx_t<BN_, L_, NA_, NB_>(c, ta, tb, out, expA, expB, maxRow, maxCol, gemmId, segPitchA, segPitch,    \
+                                   aShared, nSplit, digitBits, tl, nTiles, CMP_ ? 2 : 1, err);                 \
+    return;                                                                                                     \
   }
   FX_CASE(32, 4, 0, 2, false) FX_CASE(64, 4, 0, 2, false) FX_CASE(80, 4, 0, 2, false) FX_CASE(96, 4, 0, 2, false)
   FX_CASE(128, 4, 0, 2, false)

@@ -45,6 +45,9 @@ struct MixedBufs {
   bool compact2 = false;
   // one interaction matrix per root grid (cgpu_ctx::fxShared): slices [root][c->nG][L1 KgBig]
   // and row exponents [root][c->nG], outside the per-trajectory arena
+  // tile lists of the persistent fixed-point GEMMs (device) and their lengths
+  void *tiles1 = nullptr, *tiles2 = nullptr, *tiles3 = nullptr;
+  int nTiles1 = 0, nTiles2 = 0, nTiles3 = 0;
   int KgBig = 0;
   __nv_bfloat16* Vsh = nullptr;
   int* eVsh = nullptr;
@@ -638,6 +641,8 @@ void mixed_free(cgpu_ctx* c) {
   if (c->mixed) {
     if (c->mixed->Vsh) cudaFree(c->mixed->Vsh);
     if (c->mixed->eVsh) cudaFree(c->mixed->eVsh);
+    for (void* p : {c->mixed->tiles1, c->mixed->tiles2, c->mixed->tiles3})
+      if (p) cudaFree(p);
   }
   delete c->mixed;  // the other buffers belong to the arena
   c->mixed = nullptr;
@@ -683,6 +688,11 @@ void mixed_init(cgpu_ctx* c) {
   m->mW = tc_make_map(c, m->WxA, c->nG, pP, 128);
   m->mR = tc_make_map(c, m->RxB, Q2, pP, m->fxBits ? 16 : m->bn2);
   m->mSasB = tc_make_map(c, m->SxA, P2, pG, 128);
+  if (m->fxBits) {
+    m->tiles1 = fx_build_tiles(c, TC_GEMM_W, m->bn1, m->s1, &m->nTiles1);
+    m->tiles2 = fx_build_tiles(c, TC_GEMM_Z, m->bn2, m->s2, &m->nTiles2);
+    m->tiles3 = fx_build_tiles(c, TC_GEMM_H2, m->bn3, m->s3, &m->nTiles3);
+  }
   m->mWT = tc_make_map(c, m->WTxB, P2, pG, m->fxBits ? 16 : m->bn3);
   CODY_CUDA(cudaStreamSynchronize(c->stream));
 }
@@ -707,10 +717,11 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
     const bool one = m->s1 == 1;
     if (c->fxShared)
       fx_gemm(c, m->L1, m->b1, false, TC_GEMM_W, m->mVsh, m->mS, m->bn1, m->Wd, m->eVsh, m->eS,
-              one ? m->mWr : nullptr, one ? m->mWc : nullptr, m->KgBig, m->KgMax, 1, m->s1, nG, 2 * nP, m->err);
+              one ? m->mWr : nullptr, one ? m->mWc : nullptr, m->KgBig, m->KgMax, 1, m->s1, m->tiles1, m->nTiles1,
+              m->err);
     else
       fx_gemm(c, m->L1, m->b1, false, TC_GEMM_W, m->mV, m->mS, m->bn1, m->Wd, m->eV, m->eS, one ? m->mWr : nullptr,
-              one ? m->mWc : nullptr, m->KgMax, m->KgMax, 0, m->s1, nG, 2 * nP, m->err);
+              one ? m->mWc : nullptr, m->KgMax, m->KgMax, 0, m->s1, m->tiles1, m->nTiles1, m->err);
     if (!one) {
       k_fx_reduce_W<<<bgrid(c, ew_blocks(c, (size_t)nG * 2 * nP)), 256, 0, c->stream>>>(m->Wd, m->mWr, m->mWc, m->s1,
                                                                                      TRAJ_PASS(c));
@@ -727,7 +738,7 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
         m->RxB, m->eR, c->Rp_d, c->pairL_d, c->pairK_d, m->KpMax, m->b2, m->L2, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
     fx_gemm(c, m->L2, m->b2, m->compact2, TC_GEMM_Z, m->mW, m->mR, m->bn2, m->s2 > 1 ? m->Zp : m->Zd, m->eWr, m->eR,
-            nullptr, nullptr, m->KpMax, m->KpMax, 0, m->s2, nG, 2 * Q, m->err);
+            nullptr, nullptr, m->KpMax, m->KpMax, 0, m->s2, m->tiles2, m->nTiles2, m->err);
     if (m->s2 > 1) {
       k_reduce_Z<<<bgrid(c, ew_blocks(c, (size_t)nG * Q)), 256, 0, c->stream>>>(Z, m->Zp, m->s2, TRAJ_PASS(c));
       CODY_LAUNCHED(c);
@@ -737,7 +748,7 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   if (wantH2) {
     ProfScope prof(c, CGPU_KERNEL_H2);
     fx_gemm(c, m->L1, m->b1, false, TC_GEMM_H2, m->mSasB, m->mWT, m->bn3, m->Gd, m->eS, m->eWc, nullptr, nullptr,
-            m->KgMax, m->KgMax, 0, m->s3, 2 * nP, 2 * nP, m->err);
+            m->KgMax, m->KgMax, 0, m->s3, m->tiles3, m->nTiles3, m->err);
     k_reduce_H2<<<bgrid(c, ew_blocks(c, (size_t)Q * Q)), 256, 0, c->stream>>>(c->h2s_d, m->Gd, m->s3, c->pidx_d,
                                                                         TRAJ_PASS(c));
     CODY_LAUNCHED(c);

@@ -30,7 +30,11 @@ void tc_gemm(cgpu_ctx* c, int gemmId, const CUtensorMap& ta, const CUtensorMap& 
 // is one matrix shared by the trajectories, read at each trajectory's vRow.
 void fx_gemm(cgpu_ctx* c, int L, int digitBits, bool compact, int gemmId, const CUtensorMap& ta,
              const CUtensorMap& tb, int bn, double* out, const int* expA, const int* expB, unsigned* maxRow,
-             unsigned* maxCol, int segPitchA, int segPitch, int aShared, int nSplit, int Mmax, int Nmax, int* err);
+             unsigned* maxCol, int segPitchA, int segPitch, int aShared, int nSplit, const void* tiles, int nTiles,
+             int* err);
+// Device list of the fixed-point GEMM's tiles (trajectory, row, column, K split) of the
+// context for an N tile of bn columns: only tiles inside a trajectory's output.
+void* fx_build_tiles(cgpu_ctx* c, int gemmId, int bn, int nSplit, int* nTiles);
 // 3D TMA map over an explicit [planes][rowsMax][pitch] bf16 tensor (planes planeBytes apart).
 CUtensorMap tc_make_map_planes(const __nv_bfloat16* base, int rowsMax, int pitch, int boxRows, int planes,
                                size_t planeBytes);
@@ -71,6 +75,10 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
       : "r"(smem_u32(bar)), "r"(parity)
       : "memory");
   return ok != 0;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // mbarrier.try_wait: suspends the thread in hardware for a bounded, implementation-defined
