@@ -535,7 +535,9 @@ __global__ void k_fold_h2(z_t* __restrict__ h2Lin, float4* __restrict__ h2Df, co
 
 // FillH2Lin straight from the spatial H2s (inside the NonLin derivative: the
 // nO^4 h2 is not formed); the same values as k_h2_layout + k_fold_h2.  h2Lin
-// (FP64) is written when non-null, h2Df when non-null.
+// (FP64) is written when non-null, h2Df when non-null.  Only the codes of
+// FillH2Lin's rule are written: the CI apply reads no other code, and the
+// others keep the zeros of the set-up.
 __global__ void k_fold_h2s(z_t* __restrict__ h2Lin, float4* __restrict__ h2Df, const z_t* __restrict__ H2s,
                            const int* __restrict__ btOf, TRAJ_ARGS) {
   const TrajShape& T = shp[blockIdx.z];
@@ -547,6 +549,7 @@ __global__ void k_fold_h2s(z_t* __restrict__ h2Lin, float4* __restrict__ h2Df, c
   btOf = bat(btOf, bs);
   GRID_STRIDE(e, n4) {
     int j2 = (int)(e % nO), i2 = (int)((e / nO) % nO), j1 = (int)((e / nO / nO) % nO), i1 = (int)(e / nO / nO / nO);
+    if (!(i1 < i2 && j1 < j2 && bt_rule_ok(btOf, i1, i2, j1, j2))) continue;
     const z_t v = h2lin_value(btOf, i1, j1, i2, j2, [&](int a, int b, int c, int d) {
       return h2_from_h2s(H2s, btOf, restricted, n, a, b, c, d);
     });
