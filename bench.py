@@ -11,10 +11,12 @@ trajectories drawn from seed 1234 -- N in {2,4} electrons as two restricted
 spin body types, M uniform in 4..12 spatial orbitals, FEDVR 100..400 elements
 x 6 points on [-nE, nE], sin^2 4-cycle pulses at omega = 0.057 au with
 log-uniform intensity 1e13..1e15 W/cm^2 and uniform CEP; dt = 0.02, Krylov
-order 12; mixed precision mixed_fx (the pair-potential, correlation and h2
-contractions on tcgen05 tensor cores with every operand row carried as five
-base-64 digit slices and exact per-level accumulation; FP64 elsewhere;
-three-term Lanczos recurrence).
+order 12; mixed precision mixed_fx6 (the pair-potential, correlation and h2
+contractions on tcgen05 tensor cores with every operand row carried as digit
+slices holding 36 bits of the row maximum -- six base-64 slices on the grid
+contractions, five base-256 slices on the pair contraction -- and exact
+per-level accumulation; FP64 elsewhere; three-term Lanczos recurrence).  The
+faster mixed_fx form (30 bits) is selected with --precision mixed_fx.
 All trajectories advance together: every kernel of the step covers the whole
 batch and the step is one CUDA-graph launch.  The same batch in the plain FP64
 form is timed beside it (the "vs FP64 GPU" leg of the metric).
@@ -27,7 +29,8 @@ Synthetic seeded inputs: Gaussian orbitals and random normalised CI
 coefficients (the step cost does not depend on the values).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload batch512|trimer_large] [--precision mixed|mixed6|fp64]
+                  [--workload batch512|trimer_large|helium_small]
+                  [--precision fp64|mixed|mixed6|mixed_fx|mixed_fx6]
 """
 from __future__ import annotations
 
@@ -52,10 +55,12 @@ DTYPES = {
     "fp64": "complex128",
     "mixed": "mixed (bf16x3 tcgen05 contractions with fp32 accumulation, fp64 rest)",
     "mixed6": "mixed (bf16x6 tcgen05 contractions with fp32 accumulation, fp64 rest)",
-    "mixed_fx": "mixed (tcgen05 contractions on 5 base-64 digit slices per operand row, exact per-level "
-                "accumulation, fp64 results; fp64 rest)",
-    "mixed_fx6": "mixed (tcgen05 contractions on 6 base-64 digit slices per operand row, exact per-level "
-                 "accumulation, fp64 results; fp64 rest)",
+    "mixed_fx": "mixed (tcgen05 contractions on bf16 digit slices holding 30 bits of each operand row's maximum: "
+                "5 base-64 slices for K = n_grid, 4 base-256 for K = 2 n_pairs; exact per-level accumulation, "
+                "fp64 results; fp64 rest)",
+    "mixed_fx6": "mixed (tcgen05 contractions on bf16 digit slices holding 36 bits of each operand row's maximum: "
+                 "6 base-64 slices for K = n_grid, 5 base-256 for K = 2 n_pairs; exact per-level accumulation, "
+                 "fp64 results; fp64 rest)",
 }
 FAMILIES = ("pair_potentials", "correlation", "h2", "ci_apply", "ci_rdm", "onebody", "lanczos", "rdm_inverse",
             "projectors", "fold", "vector")
@@ -255,6 +260,20 @@ def dense_flops(systems, fam):
     return 4.0 * tot
 
 
+FX_BITS = {"mixed_fx": 30, "mixed_fx6": 36}
+
+
+def fx_grid_products(precision, systems):
+    """Slice products per algorithmic product of the fixed-point contractions
+    over the grid: digit width b = 8 / 7 / 6 for K <= 256 / 1024 / longer (the
+    two leading level sums stay exact in FP32), L = ceil(bits / b) slices and
+    the L (L + 1) / 2 slice products of the levels below L."""
+    K = max(s.nG for s in systems)
+    b = 8 if K <= 256 else 7 if K <= 1024 else 6
+    L = -(-FX_BITS[precision] // b)
+    return L * (L + 1) // 2
+
+
 def systems_of(r):
     return r["systems"]
 
@@ -340,7 +359,7 @@ def window_name(window):
 def run_batch(args):
     rank, world, local = dist_info()
     specs, cfg = workload(args.workload)
-    precision = args.precision or "mixed_fx"
+    precision = args.precision or "mixed_fx6"
     n = len(specs)
     window = krylov_window(args, precision)
     acc_steps = 0 if args.no_fp64_leg or precision == "fp64" else ACC_STEPS
@@ -385,6 +404,11 @@ def run_batch(args):
     if dom in ("pair_potentials", "correlation", "h2"):
         work = dense_flops(systems, dom) / n_dom
         roof.update(bound="tensor", achieved=work / avg_s / 1e12, peak=bf16, unit="TFLOP/s", work_per_launch=work)
+        if precision in FX_BITS and dom in ("pair_potentials", "h2"):
+            # what the tensor cores execute: every algorithmic product as slice products
+            k = fx_grid_products(precision, systems)
+            roof.update(slice_products_per_product=k, issued_tflops=k * roof["achieved"],
+                        issued_frac=k * roof["achieved"] / bf16)
     elif dom == "lanczos":
         byts, flops = lanczos_work(systems, cfg["krylov"], window)
         byts /= n_dom

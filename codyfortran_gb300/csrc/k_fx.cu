@@ -12,7 +12,8 @@
 // Each level has its own FP32 accumulator in tensor memory (L accumulators of
 // BN columns), fed by the slice products of that level.  A slice product is
 // an integer of magnitude <= 2^2b, so D_0 and D_1 stay below 2^24 -- exact in
-// FP32 -- for K <= 2^(24-2b) (b = 6: K <= 4096, 7: 1024, 8: 256) and D_2 for
+// FP32 -- for K <= 2^(24-2b) (b = 6: K <= 4096, 7: 1024, 8: 256; longer
+// contractions are split in K and the FP64 partials summed) and D_2 for
 // K <= 0.8 2^(24-2b); a higher level that passes 2^24 rounds by 2^-24 of a
 // term at least 2^-2b below the result's scale.  The epilogue combines the
 // levels in 64-bit integers (Horner in base 2^b), converts once to FP64 and
@@ -104,8 +105,10 @@ struct FxTile {
 // 32w..32w+31); warp 4: TMA producer; warp 5: MMA issuer.  The rings and their
 // phases run on across tiles; the accumulator hand-off uses accFull (MMA ->
 // epilogue) and accEmpty (epilogue -> MMA), so the producer loads the next
-// tile while the epilogue drains the current one.  maxRow/maxCol (nSplit == 1
-// only): the largest biased exponent of |C| per output row / column.
+// tile while the epilogue drains the current one.  K splits: a trajectory of
+// segTiles K blocks takes ceil(segTiles / kPer) balanced splits; the tiles of
+// the list beyond them write zero partials.  maxRow/maxCol (unsplit K only):
+// the largest biased exponent of |C| per output row / column.
 // aShared: A is shared by the trajectories (3D map with one plane per root
 // grid); the trajectory's rows start at vRow of plane vRoot, its K range at
 // vRow - gShift, its row exponents at expA[vExp].
@@ -114,7 +117,7 @@ __global__ void __launch_bounds__(192)
     k_fx_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, double* __restrict__ out,
               const int* __restrict__ expA, const int* __restrict__ expB, unsigned* __restrict__ maxRow,
               unsigned* __restrict__ maxCol, TRAJ_ARGS, int gemmId, int segPitchA, int segPitch, int aShared,
-              int nSplit, int digitBits, const FxTile* __restrict__ tiles, int nTiles, int* __restrict__ err) {
+              int kPer, int digitBits, const FxTile* __restrict__ tiles, int nTiles, int* __restrict__ err) {
   using C = FxCfg<BN, L, NA_, NB_>;
   constexpr int NA = C::NA, NB = C::NB;
   extern __shared__ uint8_t smem_raw[];
@@ -159,9 +162,10 @@ __global__ void __launch_bounds__(192)
     int segTiles;
     tc_dims(shp[tl.traj], gemmId, M, N, segTiles);
     nT = min(BN, (N - tl.n0 + 15) / 16 * 16);
-    const int per = (segTiles + nSplit - 1) / nSplit;
+    const int sT = max(1, (segTiles + kPer - 1) / kPer);  // this trajectory's splits
+    const int per = (segTiles + sT - 1) / sT;              // <= kPer
     kt0 = tl.split * per;
-    nk = max(0, min(segTiles, kt0 + per) - kt0);
+    nk = tl.split < sT ? max(0, min(segTiles, kt0 + per) - kt0) : 0;
   };
 
   if (warp == 4) {
@@ -356,7 +360,7 @@ __global__ void __launch_bounds__(192)
 template <int BN, int L, int NA_, int NB_>
 void launch_fx_t(cgpu_ctx* c, const CUtensorMap& ta, const CUtensorMap& tb, double* out, const int* expA,
                  const int* expB, unsigned* maxRow, unsigned* maxCol, int gemmId, int segPitchA, int segPitch,
-                 int aShared, int nSplit, int digitBits, const FxTile* tiles, int nTiles, int ctasPerSm, int* err) {
+                 int aShared, int kPer, int digitBits, const FxTile* tiles, int nTiles, int ctasPerSm, int* err) {
   using C = FxCfg<BN, L, NA_, NB_>;
   static bool attr = false;
   if (!attr) {
@@ -366,18 +370,31 @@ void launch_fx_t(cgpu_ctx* c, const CUtensorMap& ta, const CUtensorMap& tb, doub
   if (nTiles <= 0) return;
   const int grid = std::min(nTiles, c->numSms * ctasPerSm);
   k_fx_gemm<BN, L, NA_, NB_><<<grid, 192, C::SMEM, c->stream>>>(ta, tb, out, expA, expB, maxRow, maxCol, TRAJ_PASS(c),
-                                                                gemmId, segPitchA, segPitch, aShared, nSplit,
+                                                                gemmId, segPitchA, segPitch, aShared, kPer,
                                                                 digitBits, tiles, nTiles, err);
   CODY_LAUNCHED(c);
 }
 
 }  // namespace
 
-int fx_digit_bits(int K) { return K <= 256 ? 8 : K <= 1024 ? 7 : 6; }
+// 64-wide K blocks per split within which the two leading level sums stay
+// exact in FP32: K <= 2^(24-2b).
+static int fx_exact_tiles(int b) { return (1 << (24 - 2 * b)) / TC_BK; }
 
-int fx_slices(int K, int targetBits) {
-  const int b = fx_digit_bits(K);
-  return (targetBits + b - 1) / b;
+void fx_plan(int kTiles, int targetBits, int* digitBits, int* slices) {
+  // the widest digits whose exact range holds the whole contraction (an extra
+  // K split costs more in tile epilogues and partial sums than a slice)
+  int b = 8;
+  while (b > 6 && kTiles > fx_exact_tiles(b)) b--;
+  int L = (targetBits + b - 1) / b;
+  // |Horner sum| < K 2^(b(L+1)+1) <= 2^(25+b(L-1)) must stay inside int64
+  while (b > 6 && b * (L - 1) > 38) {
+    b--;
+    L = (targetBits + b - 1) / b;
+  }
+  if (L > 6 || b * (L - 1) > 38) throw std::string("fx_plan: no digit width carries the target bits");
+  *digitBits = b;
+  *slices = L;
 }
 
 // Largest N tile of a configuration: L accumulators of BN columns in 512
@@ -399,11 +416,12 @@ int fx_tile_n(int N, int L, bool compact) {
   return maxBn;
 }
 
-int fx_split_count(int M, int N, int BN, int kTiles, int nb) {
+int fx_split_count(int M, int N, int BN, int kTiles, int nb, int digitBits) {
   long tiles = (long)((M + TC_BM - 1) / TC_BM) * ((N + BN - 1) / BN) * nb;
   int s = (int)std::max<long>(1, (152 + tiles - 1) / tiles);
   s = std::min(s, std::max(1, kTiles / 2));
-  s = std::max(s, (kTiles + 63) / 64);  // K per split <= 4096: the exact range of the level sums at b = 6
+  const int exact = fx_exact_tiles(digitBits);
+  s = std::max(s, (kTiles + exact - 1) / exact);  // every split inside the exact range of the level sums
   int per = (kTiles + s - 1) / s;
   return (kTiles + per - 1) / per;
 }
@@ -434,12 +452,14 @@ void fx_gemm(cgpu_ctx* c, int L, int digitBits, bool compact, int gemmId, const 
   if (segPitch % TC_BK != 0 || segPitchA % TC_BK != 0)
     throw std::string("fx_gemm: segment pitch must be a multiple of 64");
   if (nSplit > 1 && (maxRow || maxCol)) throw std::string("fx_gemm: output maxima need an unsplit K");
-  if (digitBits < 6 || digitBits > 8 || digitBits * L > 52) throw std::string("fx_gemm: digit width");
+  const int kTiles = segPitch / TC_BK, kPer = (kTiles + nSplit - 1) / nSplit;  // K blocks per split
+  if (digitBits < 6 || digitBits > 8 || digitBits * (L - 1) > 38) throw std::string("fx_gemm: digit width");
+  if (kPer > fx_exact_tiles(digitBits)) throw std::string("fx_gemm: K split beyond the exact range of the digits");
   const FxTile* tl = (const FxTile*)tiles;
 #define FX_CASE(BN_, L_, NA_, NB_, CMP_)                                                                        \
   if (bn == BN_ && L == L_ && compact == CMP_) {                                                                \
     launch_fx_t<BN_, L_, NA_, NB_>(c, ta, tb, out, expA, expB, maxRow, maxCol, gemmId, segPitchA, segPitch,    \
-                                   aShared, nSplit, digitBits, tl, nTiles, CMP_ ? 2 : 1, err);                 \
+                                   aShared, kPer, digitBits, tl, nTiles, CMP_ ? 2 : 1, err);                   \
     return;                                                                                                     \
   }
   FX_CASE(32, 4, 0, 2, false) FX_CASE(64, 4, 0, 2, false) FX_CASE(80, 4, 0, 2, false) FX_CASE(96, 4, 0, 2, false)

@@ -17,11 +17,14 @@
 //
 // The fixed-point form (precision mixed_fx / mixed_fx6) carries every operand
 // row as L base-2^b digit slices under one power of two per row (k_fx.cu) and
-// returns FP64 results whose only error is the operand truncation (about 30 /
-// 36 bits of each row's maximum): S and V rows for GEMM1, W rows for GEMM2,
-// R'' rows, W columns for GEMM3.  The digit width b follows the contraction
-// length (GEMM1/3: K = nG, GEMM2: K = 2P), the slice count L = ceil(bits / b).
-// The row exponents of W come from the GEMM1 epilogue.
+// returns FP64 results whose only error is the operand truncation (at least
+// 30 / 36 bits of each row's maximum): S and V rows for GEMM1, W rows for
+// GEMM2, R'' rows, W columns for GEMM3.  fx_plan picks the digit width b of
+// each contraction length (GEMM1/3: K = nG, GEMM2: K = 2P) and the slice
+// count L = ceil(bits / b).  S carries LS = max(L1, L3) slices: GEMM1 reads
+// the first L1 (dropping balanced digits costs at most half a unit of the
+// last digit kept), GEMM3 L3.  The row exponents of W come from the GEMM1
+// epilogue, or from the reduction of its K splits.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -42,6 +45,7 @@ struct MixedBufs {
   // fixed-point form (fxBits > 0): digit width / slices of the K = nG
   // contractions (GEMM1, GEMM3) and of the K = 2P one (GEMM2)
   int fxBits = 0, b1 = 0, L1 = 0, b2 = 0, L2 = 0;
+  int fxBits3 = 0, L3 = 0, LS = 0;  // GEMM3 target and slices; S carries LS = max(L1, L3) slices
   bool compact2 = false;
   // one interaction matrix per root grid (cgpu_ctx::fxShared): slices [root][c->nG][L1 KgBig]
   // and row exponents [root][c->nG], outside the per-trajectory arena
@@ -485,13 +489,13 @@ __global__ void k_fx_reduce_W(double* __restrict__ Wd, unsigned* __restrict__ mW
 }
 
 // W (FP64 [nG][2P]) to WxA (rows g, K = 2P: b2/L2 digits) and WTxB (rows n,
-// K = nG at columns gShift + g: b1/L1 digits) planes, with the row exponents
+// K = nG at columns gShift + g: b1/L3 digits) planes, with the row exponents
 // eWr[g] / eWc[n]; 32 x 32 tiles transposed through shared memory as k_split_W.
 __global__ void __launch_bounds__(256) k_fx_split_W(__nv_bfloat16* __restrict__ WxA, __nv_bfloat16* __restrict__ WTxB,
                                                      int* __restrict__ eWr, int* __restrict__ eWc,
                                                      const double* __restrict__ Wd, const unsigned* __restrict__ mWr,
                                                      const unsigned* __restrict__ mWc, int pitchP, int pitchG, int b1,
-                                                     int L1, int b2, int L2, TRAJ_ARGS) {
+                                                     int L3, int b2, int L2, TRAJ_ARGS) {
   __shared__ double tile[SW_T][SW_T + 1];
   const TrajShape& T = shp[blockIdx.z];
   const int nG = T.nG, N2P = 2 * T.nPairs, KpP = T.Kp, KpG = T.Kg;
@@ -523,10 +527,10 @@ __global__ void __launch_bounds__(256) k_fx_split_W(__nv_bfloat16* __restrict__ 
     if (n < N2P && col < KpG) {
       const int e = fx_exp(mWc[n]);
       if (g == 0) eWc[n] = e;
-      fx_store(WTxB + (size_t)n * L1 * pitchG, pitchG, col, g < nG, tile[tx][r], e, b1, L1);
+      fx_store(WTxB + (size_t)n * L3 * pitchG, pitchG, col, g < nG, tile[tx][r], e, b1, L3);
     }
     if (n < N2P && g0 == 0)  // columns before the shifted grid
-      for (int cz = tx; cz < sh; cz += 32) fx_store(WTxB + (size_t)n * L1 * pitchG, pitchG, cz, false, 0.0, 0, b1, L1);
+      for (int cz = tx; cz < sh; cz += 32) fx_store(WTxB + (size_t)n * L3 * pitchG, pitchG, cz, false, 0.0, 0, b1, L3);
   }
 }
 
@@ -545,6 +549,7 @@ size_t mixed_layout(cgpu_ctx* c, char* base, size_t off) {
   if (!c->mixed) c->mixed = new MixedBufs();
   MixedBufs* m = c->mixed;
   m->fxBits = c->precision == CGPU_PREC_MIXED_FX ? 30 : c->precision == CGPU_PREC_MIXED_FX6 ? 36 : 0;
+  m->fxBits3 = m->fxBits;
   m->terms = c->precision == CGPU_PREC_MIXED_X6 ? 6 : 3;
   int nG = c->nG, nP = c->nPairs, Q = c->nOS * c->nOS, T = m->terms;
   m->KgMax = (nG + 63) / 64 * 64;
@@ -553,23 +558,25 @@ size_t mixed_layout(cgpu_ctx* c, char* base, size_t off) {
   if (m->fxBits) {
     m->KgMax = c->fxKgMax;  // includes the K-tile offsets of a shared interaction matrix
     // digit widths from the longest contraction of the batch (K = nG, K = 2P)
-    m->b1 = fx_digit_bits(nG);
-    m->L1 = fx_slices(nG, m->fxBits);
-    m->b2 = fx_digit_bits(2 * nP);
-    m->L2 = fx_slices(2 * nP, m->fxBits);
+    fx_plan(m->KgMax / 64, m->fxBits, &m->b1, &m->L1);
+    int b3 = 0;
+    fx_plan(m->KgMax / 64, m->fxBits3, &b3, &m->L3);
+    if (b3 != m->b1) throw std::string("mixed_fx: GEMM1 and GEMM3 share the S digits");
+    m->LS = std::max(m->L1, m->L3);
+    fx_plan(m->KpMax / 64, m->fxBits, &m->b2, &m->L2);
     const int L1 = m->L1, L2 = m->L2;
     m->compact2 = c->nb > 1 && fx_compact_ok(L2);
     m->bn1 = fx_tile_n(2 * nP, L1, false);
     m->bn2 = fx_tile_n(2 * Q, L2, m->compact2);
-    m->bn3 = fx_tile_n(2 * nP, L1, false);
-    m->s1 = fx_split_count(nG, 2 * nP, m->bn1, m->KgMax / 64, c->nb);
-    m->s2 = fx_split_count(nG, 2 * Q, m->bn2, m->KpMax / 64, c->nb);
-    m->s3 = fx_split_count(2 * nP, 2 * nP, m->bn3, m->KgMax / 64, c->nb);
+    m->bn3 = fx_tile_n(2 * nP, m->L3, false);
+    m->s1 = fx_split_count(nG, 2 * nP, m->bn1, m->KgMax / 64, c->nb, m->b1);
+    m->s2 = fx_split_count(nG, 2 * Q, m->bn2, m->KpMax / 64, c->nb, m->b2);
+    m->s3 = fx_split_count(2 * nP, 2 * nP, m->bn3, m->KgMax / 64, c->nb, m->b1);
     const size_t perTrajV = c->fxShared ? 0 : 1;
     size_t oV = take(off, perTrajV * sizeof(bf) * (size_t)nG * L1 * m->KgMax);
-    size_t oS = take(off, sizeof(bf) * (size_t)2 * nP * L1 * m->KgMax);
+    size_t oS = take(off, sizeof(bf) * (size_t)2 * nP * m->LS * m->KgMax);
     size_t oW = take(off, sizeof(bf) * (size_t)nG * L2 * m->KpMax);
-    size_t oWT = take(off, sizeof(bf) * (size_t)2 * nP * L1 * m->KgMax);
+    size_t oWT = take(off, sizeof(bf) * (size_t)2 * nP * m->L3 * m->KgMax);
     size_t oR = take(off, sizeof(bf) * (size_t)2 * Q * L2 * m->KpMax);
     size_t oWd = take(off, sizeof(double) * (size_t)m->s1 * nG * 2 * nP);
     size_t oZp = take(off, m->s2 > 1 ? sizeof(double) * (size_t)m->s2 * nG * 2 * Q : 0);
@@ -652,10 +659,12 @@ void mixed_free(cgpu_ctx* c) {
 void mixed_init(cgpu_ctx* c) {
   MixedBufs* m = c->mixed;
   if (!m) return;
-  int T = m->terms, pG = T * m->KgMax, pP = T * m->KpMax;
+  int T = m->terms, pG = T * m->KgMax, pP = T * m->KpMax, pS = pG, pWT = pG;
   if (m->fxBits) {
-    pG = m->L1 * m->KgMax;  // S, V, WT: K = nG slices
-    pP = m->L2 * m->KpMax;  // W, R: K = 2P slices
+    pG = m->L1 * m->KgMax;   // V: K = nG slices
+    pS = m->LS * m->KgMax;   // S (GEMM1 reads the first L1 slices, GEMM3 L3)
+    pWT = m->L3 * m->KgMax;  // W columns for GEMM3
+    pP = m->L2 * m->KpMax;   // W, R: K = 2P slices
   }
   size_t nGK = (size_t)c->nG * m->KgMax;
   if (m->fxBits && c->fxShared) {
@@ -684,16 +693,16 @@ void mixed_init(cgpu_ctx* c) {
   int P2 = 2 * c->nPairs, Q2 = 2 * c->nOS * c->nOS;
   if (m->VxB) m->mV = tc_make_map(c, m->VxB, c->nG, pG, 128);
   // the fixed-point GEMM loads its B operands in 16-row boxes
-  m->mS = tc_make_map(c, m->SxA, P2, pG, m->fxBits ? 16 : m->bn1);
+  m->mS = tc_make_map(c, m->SxA, P2, pS, m->fxBits ? 16 : m->bn1);
   m->mW = tc_make_map(c, m->WxA, c->nG, pP, 128);
   m->mR = tc_make_map(c, m->RxB, Q2, pP, m->fxBits ? 16 : m->bn2);
-  m->mSasB = tc_make_map(c, m->SxA, P2, pG, 128);
+  m->mSasB = tc_make_map(c, m->SxA, P2, pS, 128);
   if (m->fxBits) {
     m->tiles1 = fx_build_tiles(c, TC_GEMM_W, m->bn1, m->s1, &m->nTiles1);
     m->tiles2 = fx_build_tiles(c, TC_GEMM_Z, m->bn2, m->s2, &m->nTiles2);
     m->tiles3 = fx_build_tiles(c, TC_GEMM_H2, m->bn3, m->s3, &m->nTiles3);
   }
-  m->mWT = tc_make_map(c, m->WTxB, P2, pG, m->fxBits ? 16 : m->bn3);
+  m->mWT = tc_make_map(c, m->WTxB, P2, pWT, m->fxBits ? 16 : m->bn3);
   CODY_CUDA(cudaStreamSynchronize(c->stream));
 }
 
@@ -712,7 +721,7 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   {
     ProfScope prof(c, CGPU_KERNEL_PAIR_POTENTIALS);
     k_fx_split_S<<<dim3(2 * nP, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(
-        m->SxA, m->eS, m->mWr, m->mWc, orbs, c->w_d, c->pairL_d, c->pairK_d, m->KgMax, m->b1, m->L1, TRAJ_PASS(c));
+        m->SxA, m->eS, m->mWr, m->mWc, orbs, c->w_d, c->pairL_d, c->pairK_d, m->KgMax, m->b1, m->LS, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
     const bool one = m->s1 == 1;
     if (c->fxShared)
@@ -729,7 +738,7 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
     }
     dim3 gw(ceil_div(m->KgMax, SW_T), ceil_div(m->KpMax, SW_T), c->nb);
     k_fx_split_W<<<gw, 256, 0, c->stream>>>(m->WxA, m->WTxB, m->eWr, m->eWc, m->Wd, m->mWr, m->mWc, m->KpMax,
-                                            m->KgMax, m->b1, m->L1, m->b2, m->L2, TRAJ_PASS(c));
+                                            m->KgMax, m->b1, m->L3, m->b2, m->L2, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
   }
   {
@@ -747,7 +756,7 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   }
   if (wantH2) {
     ProfScope prof(c, CGPU_KERNEL_H2);
-    fx_gemm(c, m->L1, m->b1, false, TC_GEMM_H2, m->mSasB, m->mWT, m->bn3, m->Gd, m->eS, m->eWc, nullptr, nullptr,
+    fx_gemm(c, m->L3, m->b1, false, TC_GEMM_H2, m->mSasB, m->mWT, m->bn3, m->Gd, m->eS, m->eWc, nullptr, nullptr,
             m->KgMax, m->KgMax, 0, m->s3, m->tiles3, m->nTiles3, m->err);
     k_reduce_H2<<<bgrid(c, ew_blocks(c, (size_t)Q * Q)), 256, 0, c->stream>>>(c->h2s_d, m->Gd, m->s3, c->pidx_d,
                                                                         TRAJ_PASS(c));

@@ -38,17 +38,19 @@ void* fx_build_tiles(cgpu_ctx* c, int gemmId, int bn, int nSplit, int* nTiles);
 // 3D TMA map over an explicit [planes][rowsMax][pitch] bf16 tensor (planes planeBytes apart).
 CUtensorMap tc_make_map_planes(const __nv_bfloat16* base, int rowsMax, int pitch, int boxRows, int planes,
                                size_t planeBytes);
-// Digit width for a contraction of length K: 8 bits up to 256, 7 up to 1024, else 6
-// (the level sums of the two leading levels stay exact in FP32).
-int fx_digit_bits(int K);
-// Slices that carry targetBits fractional bits at that width.
-int fx_slices(int K, int targetBits);
+// Digit width (6..8 bits) and slice count carrying at least targetBits
+// fractional bits for a contraction of kTiles 64-wide K blocks: the widest
+// digits whose two leading level sums stay exact in FP32 over the whole K
+// (K <= 2^(24-2b)) and whose epilogue sum of the levels stays inside int64
+// (b (L-1) <= 38).
+void fx_plan(int kTiles, int targetBits, int* digitBits, int* slices);
 // N-tile width for N output columns and L slices (wide: L * BN <= 512, compact: <= 256).
 int fx_tile_n(int N, int L, bool compact);
 // Whether a compact configuration exists for L slices.
 bool fx_compact_ok(int L);
-// K splits of the fixed-point GEMM: about one wave of 152 SMs, at most 4096 K per split.
-int fx_split_count(int M, int N, int BN, int kTiles, int nb);
+// K splits of the fixed-point GEMM: about one wave of 152 SMs, and every split
+// inside the exact range of the level sums at digitBits (2^(24-2b) K).
+int fx_split_count(int M, int N, int BN, int kTiles, int nb, int digitBits);
 
 // ---- device helpers shared by the tcgen05 kernels (TMA, mbarriers, MMA, TMEM) ----
 namespace tcdev {

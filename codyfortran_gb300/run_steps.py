@@ -26,7 +26,7 @@ def main():
 
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="batch512", choices=["batch512", "trimer_large"])
-    ap.add_argument("--precision", default="mixed_fx", choices=["fp64", "mixed", "mixed6", "mixed_fx", "mixed_fx6"])
+    ap.add_argument("--precision", default="mixed_fx6", choices=["fp64", "mixed", "mixed6", "mixed_fx", "mixed_fx6"])
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--trajectories", type=int, default=512)
     ap.add_argument("--krylov-window", type=int, default=None,

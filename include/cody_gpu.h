@@ -52,12 +52,13 @@ extern "C" {
 #define CGPU_PREC_MIXED 1
 /* As CGPU_PREC_MIXED with three-way split operands (hi + mid + lo, six products). */
 #define CGPU_PREC_MIXED_X6 2
-/* Fixed-point split form: every operand row carried as 5 base-64 digit slices under one
- * power of two per row (30 bits of the row maximum), slice products of one level summed
- * exactly in their own FP32 tensor-memory accumulator, levels combined in 64-bit integers:
- * the contractions equal the products of the truncated operands; 15 products. */
+/* Fixed-point split form: every operand row carried as bf16 digit slices under one power
+ * of two per row, holding 30 bits of the row maximum (5 base-64 slices for the contractions
+ * over the grid, 4 base-256 slices for the one over orbital pairs); slice products of one
+ * level summed exactly in their own FP32 tensor-memory accumulator, levels combined in
+ * 64-bit integers: the contractions equal the products of the truncated operands. */
 #define CGPU_PREC_MIXED_FX 3
-/* As CGPU_PREC_MIXED_FX with 6 slices (36 bits, 21 products). */
+/* As CGPU_PREC_MIXED_FX with 36 bits (6 base-64 slices, 5 base-256 slices). */
 #define CGPU_PREC_MIXED_FX6 4
 
 /* Time-derivative selectors (the TimeDerivative procedure pointers). */

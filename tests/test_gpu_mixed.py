@@ -2,9 +2,9 @@
 
 Tolerances state the accuracy of each form: bf16x3 (hi + lo operands, three
 products, FP32 accumulation), bf16x6 (hi + mid + lo, six products), and the
-fixed-point forms mixed_fx / mixed_fx6 (5 / 6 base-64 digit slices per
-operand row, exact per-level accumulation: only the 30 / 36-bit operand
-truncation remains).  The relative errors measured here are what the forms
+fixed-point forms mixed_fx / mixed_fx6 (bf16 digit slices holding 30 / 36
+bits of each operand row's maximum, exact per-level accumulation: only the
+operand truncation remains).  The relative errors measured here are what the forms
 deliver; the propagation check compares energy and norm of a mixed
 trajectory with the FP64 one.
 """
