@@ -284,7 +284,7 @@ def batch_norms(b, packed):
 
 
 def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=False, e2e=True, acc_steps=0, window=0):
-    from codyfortran_gb300.engine import Batch
+    from codyfortran_gb300.engine import Batch, pinned_empty
     dt, K = cfg["dt"], cfg["krylov"]
     b = Batch(specs, precision, max_krylov=K, krylov_window=window)
     states = [initial_state(sp, s.x, s.w, cfg["seed"] + k) for k, (sp, s) in enumerate(zip(specs, b.systems))]
@@ -318,9 +318,14 @@ def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=Fals
     out = dict(ms=ms, fam_ms=fam_ms, dom=dom, n_dom=n_dom, ms_dom=ms_dom, launches=launches,
                clocks=clk.summary() if clk else None, systems=b.systems, kps=b.kernels_per_step())
     if e2e:
-        # end to end through the C ABI: packed host states in, one step, packed states out
-        n_e2e = max(1, min(steps, 5))
-        buf = host.copy()
+        # end to end through the C ABI: packed host states in, one step, packed
+        # states out, from and to page-locked host memory (cgpu_host_alloc)
+        n_e2e = max(3, min(steps, 10))
+        buf = pinned_empty(host.size)
+        buf[:] = host
+        # untimed: the step graph is re-captured without the profiling events
+        b.propagate(t, dt, 1, K)
+        t += dt
         te0 = time.perf_counter()
         for _ in range(n_e2e):
             b.upload(buf)
@@ -440,7 +445,8 @@ def run_batch(args):
         "accuracy_vs_fp64": accuracy,
         "clocks": r["clocks"],
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": r["e2e_bytes"], "d2h_bytes_per_step": r["e2e_bytes"],
-                "call": "cgpu_batch_upload + cgpu_batch_propagate(1 step) + cgpu_batch_download, pageable host buffers"},
+                "call": "cgpu_batch_upload + cgpu_batch_propagate(1 step) + cgpu_batch_download, pinned host "
+                        "buffers (cgpu_host_alloc)"},
         "gpu_launches": int(r["launches"]),
         "kernels_per_step": r["kps"],
         "roofline": roof,
@@ -458,7 +464,7 @@ def run_batch(args):
 
 def run_single(args):
     rank, world, local = dist_info()
-    from codyfortran_gb300.engine import Engine
+    from codyfortran_gb300.engine import Engine, pinned_empty
     specs, cfg = workload(args.workload)
     sp = specs[0]
     precision = args.precision or "fp64"
@@ -490,11 +496,15 @@ def run_single(args):
     t += args.steps * dt
     ms = barrier_max(ms, world)
     value = world * args.steps / (ms / 1e3)
-    host = e.download()
+    host = pinned_empty(e.nS)
+    host[:] = e.download()
     n_e2e = max(1, min(args.steps, 20))
+    # untimed: the step graph is re-captured without the profiling events
+    e.propagate_split2(host, t, t + dt, krylov_dim=K, use_metric=True, out=host)
+    t += dt
     te0 = time.perf_counter()
     for _ in range(n_e2e):
-        host = e.propagate_split2(host, t, t + dt, krylov_dim=K, use_metric=True)
+        e.propagate_split2(host, t, t + dt, krylov_dim=K, use_metric=True, out=host)
         t += dt
     te = barrier_max(time.perf_counter() - te0, world)
     e2e = world * n_e2e / te
@@ -524,7 +534,7 @@ def run_single(args):
                    "l2": "inputs larger than L2, no flush"},
         "clocks": clk.summary(),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": e.nS * 16, "d2h_bytes_per_step": e.nS * 16,
-                "steps": n_e2e, "call": "cgpu_propagate_split2 (host state in/out)"},
+                "steps": n_e2e, "call": "cgpu_propagate_split2 (host state in/out, pinned host buffer)"},
         "gpu_launches": int(launches),
         "roofline": {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
                      "frac": achieved / peak, "peak_source": src, "traffic": None,

@@ -392,6 +392,7 @@ struct cgpu_ctx {
   long* stageOff_d = nullptr;
   z_t* stage_d = nullptr;
   size_t stageCap = 0;
+  double* tStage_d = nullptr;     // the nb step start times, contiguous, before k_set_step_times
   // device operators (trajectory 0; the others at multiples of bs)
   double *x_d = nullptr, *w_d = nullptr, *V0_d = nullptr, *T_d = nullptr, *Vint_d = nullptr, *metric_d = nullptr;
   double *metricW_d = nullptr, *metricOne_d = nullptr;  // [1 | w per orbital point] and all ones

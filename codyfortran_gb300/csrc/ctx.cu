@@ -192,6 +192,11 @@ __global__ void k_build_vint(double* __restrict__ V, const double* __restrict__ 
   V[e] = s * exp(-dist * damp) / (sqrt(dist * dist + s1 * s1) + s2);
 }
 
+__global__ void k_set_step_times(double* __restrict__ stepT, const double* __restrict__ t0s, int nb, size_t bs) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < nb) *(double*)((char*)stepT + (size_t)b * bs) = t0s[b];
+}
+
 __global__ void k_scatter_states(z_t* __restrict__ dst, const z_t* __restrict__ src, const long* __restrict__ off,
                                  TRAJ_ARGS) {
   const TrajShape& S = shp[blockIdx.z];
@@ -608,8 +613,8 @@ void free_ctx(cgpu_ctx* c) {
     }
     if (s.samples_d) cudaFree(s.samples_d);
   }
-  void* ptrs[] = {c->arena, c->shape_d, c->metricUser_d, c->stageOff_d, c->stage_d, c->applyWork_d, c->rdmWork_d,
-                  c->pairWork_d};
+  void* ptrs[] = {c->arena,      c->shape_d,     c->metricUser_d, c->stageOff_d, c->stage_d,
+                  c->tStage_d,    c->applyWork_d, c->rdmWork_d,    c->pairWork_d};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->lz_h) cudaFreeHost(c->lz_h);
@@ -822,10 +827,14 @@ void capture_step_graph(cgpu_ctx* c, double t0, double dt, int krylov, int useMe
   c->graphAbsorb = c->absorbEachStep;
 }
 
-// Step start time of every trajectory (t0s has nb entries).
+// Step start time of every trajectory (t0s has nb entries): one contiguous
+// copy and a kernel that writes each trajectory's slot (a strided copy of nb
+// single doubles costs the driver one transfer per trajectory).
 void set_step_times(cgpu_ctx* c, const double* t0s) {
-  CODY_CUDA(cudaMemcpy2DAsync(c->stepT_d, c->bs, t0s, sizeof(double), sizeof(double), c->nb, cudaMemcpyHostToDevice,
-                              c->stream));
+  if (!c->tStage_d) CODY_CUDA(cudaMalloc(&c->tStage_d, sizeof(double) * c->nb));
+  CODY_CUDA(cudaMemcpyAsync(c->tStage_d, t0s, sizeof(double) * c->nb, cudaMemcpyHostToDevice, c->stream));
+  k_set_step_times<<<ceil_div(c->nb, 256), 256, 0, c->stream>>>(c->stepT_d, c->tStage_d, c->nb, c->bs);
+  CODY_LAUNCHED(c);
 }
 
 // n_steps replays of the step graph (captured when dt, order or metric changed).
@@ -1006,6 +1015,32 @@ int cgpu_ctx_destroy(cgpu_ctx* ctx) {
 
 const char* cgpu_last_error(const cgpu_ctx* ctx) { return ctx ? ctx->lastError.c_str() : g_lastGlobalError.c_str(); }
 const char* cgpu_last_global_error(void) { return g_lastGlobalError.c_str(); }
+
+int cgpu_host_alloc(size_t bytes, void** out) {
+  if (!out) {
+    cody_record_global_error("cgpu_host_alloc: null argument");
+    return CGPU_ERR_ARG;
+  }
+  *out = nullptr;
+  if (bytes == 0) return CGPU_OK;
+  const cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    cody_record_global_error(std::string("cgpu_host_alloc: ") + cudaGetErrorString(e));
+    return CGPU_ERR_CUDA;
+  }
+  return CGPU_OK;
+}
+
+int cgpu_host_free(void* ptr) {
+  if (!ptr) return CGPU_OK;
+  const cudaError_t e = cudaFreeHost(ptr);
+  if (e != cudaSuccess) {
+    cody_record_global_error(std::string("cgpu_host_free: ") + cudaGetErrorString(e));
+    return CGPU_ERR_CUDA;
+  }
+  return CGPU_OK;
+}
 
 int cgpu_sizes(const cgpu_ctx* c, int* out) {
   if (!c || !out) return CGPU_ERR_ARG;

@@ -490,7 +490,8 @@ __global__ void k_fx_reduce_W(double* __restrict__ Wd, unsigned* __restrict__ mW
 
 // W (FP64 [nG][2P]) to WxA (rows g, K = 2P: b2/L2 digits) and WTxB (rows n,
 // K = nG at columns gShift + g: b1/L3 digits) planes, with the row exponents
-// eWr[g] / eWc[n]; 32 x 32 tiles transposed through shared memory as k_split_W.
+// eWr[g] / eWc[n].  One block per 32-row strip of W, walking the trajectory's
+// own K = 2P columns in 32 x 32 tiles transposed through shared memory.
 __global__ void __launch_bounds__(256) k_fx_split_W(__nv_bfloat16* __restrict__ WxA, __nv_bfloat16* __restrict__ WTxB,
                                                      int* __restrict__ eWr, int* __restrict__ eWc,
                                                      const double* __restrict__ Wd, const unsigned* __restrict__ mWr,
@@ -499,8 +500,8 @@ __global__ void __launch_bounds__(256) k_fx_split_W(__nv_bfloat16* __restrict__ 
   __shared__ double tile[SW_T][SW_T + 1];
   const TrajShape& T = shp[blockIdx.z];
   const int nG = T.nG, N2P = 2 * T.nPairs, KpP = T.Kp, KpG = T.Kg;
-  const int g0 = blockIdx.x * SW_T, n0 = blockIdx.y * SW_T;
-  if (g0 >= KpG || n0 >= KpP) return;
+  const int g0 = blockIdx.x * SW_T;
+  if (g0 >= KpG) return;
   WxA = bat(WxA, bs);
   WTxB = bat(WTxB, bs);
   eWr = bat(eWr, bs);
@@ -509,28 +510,32 @@ __global__ void __launch_bounds__(256) k_fx_split_W(__nv_bfloat16* __restrict__ 
   mWr = bat(mWr, bs);
   mWc = bat(mWc, bs);
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-  for (int r = ty; r < SW_T; r += 8) {
-    const int g = g0 + r, n = n0 + tx;
-    const bool valid = g < nG && n < N2P;
-    const double v = valid ? Wd[(size_t)g * N2P + n] : 0.0;
-    tile[r][tx] = v;
-    if (g < nG && n < KpP) {
-      const int e = fx_exp(mWr[g]);
-      if (n == 0) eWr[g] = e;
-      fx_store(WxA + (size_t)g * L2 * pitchP, pitchP, n, valid, v, e, b2, L2);
-    }
-  }
-  __syncthreads();
   const int sh = T.gShift;
-  for (int r = ty; r < SW_T; r += 8) {
-    const int n = n0 + r, g = g0 + tx, col = g + sh;
-    if (n < N2P && col < KpG) {
-      const int e = fx_exp(mWc[n]);
-      if (g == 0) eWc[n] = e;
-      fx_store(WTxB + (size_t)n * L3 * pitchG, pitchG, col, g < nG, tile[tx][r], e, b1, L3);
+  for (int n0 = 0; n0 < KpP; n0 += SW_T) {
+    if (n0 > 0) __syncthreads();  // the previous tile has been read
+    for (int r = ty; r < SW_T; r += 8) {
+      const int g = g0 + r, n = n0 + tx;
+      const bool valid = g < nG && n < N2P;
+      const double v = valid ? Wd[(size_t)g * N2P + n] : 0.0;
+      tile[r][tx] = v;
+      if (g < nG) {
+        const int e = fx_exp(mWr[g]);
+        if (n == 0) eWr[g] = e;
+        fx_store(WxA + (size_t)g * L2 * pitchP, pitchP, n, valid, v, e, b2, L2);
+      }
     }
-    if (n < N2P && g0 == 0)  // columns before the shifted grid
-      for (int cz = tx; cz < sh; cz += 32) fx_store(WTxB + (size_t)n * L3 * pitchG, pitchG, cz, false, 0.0, 0, b1, L3);
+    __syncthreads();
+    for (int r = ty; r < SW_T; r += 8) {
+      const int n = n0 + r, g = g0 + tx, col = g + sh;
+      if (n < N2P && col < KpG) {
+        const int e = fx_exp(mWc[n]);
+        if (g == 0) eWc[n] = e;
+        fx_store(WTxB + (size_t)n * L3 * pitchG, pitchG, col, g < nG, tile[tx][r], e, b1, L3);
+      }
+      if (n < N2P && g0 == 0)  // columns before the shifted grid
+        for (int cz = tx; cz < sh; cz += 32)
+          fx_store(WTxB + (size_t)n * L3 * pitchG, pitchG, cz, false, 0.0, 0, b1, L3);
+    }
   }
 }
 
@@ -736,7 +741,7 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
                                                                                      TRAJ_PASS(c));
       CODY_LAUNCHED(c);
     }
-    dim3 gw(ceil_div(m->KgMax, SW_T), ceil_div(m->KpMax, SW_T), c->nb);
+    dim3 gw(ceil_div(m->KgMax, SW_T), 1, c->nb);
     k_fx_split_W<<<gw, 256, 0, c->stream>>>(m->WxA, m->WTxB, m->eWr, m->eWc, m->Wd, m->mWr, m->mWc, m->KpMax,
                                             m->KgMax, m->b1, m->L3, m->b2, m->L2, TRAJ_PASS(c));
     CODY_LAUNCHED(c);

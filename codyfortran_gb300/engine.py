@@ -24,7 +24,8 @@ TD_FULL, TD_ORBS_LIN, TD_NONLIN, TD_TDCI = 0, 1, 2, 3
 _WHICH = {"full": TD_FULL, "orbs_lin": TD_ORBS_LIN, "nonlin": TD_NONLIN, "tdci": TD_TDCI}
 
 EXPORTED = [
-    "cgpu_ctx_create", "cgpu_ctx_destroy", "cgpu_last_error", "cgpu_last_global_error", "cgpu_sizes", "cgpu_grid",
+    "cgpu_ctx_create", "cgpu_ctx_destroy", "cgpu_last_error", "cgpu_last_global_error", "cgpu_host_alloc",
+    "cgpu_host_free", "cgpu_sizes", "cgpu_grid",
     "cgpu_configlist_tables", "cgpu_synchronize", "cgpu_launch_count", "cgpu_time_derivative",
     "cgpu_apply_single_body_op", "cgpu_fill_h1", "cgpu_fill_h2", "cgpu_apply_correlation_op", "cgpu_energy",
     "cgpu_ci_apply_h1_fill_rdm1", "cgpu_ci_apply_h2_fill_rdm2", "cgpu_project_coeffs", "cgpu_normalize_coeffs",
@@ -91,10 +92,37 @@ def load_library(path: str = LIB_PATH):
     lib.cgpu_batch_launch_count.argtypes = [C.c_void_p, C.c_int]
     lib.cgpu_batch_shared_interactions.restype = C.c_int
     lib.cgpu_batch_shared_interactions.argtypes = [C.c_void_p]
+    lib.cgpu_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
+    lib.cgpu_host_free.argtypes = [C.c_void_p]
     lib.cgpu_save_restart.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
     lib.cgpu_load_restart.argtypes = [C.c_void_p, C.c_char_p]
     _lib = lib
     return lib
+
+
+class _PinnedBlock:
+    """Page-locked host block from cgpu_host_alloc, exposed to numpy through the
+    array interface and released when the last array over it is gone."""
+
+    def __init__(self, n, dtype):
+        self._lib = load_library()
+        dt = np.dtype(dtype)
+        ptr = C.c_void_p()
+        if self._lib.cgpu_host_alloc(C.c_size_t(max(1, int(n)) * dt.itemsize), C.byref(ptr)) != 0:
+            raise CodyError(self._lib.cgpu_last_global_error().decode())
+        self._ptr = ptr.value
+        self.__array_interface__ = {"shape": (int(n),), "typestr": dt.str, "data": (self._ptr, False), "version": 3}
+
+    def __del__(self):
+        if getattr(self, "_ptr", None):
+            self._lib.cgpu_host_free(C.c_void_p(self._ptr))
+            self._ptr = None
+
+
+def pinned_empty(n, dtype=np.complex128):
+    """Uninitialised 1-D array of n elements in page-locked host memory: state
+    buffers whose uploads and downloads run as direct DMA."""
+    return np.asarray(_PinnedBlock(n, dtype))
 
 
 def _p(a):
@@ -322,9 +350,18 @@ class Engine:
                                                 max_restarts, _p(m), C.byref(warn)))
         return s
 
-    def propagate_split2(self, state, t0, t1, krylov_dim=0, tol=0.0, max_restarts=0, use_metric=False):
-        """Propagator_Propagate for SplitStep Order2 (host state in, host state out)."""
-        s = np.array(state, dtype=np.complex128)
+    def propagate_split2(self, state, t0, t1, krylov_dim=0, tol=0.0, max_restarts=0, use_metric=False, out=None):
+        """Propagator_Propagate for SplitStep Order2 (host state in, host state
+        out); `out` (complex128, contiguous, may be `state` itself) receives the
+        result in place."""
+        if out is None:
+            s = np.array(state, dtype=np.complex128)
+        else:
+            if out.dtype != np.complex128 or not out.flags.c_contiguous or out.size != self.nS:
+                raise CodyError("propagate_split2: out must be a contiguous complex128 array of nS entries")
+            s = out
+            if s is not state:
+                s[:] = state
         self._check(self.lib.cgpu_propagate_split2(self.h, _p(s), _d(t0), _d(t1), krylov_dim, _d(tol), max_restarts,
                                                    int(use_metric)))
         return s

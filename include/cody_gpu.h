@@ -118,6 +118,13 @@ int cgpu_ctx_create(const cgpu_desc* desc, cgpu_ctx** out);
 int cgpu_ctx_destroy(cgpu_ctx* ctx);
 const char* cgpu_last_error(const cgpu_ctx* ctx);
 const char* cgpu_last_global_error(void);
+/* Page-locked host memory for the state buffers of the upload / download /
+ * propagate entry points: their host<->device copies then run as direct DMA
+ * at the link rate instead of through the driver's pageable staging.  An
+ * addition of the GPU boundary (the reference keeps its states in ordinary
+ * host arrays).  bytes == 0 gives *out = NULL; cgpu_host_free(NULL) is a no-op. */
+int cgpu_host_alloc(size_t bytes, void** out);
+int cgpu_host_free(void* ptr);
 /* out[0..5] = nG, nO (spin-orbitals), nOS (stored orbitals), nC, nBodyTypes, nState */
 int cgpu_sizes(const cgpu_ctx* ctx, int* out);
 /* Grid_Linear_xCoord / Grid_Linear_weights */

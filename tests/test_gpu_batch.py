@@ -176,3 +176,38 @@ def test_mixed_fx_shared_interaction_matches_per_trajectory():
         assert abs(Ea[k] - Eb[k]) <= 1e-12 * abs(Eb[k]), (k, Ea[k], Eb[k])
     shared.close()
     single.close()
+
+
+def test_pinned_host_buffers():
+    """Page-locked buffers from cgpu_host_alloc: batch upload / download and an
+    in-place propagate_split2 give bit for bit what ordinary arrays give.  Each
+    arm runs on a fresh context: the rho^-1 eigensolver starts from the previous
+    call's eigenvectors, so a second run on the same context may differ in the
+    last bits."""
+    from codyfortran_gb300.engine import Batch, Engine, pinned_empty
+    specs = [_small_helium(), _two_per_spin()]
+    outs = []
+    for pinned in (True, False):
+        b = Batch(specs, "fp64")
+        packed = b.pack(_states(b.systems, 7))
+        src = packed
+        if pinned:
+            src = pinned_empty(packed.size)
+            src[:] = packed
+        b.upload(src)
+        b.propagate(np.zeros(2), 0.02, 2, 10)
+        dst = pinned_empty(packed.size) if pinned else None
+        outs.append(b.download_packed(dst).copy())
+        b.close()
+    assert np.array_equal(outs[0], outs[1])
+    e = Engine(specs[0])
+    st = _states([e], 9)[0]
+    ref = e.propagate_split2(st, 0.0, 0.02, krylov_dim=10, use_metric=True)
+    e.close()
+    e = Engine(specs[0])
+    buf = pinned_empty(e.nS)
+    buf[:] = st
+    e.propagate_split2(buf, 0.0, 0.02, krylov_dim=10, use_metric=True, out=buf)
+    e.close()
+    assert np.array_equal(buf, ref)
+    assert pinned_empty(0).size == 0
