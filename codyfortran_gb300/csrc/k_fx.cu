@@ -397,23 +397,35 @@ void fx_plan(int kTiles, int targetBits, int* digitBits, int* slices) {
   *slices = L;
 }
 
-// Largest N tile of a configuration: L accumulators of BN columns in 512
-// (wide) or 256 (compact) TMEM columns, from the instantiated widths.
+// The instantiated N tiles (fx_gemm's cases): L accumulators of BN columns in
+// 512 (wide) or 256 (compact, two CTAs per SM) tensor-memory columns.
+struct FxTileCfg {
+  int bn, L;
+  bool compact;
+};
+static const FxTileCfg kFxTiles[] = {
+    {32, 4, false}, {64, 4, false}, {80, 4, false}, {96, 4, false}, {128, 4, false}, {32, 5, false},
+    {64, 5, false}, {80, 5, false}, {96, 5, false}, {32, 6, false}, {64, 6, false},  {80, 6, false},
+    {32, 4, true},  {64, 4, true},  {32, 5, true},  {48, 5, true}};
+
 static int fx_max_bn(int L, bool compact) {
-  if (compact) return L == 4 ? 64 : L == 5 ? 32 : 0;
-  return L == 4 ? 128 : L == 5 ? 96 : 80;
+  int m = 0;
+  for (const FxTileCfg& t : kFxTiles)
+    if (t.L == L && t.compact == compact) m = std::max(m, t.bn);
+  return m;
 }
 
 bool fx_compact_ok(int L) { return fx_max_bn(L, true) > 0; }
 
 int fx_tile_n(int N, int L, bool compact) {
-  const int widths[] = {32, 64, 80, 96, 128};
   const int maxBn = fx_max_bn(L, compact);
+  if (maxBn == 0) throw std::string("fx_tile_n: no configuration for this slice count");
   const int tiles = (N + maxBn - 1) / maxBn;
   const int want = ((N + tiles - 1) / tiles + 15) / 16 * 16;  // balanced tiles
-  for (int w : widths)
-    if (w >= want && w <= maxBn) return w;
-  return maxBn;
+  int best = maxBn;
+  for (const FxTileCfg& t : kFxTiles)
+    if (t.L == L && t.compact == compact && t.bn >= want && t.bn < best) best = t.bn;
+  return best;
 }
 
 int fx_split_count(int M, int N, int BN, int kTiles, int nb, int digitBits) {
@@ -467,7 +479,7 @@ void fx_gemm(cgpu_ctx* c, int L, int digitBits, bool compact, int gemmId, const 
   FX_CASE(32, 5, 0, 2, false) FX_CASE(64, 5, 0, 2, false) FX_CASE(80, 5, 0, 2, false) FX_CASE(96, 5, 0, 2, false)
   FX_CASE(32, 6, 0, 2, false) FX_CASE(64, 6, 0, 2, false) FX_CASE(80, 6, 0, 2, false)
   FX_CASE(32, 4, 4, 1, true) FX_CASE(64, 4, 4, 1, true)
-  FX_CASE(32, 5, 5, 1, true)
+  FX_CASE(32, 5, 5, 1, true) FX_CASE(48, 5, 5, 1, true)
 #undef FX_CASE
   throw std::string("fx_gemm: unsupported tile");
 }
