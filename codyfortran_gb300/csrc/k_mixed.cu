@@ -302,7 +302,12 @@ constexpr int FX_LMAX = 8;
 
 // Signed base-2^b digits of x relative to 2^e (|x| < 2^e): X = round(x 2^(bL-e))
 // = sum_i d_i 2^(b(L-1-i)), d_i in [-2^(b-1), 2^(b-1)) for i > 0, |d_0| <= 2^b.
-// Integer operations only (bL <= 52); 32-bit arithmetic when bL <= 30.
+// Integer operations only (bL <= 52; 32-bit arithmetic when bL <= 30).  With
+// H = 2^(b-1) sum_{k<L-1} 2^(bk), the digits of Y = X + H below the top one
+// are the plain base-2^b digits d_i + 2^(b-1), so every digit is an
+// independent bit field of Y: d_i = field_i(Y) - 2^(b-1), d_0 = Y >> b(L-1)
+// (arithmetic shift).  The balanced representation is unique, so this gives
+// the digits of the carry-by-carry division.
 __device__ __forceinline__ void fx_digits(double x, int e, int b, int L, int (&d)[FX_LMAX]) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   const int ex = (int)((u >> 52) & 0x7FF);
@@ -313,30 +318,28 @@ __device__ __forceinline__ void fx_digits(double x, int e, int b, int L, int (&d
     if (sh < 63) X = (long long)((mant + (1ull << (sh - 1))) >> sh);
     if (u >> 63) X = -X;
   }
-  if (b * L <= 30) {  // |X| <= 2^30
-    int Y = (int)X;
-    const int base = 1 << b, half = base >> 1, mask = base - 1;
+  const int mask = (1 << b) - 1, half = 1 << (b - 1);
+  if (b * L <= 30) {  // |X| <= 2^30, H < 2^30
+    int H = 0;
 #pragma unroll
-    for (int i = FX_LMAX - 1; i >= 1; i--) {
-      if (i >= L) continue;
-      int t = Y & mask;
-      if (t >= half) t -= base;
-      d[i] = t;
-      Y = (Y - t) >> b;
-    }
-    d[0] = Y;
+    for (int i = 1; i < FX_LMAX; i++)
+      if (i < L) H = (H << b) | half;
+    const int Y = (int)X + H;
+#pragma unroll
+    for (int i = 1; i < FX_LMAX; i++)
+      if (i < L) d[i] = ((int)((unsigned)Y >> (b * (L - 1 - i))) & mask) - half;
+    d[0] = Y >> (b * (L - 1));
     return;
   }
-  const long long base = 1LL << b, half = base >> 1, mask = base - 1;
+  long long H = 0;
 #pragma unroll
-  for (int i = FX_LMAX - 1; i >= 1; i--) {
-    if (i >= L) continue;
-    long long t = X & mask;
-    if (t >= half) t -= base;
-    d[i] = (int)t;
-    X = (X - t) >> b;
-  }
-  d[0] = (int)X;
+  for (int i = 1; i < FX_LMAX; i++)
+    if (i < L) H = (H << b) | half;
+  const long long Y = X + H;
+#pragma unroll
+  for (int i = 1; i < FX_LMAX; i++)
+    if (i < L) d[i] = ((int)((unsigned long long)Y >> (b * (L - 1 - i))) & mask) - half;
+  d[0] = (int)(Y >> (b * (L - 1)));
 }
 
 // bf16 of an integer |d| <= 256 without a conversion instruction: the FP32
