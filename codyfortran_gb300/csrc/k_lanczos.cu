@@ -13,8 +13,12 @@
 // to the rest in exact arithmetic).  k = 1 is the three-term recurrence
 // proper: w = H v_j - beta_{j-1} v_{j-1}, alpha_j = Re<v_j, w>_m,
 // w -= alpha_j v_j, with beta_{j-1} known from the previous iteration (no dot
-// with v_{j-1}; about 30% fewer FP64 operations per entry than k = 2).  Every reduction is deterministic: per-block
-// partials in a fixed order, re-summed identically by every consumer block.
+// with v_{j-1}; about 30% fewer FP64 operations per entry than k = 2).  Its
+// basis vectors stay unnormalised (v_k = s_k u_k): the operator is linear, so
+// the recurrence applies the scales inside its two passes and the separate
+// v_{j+1} = w / beta_j pass disappears.  Every reduction is deterministic:
+// per-block partials in a fixed order, re-summed identically by every
+// consumer block.
 //
 // Device scalar block lz[] (doubles):
 #include <algorithm>
@@ -34,6 +38,8 @@ constexpr int LZ_DONE = 387;    // breakdown flag (1 = stop growing)
 constexpr int LZ_ZERO = 388;    // zero-norm start (output = input)
 constexpr int LZ_DT = 389;      // dt of the current sub-step
 constexpr int LZ_BREAKJ = 390;  // iteration at which breakdown happened
+constexpr int LZ_S = 400;       // scale of basis slot k: v_(k+1) = s_k u_k  [400, 433)
+constexpr int LZ_SMAX = 33;
 
 constexpr int LZ_THREADS = 256;
 
@@ -167,7 +173,7 @@ __global__ void __launch_bounds__(LZ_THREADS) k_cgs_pass(z_t* __restrict__ w, co
                                                           const double* __restrict__ m, TRAJ_ARGS,
                                                           double* __restrict__ lz, int dotBase, int E,
                                                           const z_t* __restrict__ gate0, int gateStride,
-                                                          const z_t* __restrict__ gate1) {
+                                                          const z_t* __restrict__ gate1, int scaleIdx) {
   const TrajShape& S = shp[blockIdx.z];
   lz = bat(lz, bs);
   if (lz[LZ_DONE] != 0.0) return;
@@ -181,6 +187,11 @@ __global__ void __launch_bounds__(LZ_THREADS) k_cgs_pass(z_t* __restrict__ w, co
   const size_t n = S.nS;
   const int CH = LZ_THREADS * E;
   sum_partials(partIn, nBlkIn, inStride, nVec, coef);
+  if (scaleIdx >= 0) {  // unnormalised basis vectors u_k: the projection on u_k is <u_k, w> s_k^2 u_k
+    __syncthreads();
+    for (int k = threadIdx.x; k < nVec; k += blockDim.x) coef[k] = zscale(coef[k], lz[scaleIdx + k] * lz[scaleIdx + k]);
+    __syncthreads();
+  }
   if (dotBase >= 0 && blockIdx.x == 0)
     for (int k = threadIdx.x; k < nVec; k += blockDim.x) {
       lz[LZ_D + 2 * (dotBase + k)] = coef[k].x;
@@ -364,7 +375,7 @@ __global__ void k_lz_expsub(double* __restrict__ lz, int mFixed, double dt, doub
 }
 
 
-// out = nrm * sum_{j < mDim} phi_j V_j   (or out = in when the start vector had zero norm)
+// out = nrm * sum_{j < mDim} phi_j s_j V_j   (or out = in when the start vector had zero norm)
 __global__ void k_lz_combine(z_t* __restrict__ out, const z_t* __restrict__ in, const z_t* __restrict__ V,
                              size_t ldv, TRAJ_ARGS, const double* __restrict__ lz) {
   const TrajShape& S = shp[blockIdx.z];
@@ -377,7 +388,8 @@ __global__ void k_lz_combine(z_t* __restrict__ out, const z_t* __restrict__ in, 
   int m = (int)lz[LZ_MDIM];
   double nrm = lz[LZ_NRM];
   bool zero = lz[LZ_ZERO] != 0.0;
-  for (int k = threadIdx.x; k < m; k += blockDim.x) phi[k] = zmk(lz[LZ_PHI + 2 * k], lz[LZ_PHI + 2 * k + 1]);
+  for (int k = threadIdx.x; k < m; k += blockDim.x)
+    phi[k] = zscale(zmk(lz[LZ_PHI + 2 * k], lz[LZ_PHI + 2 * k + 1]), lz[LZ_S + k]);
   __syncthreads();
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
     size_t i = vidx(S, l);
@@ -412,6 +424,8 @@ __global__ void k_lz_start(z_t* __restrict__ v1, const z_t* __restrict__ s, cons
     lz[LZ_MDIM] = 0.0;
     lz[LZ_ERR] = 0.0;
   }
+  if (blockIdx.x == 0)
+    for (int k = threadIdx.x; k < LZ_SMAX; k += blockDim.x) lz[LZ_S + k] = 1.0;
   if (zero) return;
   const double inv = 1.0 / nr;
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
@@ -437,8 +451,13 @@ __global__ void k_norm_partial(z_t* __restrict__ part, const z_t* __restrict__ v
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-// Three-term recurrence, pass 1: part[blk*2] = sum m Re(conj(v_j) w'),
-// part[blk*2+1] = sum m |w'|^2, w' = w - beta_{j-1} v_{j-1} (formed on the fly).
+// Three-term recurrence on unnormalised basis vectors u_k (v_k = s_k u_k,
+// s_k at lz[LZ_S + k - 1]): the operator is linear, so h = H u_j = H v_j / s_j
+// and every pass forms the reference's w from h on the fly; u_(j+1) = w and
+// s_(j+1) = 1 / beta_j replace the separate normalisation pass.
+//
+// Pass 1: part[blk*2] = sum m Re(conj(v_j) w'), part[blk*2+1] = sum m |w'|^2,
+// w' = s_j h - beta_{j-1} v_{j-1}.
 __global__ void __launch_bounds__(LZ_THREADS) k_lz3_dot(z_t* __restrict__ part, const z_t* __restrict__ vPrev,
                                                          const z_t* __restrict__ vCur, const z_t* __restrict__ w,
                                                          const double* __restrict__ m, TRAJ_ARGS,
@@ -449,34 +468,37 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz3_dot(z_t* __restrict__ part, 
   vCur = bat(vCur, bs);
   w = bat(w, bs);
   m = bat(m, bs);
-  const double beta = (j > 1) ? lz[LZ_BETA + j - 2] : 0.0;
+  const double sj = lz[LZ_S + j - 1];
+  const double bp = (j > 1) ? lz[LZ_BETA + j - 2] * lz[LZ_S + j - 2] : 0.0;  // beta_{j-1} s_{j-1}
   vPrev = (j > 1) ? bat(vPrev, bs) : nullptr;
   const size_t n = S.nS;
   double a = 0.0, q = 0.0;
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
     const size_t i = vidx(S, l);
-    z_t x = w[i];
+    const z_t h = w[i];
+    z_t x = zmk(sj * h.x, sj * h.y);
     if (vPrev) {
       const z_t p = vPrev[i];
-      x.x = fma(-beta, p.x, x.x);
-      x.y = fma(-beta, p.y, x.y);
+      x.x = fma(-bp, p.x, x.x);
+      x.y = fma(-bp, p.y, x.y);
     }
     const z_t v = vCur[i];
     const double mi = m[i];
     a = fma(mi, fma(v.x, x.x, v.y * x.y), a);
     q = fma(mi, fma(x.x, x.x, x.y * x.y), q);
   }
-  const z_t t = block_sum2(zmk(a, q));
+  const z_t t = block_sum2(zmk(a * sj, q));
   if (threadIdx.x == 0) {
     part[(size_t)blockIdx.x * 2] = zmk(t.x, 0.0);
     part[(size_t)blockIdx.x * 2 + 1] = zmk(t.y, 0.0);
   }
 }
 
-// Three-term recurrence, pass 2: alpha_j from the pass-1 partials (stored at
-// lz[LZ_D + 2 (j-1)] for k_lz_finish), w <- w - beta_{j-1} v_{j-1} - alpha_j v_j,
-// partials of the new ||w||_m^2.
-__global__ void __launch_bounds__(LZ_THREADS) k_lz3_update(z_t* __restrict__ w, const z_t* __restrict__ vPrev,
+// Pass 2: alpha_j from the pass-1 partials (stored at lz[LZ_D + 2 (j-1)]),
+// u_(j+1) = s_j h - beta_{j-1} v_{j-1} - alpha_j v_j into dst (the next basis
+// slot, or h itself after the last iteration), partials of ||u_(j+1)||_m^2.
+__global__ void __launch_bounds__(LZ_THREADS) k_lz3_update(z_t* __restrict__ dst, const z_t* __restrict__ w,
+                                                            const z_t* __restrict__ vPrev,
                                                             const z_t* __restrict__ vCur, const z_t* __restrict__ partIn,
                                                             int nBlkIn, z_t* __restrict__ partOut,
                                                             const double* __restrict__ m, TRAJ_ARGS,
@@ -484,12 +506,14 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz3_update(z_t* __restrict__ w, 
   const TrajShape& S = shp[blockIdx.z];
   lz = bat(lz, bs);
   if (lz[LZ_DONE] != 0.0) return;
+  dst = bat(dst, bs);
   w = bat(w, bs);
   vCur = bat(vCur, bs);
   partIn = bat(partIn, bs);
   partOut = bat(partOut, bs);
   m = bat(m, bs);
-  const double beta = (j > 1) ? lz[LZ_BETA + j - 2] : 0.0;
+  const double sj = lz[LZ_S + j - 1];
+  const double bp = (j > 1) ? lz[LZ_BETA + j - 2] * lz[LZ_S + j - 2] : 0.0;
   vPrev = (j > 1) ? bat(vPrev, bs) : nullptr;
   __shared__ z_t al[1];
   sum_partials(partIn, nBlkIn, 2, 1, al);
@@ -498,24 +522,58 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz3_update(z_t* __restrict__ w, 
     lz[LZ_D + 2 * (j - 1)] = alpha;
     lz[LZ_D + 2 * (j - 1) + 1] = 0.0;
   }
+  const double as = alpha * sj;
   const size_t n = S.nS;
   double q = 0.0;
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
     const size_t i = vidx(S, l);
-    z_t x = w[i];
+    const z_t h = w[i];
+    z_t x = zmk(sj * h.x, sj * h.y);
     if (vPrev) {
       const z_t p = vPrev[i];
-      x.x = fma(-beta, p.x, x.x);
-      x.y = fma(-beta, p.y, x.y);
+      x.x = fma(-bp, p.x, x.x);
+      x.y = fma(-bp, p.y, x.y);
     }
     const z_t v = vCur[i];
-    x.x = fma(-alpha, v.x, x.x);
-    x.y = fma(-alpha, v.y, x.y);
-    w[i] = x;
+    x.x = fma(-as, v.x, x.x);
+    x.y = fma(-as, v.y, x.y);
+    dst[i] = x;
     q = fma(m[i], fma(x.x, x.x, x.y * x.y), q);
   }
   const z_t t = block_sum2(zmk(q, 0.0));
   if (threadIdx.x == 0) partOut[blockIdx.x] = t;
+}
+
+// End of a three-term iteration, one block per trajectory: beta_j from the norm
+// partials of the first pass (or of the second, when the reorthogonalisation
+// test fired), alpha_j and beta_j into the tridiagonal, s_(j+1) = 1 / beta_j;
+// a breakdown or the last iteration fixes the subspace dimension, a breakdown
+// also stops the growth.
+__global__ void __launch_bounds__(LZ_THREADS) k_lz_scalars(const z_t* __restrict__ partIn,
+                                                            const z_t* __restrict__ partAlt,
+                                                            const z_t* __restrict__ gate0, int gateStride, int nBlkIn,
+                                                            TRAJ_ARGS, double* __restrict__ lz, int j, int maxDim,
+                                                            double zeroThr) {
+  lz = bat(lz, bs);
+  if (lz[LZ_DONE] != 0.0) return;
+  partIn = bat(partIn, bs);
+  if (reorth_needed(bat(gate0, bs), gateStride, partIn, nBlkIn)) partIn = bat(partAlt, bs);
+  __shared__ z_t tot[1];
+  sum_partials(partIn, nBlkIn, 1, 1, tot);
+  if (threadIdx.x != 0) return;
+  const double be = sqrt(tot[0].x);
+  lz[LZ_ALPHA + j - 1] = lz[LZ_D + 2 * (j - 1)];
+  lz[LZ_BETA + j - 1] = be;
+  const bool breakdown = be <= zeroThr;
+  if (breakdown || j == maxDim) {
+    lz[LZ_MDIM] = j;
+    if (breakdown) {
+      lz[LZ_BREAKJ] = j;
+      lz[LZ_DONE] = 1.0;
+    }
+    return;
+  }
+  lz[LZ_S + j] = 1.0 / be;
 }
 
 }  // namespace
@@ -547,27 +605,26 @@ void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
   z_t* p4 = p3 + (size_t)nBlk * (c->maxKrylov + 1);
   if (j > 32) throw std::string("SIL: Krylov order above 32");
   if (c->krylovWindow == 1) {
-    // three-term recurrence; the gated second pass re-orthogonalises against v_j
+    // three-term recurrence on unnormalised basis vectors; the gated second
+    // pass re-orthogonalises the new vector against u_j
     const z_t* vCur = c->basis_d + ld * (size_t)(j - 1);
     const z_t* vPrev = (j > 1) ? c->basis_d + ld * (size_t)(j - 2) : nullptr;
+    z_t* uNext = (j < maxDim) ? c->basis_d + ld * (size_t)j : c->lw_d;
     dim3 g = bgrid(c, nBlk);
     const int E = c->lzElems;
     k_lz3_dot<<<g, LZ_THREADS, 0, c->stream>>>(p1, vPrev, vCur, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, j);
     CODY_LAUNCHED(c);
-    k_lz3_update<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, vPrev, vCur, p1, nBlk, p2, c->metric_d, TRAJ_PASS(c),
-                                                  c->lz_d, j);
+    k_lz3_update<<<g, LZ_THREADS, 0, c->stream>>>(uNext, c->lw_d, vPrev, vCur, p1, nBlk, p2, c->metric_d,
+                                                  TRAJ_PASS(c), c->lz_d, j);
     CODY_LAUNCHED(c);
-    k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p3, 1, vCur, ld, 1, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 0,
+    k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p3, 1, vCur, ld, 1, uNext, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 0,
                                             p1 + 1, 2, p2, nBlk);
     CODY_LAUNCHED(c);
-    k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, vCur, ld, 1, p3, 1, nBlk, p4, c->metric_d, TRAJ_PASS(c),
-                                                c->lz_d, -1, E, p1 + 1, 2, p2);
+    k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(uNext, vCur, ld, 1, p3, 1, nBlk, p4, c->metric_d, TRAJ_PASS(c),
+                                                c->lz_d, -1, E, p1 + 1, 2, p2, LZ_S + j - 1);
     CODY_LAUNCHED(c);
-    z_t* vNext = (j < maxDim) ? c->basis_d + ld * (size_t)j : nullptr;
-    k_lz_finish<<<g, LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p2, p4, p1 + 1, 2, nBlk, TRAJ_PASS(c), c->lz_d, j,
-                                                 maxDim, 1.0e-14);
-    CODY_LAUNCHED(c);
-    k_lz_mark_done<<<bgrid(c, 1), 1, 0, c->stream>>>(c->lz_d, j, c->bs);
+    k_lz_scalars<<<bgrid(c, 1), LZ_THREADS, 0, c->stream>>>(p2, p4, p1 + 1, 2, nBlk, TRAJ_PASS(c), c->lz_d, j, maxDim,
+                                                            1.0e-14);
     CODY_LAUNCHED(c);
     return;
   }
@@ -580,13 +637,13 @@ void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
                                           nullptr, 0, nullptr, nBlk);
   CODY_LAUNCHED(c);
   k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, V, ld, nv, p1, s1, nBlk, p2, c->metric_d, TRAJ_PASS(c),
-                                              c->lz_d, base, E, nullptr, 0, nullptr);
+                                              c->lz_d, base, E, nullptr, 0, nullptr, -1);
   CODY_LAUNCHED(c);
   k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p3, nv, V, ld, nv, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 0,
                                           p1 + nv, s1, p2, nBlk);
   CODY_LAUNCHED(c);
   k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, V, ld, nv, p3, nv, nBlk, p4, c->metric_d, TRAJ_PASS(c),
-                                              c->lz_d, -1, E, p1 + nv, s1, p2);
+                                              c->lz_d, -1, E, p1 + nv, s1, p2, -1);
   CODY_LAUNCHED(c);
   z_t* vNext = (j < maxDim) ? c->basis_d + ld * (size_t)j : nullptr;
   k_lz_finish<<<g, LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p2, p4, p1 + nv, s1, nBlk, TRAJ_PASS(c), c->lz_d, j,
