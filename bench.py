@@ -51,6 +51,7 @@ METRIC = "MCTDHF traj-steps/s: mixed-prec batched vs FP64 GPU at ≤1e-8 energy/
 UNIT = "traj-steps/s"
 L2_BYTES = 129 * 1024 * 1024
 ACC_STEPS = 10
+ACC_STEPS_SINGLE = 20
 DTYPES = {
     "fp64": "complex128",
     "mixed": "mixed (bf16x3 tcgen05 contractions with fp32 accumulation, fp64 rest)",
@@ -462,6 +463,42 @@ def run_batch(args):
     return 0
 
 
+def orbital_span_defect(a, b, nC, nG, n, w):
+    """1 - |det <phi_a|phi_b>_w| over the stored orbitals of two states (0 when
+    both orbital sets span the same space; invariant under rotations within it)."""
+    fa = a[nC:nC + nG * n].reshape(n, nG)
+    fb = b[nC:nC + nG * n].reshape(n, nG)
+    return float(abs(1.0 - abs(np.linalg.det((fa.conj() * w) @ fb.T))))
+
+
+def mixed_deviation(sp, cfg, precision, window, st, n_steps):
+    """Per-step deviation of a mixed-precision trajectory from the FP64 form with
+    the reference's Krylov loop, from the same state: |dE|/|E|, |d||C|||,
+    |d<x>| and the orbital-span defect, each maximised over the steps."""
+    from codyfortran_gb300.engine import Engine
+    K, dt = cfg["krylov"], cfg["dt"]
+    f = Engine(sp, precision="fp64", max_krylov=K, krylov_window=0)
+    m = Engine(sp, precision=precision, max_krylov=K, krylov_window=window)
+    f.upload(st)
+    m.upload(st)
+    t, rows = 0.0, []
+    for _ in range(n_steps):
+        f.propagate_resident(t, dt, 1, K, use_metric=True, use_graph=True)
+        m.propagate_resident(t, dt, 1, K, use_metric=True, use_graph=True)
+        t += dt
+        of, om = f.observables(t), m.observables(t)
+        rows.append((abs(om["energy"] - of["energy"]) / abs(of["energy"]), abs(om["norm"] - of["norm"]),
+                     abs(om["dipole"] - of["dipole"]),
+                     orbital_span_defect(m.download(), f.download(), f.nC, f.nG, f.nOS, f.w)))
+    f.close()
+    m.close()
+    r = np.array(rows)
+    return {"steps": n_steps, "energy_rel_max": float(r[:, 0].max()), "norm_abs_max": float(r[:, 1].max()),
+            "dipole_abs_max": float(r[:, 2].max()), "orbital_span_defect_max": float(r[:, 3].max()),
+            "energy_rel_last": float(r[-1, 0]), "target": 1e-8,
+            "reference": "same state, plain FP64 form with the reference's Krylov loop on the GPU"}
+
+
 def run_single(args):
     rank, world, local = dist_info()
     from codyfortran_gb300.engine import Engine, pinned_empty
@@ -541,6 +578,8 @@ def run_single(args):
                      "launches": n_dom, "avg_launch_us": avg_s * 1e6, "work_per_launch": work},
         "kernel_ms_per_step": {k: v[1] for k, v in fam_ms.items()},
     }
+    if rank == 0 and precision != "fp64" and not args.no_fp64_leg:
+        line["accuracy_vs_fp64"] = mixed_deviation(sp, cfg, precision, window, st, ACC_STEPS_SINGLE)
     if rank == 0 and not args.no_cpu_baseline:
         steps_cpu, el, used = oracle_traj_steps(specs, cfg, os.cpu_count(), args.cpu_budget)
         line["cpu_baseline"] = {"value": steps_cpu / el, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",

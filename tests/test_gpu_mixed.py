@@ -76,9 +76,17 @@ def test_mixed_nonlin_full_size(precision):
     e.close()
 
 
+def _span_defect(a, b, nC, nG, n, w):
+    """1 - |det <phi_a|phi_b>_w| of the stored orbitals of two states."""
+    fa = a[nC:nC + nG * n].reshape(n, nG)
+    fb = b[nC:nC + nG * n].reshape(n, nG)
+    return abs(1.0 - abs(np.linalg.det((fa.conj() * w) @ fb.T)))
+
+
 @pytest.mark.parametrize("precision", PRECISIONS)
 def test_mixed_trajectory_energy_norm(precision):
-    """Energy and norm of a mixed-precision trajectory against the FP64 GPU trajectory."""
+    """Energy, norm, dipole and orbital span of a mixed-precision trajectory
+    against the FP64 GPU trajectory."""
     from codyfortran_gb300.engine import Engine
     sp = S.cfg_helium_small()
     f = Engine(sp, precision="fp64")
@@ -96,9 +104,40 @@ def test_mixed_trajectory_energy_norm(precision):
     w = f.metric_weights()
     nf, nm = np.sqrt(np.sum(np.abs(sf) ** 2 * w)), np.sqrt(np.sum(np.abs(sm) ** 2 * w))
     de, dn = abs(em - ef) / abs(ef), abs(nm - nf)
-    print(f"{precision}: {n_steps} steps, |dE|/|E| = {de:.3e}, |d norm| = {dn:.3e}")
-    # measured on GB300: bf16x3 |dE|/|E| ~ 2e-6, |d norm| ~ 1e-7 over these 200 steps
-    lim = {"mixed": (1e-5, 1e-6), "mixed6": (2e-6, 2e-7), "mixed_fx": (1e-8, 1e-9), "mixed_fx6": (1e-9, 1e-10)}[precision]
-    assert de < lim[0] and dn < lim[1]
+    dx = abs(m.observables(t)["dipole"] - f.observables(t)["dipole"])
+    print(f"{precision}: {n_steps} steps, |dE|/|E| = {de:.3e}, |d norm| = {dn:.3e}, |d<x>| = {dx:.3e}")
+    # measured on GB300 over these 200 steps: |dE|/|E| 1.2e-6 / 1.2e-7 / 2.5e-10 / 2.3e-12,
+    # |d<x>| 1.3e-4 / 4.4e-6 / 7.2e-9 / 1.7e-10 (bf16x3, bf16x6, fx, fx6)
+    lim = {"mixed": (1e-5, 1e-6, 1e-3), "mixed6": (2e-6, 2e-7, 5e-5), "mixed_fx": (1e-8, 1e-9, 1e-7),
+           "mixed_fx6": (1e-9, 1e-10, 2e-9)}[precision]
+    assert de < lim[0] and dn < lim[1] and dx < lim[2]
+    f.close()
+    m.close()
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_mixed_trajectory_orbital_span(precision):
+    """1 - |det <phi_mixed|phi_FP64>_w| from a random CI vector (every orbital
+    occupied).  From a single determinant the empty orbitals are fixed only
+    through the regularised rho^-1, and their span differs between any two
+    runs (2.7e-3 for every form here, FP64-level forms included), so the
+    span is compared where all orbitals carry weight."""
+    from codyfortran_gb300.engine import Engine
+    sp = S.cfg_helium_small()
+    f = Engine(sp, precision="fp64")
+    m = Engine(sp, precision=precision)
+    rng = np.random.default_rng(5)
+    c = rng.normal(size=f.nC) + 1j * rng.normal(size=f.nC)
+    st = I.pack_state(c / np.linalg.norm(c), I.seeded_gaussian_orbitals(sp, f.x, f.w, 42))
+    f.upload(st)
+    m.upload(st)
+    n_steps, dt = 50, 0.01
+    f.propagate_resident(0.0, dt, n_steps, 12, use_metric=True)
+    m.propagate_resident(0.0, dt, n_steps, 12, use_metric=True)
+    t = n_steps * dt
+    ds = _span_defect(m.download(), f.download(), f.nC, f.nG, f.nOS, f.w)
+    de = abs(m.energy_resident(t) - f.energy_resident(t)) / abs(f.energy_resident(t))
+    print(f"{precision}: {n_steps} steps from a random CI vector, span defect = {ds:.3e}, |dE|/|E| = {de:.3e}")
+    assert ds < 1e-9
     f.close()
     m.close()
