@@ -6,7 +6,10 @@
 // the device data of all systems in one arena: trajectory b's buffers sit at
 // byte offset b * bs from trajectory 0's, every buffer sized for the largest
 // system.  The orchestration below is written once for all trajectories.
+#include <sys/stat.h>
+
 #include <algorithm>
+#include <cerrno>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -891,6 +894,107 @@ void down_state(cgpu_ctx* c, int b, cgpu_complex* dst, const z_t* src0) {
     CODY_CUDA(cudaMemcpyAsync(dst + s.nC, base + sizeof(z_t) * c->nC, sizeof(z_t) * (s.nS - s.nC),
                               cudaMemcpyDeviceToHost, c->stream));
 }
+// ---- restart files (M_Utils_DataStorage raw format) of one trajectory --------
+// coeffs.in (nC complex), orbBB_KK.in per stored orbital (nG complex each), and
+// with rdm2 the blocks rdm2BtXX_YY.in (n1 x n2 x n1 x n2, Fortran order).
+std::string dir_prefix(const char* dir) {
+  std::string pre = dir ? std::string(dir) : std::string();
+  if (!pre.empty() && pre.back() != '/') pre += '/';
+  return pre;
+}
+
+void write_file(const std::string& path, const void* p, size_t bytes) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) throw std::string("save_restart: cannot open ") + path;
+  const size_t w = std::fwrite(p, 1, bytes, f);
+  std::fclose(f);
+  if (w != bytes) throw std::string("save_restart: short write to ") + path;
+}
+
+void read_file(const std::string& path, void* p, size_t bytes) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) throw std::string("load_restart: cannot open ") + path;
+  const size_t r = std::fread(p, 1, bytes, f);
+  std::fclose(f);
+  if (r != bytes) throw std::string("load_restart: more data requested than stored in ") + path;
+}
+
+void down_state(cgpu_ctx* c, int b, cgpu_complex* dst, const z_t* src0);
+void up_state(cgpu_ctx* c, int b, z_t* dst0, const cgpu_complex* src);
+void sync(cgpu_ctx* c);
+
+// Trajectory b's resident state (and, when withRdm2, its rdm2 as left by
+// launch_ci_rdm) into the files under pre.
+void save_traj(cgpu_ctx* c, int b, const std::string& pre, bool withRdm2) {
+  const SysHost& s = c->sys[b];
+  std::vector<cgpu_complex> st(s.nS);
+  down_state(c, b, st.data(), c->state_d);
+  std::vector<cgpu_complex> r2;
+  const size_t nO = s.nO;
+  if (withRdm2) {
+    r2.resize(nO * nO * nO * nO);
+    CODY_CUDA(cudaMemcpyAsync(r2.data(), (const char*)c->rdm2_d + (size_t)b * c->bs, sizeof(z_t) * r2.size(),
+                              cudaMemcpyDeviceToHost, c->stream));
+  }
+  sync(c);
+  write_file(pre + "coeffs.in", st.data(), sizeof(cgpu_complex) * s.nC);
+  if (c->method != CGPU_METHOD_TDCI) {
+    const int nBt = c->restricted ? 1 : c->nBt;
+    int i1 = 0;
+    for (int bt = 0; bt < nBt; bt++)
+      for (int k = 0; k < s.nOrbs[bt]; k++, i1++) {
+        char name[32];
+        std::snprintf(name, sizeof(name), "orb%02d_%02d.in", bt + 1, k + 1);
+        write_file(pre + name, st.data() + s.nC + (size_t)i1 * s.nG, sizeof(cgpu_complex) * s.nG);
+      }
+  }
+  if (!withRdm2) return;
+  for (int b1 = 0; b1 < c->nBt; b1++)
+    for (int b2 = 0; b2 < c->nBt; b2++) {
+      const int s1 = s.orbStart[b1], n1 = s.nOrbs[b1], s2 = s.orbStart[b2], n2 = s.nOrbs[b2];
+      std::vector<cgpu_complex> blk((size_t)n1 * n2 * n1 * n2);
+      size_t q = 0;
+      for (int l = 0; l < n2; l++)
+        for (int k = 0; k < n1; k++)
+          for (int j = 0; j < n2; j++)
+            for (int i = 0; i < n1; i++, q++)
+              blk[q] = r2[(s1 + i) + nO * ((s2 + j) + nO * ((s1 + k) + nO * (size_t)(s2 + l)))];
+      char name[32];
+      std::snprintf(name, sizeof(name), "rdm2Bt%02d_%02d.in", b1 + 1, b2 + 1);
+      write_file(pre + name, blk.data(), sizeof(cgpu_complex) * blk.size());
+    }
+}
+
+// The files under pre into trajectory b's resident state.
+void load_traj(cgpu_ctx* c, int b, const std::string& pre) {
+  const SysHost& s = c->sys[b];
+  std::vector<cgpu_complex> st(s.nS);
+  read_file(pre + "coeffs.in", st.data(), sizeof(cgpu_complex) * s.nC);
+  if (c->method != CGPU_METHOD_TDCI) {
+    const int nBt = c->restricted ? 1 : c->nBt;
+    int i1 = 0;
+    for (int bt = 0; bt < nBt; bt++)
+      for (int k = 0; k < s.nOrbs[bt]; k++, i1++) {
+        char name[32];
+        std::snprintf(name, sizeof(name), "orb%02d_%02d.in", bt + 1, k + 1);
+        read_file(pre + name, st.data() + s.nC + (size_t)i1 * s.nG, sizeof(cgpu_complex) * s.nG);
+      }
+  }
+  up_state(c, b, c->state_d, st.data());
+  sync(c);  // st is freed on return
+}
+
+// Subdirectory of trajectory b of a batch: <dir>/trajNNNNN/ (created on save).
+std::string traj_prefix(const char* dir, int b, bool create) {
+  std::string base = dir_prefix(dir);
+  char name[32];
+  std::snprintf(name, sizeof(name), "traj%05d", b);
+  std::string path = base + name;
+  if (create && mkdir(path.c_str(), 0755) != 0 && errno != EEXIST)
+    throw std::string("batch_save_restart: cannot create ") + path;
+  return path + "/";
+}
+
 void sync(cgpu_ctx* c) {
   CODY_CUDA(cudaStreamSynchronize(c->stream));
   if (c->mixed && mixed_error(c)) throw std::string("tensor-core GEMM: a bounded mbarrier wait expired");
@@ -1451,50 +1555,8 @@ int cgpu_relax(cgpu_ctx* c, cgpu_complex* state, double dt, int n_inner, double 
 int cgpu_save_restart(cgpu_ctx* c, const char* dir, int with_rdm2) {
   CODY_API_BEGIN(c)
   if (c->nb != 1) throw std::string("save_restart: a single system");
-  const SysHost& s = c->sys[0];
-  std::string pre = dir ? std::string(dir) : std::string();
-  if (!pre.empty() && pre.back() != '/') pre += '/';
-  std::vector<cgpu_complex> st(s.nS);
-  down_state(c, 0, st.data(), c->state_d);
-  sync(c);
-  auto write = [&](const std::string& name, const void* p, size_t bytes) {
-    FILE* f = std::fopen((pre + name).c_str(), "wb");
-    if (!f) throw std::string("save_restart: cannot open ") + pre + name;
-    size_t w = std::fwrite(p, 1, bytes, f);
-    std::fclose(f);
-    if (w != bytes) throw std::string("save_restart: short write to ") + pre + name;
-  };
-  write("coeffs.in", st.data(), sizeof(cgpu_complex) * s.nC);
-  if (c->method != CGPU_METHOD_TDCI) {
-    int nBt = c->restricted ? 1 : c->nBt, i1 = 0;
-    for (int bt = 0; bt < nBt; bt++)
-      for (int k = 0; k < s.nOrbs[bt]; k++, i1++) {
-        char name[32];
-        std::snprintf(name, sizeof(name), "orb%02d_%02d.in", bt + 1, k + 1);
-        write(name, st.data() + s.nC + (size_t)i1 * s.nG, sizeof(cgpu_complex) * s.nG);
-      }
-  }
-  if (with_rdm2) {
-    launch_ci_rdm(c, c->state_d, 0, 1);
-    const size_t nO = s.nO;
-    std::vector<cgpu_complex> r2(nO * nO * nO * nO);
-    down(c, r2.data(), c->rdm2_d, r2.size());
-    sync(c);
-    for (int b1 = 0; b1 < c->nBt; b1++)
-      for (int b2 = 0; b2 < c->nBt; b2++) {
-        const int s1 = s.orbStart[b1], n1 = s.nOrbs[b1], s2 = s.orbStart[b2], n2 = s.nOrbs[b2];
-        std::vector<cgpu_complex> blk((size_t)n1 * n2 * n1 * n2);
-        size_t q = 0;
-        for (int l = 0; l < n2; l++)
-          for (int k = 0; k < n1; k++)
-            for (int j = 0; j < n2; j++)
-              for (int i = 0; i < n1; i++, q++)
-                blk[q] = r2[(s1 + i) + nO * ((s2 + j) + nO * ((s1 + k) + nO * (size_t)(s2 + l)))];
-        char name[32];
-        std::snprintf(name, sizeof(name), "rdm2Bt%02d_%02d.in", b1 + 1, b2 + 1);
-        write(name, blk.data(), sizeof(cgpu_complex) * blk.size());
-      }
-  }
+  if (with_rdm2) launch_ci_rdm(c, c->state_d, 0, 1);
+  save_traj(c, 0, dir_prefix(dir), with_rdm2 != 0);
   CODY_API_END(c)
 }
 
@@ -1503,28 +1565,7 @@ int cgpu_save_restart(cgpu_ctx* c, const char* dir, int with_rdm2) {
 int cgpu_load_restart(cgpu_ctx* c, const char* dir) {
   CODY_API_BEGIN(c)
   if (c->nb != 1) throw std::string("load_restart: a single system");
-  const SysHost& s = c->sys[0];
-  std::string pre = dir ? std::string(dir) : std::string();
-  if (!pre.empty() && pre.back() != '/') pre += '/';
-  std::vector<cgpu_complex> st(s.nS);
-  auto read = [&](const std::string& name, void* p, size_t bytes) {
-    FILE* f = std::fopen((pre + name).c_str(), "rb");
-    if (!f) throw std::string("load_restart: cannot open ") + pre + name;
-    size_t r = std::fread(p, 1, bytes, f);
-    std::fclose(f);
-    if (r != bytes) throw std::string("load_restart: more data requested than stored in ") + pre + name;
-  };
-  read("coeffs.in", st.data(), sizeof(cgpu_complex) * s.nC);
-  if (c->method != CGPU_METHOD_TDCI) {
-    int nBt = c->restricted ? 1 : c->nBt, i1 = 0;
-    for (int bt = 0; bt < nBt; bt++)
-      for (int k = 0; k < s.nOrbs[bt]; k++, i1++) {
-        char name[32];
-        std::snprintf(name, sizeof(name), "orb%02d_%02d.in", bt + 1, k + 1);
-        read(name, st.data() + s.nC + (size_t)i1 * s.nG, sizeof(cgpu_complex) * s.nG);
-      }
-  }
-  up_state(c, 0, c->state_d, st.data());
+  load_traj(c, 0, dir_prefix(dir));
   sync(c);
   CODY_API_END(c)
 }
@@ -1646,6 +1687,23 @@ int cgpu_batch_download(cgpu_batch* b, cgpu_complex* states) {
   CODY_LAUNCHED(c);
   CODY_CUDA(cudaMemcpyAsync(states, c->stage_d, sizeof(z_t) * c->stageOff.back(), cudaMemcpyDeviceToHost, c->stream));
   sync(c);
+  CODY_BATCH_END
+}
+
+int cgpu_batch_save_restart(cgpu_batch* b, const char* dir, int with_rdm2) {
+  CODY_BATCH_BEGIN(b)
+  cgpu_ctx* c = c_;
+  if (!dir) throw std::string("batch_save_restart: null directory");
+  if (with_rdm2) launch_ci_rdm(c, c->state_d, 0, 1);
+  for (int i = 0; i < c->nb; i++) save_traj(c, i, traj_prefix(dir, i, true), with_rdm2 != 0);
+  CODY_BATCH_END
+}
+
+int cgpu_batch_load_restart(cgpu_batch* b, const char* dir) {
+  CODY_BATCH_BEGIN(b)
+  cgpu_ctx* c = c_;
+  if (!dir) throw std::string("batch_load_restart: null directory");
+  for (int i = 0; i < c->nb; i++) load_traj(c, i, traj_prefix(dir, i, false));
   CODY_BATCH_END
 }
 

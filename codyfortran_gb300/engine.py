@@ -38,6 +38,7 @@ EXPORTED = [
     "cgpu_batch_kernels_per_step", "cgpu_batch_launch_count", "cgpu_batch_shared_interactions", "cgpu_batch_profile_begin", "cgpu_batch_profile_end",
     "cgpu_tdci_adjoint", "cgpu_observables", "cgpu_relax", "cgpu_batch_observables", "cgpu_save_restart",
     "cgpu_load_restart", "cgpu_absorber_setup", "cgpu_absorber_apply", "cgpu_batch_absorber_setup",
+    "cgpu_batch_save_restart", "cgpu_batch_load_restart",
 ]
 
 KERNELS = {"pair_potentials": 1, "correlation": 2, "h2": 3, "ci_apply": 4, "ci_rdm": 5, "onebody": 6, "lanczos": 7,
@@ -96,6 +97,8 @@ def load_library(path: str = LIB_PATH):
     lib.cgpu_host_free.argtypes = [C.c_void_p]
     lib.cgpu_save_restart.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
     lib.cgpu_load_restart.argtypes = [C.c_void_p, C.c_char_p]
+    lib.cgpu_batch_save_restart.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
+    lib.cgpu_batch_load_restart.argtypes = [C.c_void_p, C.c_char_p]
     _lib = lib
     return lib
 
@@ -531,6 +534,13 @@ class Batch:
         self._check(self.lib.cgpu_batch_propagate(self.h, _p(t), _d(dt), int(n_steps), int(krylov_dim),
                                                   int(use_metric), C.byref(ms)))
         return ms.value
+
+    def save_restart(self, directory, with_rdm2=False):
+        """Every trajectory's restart files under directory/trajNNNNN/."""
+        self._check(self.lib.cgpu_batch_save_restart(self.h, str(directory).encode(), int(with_rdm2)))
+
+    def load_restart(self, directory):
+        self._check(self.lib.cgpu_batch_load_restart(self.h, str(directory).encode()))
 
     def observables(self, t):
         """(energy, norm, dipole, occupations[nOSmax]) arrays over the systems at times t."""

@@ -293,6 +293,12 @@ int cgpu_batch_grid(const cgpu_batch* batch, int i, double* x, double* w);
 /* All states, concatenated in system order (nS_i entries each, layout
  * [C | orbitals] as cgpu_state_upload). */
 int cgpu_batch_upload(cgpu_batch* batch, const cgpu_complex* states);
+/* cgpu_save_restart / cgpu_load_restart for every trajectory of a batch: the
+ * files of trajectory i (the same raw format: coeffs.in, orbBB_KK.in, with
+ * with_rdm2 the rdm2BtXX_YY.in blocks) under <dir>/traj<i, 5 digits>/; save
+ * creates the subdirectories, dir itself must exist. */
+int cgpu_batch_save_restart(cgpu_batch* batch, const char* dir, int with_rdm2);
+int cgpu_batch_load_restart(cgpu_batch* batch, const char* dir);
 int cgpu_batch_download(cgpu_batch* batch, cgpu_complex* states);
 /* n_steps steps of size dt; system i starts at t0[i].  *elapsed_ms (may be
  * NULL) receives the device time from CUDA events around the launches. */

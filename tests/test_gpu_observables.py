@@ -111,6 +111,37 @@ def test_restart_files_round_trip(tmp_path):
     e2.close()
 
 
+def test_batch_restart_files_match_single_system(tmp_path):
+    """cgpu_batch_save_restart writes, per trajectory, the files a single
+    context writes for the same state (bit for bit, rdm2 blocks included), and
+    cgpu_batch_load_restart reads them back into every trajectory."""
+    from codyfortran_gb300.engine import Batch, Engine
+    specs = [S.he1d_findiff((4, 4), False), S.he1d_findiff((3, 3), False)]
+    b = Batch(specs, "fp64")
+    states = [_state(sp, s.x, s.w, 11 + k, s.nC)[0] for k, (sp, s) in enumerate(zip(specs, b.systems))]
+    b.upload(states)
+    b.save_restart(tmp_path, with_rdm2=True)
+    for k, sp in enumerate(specs):
+        one = tmp_path / f"single{k}"
+        one.mkdir()
+        e = Engine(sp)
+        e.upload(states[k])
+        e.save_restart(one, with_rdm2=True)
+        e.close()
+        names = sorted(p.name for p in one.iterdir())
+        assert names == sorted(p.name for p in (tmp_path / f"traj{k:05d}").iterdir())
+        assert any(n.startswith("rdm2Bt") for n in names)
+        for n in names:
+            assert (one / n).read_bytes() == (tmp_path / f"traj{k:05d}" / n).read_bytes(), (k, n)
+    b2 = Batch(specs, "fp64")
+    b2.load_restart(tmp_path)
+    got = b2.download()
+    for k in range(len(specs)):
+        assert np.array_equal(got[k], states[k])
+    b.close()
+    b2.close()
+
+
 def test_absorber_mask_and_per_step_application():
     from codyfortran_gb300.engine import Engine
     sp = _helium()
