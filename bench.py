@@ -263,6 +263,13 @@ def dense_flops(systems, fam):
 
 FX_BITS = {"mixed_fx": 30, "mixed_fx6": 36}
 
+# DRAM bytes per launch of the dominant family, from one full-size ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum over the family's kernels of
+# one evaluation; the summary and its command are in the named file)
+PROFILED_TRAFFIC = {
+    ("batch512", "mixed_fx6", "pair_potentials"): (10.91e9, "profiles/dram_traffic_pair_potentials_fx6_batch512.md"),
+}
+
 
 def fx_grid_products(precision, systems):
     """Slice products per algorithmic product of the fixed-point contractions
@@ -424,6 +431,9 @@ def run_batch(args):
         byts = sum(s.nS for s in systems) * 16.0 * 4
         roof.update(bound="hbm", achieved=byts / avg_s / 1e9, peak=hbm, unit="GB/s", work_per_launch=byts)
     roof["frac"] = roof["achieved"] / roof["peak"]
+    prof = PROFILED_TRAFFIC.get((args.workload, precision, dom))
+    if prof:
+        roof.update(traffic=prof[0], traffic_unit="bytes per launch", traffic_source=prof[1])
     e2e = world * n / r["e2e_s"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
