@@ -570,7 +570,7 @@ void adjoint_tdci(cgpu_ctx* c, const z_t* C0_h, const double* E_h, int nT, doubl
 void launch_lanczos_start(cgpu_ctx* c, const z_t* v);
 void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim);
 void launch_lanczos_tail(cgpu_ctx* c, int j, double dt, int evalExp);  // j = 0: use the device mDim
-void launch_lanczos_combine(cgpu_ctx* c, z_t* out);
+void launch_lanczos_combine(cgpu_ctx* c, z_t* out, const z_t* start);
 void launch_lz_set(cgpu_ctx* c, int idx, double v);
 size_t lanczos_partial_need(const cgpu_ctx* c);
 #define CODY_LZ_ERR 385

@@ -704,9 +704,11 @@ void euler_device(cgpu_ctx* c, int which, int imag, z_t* state, double t0, doubl
   launch_axpby(c, state, c->dstate_d, zmk(t1 - t0, 0.0), zmk(1.0, 0.0), VSEL_STATE);
 }
 
-// One PerformLanczosStep on work_d -> trial_d.  Returns converged (adaptive) or -1 (not checked).
-int lanczos_pass(cgpu_ctx* c, int which, double tBase, double dt, int maxDim, double tol, double* errOut) {
-  launch_lanczos_start(c, c->work_d);
+// One PerformLanczosStep from start (device) into out (may be start itself).
+// Returns converged (adaptive) or -1 (not checked).
+int lanczos_pass(cgpu_ctx* c, int which, double tBase, double dt, int maxDim, double tol, double* errOut,
+                 const z_t* start, z_t* out) {
+  launch_lanczos_start(c, start);
   double tEval = tBase + 0.5 * dt;
   int adaptive = tol > 0.0;
   if (adaptive && c->nb > 1) throw std::string("SIL: adaptive (tolerance > 0) steps need a single system");
@@ -737,7 +739,7 @@ int lanczos_pass(cgpu_ctx* c, int which, double tBase, double dt, int maxDim, do
   } else {
     launch_lanczos_tail(c, 0, dt, 1);
   }
-  launch_lanczos_combine(c, c->trial_d);
+  launch_lanczos_combine(c, out, start);
   return converged;
 }
 
@@ -750,6 +752,13 @@ int sil_device(cgpu_ctx* c, int which, z_t* state, double t0, double t1, int kry
   if (maxDim > c->maxKrylov) throw std::string("SIL: krylovDim exceeds the context's max_krylov");
   c->metric_d = const_cast<double*>(metric_d);
   int warnings = 0;
+  if (!(tol > 0.0)) {
+    // fixed order: one pass, no acceptance test; the basis holds the start
+    // vector, so the pass reads and overwrites the state in place (the
+    // reference counts the unconverged pass as a warning)
+    lanczos_pass(c, which, t0, t1 - t0, maxDim, tol, nullptr, state, state);
+    return 1;
+  }
   batch_copy(c, c->work_d, state, sizeof(z_t) * c->nS);
   double tCur = t0, rem = t1 - t0;
   while (std::fabs(rem) > zeroThreshold) {
@@ -758,7 +767,7 @@ int sil_device(cgpu_ctx* c, int which, z_t* state, double t0, double t1, int kry
     int conv = 0;
     for (;;) {
       double err = 0.0;
-      conv = lanczos_pass(c, which, tCur, dtS, maxDim, tol, &err);
+      conv = lanczos_pass(c, which, tCur, dtS, maxDim, tol, &err, c->work_d, c->trial_d);
       if (conv == 1) break;
       if (conv < 0) break;  // fixed-order pass: no convergence test (tolerance 0)
       if (std::fabs(dtS) <= zeroThreshold || restarts >= maxRestarts) break;

@@ -173,11 +173,11 @@ __global__ void __launch_bounds__(LZ_THREADS) k_cgs_pass(z_t* __restrict__ w, co
                                                           const double* __restrict__ m, TRAJ_ARGS,
                                                           double* __restrict__ lz, int dotBase, int E,
                                                           const z_t* __restrict__ gate0, int gateStride,
-                                                          const z_t* __restrict__ gate1, int scaleIdx) {
+                                                          const z_t* __restrict__ gate1, int scaleIdx, int nBlkGate) {
   const TrajShape& S = shp[blockIdx.z];
   lz = bat(lz, bs);
   if (lz[LZ_DONE] != 0.0) return;
-  if (gate0 && !reorth_needed(bat(gate0, bs), gateStride, bat(gate1, bs), nBlkIn)) return;
+  if (gate0 && !reorth_needed(bat(gate0, bs), gateStride, bat(gate1, bs), nBlkGate)) return;
   w = bat(w, bs);
   V = bat(V, bs);
   partIn = bat(partIn, bs);
@@ -549,17 +549,21 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz3_update(z_t* __restrict__ dst
 // test fired), alpha_j and beta_j into the tridiagonal, s_(j+1) = 1 / beta_j;
 // a breakdown or the last iteration fixes the subspace dimension, a breakdown
 // also stops the growth.
-__global__ void __launch_bounds__(LZ_THREADS) k_lz_scalars(const z_t* __restrict__ partIn,
-                                                            const z_t* __restrict__ partAlt,
-                                                            const z_t* __restrict__ gate0, int gateStride, int nBlkIn,
+__global__ void __launch_bounds__(LZ_THREADS) k_lz_scalars(const z_t* __restrict__ partIn, int nBlkIn,
+                                                            const z_t* __restrict__ partAlt, int nBlkAlt,
+                                                            const z_t* __restrict__ gate0, int gateStride,
                                                             TRAJ_ARGS, double* __restrict__ lz, int j, int maxDim,
                                                             double zeroThr) {
   lz = bat(lz, bs);
   if (lz[LZ_DONE] != 0.0) return;
   partIn = bat(partIn, bs);
-  if (reorth_needed(bat(gate0, bs), gateStride, partIn, nBlkIn)) partIn = bat(partAlt, bs);
+  int nPart = nBlkIn;
+  if (reorth_needed(bat(gate0, bs), gateStride, partIn, nBlkIn)) {
+    partIn = bat(partAlt, bs);
+    nPart = nBlkAlt;
+  }
   __shared__ z_t tot[1];
-  sum_partials(partIn, nBlkIn, 1, 1, tot);
+  sum_partials(partIn, nPart, 1, 1, tot);
   if (threadIdx.x != 0) return;
   const double be = sqrt(tot[0].x);
   lz[LZ_ALPHA + j - 1] = lz[LZ_D + 2 * (j - 1)];
@@ -617,14 +621,17 @@ void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
     k_lz3_update<<<g, LZ_THREADS, 0, c->stream>>>(uNext, c->lw_d, vPrev, vCur, p1, nBlk, p2, c->metric_d,
                                                   TRAJ_PASS(c), c->lz_d, j);
     CODY_LAUNCHED(c);
-    k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p3, 1, vCur, ld, 1, uNext, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 0,
-                                            p1 + 1, 2, p2, nBlk);
+    // the gated second pass rarely fires: one block per trajectory reads the
+    // gate (and, when it fires, walks the whole vector)
+    dim3 g1 = bgrid(c, 1);
+    k_mdot<<<g1, LZ_THREADS, 0, c->stream>>>(p3, 1, vCur, ld, 1, uNext, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 0,
+                                             p1 + 1, 2, p2, nBlk);
     CODY_LAUNCHED(c);
-    k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(uNext, vCur, ld, 1, p3, 1, nBlk, p4, c->metric_d, TRAJ_PASS(c),
-                                                c->lz_d, -1, E, p1 + 1, 2, p2, LZ_S + j - 1);
+    k_cgs_pass<<<g1, LZ_THREADS, 0, c->stream>>>(uNext, vCur, ld, 1, p3, 1, 1, p4, c->metric_d, TRAJ_PASS(c), c->lz_d,
+                                                 -1, E, p1 + 1, 2, p2, LZ_S + j - 1, nBlk);
     CODY_LAUNCHED(c);
-    k_lz_scalars<<<bgrid(c, 1), LZ_THREADS, 0, c->stream>>>(p2, p4, p1 + 1, 2, nBlk, TRAJ_PASS(c), c->lz_d, j, maxDim,
-                                                            1.0e-14);
+    k_lz_scalars<<<g1, LZ_THREADS, 0, c->stream>>>(p2, nBlk, p4, 1, p1 + 1, 2, TRAJ_PASS(c), c->lz_d, j, maxDim,
+                                                   1.0e-14);
     CODY_LAUNCHED(c);
     return;
   }
@@ -637,13 +644,13 @@ void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
                                           nullptr, 0, nullptr, nBlk);
   CODY_LAUNCHED(c);
   k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, V, ld, nv, p1, s1, nBlk, p2, c->metric_d, TRAJ_PASS(c),
-                                              c->lz_d, base, E, nullptr, 0, nullptr, -1);
+                                              c->lz_d, base, E, nullptr, 0, nullptr, -1, nBlk);
   CODY_LAUNCHED(c);
   k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p3, nv, V, ld, nv, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 0,
                                           p1 + nv, s1, p2, nBlk);
   CODY_LAUNCHED(c);
   k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, V, ld, nv, p3, nv, nBlk, p4, c->metric_d, TRAJ_PASS(c),
-                                              c->lz_d, -1, E, p1 + nv, s1, p2, -1);
+                                              c->lz_d, -1, E, p1 + nv, s1, p2, -1, nBlk);
   CODY_LAUNCHED(c);
   z_t* vNext = (j < maxDim) ? c->basis_d + ld * (size_t)j : nullptr;
   k_lz_finish<<<g, LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p2, p4, p1 + nv, s1, nBlk, TRAJ_PASS(c), c->lz_d, j,
@@ -660,9 +667,9 @@ void launch_lanczos_tail(cgpu_ctx* c, int j, double dt, int evalExp) {
   CODY_LAUNCHED(c);
 }
 
-void launch_lanczos_combine(cgpu_ctx* c, z_t* out) {
+void launch_lanczos_combine(cgpu_ctx* c, z_t* out, const z_t* start) {
   ProfScope prof(c, CGPU_KERNEL_VECTOR);
-  k_lz_combine<<<bgrid(c, c->lzBlocks), LZ_THREADS, 0, c->stream>>>(out, c->work_d, c->basis_d, c->nS, TRAJ_PASS(c),
+  k_lz_combine<<<bgrid(c, c->lzBlocks), LZ_THREADS, 0, c->stream>>>(out, start, c->basis_d, c->nS, TRAJ_PASS(c),
                                                                     c->lz_d);
   CODY_LAUNCHED(c);
 }
