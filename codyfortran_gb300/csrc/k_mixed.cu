@@ -308,7 +308,11 @@ constexpr int FX_LMAX = 8;
 // independent bit field of Y: d_i = field_i(Y) - 2^(b-1), d_0 = Y >> b(L-1)
 // (arithmetic shift).  The balanced representation is unique, so this gives
 // the digits of the carry-by-carry division.
-__device__ __forceinline__ void fx_digits(double x, int e, int b, int L, int (&d)[FX_LMAX]) {
+// BT / LT > 0 fix the digit width / slice count at compile time (constant
+// shifts); 0 takes them from bRt / LRt.
+template <int BT, int LT>
+__device__ __forceinline__ void fx_digits_t(double x, int e, int bRt, int LRt, int (&d)[FX_LMAX]) {
+  const int b = BT > 0 ? BT : bRt, L = LT > 0 ? LT : LRt;
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   const int ex = (int)((u >> 52) & 0x7FF);
   long long X = 0;
@@ -354,15 +358,26 @@ __device__ __forceinline__ unsigned fx_biased_exp(double v) { return (unsigned)(
 // smallest e with |x| < 2^e for the largest biased exponent m of a row (0: all zero)
 __device__ __forceinline__ int fx_exp(unsigned m) { return m ? (int)m - 1022 : 0; }
 
-__device__ __forceinline__ void fx_store(__nv_bfloat16* rowBase, size_t pitch, int k, bool valid, double v, int e,
-                                         int b, int L) {
+__device__ __forceinline__ void fx_digits(double x, int e, int b, int L, int (&d)[FX_LMAX]) {
+  fx_digits_t<0, 0>(x, e, b, L, d);
+}
+
+template <int BT, int LT>
+__device__ __forceinline__ void fx_store_t(__nv_bfloat16* rowBase, size_t pitch, int k, bool valid, double v, int e,
+                                           int bRt, int LRt) {
+  const int L = LT > 0 ? LT : LRt;
   int d[FX_LMAX];
 #pragma unroll
   for (int l = 0; l < FX_LMAX; l++) d[l] = 0;
-  if (valid) fx_digits(v, e, b, L, d);
+  if (valid) fx_digits_t<BT, LT>(v, e, bRt, LRt, d);
 #pragma unroll
   for (int l = 0; l < FX_LMAX; l++)
     if (l < L) rowBase[(size_t)l * pitch + k] = fx_bf16(d[l]);
+}
+
+__device__ __forceinline__ void fx_store(__nv_bfloat16* rowBase, size_t pitch, int k, bool valid, double v, int e,
+                                         int b, int L) {
+  fx_store_t<0, 0>(rowBase, pitch, k, valid, v, e, b, L);
 }
 
 __device__ unsigned fx_block_max(unsigned m) {
@@ -381,7 +396,7 @@ __device__ unsigned fx_block_max(unsigned m) {
 // One block per row: the row's values in dynamic shared memory, the exponent
 // of its maximum, then the L digit planes: value k at column shift + k, zero
 // elsewhere in [0, Kpad).
-template <class F>
+template <int BT = 0, int LT = 0, class F>
 __device__ void fx_row(__nv_bfloat16* rowBase, int* expOut, int K, int Kpad, int pitch, int b, int L, int shift,
                        F value) {
   extern __shared__ double fxbuf[];
@@ -396,7 +411,7 @@ __device__ void fx_row(__nv_bfloat16* rowBase, int* expOut, int K, int Kpad, int
   for (int k = threadIdx.x; k < Kpad; k += blockDim.x) {
     const int src = k - shift;
     const bool valid = src >= 0 && src < K;
-    fx_store(rowBase, pitch, k, valid, valid ? fxbuf[src] : 0.0, e, b, L);
+    fx_store_t<BT, LT>(rowBase, pitch, k, valid, valid ? fxbuf[src] : 0.0, e, b, L);
   }
 }
 
@@ -415,6 +430,7 @@ __global__ void __launch_bounds__(256) k_fx_split_V(__nv_bfloat16* __restrict__ 
 
 // Row 2p + s of S: (re, im)[conj(phi_l) phi_k w] over the grid (p = (l, k)).
 // Block 0 of a trajectory also clears the W exponent maxima for GEMM1.
+template <int BT, int LT>
 __global__ void __launch_bounds__(256) k_fx_split_S(__nv_bfloat16* __restrict__ out, int* __restrict__ eS,
                                                      unsigned* __restrict__ mWr, unsigned* __restrict__ mWc,
                                                      const z_t* __restrict__ orbs, const double* __restrict__ w,
@@ -438,7 +454,7 @@ __global__ void __launch_bounds__(256) k_fx_split_S(__nv_bfloat16* __restrict__ 
   const int p = row >> 1, s = row & 1;
   const z_t* a = orbs + (size_t)nG * pl[p];
   const z_t* bo = orbs + (size_t)nG * pk[p];
-  fx_row(out + (size_t)row * L * pitch, eS + row, nG, T.Kg, pitch, b, L, T.gShift, [&](int g) {
+  fx_row<BT, LT>(out + (size_t)row * L * pitch, eS + row, nG, T.Kg, pitch, b, L, T.gShift, [&](int g) {
     const z_t v = zcmul(a[g], bo[g]);
     return (s ? v.y : v.x) * w[g];
   });
@@ -495,11 +511,14 @@ __global__ void k_fx_reduce_W(double* __restrict__ Wd, unsigned* __restrict__ mW
 // K = nG at columns gShift + g: b1/L3 digits) planes, with the row exponents
 // eWr[g] / eWc[n].  One block per 32-row strip of W, walking the trajectory's
 // own K = 2P columns in 32 x 32 tiles transposed through shared memory.
+// B1/L3T, B2/L2T > 0: the digit plans fixed at compile time (0: run-time b1, L3, b2, L2).
+template <int B1, int L3T, int B2, int L2T>
 __global__ void __launch_bounds__(256) k_fx_split_W(__nv_bfloat16* __restrict__ WxA, __nv_bfloat16* __restrict__ WTxB,
                                                      int* __restrict__ eWr, int* __restrict__ eWc,
                                                      const double* __restrict__ Wd, const unsigned* __restrict__ mWr,
                                                      const unsigned* __restrict__ mWc, int pitchP, int pitchG, int b1,
-                                                     int L3, int b2, int L2, TRAJ_ARGS) {
+                                                     int L3rt, int b2, int L2rt, TRAJ_ARGS) {
+  const int L3 = L3T > 0 ? L3T : L3rt, L2 = L2T > 0 ? L2T : L2rt;
   __shared__ double tile[SW_T][SW_T + 1];
   const TrajShape& T = shp[blockIdx.z];
   const int nG = T.nG, N2P = 2 * T.nPairs, KpP = T.Kp, KpG = T.Kg;
@@ -524,7 +543,7 @@ __global__ void __launch_bounds__(256) k_fx_split_W(__nv_bfloat16* __restrict__ 
       if (g < nG) {
         const int e = fx_exp(mWr[g]);
         if (n == 0) eWr[g] = e;
-        fx_store(WxA + (size_t)g * L2 * pitchP, pitchP, n, valid, v, e, b2, L2);
+        fx_store_t<B2, L2T>(WxA + (size_t)g * L2 * pitchP, pitchP, n, valid, v, e, b2, L2);
       }
     }
     __syncthreads();
@@ -533,11 +552,11 @@ __global__ void __launch_bounds__(256) k_fx_split_W(__nv_bfloat16* __restrict__ 
       if (n < N2P && col < KpG) {
         const int e = fx_exp(mWc[n]);
         if (g == 0) eWc[n] = e;
-        fx_store(WTxB + (size_t)n * L3 * pitchG, pitchG, col, g < nG, tile[tx][r], e, b1, L3);
+        fx_store_t<B1, L3T>(WTxB + (size_t)n * L3 * pitchG, pitchG, col, g < nG, tile[tx][r], e, b1, L3);
       }
       if (n < N2P && g0 == 0)  // columns before the shifted grid
         for (int cz = tx; cz < sh; cz += 32)
-          fx_store(WTxB + (size_t)n * L3 * pitchG, pitchG, cz, false, 0.0, 0, b1, L3);
+          fx_store_t<B1, L3T>(WTxB + (size_t)n * L3 * pitchG, pitchG, cz, false, 0.0, 0, b1, L3);
     }
   }
 }
@@ -728,7 +747,10 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   z_t* Z = (z_t*)m->Zd;
   {
     ProfScope prof(c, CGPU_KERNEL_PAIR_POTENTIALS);
-    k_fx_split_S<<<dim3(2 * nP, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(
+    auto split_s = k_fx_split_S<0, 0>;
+    if (m->b1 == 6 && m->LS == 6) split_s = k_fx_split_S<6, 6>;
+    else if (m->b1 == 6 && m->LS == 5) split_s = k_fx_split_S<6, 5>;
+    split_s<<<dim3(2 * nP, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(
         m->SxA, m->eS, m->mWr, m->mWc, orbs, c->w_d, c->pairL_d, c->pairK_d, m->KgMax, m->b1, m->LS, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
     const bool one = m->s1 == 1;
@@ -745,8 +767,12 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
       CODY_LAUNCHED(c);
     }
     dim3 gw(ceil_div(m->KgMax, SW_T), 1, c->nb);
-    k_fx_split_W<<<gw, 256, 0, c->stream>>>(m->WxA, m->WTxB, m->eWr, m->eWc, m->Wd, m->mWr, m->mWc, m->KpMax,
-                                            m->KgMax, m->b1, m->L3, m->b2, m->L2, TRAJ_PASS(c));
+    // the digit plans of the two fixed-point forms on long grids, compiled in
+    auto split_w = k_fx_split_W<0, 0, 0, 0>;
+    if (m->b1 == 6 && m->L3 == 6 && m->b2 == 8 && m->L2 == 5) split_w = k_fx_split_W<6, 6, 8, 5>;
+    else if (m->b1 == 6 && m->L3 == 5 && m->b2 == 8 && m->L2 == 4) split_w = k_fx_split_W<6, 5, 8, 4>;
+    split_w<<<gw, 256, 0, c->stream>>>(m->WxA, m->WTxB, m->eWr, m->eWc, m->Wd, m->mWr, m->mWc, m->KpMax, m->KgMax,
+                                       m->b1, m->L3, m->b2, m->L2, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
   }
   {
