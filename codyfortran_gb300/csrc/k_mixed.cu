@@ -461,6 +461,7 @@ __global__ void __launch_bounds__(256) k_fx_split_S(__nv_bfloat16* __restrict__ 
 }
 
 // Row n = 2q + s of R'' (K = 2p + t), as k_split_R.
+template <int BT, int LT>
 __global__ void k_fx_split_R(__nv_bfloat16* __restrict__ out, int* __restrict__ eR, const z_t* __restrict__ Rp,
                              const int* __restrict__ pl, const int* __restrict__ pk, int pitch, int b, int L,
                              TRAJ_ARGS) {
@@ -474,7 +475,7 @@ __global__ void k_fx_split_R(__nv_bfloat16* __restrict__ out, int* __restrict__ 
   pl = bat(pl, bs);
   pk = bat(pk, bs);
   const int q = row >> 1, s = row & 1;
-  fx_row(out + (size_t)row * L * pitch, eR + row, 2 * nP, T.Kp, pitch, b, L, 0, [&](int k) {
+  fx_row<BT, LT>(out + (size_t)row * L * pitch, eR + row, 2 * nP, T.Kp, pitch, b, L, 0, [&](int k) {
     const int p = k >> 1, t = k & 1;
     const int l = pl[p], kk = pk[p];
     const z_t R1 = Rp[(size_t)(l * n + kk) * Q + q];
@@ -777,7 +778,10 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   }
   {
     ProfScope prof(c, CGPU_KERNEL_CORRELATION);
-    k_fx_split_R<<<dim3(2 * Q, 1, c->nb), 64, sizeof(double) * m->KpMax, c->stream>>>(
+    auto split_r = k_fx_split_R<0, 0>;
+    if (m->b2 == 8 && m->L2 == 5) split_r = k_fx_split_R<8, 5>;
+    else if (m->b2 == 8 && m->L2 == 4) split_r = k_fx_split_R<8, 4>;
+    split_r<<<dim3(2 * Q, 1, c->nb), 64, sizeof(double) * m->KpMax, c->stream>>>(
         m->RxB, m->eR, c->Rp_d, c->pairL_d, c->pairK_d, m->KpMax, m->b2, m->L2, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
     fx_gemm(c, m->L2, m->b2, m->compact2, TC_GEMM_Z, m->mW, m->mR, m->bn2, m->s2 > 1 ? m->Zp : m->Zd, m->eWr, m->eR,
