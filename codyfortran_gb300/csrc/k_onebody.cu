@@ -61,9 +61,8 @@ __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, c
   extern __shared__ z_t sh[];
   const TrajShape& S = shp[blockIdx.z];
   const int nG = S.nG, band = S.band;
-  int i = blockIdx.y;
-  int g0 = blockIdx.x * OB_THREADS;
-  if (i >= S.nOS || g0 >= nG) return;
+  const int g0 = blockIdx.x * OB_THREADS;
+  if (g0 >= nG) return;
   out = bat(out, bs);
   orbs = bat(orbs, bs);
   T = bat(T, bs);
@@ -71,36 +70,42 @@ __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, c
   x = bat(x, bs);
   btOf = bat(btOf, bs);
   const double E = *bat(Efield, bs);
-  const z_t* f = orbs + (size_t)nG * i;
-  int nTile = OB_THREADS + 2 * band;
-  for (int t = threadIdx.x; t < nTile; t += OB_THREADS) {
-    int g = g0 - band + t;
-    sh[t] = (g >= 0 && g < nG) ? f[g] : zmk(0.0, 0.0);
+  const int nTile = OB_THREADS + 2 * band, nd = 2 * band + 1;
+  const int g = g0 + threadIdx.x;
+  const bool live = g < nG;
+  const double pot = (S.hasPot && live) ? V0[g] + E * x[g] : 0.0;
+  // the block walks every stored orbital of its grid tile (one launch-sized
+  // block per tile instead of one per orbital and tile)
+  for (int i = 0; i < S.nOS; i++) {
+    const z_t* f = orbs + (size_t)nG * i;
+    if (i > 0) __syncthreads();  // the previous orbital's tile has been read
+    for (int t = threadIdx.x; t < nTile; t += OB_THREADS) {
+      const int gg = g0 - band + t;
+      sh[t] = (gg >= 0 && gg < nG) ? f[gg] : zmk(0.0, 0.0);
+    }
+    __syncthreads();
+    if (!live) continue;
+    const int bt = S.restricted ? 0 : btOf[i];
+    const double* Tb = T + (size_t)bt * nd * nG;
+    z_t acc = zmk(0.0, 0.0);
+    for (int d = 0; d < nd; d++) {
+      double c = Tb[(size_t)d * nG + g];
+      z_t v = sh[threadIdx.x + d];
+      acc.x = fma(c, v.x, acc.x);
+      acc.y = fma(c, v.y, acc.y);
+    }
+    if (S.hasPot) {
+      z_t v = sh[threadIdx.x + band];
+      acc.x = fma(pot, v.x, acc.x);
+      acc.y = fma(pot, v.y, acc.y);
+    }
+    // alpha is 1 or -i on the propagation paths: no FP64 multiply for those
+    z_t r = (alpha.x == 1.0 && alpha.y == 0.0) ? acc : (alpha.x == 0.0 && alpha.y == -1.0) ? zmi(acc)
+                                                                                             : zmul(alpha, acc);
+    size_t o = (size_t)nG * i + g;
+    if (accumulate) r = zadd(out[o], r);
+    out[o] = r;
   }
-  __syncthreads();
-  int g = g0 + threadIdx.x;
-  if (g >= nG) return;
-  int bt = S.restricted ? 0 : btOf[i];
-  int nd = 2 * band + 1;
-  const double* Tb = T + (size_t)bt * nd * nG;
-  z_t acc = zmk(0.0, 0.0);
-  for (int d = 0; d < nd; d++) {
-    double c = Tb[(size_t)d * nG + g];
-    z_t v = sh[threadIdx.x + d];
-    acc.x = fma(c, v.x, acc.x);
-    acc.y = fma(c, v.y, acc.y);
-  }
-  if (S.hasPot) {
-    double pot = V0[g] + E * x[g];
-    z_t v = sh[threadIdx.x + band];
-    acc.x = fma(pot, v.x, acc.x);
-    acc.y = fma(pot, v.y, acc.y);
-  }
-  // alpha is 1 or -i on the propagation paths: no FP64 multiply for those
-  z_t r = (alpha.x == 1.0 && alpha.y == 0.0) ? acc : (alpha.x == 0.0 && alpha.y == -1.0) ? zmi(acc) : zmul(alpha, acc);
-  size_t o = (size_t)nG * i + g;
-  if (accumulate) r = zadd(out[o], r);
-  out[o] = r;
 }
 
 // The one-body apply in double-float arithmetic (the fixed-point forms): the
@@ -114,9 +119,8 @@ __global__ void k_onebody_df(z_t* __restrict__ out, const z_t* __restrict__ orbs
   extern __shared__ float4 shf[];
   const TrajShape& S = shp[blockIdx.z];
   const int nG = S.nG, band = S.band;
-  int i = blockIdx.y;
-  int g0 = blockIdx.x * OB_THREADS;
-  if (i >= S.nOS || g0 >= nG) return;
+  const int g0 = blockIdx.x * OB_THREADS;
+  if (g0 >= nG) return;
   out = bat(out, bs);
   orbs = bat(orbs, bs);
   Tdf = bat(Tdf, bs);
@@ -124,36 +128,39 @@ __global__ void k_onebody_df(z_t* __restrict__ out, const z_t* __restrict__ orbs
   x = bat(x, bs);
   btOf = bat(btOf, bs);
   const double E = *bat(Efield, bs);
-  const z_t* f = orbs + (size_t)nG * i;
-  int nTile = OB_THREADS + 2 * band;
-  for (int t = threadIdx.x; t < nTile; t += OB_THREADS) {
-    int g = g0 - band + t;
-    shf[t] = (g >= 0 && g < nG) ? zdf_from(f[g]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const int nTile = OB_THREADS + 2 * band, nd = 2 * band + 1;
+  const int g = g0 + threadIdx.x;
+  const bool live = g < nG;
+  const float2 pd = (S.hasPot && live) ? df_split(fma(E, x[g], V0[g])) : make_float2(0.0f, 0.0f);
+  for (int i = 0; i < S.nOS; i++) {  // every stored orbital of the grid tile
+    const z_t* f = orbs + (size_t)nG * i;
+    if (i > 0) __syncthreads();
+    for (int t = threadIdx.x; t < nTile; t += OB_THREADS) {
+      const int gg = g0 - band + t;
+      shf[t] = (gg >= 0 && gg < nG) ? zdf_from(f[gg]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    __syncthreads();
+    if (!live) continue;
+    const int bt = S.restricted ? 0 : btOf[i];
+    const float2* Tb = Tdf + (size_t)bt * nd * nG;
+    zdf_acc acc = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int d = 0; d < nd; d++) {
+      const float2 cf = Tb[(size_t)d * nG + g];
+      const float4 v = shf[threadIdx.x + d];
+      df_mul_acc(acc.rs, acc.rc, cf.x, cf.y, v.x, v.y);
+      df_mul_acc(acc.is, acc.ic, cf.x, cf.y, v.z, v.w);
+    }
+    if (S.hasPot) {
+      const float4 v = shf[threadIdx.x + band];
+      df_mul_acc(acc.rs, acc.rc, pd.x, pd.y, v.x, v.y);
+      df_mul_acc(acc.is, acc.ic, pd.x, pd.y, v.z, v.w);
+    }
+    const z_t a = zdf_to_z(acc);
+    z_t r = (alpha.x == 1.0 && alpha.y == 0.0) ? a : (alpha.x == 0.0 && alpha.y == -1.0) ? zmi(a) : zmul(alpha, a);
+    size_t o = (size_t)nG * i + g;
+    if (accumulate) r = zadd(out[o], r);
+    out[o] = r;
   }
-  __syncthreads();
-  int g = g0 + threadIdx.x;
-  if (g >= nG) return;
-  int bt = S.restricted ? 0 : btOf[i];
-  int nd = 2 * band + 1;
-  const float2* Tb = Tdf + (size_t)bt * nd * nG;
-  zdf_acc acc = {0.0f, 0.0f, 0.0f, 0.0f};
-  for (int d = 0; d < nd; d++) {
-    const float2 cf = Tb[(size_t)d * nG + g];
-    const float4 v = shf[threadIdx.x + d];
-    df_mul_acc(acc.rs, acc.rc, cf.x, cf.y, v.x, v.y);
-    df_mul_acc(acc.is, acc.ic, cf.x, cf.y, v.z, v.w);
-  }
-  if (S.hasPot) {
-    const float2 pd = df_split(fma(E, x[g], V0[g]));
-    const float4 v = shf[threadIdx.x + band];
-    df_mul_acc(acc.rs, acc.rc, pd.x, pd.y, v.x, v.y);
-    df_mul_acc(acc.is, acc.ic, pd.x, pd.y, v.z, v.w);
-  }
-  const z_t a = zdf_to_z(acc);
-  z_t r = (alpha.x == 1.0 && alpha.y == 0.0) ? a : (alpha.x == 0.0 && alpha.y == -1.0) ? zmi(a) : zmul(alpha, a);
-  size_t o = (size_t)nG * i + g;
-  if (accumulate) r = zadd(out[o], r);
-  out[o] = r;
 }
 
 // Column range of a Gram / projector call: group < 0 = all stored orbitals,
@@ -666,7 +673,7 @@ size_t gram_partial_need(const cgpu_ctx* c, int n) {
 
 void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha, int accumulate) {
   ProfScope prof(c, CGPU_KERNEL_ONEBODY);
-  dim3 grid(ceil_div(c->nG, OB_THREADS), c->nOS, c->nb);
+  dim3 grid(ceil_div(c->nG, OB_THREADS), 1, c->nb);
   size_t sh = sizeof(z_t) * (OB_THREADS + 2 * c->band);
   const double* base = (c->inCapture || c->useStepTime) ? c->stepT_d : c->zero_d;
   double off = c->inCapture ? t - c->captureT0 : t;
