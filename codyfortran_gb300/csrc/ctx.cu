@@ -841,7 +841,7 @@ void capture_step_graph(cgpu_ctx* c, double t0, double dt, int krylov, int useMe
 
 // Step start time of every trajectory (t0s has nb entries): one contiguous
 // copy and a kernel that writes each trajectory's slot (a strided copy of nb
-// single doubles costs the driver one transfer per trajectory).
+// single doubles costs the CUDA driver one transfer per trajectory).
 void set_step_times(cgpu_ctx* c, const double* t0s) {
   if (!c->tStage_d) CODY_CUDA(cudaMalloc(&c->tStage_d, sizeof(double) * c->nb));
   CODY_CUDA(cudaMemcpyAsync(c->tStage_d, t0s, sizeof(double) * c->nb, cudaMemcpyHostToDevice, c->stream));

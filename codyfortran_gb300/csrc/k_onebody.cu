@@ -74,11 +74,11 @@ __global__ void k_onebody(z_t* __restrict__ out, const z_t* __restrict__ orbs, c
   const int g = g0 + threadIdx.x;
   const bool live = g < nG;
   const double pot = (S.hasPot && live) ? V0[g] + E * x[g] : 0.0;
-  // the block walks every stored orbital of its grid tile (one launch-sized
-  // block per tile instead of one per orbital and tile)
-  for (int i = 0; i < S.nOS; i++) {
+  // orbitals blockIdx.y, blockIdx.y + gridDim.y, ... of the grid tile (a batch
+  // launches one orbital group: one block per tile instead of per orbital and tile)
+  for (int i = blockIdx.y; i < S.nOS; i += gridDim.y) {
     const z_t* f = orbs + (size_t)nG * i;
-    if (i > 0) __syncthreads();  // the previous orbital's tile has been read
+    if (i != (int)blockIdx.y) __syncthreads();  // the previous orbital's tile has been read
     for (int t = threadIdx.x; t < nTile; t += OB_THREADS) {
       const int gg = g0 - band + t;
       sh[t] = (gg >= 0 && gg < nG) ? f[gg] : zmk(0.0, 0.0);
@@ -132,9 +132,9 @@ __global__ void k_onebody_df(z_t* __restrict__ out, const z_t* __restrict__ orbs
   const int g = g0 + threadIdx.x;
   const bool live = g < nG;
   const float2 pd = (S.hasPot && live) ? df_split(fma(E, x[g], V0[g])) : make_float2(0.0f, 0.0f);
-  for (int i = 0; i < S.nOS; i++) {  // every stored orbital of the grid tile
+  for (int i = blockIdx.y; i < S.nOS; i += gridDim.y) {  // the block's orbitals of the grid tile
     const z_t* f = orbs + (size_t)nG * i;
-    if (i > 0) __syncthreads();
+    if (i != (int)blockIdx.y) __syncthreads();
     for (int t = threadIdx.x; t < nTile; t += OB_THREADS) {
       const int gg = g0 - band + t;
       shf[t] = (gg >= 0 && gg < nG) ? zdf_from(f[gg]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -673,7 +673,11 @@ size_t gram_partial_need(const cgpu_ctx* c, int n) {
 
 void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha, int accumulate) {
   ProfScope prof(c, CGPU_KERNEL_ONEBODY);
-  dim3 grid(ceil_div(c->nG, OB_THREADS), 1, c->nb);
+  // one block per grid tile walking every orbital when the tiles alone fill
+  // the SMs several times over (batches), else one block per tile and orbital
+  const unsigned tiles = ceil_div(c->nG, OB_THREADS);
+  const unsigned groups = (size_t)tiles * c->nb >= 4 * (size_t)c->numSms ? 1 : (unsigned)c->nOS;
+  dim3 grid(tiles, groups, c->nb);
   size_t sh = sizeof(z_t) * (OB_THREADS + 2 * c->band);
   const double* base = (c->inCapture || c->useStepTime) ? c->stepT_d : c->zero_d;
   double off = c->inCapture ? t - c->captureT0 : t;

@@ -120,7 +120,7 @@ const char* cgpu_last_error(const cgpu_ctx* ctx);
 const char* cgpu_last_global_error(void);
 /* Page-locked host memory for the state buffers of the upload / download /
  * propagate entry points: their host<->device copies then run as direct DMA
- * at the link rate instead of through the driver's pageable staging.  An
+ * at the link rate instead of through the CUDA driver's pageable staging.  An
  * addition of the GPU boundary (the reference keeps its states in ordinary
  * host arrays).  bytes == 0 gives *out = NULL; cgpu_host_free(NULL) is a no-op. */
 int cgpu_host_alloc(size_t bytes, void** out);
