@@ -28,6 +28,9 @@ void tc_gemm(cgpu_ctx* c, int gemmId, const CUtensorMap& ta, const CUtensorMap& 
 // maxCol (unsplit K only) receive the largest biased exponent of |C| per row /
 // column.  compact: the two-CTAs-per-SM configuration (small K).  aShared: A
 // is one matrix shared by the trajectories, read at each trajectory's vRow.
+// nSplit: K splits of the longest contraction (segPitch / 64 K blocks, kPer
+// blocks per split); a trajectory of fewer K blocks takes only the splits its
+// own K needs, balanced, and its remaining partials are written as zeros.
 void fx_gemm(cgpu_ctx* c, int L, int digitBits, bool compact, int gemmId, const CUtensorMap& ta,
              const CUtensorMap& tb, int bn, double* out, const int* expA, const int* expB, unsigned* maxRow,
              unsigned* maxCol, int segPitchA, int segPitch, int aShared, int nSplit, const void* tiles, int nTiles,
