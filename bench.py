@@ -626,6 +626,9 @@ def main():
         dist.init_process_group("gloo")
     from codyfortran_gb300 import build as B
     B.build()
+    if world > 1:
+        from codyfortran_gb300.engine import select_device
+        select_device(local)  # one replica per GPU
     if args.workload == "batch512":
         return run_batch(args)
     return run_single(args)

@@ -1145,6 +1145,21 @@ int cgpu_host_alloc(size_t bytes, void** out) {
   return CGPU_OK;
 }
 
+int cgpu_select_device(int device) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e == cudaSuccess && (device < 0 || device >= n)) {
+    cody_record_global_error("cgpu_select_device: no device " + std::to_string(device));
+    return CGPU_ERR_ARG;
+  }
+  if (e == cudaSuccess) e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    cody_record_global_error(std::string("cgpu_select_device: ") + cudaGetErrorString(e));
+    return CGPU_ERR_CUDA;
+  }
+  return CGPU_OK;
+}
+
 int cgpu_host_free(void* ptr) {
   if (!ptr) return CGPU_OK;
   const cudaError_t e = cudaFreeHost(ptr);

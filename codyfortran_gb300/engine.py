@@ -25,7 +25,7 @@ _WHICH = {"full": TD_FULL, "orbs_lin": TD_ORBS_LIN, "nonlin": TD_NONLIN, "tdci":
 
 EXPORTED = [
     "cgpu_ctx_create", "cgpu_ctx_destroy", "cgpu_last_error", "cgpu_last_global_error", "cgpu_host_alloc",
-    "cgpu_host_free", "cgpu_sizes", "cgpu_grid",
+    "cgpu_host_free", "cgpu_select_device", "cgpu_sizes", "cgpu_grid",
     "cgpu_configlist_tables", "cgpu_synchronize", "cgpu_launch_count", "cgpu_time_derivative",
     "cgpu_apply_single_body_op", "cgpu_fill_h1", "cgpu_fill_h2", "cgpu_apply_correlation_op", "cgpu_energy",
     "cgpu_ci_apply_h1_fill_rdm1", "cgpu_ci_apply_h2_fill_rdm2", "cgpu_project_coeffs", "cgpu_normalize_coeffs",
@@ -120,6 +120,14 @@ class _PinnedBlock:
         if getattr(self, "_ptr", None):
             self._lib.cgpu_host_free(C.c_void_p(self._ptr))
             self._ptr = None
+
+
+def select_device(device):
+    """The CUDA device of the contexts this process creates from now on (one
+    process per GPU passes its local rank)."""
+    lib = load_library()
+    if lib.cgpu_select_device(int(device)) != 0:
+        raise CodyError(lib.cgpu_last_global_error().decode())
 
 
 def pinned_empty(n, dtype=np.complex128):

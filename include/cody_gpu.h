@@ -125,6 +125,10 @@ const char* cgpu_last_global_error(void);
  * host arrays).  bytes == 0 gives *out = NULL; cgpu_host_free(NULL) is a no-op. */
 int cgpu_host_alloc(size_t bytes, void** out);
 int cgpu_host_free(void* ptr);
+/* Makes device the calling thread's CUDA device for the contexts and batches
+ * it creates afterwards (one process per GPU passes its local rank).  An
+ * addition of the GPU boundary. */
+int cgpu_select_device(int device);
 /* out[0..5] = nG, nO (spin-orbitals), nOS (stored orbitals), nC, nBodyTypes, nState */
 int cgpu_sizes(const cgpu_ctx* ctx, int* out);
 /* Grid_Linear_xCoord / Grid_Linear_weights */
