@@ -87,13 +87,36 @@ def initial_state(sp, x, w, seed):
     return I.pack_state(c, orbs)
 
 
-def measured_peaks():
+def measured_peaks(sustained=False):
+    """(HBM GB/s, bf16 TFLOP/s, source).  sustained: the bf16 figure of a
+    seconds-long GEMM loop under the power cap, the denominator for a kernel
+    timed inside a long step; otherwise the burst figure."""
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
-        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
-    return 6800.0, 1900.0, "fallback"
+        key = "bf16_tflops_sustained" if sustained and "bf16_tflops_sustained" in d else "bf16_tflops"
+        return d.get("hbm_gbs", 6800.0), d.get(key, 1900.0), f"measured ({key})"
+    return 6800.0, 1700.0 if sustained else 1900.0, "fallback"
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu / /proc/cpuinfo), or the machine type."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
 
 
 class ClockSampler:
@@ -200,6 +223,51 @@ def oracle_traj_steps(specs, cfg, n_threads, budget_s, max_traj=None):
     return steps, el, used
 
 
+def _oracle_traj_worker(job):
+    """One trajectory of the CPU port on one host core: set-up and one untimed
+    step, then `steps` timed Strang steps.  Returns (steps, seconds)."""
+    sp, seed, dt, K, steps = job
+    os.environ["OMP_NUM_THREADS"] = "1"
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, ROOT)
+    from oracle import Oracle
+    o = Oracle(sp, n_threads=1)
+    m = o.metric_weights()
+    st = initial_state(sp, o.x, o.w, seed)
+    st = o.propagate_split2(st, 0.0, dt, krylov_dim=K, metric=m)
+    t = dt
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        st = o.propagate_split2(st, t, t + dt, krylov_dim=K, metric=m)
+        t += dt
+    return steps, time.perf_counter() - t0
+
+
+def oracle_parallel_traj_steps(specs, cfg, n_workers, n_sample=64, steps=2):
+    """Trajectory-parallel throughput of the CPU port: a sample of n_sample
+    trajectories spread evenly over the workload (every len/n_sample-th), one
+    trajectory per worker process and host core (one OpenMP thread each),
+    largest first.  Throughput = n_workers x (timed steps / summed
+    single-core seconds), the rate of n_workers cores that stay busy.
+    Returns (value, dict describing the sample)."""
+    import multiprocessing as mp
+    stride = max(1, len(specs) // n_sample)
+    idx = list(range(0, len(specs), stride))[:n_sample]
+    cost = lambda sp: sp.n_grid ** 2 * sp.n_orbs[0] ** 2 + sp.n_grid * sp.n_orbs[0] ** 4
+    idx.sort(key=lambda i: -cost(specs[i]))
+    jobs = [(specs[i], cfg["seed"] + i, cfg["dt"], cfg["krylov"], steps) for i in idx]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(n_workers) as pool:
+        res = pool.map(_oracle_traj_worker, jobs, chunksize=1)
+    wall = time.perf_counter() - t0
+    n_steps = sum(r[0] for r in res)
+    core_s = sum(r[1] for r in res)
+    value = n_workers * n_steps / core_s
+    return value, {"trajectories": len(idx), "steps_per_trajectory": steps, "timed_steps": n_steps,
+                   "core_seconds": core_s, "wall_seconds": wall}
+
+
 def run_reference(args):
     """The reference's algorithm on the host CPU (the oracle port; the Fortran
     reference cannot be built in this environment), on the workload's trajectories."""
@@ -207,18 +275,28 @@ def run_reference(args):
     if rank != 0:
         return 0
     specs, cfg = workload(args.workload)
-    budget = 60.0
-    steps, el, used = oracle_traj_steps(specs, cfg, os.cpu_count(), budget)
-    val = steps / el
+    cores = os.cpu_count()
+    if len(specs) > 1:
+        val, smp = oracle_parallel_traj_steps(specs, cfg, cores)
+        steps, el = smp["timed_steps"], smp["core_seconds"] / cores
+        form = "CPU port of the reference algorithm (FP64), one trajectory per host core"
+        sample = (f"{smp['timed_steps']} Strang steps over {smp['trajectories']} trajectories spread over "
+                  f"{args.workload} ({smp['steps_per_trajectory']} timed steps each after one untimed), one "
+                  f"trajectory per worker process on {cores} cores of {cpu_model()}: {cores} x steps / "
+                  f"{smp['core_seconds']:.1f} summed core-seconds ({smp['wall_seconds']:.1f} s wall)")
+    else:
+        steps, el, used = oracle_traj_steps(specs, cfg, cores, 60.0)
+        val = steps / el
+        form = "CPU port of the reference algorithm (FP64), one trajectory on all host threads"
+        sample = f"{steps} Strang steps of {args.workload} on {cores} host threads of {cpu_model()}"
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
         "warmup": 0, "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "complex128", "data": "synthetic (seeded Gaussian orbitals, random CI vector)",
         "config": {"workload": args.workload, "trajectories": len(specs), "krylov_order": cfg["krylov"],
-                   "dt": cfg["dt"], "form": "CPU port of the reference algorithm (FP64), one trajectory at a time"},
-        "cpu_baseline": {"value": val, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"{steps} Strang steps over the first {used} trajectories of {args.workload} "
-                                   f"on {os.cpu_count()} host threads"},
+                   "dt": cfg["dt"], "form": form},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "cpu": cpu_model(),
+                         "sample": sample},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -291,13 +369,23 @@ def batch_norms(b, packed):
     return np.array([np.linalg.norm(packed[b.offsets[i]:b.offsets[i] + b.systems[i].nC]) for i in range(len(b))])
 
 
-def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=False, e2e=True, acc_steps=0, window=0):
+def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=False, e2e=True, acc_steps=0, window=0,
+                  tune=True):
     from codyfortran_gb300.engine import Batch, pinned_empty
     dt, K = cfg["dt"], cfg["krylov"]
     b = Batch(specs, precision, max_krylov=K, krylov_window=window)
     states = [initial_state(sp, s.x, s.w, cfg["seed"] + k) for k, (sp, s) in enumerate(zip(specs, b.systems))]
     host = b.pack(states)
     b.upload(host)
+    tiles = None
+    if tune:
+        # the project's tile autotuner on the batch's own shapes (outside the timed region)
+        t0 = time.perf_counter()
+        heuristic = b.tiles()
+        rep = b.autotune()
+        tiles = {"tiles": "autotuned", "source": rep["source"], "table": rep["tiles"], "heuristic": heuristic,
+                 "seconds": time.perf_counter() - t0}
+        b.upload(host)
     t = 0.0
     b.propagate(t, dt, warmup, K)
     t += warmup * dt
@@ -324,7 +412,7 @@ def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=Fals
     n_dom, ms_dom = b.profile_end() if dom else (0, 0.0)
     launches = b.launch_count()
     out = dict(ms=ms, fam_ms=fam_ms, dom=dom, n_dom=n_dom, ms_dom=ms_dom, launches=launches,
-               clocks=clk.summary() if clk else None, systems=b.systems, kps=b.kernels_per_step())
+               clocks=clk.summary() if clk else None, systems=b.systems, kps=b.kernels_per_step(), tiles=tiles)
     if e2e:
         # end to end through the C ABI: packed host states in, one step, packed
         # states out, from and to page-locked host memory (cgpu_host_alloc)
@@ -350,6 +438,63 @@ def run_batch_leg(specs, cfg, precision, steps, warmup, profile=True, clock=Fals
         out["acc_norm"] = batch_norms(b, b.download_packed())
     b.close()
     return out
+
+
+def accuracy_horizon(specs, cfg, precision, n_steps, every=10, window=1):
+    """Deviation of a mixed-precision batch from the same batch in the FP64 form
+    (the reference's full Krylov loop), both advanced from the same states for
+    n_steps steps: every `every` steps the per-trajectory relative energy
+    deviation |E_mixed - E_fp64| / |E_fp64|, the absolute one |E_mixed - E_fp64|
+    (Hartree), the one against max(|E_fp64|, 1 Hartree) and the norm deviation
+    | ||C_mixed|| - ||C_fp64|| |.  Returns rows (step, max, median, p99 of the
+    relative energy deviation, max norm deviation, trajectory of the max,
+    |E_fp64| of that trajectory, max absolute deviation, max deviation against
+    max(|E|, 1))."""
+    from codyfortran_gb300.engine import Batch
+    K, dt = cfg["krylov"], cfg["dt"]
+    f = Batch(specs, "fp64", max_krylov=K, krylov_window=0)
+    m = Batch(specs, precision, max_krylov=K, krylov_window=window)
+    states = [initial_state(sp, s.x, s.w, cfg["seed"] + k) for k, (sp, s) in enumerate(zip(specs, f.systems))]
+    host = f.pack(states)
+    f.upload(host)
+    m.upload(host)
+    rows, t = [], 0.0
+    for step in range(every, n_steps + 1, every):
+        f.propagate(t, dt, every, K)
+        m.propagate(t, dt, every, K)
+        t += every * dt
+        ef, em = f.energies(t), m.energies(t)
+        da = np.abs(em - ef)
+        de = da / np.abs(ef)
+        dn = np.abs(batch_norms(m, m.download_packed()) - batch_norms(f, f.download_packed()))
+        w = int(np.argmax(de))
+        rows.append((step, float(de.max()), float(np.median(de)), float(np.quantile(de, 0.99)), float(dn.max()), w,
+                     float(abs(ef[w])), float(da.max()), float((da / np.maximum(np.abs(ef), 1.0)).max())))
+    f.close()
+    m.close()
+    return rows
+
+
+def run_accuracy_horizon(args):
+    """--accuracy-horizon N: the per-step deviation table of accuracy_horizon on the
+    first --accuracy-trajectories trajectories of the workload, as one JSON line."""
+    specs, cfg = workload(args.workload)
+    precision = args.precision or "mixed_fx6"
+    n = min(args.accuracy_trajectories, len(specs))
+    from codyfortran_gb300 import build as B
+    B.build()
+    t0 = time.perf_counter()
+    rows = accuracy_horizon(specs[:n], cfg, precision, args.accuracy_horizon, args.accuracy_every,
+                            krylov_window(args, precision))
+    print(json.dumps({"mode": "accuracy_horizon", "workload": args.workload, "precision": precision,
+                      "trajectories": n, "steps": args.accuracy_horizon, "dt": cfg["dt"], "krylov_order": cfg["krylov"],
+                      "energy_rel_max": max(r[1] for r in rows), "norm_abs_max": max(r[4] for r in rows),
+                      "energy_abs_max": max(r[7] for r in rows), "energy_rel_floor1_max": max(r[8] for r in rows),
+                      "seconds": time.perf_counter() - t0,
+                      "columns": ["step", "energy_rel_max", "energy_rel_median", "energy_rel_p99", "norm_abs_max",
+                                  "worst_trajectory", "worst_abs_energy", "energy_abs_max", "energy_rel_floor1_max"],
+                      "rows": rows}))
+    return 0
 
 
 def krylov_window(args, precision):
@@ -408,8 +553,9 @@ def run_batch(args):
                     "norm_abs_max": float(dN.max()), "norm_abs_median": float(np.median(dN)),
                     "target": 1e-8, "reference": "same batch, plain FP64 form on the GPU (parity-tested against "
                                                   "the CPU port to 1e-12)"}
-    # roofline of the dominant kernel family
-    hbm, bf16, src = measured_peaks()
+    # roofline of the dominant kernel family, timed inside seconds of steps:
+    # the sustained bf16 figure is its tensor denominator
+    hbm, bf16, src = measured_peaks(sustained=True)
     dom, n_dom = r["dom"], max(r["n_dom"], 1)
     avg_s = r["ms_dom"] / n_dom / 1e3
     systems = r["systems"]
@@ -443,6 +589,7 @@ def run_batch(args):
         "config": {"workload": args.workload, "trajectories": n, "krylov_order": cfg["krylov"], "dt": cfg["dt"],
                    "precision": precision, "krylov_reorthogonalisation": window_name(window),
                    "parallelism": f"batch of {n} per GPU, replicas x{world}",
+                   "tiles": "autotuned", "tile_table": r["tiles"],
                    "n_grid_range": [min(s.nG for s in systems), max(s.nG for s in systems)],
                    "n_determinants_range": [min(s.nC for s in systems), max(s.nC for s in systems)],
                    "l2": f"per-step working set {sum(s.nS for s in systems) * 16 * (cfg['krylov'] + 8) / 1e9:.1f} GB "
@@ -464,10 +611,14 @@ def run_batch(args):
         "kernel_ms_per_step": {k: v[1] for k, v in r["fam_ms"].items()},
     }
     if rank == 0 and not args.no_cpu_baseline:
-        steps_cpu, el, used = oracle_traj_steps(specs, cfg, os.cpu_count(), args.cpu_budget)
-        line["cpu_baseline"] = {"value": steps_cpu / el, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"{steps_cpu} Strang steps over the first {used} trajectories "
-                                          f"({el:.1f} s, one trajectory at a time)"}
+        cores = os.cpu_count()
+        val, smp = oracle_parallel_traj_steps(specs, cfg, cores, n_sample=32, steps=1)
+        line["cpu_baseline"] = {
+            "value": val, "unit": UNIT, "cores": cores, "kind": "port", "cpu": cpu_model(),
+            "sample": f"{smp['timed_steps']} Strang steps over {smp['trajectories']} trajectories spread over "
+                      f"{args.workload}, one trajectory per worker process and core (one OpenMP thread each): "
+                      f"{cores} x steps / {smp['core_seconds']:.1f} summed core-seconds "
+                      f"({smp['wall_seconds']:.1f} s wall)"}
     if rank == 0:
         print(json.dumps(line))
     return 0
@@ -520,6 +671,10 @@ def run_single(args):
     st = initial_state(sp, e.x, e.w, cfg["seed"])
     dt, K = cfg["dt"], cfg["krylov"]
     e.upload(st)
+    heuristic = e.tiles()
+    rep = e.autotune()
+    tiles = {"tiles": "autotuned", "source": rep["source"], "table": rep["tiles"], "heuristic": heuristic}
+    e.upload(st)
     t = 0.0
     graph = not args.no_graph
     e.propagate_resident(t, dt, args.warmup, K, use_metric=True, use_graph=graph)
@@ -555,7 +710,7 @@ def run_single(args):
         t += dt
     te = barrier_max(time.perf_counter() - te0, world)
     e2e = world * n_e2e / te
-    hbm, bf16, src = measured_peaks()
+    hbm, bf16, src = measured_peaks(sustained=True)
     nG, P, Q, nC = e.nG, e.nOS * (e.nOS + 1) // 2, e.nOS * e.nOS, e.nC
     avg_s = (ms_dom / max(n_dom, 1)) / 1e3
     if dom == "pair_potentials":
@@ -578,6 +733,7 @@ def run_single(args):
         "config": {"workload": args.workload, "n_grid": nG, "n_orbitals": e.nOS, "n_determinants": nC,
                    "krylov_order": K, "dt": dt, "precision": precision,
                    "krylov_reorthogonalisation": window_name(window), "parallelism": f"replicas x{world}",
+                   "tiles": "autotuned", "tile_table": tiles,
                    "l2": "inputs larger than L2, no flush"},
         "clocks": clk.summary(),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": e.nS * 16, "d2h_bytes_per_step": e.nS * 16,
@@ -612,6 +768,10 @@ def main():
     ap.add_argument("--no-fp64-leg", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=25.0)
     ap.add_argument("--no-graph", action="store_true", help="launch kernels one by one instead of a step graph")
+    ap.add_argument("--accuracy-horizon", type=int, default=0,
+                    help="instead of timing: per-step deviation of the mixed form from FP64 over this many steps")
+    ap.add_argument("--accuracy-trajectories", type=int, default=32)
+    ap.add_argument("--accuracy-every", type=int, default=10)
     ap.add_argument("--krylov-window", type=int, default=None,
                     help="0: Gram-Schmidt against all Krylov vectors; 1: three-term recurrence; k > 1: against the "
                          "last k (default 0 for fp64, 1 otherwise)")
@@ -620,6 +780,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.accuracy_horizon:
+        return run_accuracy_horizon(args)
     rank, world, local = dist_info()
     if world > 1:
         import torch.distributed as dist

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <array>
 #include <string>
 #include <vector>
 
@@ -289,6 +290,7 @@ struct CiView {
 };
 
 struct MixedBufs;  // mixed-precision operand layout (k_mixed.cu)
+struct McAdjoint;  // MCTDHF pulse-gradient buffers (k_adjoint_mc.cu)
 
 // Laser parameters as the device sees them (E(t) is evaluated in the kernels so
 // that a captured step can be replayed at any time).
@@ -425,6 +427,7 @@ struct cgpu_ctx {
   z_t* partial_d = nullptr;
   size_t partialCap = 0;                      // complex entries per trajectory
   int lzBlocks = 148;                         // blocks per trajectory of the Lanczos reductions
+  int lzBlocksHeur = 148, lzBlocksCap = 148;  // the set-up heuristic's count and the most the partials hold
   int lzElems = 1;                            // state entries per thread and chunk in those blocks
   int redBlocks = 148;                        // blocks per trajectory of the Gram reductions
   z_t *gram_d = nullptr;                      // (nOS, nOS)
@@ -461,6 +464,8 @@ struct cgpu_ctx {
   std::string lastError;
   long launches = 0;  // kernels launched by this context (since the last reset)
   MixedBufs* mixed = nullptr;
+  z_t* sysTmp_d = nullptr;  // three nG-point vectors of the Sys* entry points (first use)
+  McAdjoint* mcAdj = nullptr;  // MCTDHF pulse gradient: checkpoints and work buffers (first use)
   // profiling: CUDA events around every launch of one kernel family
   int profTarget = 0;
   std::vector<cudaEvent_t> profEvents;  // start/stop pairs
@@ -523,6 +528,13 @@ void batch_copy(cgpu_ctx* c, void* dst, const void* src, size_t bytes);
 
 // k_onebody.cu
 void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha, int accumulate);
+void launch_field(cgpu_ctx* c, double* E, double t);  // E(t) of every trajectory into its slot E
+// k_sys.cu: one orbital of a single-system context (the Sys* procedure pointers)
+void sys_kinetic(cgpu_ctx* c, z_t* out, const z_t* in, int btBlock);
+void sys_potential(cgpu_ctx* c, z_t* V, double t);
+void sys_multiply(cgpu_ctx* c, z_t* out, const z_t* a, const z_t* b);
+void sys_interaction_src(cgpu_ctx* c, z_t* src, const z_t* a, const z_t* b);
+void sys_interaction_potential(cgpu_ctx* c, z_t* W, const z_t* src);
 void launch_project_orbs(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs);
 void launch_project_coeffs(cgpu_ctx* c, z_t* dC, const z_t* C);
 void launch_fill_h1_from(cgpu_ctx* c, const z_t* orbs, const z_t* hOrbs, z_t* h1);
@@ -561,6 +573,34 @@ void mixed_init(cgpu_ctx* c);
 void mixed_free(cgpu_ctx* c);
 int mixed_error(cgpu_ctx* c);
 void launch_correlation_mixed(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2);
+// Tile tuner hooks of the fixed-point contractions.  A tile table t[9] holds,
+// for W = V S, Z = W R'' and h2 = S^T W in turn: N-tile width, compact (two
+// CTAs per SM) flag, K splits.  fx_tiles_get returns false outside the
+// fixed-point forms; fx_tiles_set validates and rebuilds the tile lists;
+// fx_time_contraction times GEMM g (with its K-split reduction) on the
+// operands in the arena, ms per launch.
+bool fx_tiles_get(const cgpu_ctx* c, int* t);
+void fx_tiles_set(cgpu_ctx* c, const int* t);
+void fx_tile_candidates(const cgpu_ctx* c, int g, std::vector<std::array<int, 3>>& out);
+double fx_time_contraction(cgpu_ctx* c, int g, int reps);
+// ctx.cu: device ms of the Lanczos family over one fixed-order SIL half step
+// (OrbsLin, krylov vectors) on a scratch copy of the resident states; drops the
+// captured step graph (tile and block choices are baked into it).
+double time_sil_lanczos(cgpu_ctx* c, int krylov);
+void drop_step_graph(cgpu_ctx* c);
+// ctx.cu: the time derivative `which` of every trajectory's state `in` into `out`.
+void td_device_public(cgpu_ctx* c, int which, z_t* out, const z_t* in, double t);
+// autotune.cu: the tile table t[10] (fx_tiles_get's nine entries, zero outside
+// the fixed-point forms, then the Lanczos blocks per trajectory), and the tuner.
+void tiles_get(const cgpu_ctx* c, int* t);
+void tiles_set(cgpu_ctx* c, const int* t);
+void autotune_run(cgpu_ctx* c, const char* cachePath, int force, std::string& report);
+// k_adjoint_mc.cu: the MCTDHF pulse gradient (host states, field[nT]); the
+// forward keeps checkpoints in the context for the backward sweep.
+void mc_adjoint_forward(cgpu_ctx* c, const z_t* state0_h, const z_t* ref_h, const double* field_h, int nT, double dt,
+                        int K, int checkpoint, double* J, double* overlap, z_t* final_h);
+void mc_adjoint_backward(cgpu_ctx* c, double* grad_h);
+void mc_adjoint_free(cgpu_ctx* c);
 // k_adjoint.cu
 void adjoint_tdci(cgpu_ctx* c, const z_t* C0_h, const double* E_h, int nT, double dt, int K, double* J,
                   double* aOut, z_t* CN_h, double* grad_h);

@@ -513,9 +513,14 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
     size_t need = ((size_t)c->nS + chunk - 1) / chunk;
     size_t cap = nSys == 1 ? 4 * 148 : std::max<size_t>(2, 4096 / (size_t)nSys);
     c->lzBlocks = (int)std::max<size_t>(1, std::min(cap, need));
+    // the partials hold twice as many blocks (room for the tile tuner)
+    c->lzBlocksHeur = c->lzBlocks;
+    c->lzBlocksCap = (int)std::max<size_t>(1, std::min(need, (size_t)2 * c->lzBlocks));
   }
+  c->lzBlocks = c->lzBlocksCap;
   c->partialCap = std::max({lanczos_partial_need(c), gram_partial_need(c, c->nOS), zgemm_partial_need(c),
                             (size_t)148});
+  c->lzBlocks = c->lzBlocksHeur;
   // arena
   c->bs = layout(c, nullptr);
   size_t total = c->bs * (size_t)nSys;
@@ -603,6 +608,7 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
 
 void free_ctx(cgpu_ctx* c) {
   mixed_free(c);
+  mc_adjoint_free(c);
   if (c->stepGraph) cudaGraphExecDestroy(c->stepGraph);
   for (cudaEvent_t e : c->profEvents) cudaEventDestroy(e);
   for (SysHost& s : c->sys) {
@@ -617,7 +623,7 @@ void free_ctx(cgpu_ctx* c) {
     if (s.samples_d) cudaFree(s.samples_d);
   }
   void* ptrs[] = {c->arena,      c->shape_d,     c->metricUser_d, c->stageOff_d, c->stage_d,
-                  c->tStage_d,    c->applyWork_d, c->rdmWork_d,    c->pairWork_d};
+                  c->tStage_d,    c->applyWork_d, c->rdmWork_d,    c->pairWork_d,  c->sysTmp_d};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->lz_h) cudaFreeHost(c->lz_h);
@@ -838,6 +844,40 @@ void capture_step_graph(cgpu_ctx* c, double t0, double dt, int krylov, int useMe
   c->graphMetric = useMetric;
   c->graphAbsorb = c->absorbEachStep;
 }
+
+}  // namespace
+
+void td_device_public(cgpu_ctx* c, int which, z_t* out, const z_t* in, double t) {
+  td_device(c, which, out, in, t, zmk(0.0, 1.0));
+}
+
+void drop_step_graph(cgpu_ctx* c) {
+  if (c->stepGraph) {
+    cudaGraphExecDestroy(c->stepGraph);
+    c->stepGraph = nullptr;
+  }
+  c->graphDt = 0.0;
+}
+
+double time_sil_lanczos(cgpu_ctx* c, int krylov) {
+  drop_step_graph(c);
+  batch_copy(c, c->warm_d, c->state_d, sizeof(z_t) * c->nS);
+  c->profTarget = CGPU_KERNEL_LANCZOS;
+  c->profUsed = 0;
+  sil_device(c, CGPU_TD_ORBS_LIN, c->warm_d, 0.0, 0.005, krylov, 0.0, 0, c->metricW_d);
+  CODY_CUDA(cudaStreamSynchronize(c->stream));
+  double tot = 0.0;
+  for (size_t i = 0; i + 1 < c->profUsed; i += 2) {
+    float ms = 0.f;
+    CODY_CUDA(cudaEventElapsedTime(&ms, c->profEvents[i], c->profEvents[i + 1]));
+    tot += ms;
+  }
+  c->profTarget = 0;
+  c->profUsed = 0;
+  return tot;
+}
+
+namespace {
 
 // Step start time of every trajectory (t0s has nb entries): one contiguous
 // copy and a kernel that writes each trajectory's slot (a strided copy of nb
@@ -1808,6 +1848,151 @@ int cgpu_batch_profile_begin(cgpu_batch* b, int kernel) {
 int cgpu_batch_profile_end(cgpu_batch* b, long* launches, double* total_ms) {
   if (!b || !b->c) return fail(nullptr, "null batch", CGPU_ERR_ARG);
   return cgpu_profile_end(b->c, launches, total_ms);
+}
+
+// ---- Sys* operators on one orbital ------------------------------------------
+}  // extern "C"
+
+namespace {
+// Three nG-point device vectors for the Sys* entry points (allocated on first use).
+z_t* sys_scratch(cgpu_ctx* c) {
+  if (c->nb != 1) throw std::string("Sys* operators: a single-system context");
+  if (!c->sysTmp_d) CODY_CUDA(cudaMalloc(&c->sysTmp_d, sizeof(z_t) * 3 * (size_t)c->nG));
+  return c->sysTmp_d;
+}
+}  // namespace
+
+extern "C" {
+
+int cgpu_sys_kinetic_multiply(cgpu_ctx* c, cgpu_complex* d_orb, const cgpu_complex* orb, double time, int bt) {
+  CODY_API_BEGIN(c)
+  (void)time;  // the kinetic operators are time independent (src/SysKinetic/M_SysKinetic.f90:139)
+  if (!d_orb || !orb) throw std::string("sys_kinetic_multiply: null array");
+  const int b = bt <= 0 ? 0 : bt - 1;
+  if (b >= c->nBt) throw std::string("sys_kinetic_multiply: body type out of range");
+  z_t* v = sys_scratch(c);
+  up(c, v, orb, c->nG);
+  sys_kinetic(c, v + c->nG, v, c->restricted ? 0 : b);
+  down(c, d_orb, v + c->nG, c->nG);
+  sync(c);
+  CODY_API_END(c)
+}
+
+int cgpu_sys_potential_fill(cgpu_ctx* c, cgpu_complex* potential, double time, int bt) {
+  CODY_API_BEGIN(c)
+  if (!potential) throw std::string("sys_potential_fill: null array");
+  if (bt > c->nBt) throw std::string("sys_potential_fill: body type out of range");
+  z_t* v = sys_scratch(c);
+  sys_potential(c, v, time);
+  down(c, potential, v, c->nG);
+  sync(c);
+  CODY_API_END(c)
+}
+
+int cgpu_sys_potential_multiply(cgpu_ctx* c, cgpu_complex* d_orb, const cgpu_complex* potential,
+                                const cgpu_complex* orb) {
+  CODY_API_BEGIN(c)
+  if (!d_orb || !potential || !orb) throw std::string("sys_potential_multiply: null array");
+  z_t* v = sys_scratch(c);
+  up(c, v, potential, c->nG);
+  up(c, v + c->nG, orb, c->nG);
+  sys_multiply(c, v + 2 * c->nG, v, v + c->nG);
+  down(c, d_orb, v + 2 * c->nG, c->nG);
+  sync(c);
+  CODY_API_END(c)
+}
+
+int cgpu_sys_interaction_src(cgpu_ctx* c, cgpu_complex* src, const cgpu_complex* orb_conjg, const cgpu_complex* orb) {
+  CODY_API_BEGIN(c)
+  if (!src || !orb_conjg || !orb) throw std::string("sys_interaction_src: null array");
+  z_t* v = sys_scratch(c);
+  up(c, v, orb_conjg, c->nG);
+  up(c, v + c->nG, orb, c->nG);
+  sys_interaction_src(c, v + 2 * c->nG, v, v + c->nG);
+  down(c, src, v + 2 * c->nG, c->nG);
+  sync(c);
+  CODY_API_END(c)
+}
+
+int cgpu_sys_interaction_potential(cgpu_ctx* c, cgpu_complex* potential, const cgpu_complex* src, double time,
+                                   int bt1, int bt2) {
+  CODY_API_BEGIN(c)
+  (void)time;  // the soft-Yukawa interaction is time independent
+  if (!potential || !src) throw std::string("sys_interaction_potential: null array");
+  if (!c->hasInteraction) throw std::string("sys_interaction_potential: the context has no interaction");
+  if (bt1 > c->nBt || bt2 > c->nBt) throw std::string("sys_interaction_potential: body type out of range");
+  z_t* v = sys_scratch(c);
+  up(c, v, src, c->nG);
+  sys_interaction_potential(c, v + c->nG, v);
+  down(c, potential, v + c->nG, c->nG);
+  sync(c);
+  CODY_API_END(c)
+}
+
+int cgpu_sys_interaction_multiply(cgpu_ctx* c, cgpu_complex* res, const cgpu_complex* potential,
+                                  const cgpu_complex* orb) {
+  return cgpu_sys_potential_multiply(c, res, potential, orb);
+}
+
+// ---- MCTDHF pulse gradient -------------------------------------------------
+int cgpu_mc_adjoint_forward(cgpu_ctx* c, const cgpu_complex* state0, const cgpu_complex* ref_state,
+                            const double* field, int n_steps, double dt, int krylov_dim, int checkpoint,
+                            double* objective, double* overlap, cgpu_complex* state_final) {
+  CODY_API_BEGIN(c)
+  if (!state0 || !field) throw std::string("mc_adjoint_forward: null array");
+  mc_adjoint_forward(c, (const z_t*)state0, (const z_t*)ref_state, field, n_steps, dt, krylov_dim, checkpoint,
+                     objective, overlap, (z_t*)state_final);
+  CODY_API_END(c)
+}
+
+int cgpu_mc_adjoint_backward(cgpu_ctx* c, double* d_objective) {
+  CODY_API_BEGIN(c)
+  if (!d_objective) throw std::string("mc_adjoint_backward: null array");
+  mc_adjoint_backward(c, d_objective);
+  CODY_API_END(c)
+}
+
+// ---- tile autotuner -------------------------------------------------------
+int cgpu_autotune(cgpu_ctx* c, const char* cache_path, int mode, char* report, int report_len) {
+  CODY_API_BEGIN(c)
+  if (mode != CGPU_TUNE_CACHED && mode != CGPU_TUNE_FORCE) throw std::string("autotune: unknown mode");
+  std::string rep;
+  autotune_run(c, cache_path, mode == CGPU_TUNE_FORCE, rep);
+  sync(c);
+  if (report && report_len > 0) {
+    std::strncpy(report, rep.c_str(), (size_t)report_len - 1);
+    report[report_len - 1] = '\0';
+  }
+  CODY_API_END(c)
+}
+
+int cgpu_get_tiles(const cgpu_ctx* c, int* tiles) {
+  if (!c || !tiles) return fail(nullptr, "get_tiles: null argument", CGPU_ERR_ARG);
+  tiles_get(c, tiles);
+  return CGPU_OK;
+}
+
+int cgpu_set_tiles(cgpu_ctx* c, const int* tiles) {
+  CODY_API_BEGIN(c)
+  if (!tiles) throw std::string("set_tiles: null table");
+  tiles_set(c, tiles);
+  sync(c);
+  CODY_API_END(c)
+}
+
+int cgpu_batch_autotune(cgpu_batch* b, const char* cache_path, int mode, char* report, int report_len) {
+  if (!b || !b->c) return fail(nullptr, "null batch", CGPU_ERR_ARG);
+  return cgpu_autotune(b->c, cache_path, mode, report, report_len);
+}
+
+int cgpu_batch_get_tiles(const cgpu_batch* b, int* tiles) {
+  if (!b || !b->c) return fail(nullptr, "null batch", CGPU_ERR_ARG);
+  return cgpu_get_tiles(b->c, tiles);
+}
+
+int cgpu_batch_set_tiles(cgpu_batch* b, const int* tiles) {
+  if (!b || !b->c) return fail(nullptr, "null batch", CGPU_ERR_ARG);
+  return cgpu_set_tiles(b->c, tiles);
 }
 
 }  // extern "C"

@@ -417,6 +417,29 @@ static int fx_max_bn(int L, bool compact) {
 
 bool fx_compact_ok(int L) { return fx_max_bn(L, true) > 0; }
 
+void fx_tile_configs(int L, std::vector<std::pair<int, bool>>& out) {
+  out.clear();
+  for (const FxTileCfg& t : kFxTiles)
+    if (t.L == L) out.push_back({t.bn, t.compact});
+}
+
+bool fx_tile_supported(int bn, int L, bool compact) {
+  for (const FxTileCfg& t : kFxTiles)
+    if (t.bn == bn && t.L == L && t.compact == compact) return true;
+  return false;
+}
+
+int fx_min_splits(int kTiles, int digitBits) {
+  const int exact = fx_exact_tiles(digitBits);
+  return std::max(1, (kTiles + exact - 1) / exact);
+}
+
+int fx_normalize_splits(int kTiles, int s) {
+  s = std::max(1, std::min(s, kTiles));
+  const int per = (kTiles + s - 1) / s;
+  return (kTiles + per - 1) / per;
+}
+
 int fx_tile_n(int N, int L, bool compact) {
   const int maxBn = fx_max_bn(L, compact);
   if (maxBn == 0) throw std::string("fx_tile_n: no configuration for this slice count");

@@ -27,6 +27,8 @@
 // epilogue, or from the reduction of its K splits.
 #include <cuda_bf16.h>
 
+#include <array>
+
 #include <algorithm>
 
 #include "common.cuh"
@@ -46,7 +48,8 @@ struct MixedBufs {
   // contractions (GEMM1, GEMM3) and of the K = 2P one (GEMM2)
   int fxBits = 0, b1 = 0, L1 = 0, b2 = 0, L2 = 0;
   int fxBits3 = 0, L3 = 0, LS = 0;  // GEMM3 target and slices; S carries LS = max(L1, L3) slices
-  bool compact2 = false;
+  bool compact1 = false, compact2 = false, compact3 = false;  // two-CTAs-per-SM configuration per GEMM
+  int sCap1 = 1, sCap2 = 1, sCap3 = 1;  // K splits the FP64 partial buffers hold (the tuner stays within them)
   // one interaction matrix per root grid (cgpu_ctx::fxShared): slices [root][c->nG][L1 KgBig]
   // and row exponents [root][c->nG], outside the per-trajectory arena
   // tile lists of the persistent fixed-point GEMMs (device) and their lengths
@@ -600,15 +603,21 @@ size_t mixed_layout(cgpu_ctx* c, char* base, size_t off) {
     m->s1 = fx_split_count(nG, 2 * nP, m->bn1, m->KgMax / 64, c->nb, m->b1);
     m->s2 = fx_split_count(nG, 2 * Q, m->bn2, m->KpMax / 64, c->nb, m->b2);
     m->s3 = fx_split_count(2 * nP, 2 * nP, m->bn3, m->KgMax / 64, c->nb, m->b1);
+    // partial buffers: a single system holds twice the heuristic's K splits
+    // (room for the tile tuner), a batch exactly the heuristic's
+    const int grow = c->nb == 1 ? 2 : 1;
+    m->sCap1 = std::min(m->s1 * grow, m->KgMax / 64);
+    m->sCap2 = std::min(m->s2 * grow, m->KpMax / 64);
+    m->sCap3 = std::min(m->s3 * grow, m->KgMax / 64);
     const size_t perTrajV = c->fxShared ? 0 : 1;
     size_t oV = take(off, perTrajV * sizeof(bf) * (size_t)nG * L1 * m->KgMax);
     size_t oS = take(off, sizeof(bf) * (size_t)2 * nP * m->LS * m->KgMax);
     size_t oW = take(off, sizeof(bf) * (size_t)nG * L2 * m->KpMax);
     size_t oWT = take(off, sizeof(bf) * (size_t)2 * nP * m->L3 * m->KgMax);
     size_t oR = take(off, sizeof(bf) * (size_t)2 * Q * L2 * m->KpMax);
-    size_t oWd = take(off, sizeof(double) * (size_t)m->s1 * nG * 2 * nP);
-    size_t oZp = take(off, m->s2 > 1 ? sizeof(double) * (size_t)m->s2 * nG * 2 * Q : 0);
-    size_t oGd = take(off, sizeof(double) * (size_t)m->s3 * 2 * nP * 2 * nP);
+    size_t oWd = take(off, sizeof(double) * (size_t)m->sCap1 * nG * 2 * nP);
+    size_t oZp = take(off, m->sCap2 > 1 ? sizeof(double) * (size_t)m->sCap2 * nG * 2 * Q : 0);
+    size_t oGd = take(off, sizeof(double) * (size_t)m->sCap3 * 2 * nP * 2 * nP);
     size_t oE = take(off, sizeof(int));
     size_t oZ = take(off, sizeof(double) * (size_t)2 * nG * Q);
     size_t oeV = take(off, perTrajV * sizeof(int) * (size_t)nG);
@@ -625,7 +634,7 @@ size_t mixed_layout(cgpu_ctx* c, char* base, size_t off) {
       m->WTxB = (bf*)(base + oWT);
       m->RxB = (bf*)(base + oR);
       m->Wd = (double*)(base + oWd);
-      m->Zp = m->s2 > 1 ? (double*)(base + oZp) : nullptr;
+      m->Zp = m->sCap2 > 1 ? (double*)(base + oZp) : nullptr;
       m->Gd = (double*)(base + oGd);
       m->err = (int*)(base + oE);
       m->Zd = (double*)(base + oZ);
@@ -741,6 +750,142 @@ int mixed_error(cgpu_ctx* c) {
   return e;
 }
 
+// The three fixed-point contractions with their K-split reductions, on the
+// operands the digit splits left in the arena (one call = one launch of the
+// GEMM, plus the reduction when K is split).
+// W = V S (pair potentials; row / column exponent maxima for the W split).
+static void fx_run_W(cgpu_ctx* c) {
+  MixedBufs* m = c->mixed;
+  const int nG = c->nG, nP = c->nPairs;
+  const bool one = m->s1 == 1;
+  if (c->fxShared)
+    fx_gemm(c, m->L1, m->b1, m->compact1, TC_GEMM_W, m->mVsh, m->mS, m->bn1, m->Wd, m->eVsh, m->eS,
+            one ? m->mWr : nullptr, one ? m->mWc : nullptr, m->KgBig, m->KgMax, 1, m->s1, m->tiles1, m->nTiles1,
+            m->err);
+  else
+    fx_gemm(c, m->L1, m->b1, m->compact1, TC_GEMM_W, m->mV, m->mS, m->bn1, m->Wd, m->eV, m->eS,
+            one ? m->mWr : nullptr, one ? m->mWc : nullptr, m->KgMax, m->KgMax, 0, m->s1, m->tiles1, m->nTiles1,
+            m->err);
+  if (!one) {
+    k_fx_reduce_W<<<bgrid(c, ew_blocks(c, (size_t)nG * 2 * nP)), 256, 0, c->stream>>>(m->Wd, m->mWr, m->mWc, m->s1,
+                                                                                   TRAJ_PASS(c));
+    CODY_LAUNCHED(c);
+  }
+}
+
+// Z = W R'' (the correlation contraction) into Zd.
+static void fx_run_Z(cgpu_ctx* c) {
+  MixedBufs* m = c->mixed;
+  const int nG = c->nG, Q = c->nOS * c->nOS;
+  fx_gemm(c, m->L2, m->b2, m->compact2, TC_GEMM_Z, m->mW, m->mR, m->bn2, m->s2 > 1 ? m->Zp : m->Zd, m->eWr, m->eR,
+          nullptr, nullptr, m->KpMax, m->KpMax, 0, m->s2, m->tiles2, m->nTiles2, m->err);
+  if (m->s2 > 1) {
+    k_reduce_Z<<<bgrid(c, ew_blocks(c, (size_t)nG * Q)), 256, 0, c->stream>>>((z_t*)m->Zd, m->Zp, m->s2,
+                                                                        TRAJ_PASS(c));
+    CODY_LAUNCHED(c);
+  }
+}
+
+// G = S^T W (h2) and its reduction into the spatial h2 block.
+static void fx_run_H2(cgpu_ctx* c) {
+  MixedBufs* m = c->mixed;
+  const int Q = c->nOS * c->nOS;
+  fx_gemm(c, m->L3, m->b1, m->compact3, TC_GEMM_H2, m->mSasB, m->mWT, m->bn3, m->Gd, m->eS, m->eWc, nullptr, nullptr,
+          m->KgMax, m->KgMax, 0, m->s3, m->tiles3, m->nTiles3, m->err);
+  k_reduce_H2<<<bgrid(c, ew_blocks(c, (size_t)Q * Q)), 256, 0, c->stream>>>(c->h2s_d, m->Gd, m->s3, c->pidx_d,
+                                                                      TRAJ_PASS(c));
+  CODY_LAUNCHED(c);
+}
+
+// ---- tile tuner hooks ---------------------------------------------------------
+
+bool fx_tiles_get(const cgpu_ctx* c, int* t) {
+  const MixedBufs* m = c->mixed;
+  if (!m || !m->fxBits) return false;
+  const int v[9] = {m->bn1, m->compact1, m->s1, m->bn2, m->compact2, m->s2, m->bn3, m->compact3, m->s3};
+  for (int i = 0; i < 9; i++) t[i] = v[i];
+  return true;
+}
+
+// Slices, digit width, K blocks, split capacity and output columns of GEMM g.
+static void fx_gemm_plan(const cgpu_ctx* c, int g, int& L, int& b, int& kTiles, int& cap, int& N) {
+  const MixedBufs* m = c->mixed;
+  if (g == TC_GEMM_W) { L = m->L1; b = m->b1; kTiles = m->KgMax / 64; cap = m->sCap1; N = 2 * c->nPairs; }
+  else if (g == TC_GEMM_Z) { L = m->L2; b = m->b2; kTiles = m->KpMax / 64; cap = m->sCap2; N = 2 * c->nOS * c->nOS; }
+  else { L = m->L3; b = m->b1; kTiles = m->KgMax / 64; cap = m->sCap3; N = 2 * c->nPairs; }
+}
+
+void fx_tiles_set(cgpu_ctx* c, const int* t) {
+  MixedBufs* m = c->mixed;
+  if (!m || !m->fxBits) throw std::string("tiles: not a fixed-point context");
+  int bn[3], sp[3];
+  bool cm[3];
+  for (int g = 0; g < 3; g++) {
+    int L, b, kTiles, cap, N;
+    fx_gemm_plan(c, g, L, b, kTiles, cap, N);
+    bn[g] = t[3 * g];
+    cm[g] = t[3 * g + 1] != 0;
+    if (!fx_tile_supported(bn[g], L, cm[g])) throw std::string("tiles: no fixed-point GEMM configuration for that tile");
+    if (t[3 * g + 2] < 1 || t[3 * g + 2] > kTiles) throw std::string("tiles: K split count outside 1..K blocks");
+    sp[g] = fx_normalize_splits(kTiles, t[3 * g + 2]);
+    // every split keeps at least two K blocks, as the set-up heuristic does
+    if (sp[g] < fx_min_splits(kTiles, b) || sp[g] > cap || (sp[g] > 1 && sp[g] > kTiles / 2))
+      throw std::string("tiles: K split outside the exact range of the digits or the partial buffers");
+  }
+  void** lists[3] = {&m->tiles1, &m->tiles2, &m->tiles3};
+  int* counts[3] = {&m->nTiles1, &m->nTiles2, &m->nTiles3};
+  CODY_CUDA(cudaStreamSynchronize(c->stream));
+  for (int g = 0; g < 3; g++) {
+    if (*lists[g]) CODY_CUDA(cudaFree(*lists[g]));
+    *lists[g] = fx_build_tiles(c, g, bn[g], sp[g], counts[g]);
+  }
+  m->bn1 = bn[0]; m->compact1 = cm[0]; m->s1 = sp[0];
+  m->bn2 = bn[1]; m->compact2 = cm[1]; m->s2 = sp[1];
+  m->bn3 = bn[2]; m->compact3 = cm[2]; m->s3 = sp[2];
+}
+
+void fx_tile_candidates(const cgpu_ctx* c, int g, std::vector<std::array<int, 3>>& out) {
+  out.clear();
+  if (!c->mixed || !c->mixed->fxBits) return;
+  int L, b, kTiles, cap, N;
+  fx_gemm_plan(c, g, L, b, kTiles, cap, N);
+  std::vector<std::pair<int, bool>> cfgs;
+  fx_tile_configs(L, cfgs);
+  std::vector<int> splits;
+  for (int s : {1, 2, 3, 4, cap}) {
+    int v = fx_normalize_splits(kTiles, s);
+    if (v >= fx_min_splits(kTiles, b) && v <= cap && (v == 1 || v <= kTiles / 2) &&
+        std::find(splits.begin(), splits.end(), v) == splits.end())
+      splits.push_back(v);
+  }
+  for (const auto& cf : cfgs) {
+    if (cf.first >= 2 * ((N + 15) / 16 * 16)) continue;  // wider than twice the output: idle MMA columns only
+    for (int v : splits) out.push_back({cf.first, cf.second ? 1 : 0, v});
+  }
+}
+
+double fx_time_contraction(cgpu_ctx* c, int g, int reps) {
+  auto run = [&]() {
+    if (g == TC_GEMM_W) fx_run_W(c);
+    else if (g == TC_GEMM_Z) fx_run_Z(c);
+    else fx_run_H2(c);
+  };
+  run();
+  cudaEvent_t e0, e1;
+  CODY_CUDA(cudaEventCreate(&e0));
+  CODY_CUDA(cudaEventCreate(&e1));
+  CODY_CUDA(cudaEventRecord(e0, c->stream));
+  for (int r = 0; r < reps; r++) run();
+  CODY_CUDA(cudaEventRecord(e1, c->stream));
+  CODY_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  CODY_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (mixed_error(c)) throw std::string("tiles: a fixed-point GEMM reported a wait timeout while timing");
+  return ms / reps;
+}
+
 // The fixed-point form of the three contractions.
 void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
   MixedBufs* m = c->mixed;
@@ -754,19 +899,7 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
     split_s<<<dim3(2 * nP, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(
         m->SxA, m->eS, m->mWr, m->mWc, orbs, c->w_d, c->pairL_d, c->pairK_d, m->KgMax, m->b1, m->LS, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
-    const bool one = m->s1 == 1;
-    if (c->fxShared)
-      fx_gemm(c, m->L1, m->b1, false, TC_GEMM_W, m->mVsh, m->mS, m->bn1, m->Wd, m->eVsh, m->eS,
-              one ? m->mWr : nullptr, one ? m->mWc : nullptr, m->KgBig, m->KgMax, 1, m->s1, m->tiles1, m->nTiles1,
-              m->err);
-    else
-      fx_gemm(c, m->L1, m->b1, false, TC_GEMM_W, m->mV, m->mS, m->bn1, m->Wd, m->eV, m->eS, one ? m->mWr : nullptr,
-              one ? m->mWc : nullptr, m->KgMax, m->KgMax, 0, m->s1, m->tiles1, m->nTiles1, m->err);
-    if (!one) {
-      k_fx_reduce_W<<<bgrid(c, ew_blocks(c, (size_t)nG * 2 * nP)), 256, 0, c->stream>>>(m->Wd, m->mWr, m->mWc, m->s1,
-                                                                                     TRAJ_PASS(c));
-      CODY_LAUNCHED(c);
-    }
+    fx_run_W(c);
     dim3 gw(ceil_div(m->KgMax, SW_T), 1, c->nb);
     // the digit plans of the two fixed-point forms on long grids, compiled in
     auto split_w = k_fx_split_W<0, 0, 0, 0>;
@@ -784,21 +917,12 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
     split_r<<<dim3(2 * Q, 1, c->nb), 64, sizeof(double) * m->KpMax, c->stream>>>(
         m->RxB, m->eR, c->Rp_d, c->pairL_d, c->pairK_d, m->KpMax, m->b2, m->L2, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
-    fx_gemm(c, m->L2, m->b2, m->compact2, TC_GEMM_Z, m->mW, m->mR, m->bn2, m->s2 > 1 ? m->Zp : m->Zd, m->eWr, m->eR,
-            nullptr, nullptr, m->KpMax, m->KpMax, 0, m->s2, m->tiles2, m->nTiles2, m->err);
-    if (m->s2 > 1) {
-      k_reduce_Z<<<bgrid(c, ew_blocks(c, (size_t)nG * Q)), 256, 0, c->stream>>>(Z, m->Zp, m->s2, TRAJ_PASS(c));
-      CODY_LAUNCHED(c);
-    }
+    fx_run_Z(c);
     launch_corr_epilogue(c, dOrbs, orbs, Z);
   }
   if (wantH2) {
     ProfScope prof(c, CGPU_KERNEL_H2);
-    fx_gemm(c, m->L3, m->b1, false, TC_GEMM_H2, m->mSasB, m->mWT, m->bn3, m->Gd, m->eS, m->eWc, nullptr, nullptr,
-            m->KgMax, m->KgMax, 0, m->s3, m->tiles3, m->nTiles3, m->err);
-    k_reduce_H2<<<bgrid(c, ew_blocks(c, (size_t)Q * Q)), 256, 0, c->stream>>>(c->h2s_d, m->Gd, m->s3, c->pidx_d,
-                                                                        TRAJ_PASS(c));
-    CODY_LAUNCHED(c);
+    fx_run_H2(c);
     launch_h2_layout(c);
   }
 }

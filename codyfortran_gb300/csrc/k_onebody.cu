@@ -671,6 +671,13 @@ size_t gram_partial_need(const cgpu_ctx* c, int n) {
   return (size_t)gram_blocks(c, chunk) * n * n;
 }
 
+void launch_field(cgpu_ctx* c, double* E, double t) {
+  const double* base = (c->inCapture || c->useStepTime) ? c->stepT_d : c->zero_d;
+  const double off = c->inCapture ? t - c->captureT0 : t;
+  k_field<<<bgrid(c, 1), 1, 0, c->stream>>>(E, TRAJ_PASS(c), base, off);
+  CODY_LAUNCHED(c);
+}
+
 void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha, int accumulate) {
   ProfScope prof(c, CGPU_KERNEL_ONEBODY);
   // one block per grid tile walking every orbital when the tiles alone fill

@@ -34,7 +34,10 @@ std::mutex g_scratchMutex;
 void* g_scratchAddr[kMaxDevices] = {nullptr};  // device address of g_gram_scratch, per device ordinal
 
 // The host-side name g_gram_scratch is only a stand-in for the device array;
-// its device address is looked up once per device, with that device current.
+// its device address is looked up once per device, with that device current,
+// and kept for the life of the process.  A host that destroys and re-creates
+// the device's primary context (cudaDeviceReset) reloads the module at a new
+// address: calls after such a reset are not supported.
 cudaError_t scratch_address(void** out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -129,6 +132,13 @@ extern "C" int cgpu_weighted_gram_noalloc(const cgpu_complex* a, const cgpu_comp
   cudaError_t e = scratch_address(&scratch);
   if (e != cudaSuccess)
     return fail_noalloc(std::string("cgpu_weighted_gram_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e),
+                        CGPU_ERR_CUDA);
+  // An error left by earlier, unrelated work on this thread is reported as
+  // such and left in place for its owner (cudaGetLastError below would clear it).
+  e = cudaPeekAtLastError();
+  if (e != cudaSuccess)
+    return fail_noalloc(std::string("cgpu_weighted_gram_noalloc: a CUDA error was pending before the call: ") +
+                            cudaGetErrorString(e),
                         CGPU_ERR_CUDA);
   cudaStream_t s = (cudaStream_t)stream;
   int chunk = CGPU_GRAM_NOALLOC_CHUNK;

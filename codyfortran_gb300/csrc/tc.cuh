@@ -3,6 +3,9 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <utility>
+#include <vector>
+
 #include "common.cuh"
 
 // The three contractions of the mixed form; their per-trajectory sizes come
@@ -51,6 +54,13 @@ void fx_plan(int kTiles, int targetBits, int* digitBits, int* slices);
 int fx_tile_n(int N, int L, bool compact);
 // Whether a compact configuration exists for L slices.
 bool fx_compact_ok(int L);
+// The instantiated (N tile width, compact) configurations for L slices.
+void fx_tile_configs(int L, std::vector<std::pair<int, bool>>& out);
+bool fx_tile_supported(int bn, int L, bool compact);
+// Fewest K splits that keep every split inside the exact range of the digits.
+int fx_min_splits(int kTiles, int digitBits);
+// The split count fx_gemm runs for a request of s splits (balanced K blocks per split).
+int fx_normalize_splits(int kTiles, int s);
 // K splits of the fixed-point GEMM: about one wave of 152 SMs, and every split
 // inside the exact range of the level sums at digitBits (2^(24-2b) K).
 int fx_split_count(int M, int N, int BN, int kTiles, int nb, int digitBits);

@@ -39,7 +39,15 @@ EXPORTED = [
     "cgpu_tdci_adjoint", "cgpu_observables", "cgpu_relax", "cgpu_batch_observables", "cgpu_save_restart",
     "cgpu_load_restart", "cgpu_absorber_setup", "cgpu_absorber_apply", "cgpu_batch_absorber_setup",
     "cgpu_batch_save_restart", "cgpu_batch_load_restart",
+    "cgpu_autotune", "cgpu_get_tiles", "cgpu_set_tiles", "cgpu_batch_autotune", "cgpu_batch_get_tiles",
+    "cgpu_batch_set_tiles", "cgpu_sys_kinetic_multiply", "cgpu_sys_potential_fill", "cgpu_sys_potential_multiply",
+    "cgpu_sys_interaction_src", "cgpu_sys_interaction_potential", "cgpu_sys_interaction_multiply",
+    "cgpu_mc_adjoint_forward", "cgpu_mc_adjoint_backward",
 ]
+
+TUNE_CACHED, TUNE_FORCE = 0, 1
+DEFAULT_TILE_CACHE = os.path.join(PKG, "_build", "tile_cache.jsonl")
+TILE_KEYS = ("W", "Z", "H2")
 
 KERNELS = {"pair_potentials": 1, "correlation": 2, "h2": 3, "ci_apply": 4, "ci_rdm": 5, "onebody": 6, "lanczos": 7,
            "rdm_inverse": 8, "projectors": 9, "fold": 10, "vector": 11}
@@ -99,6 +107,10 @@ def load_library(path: str = LIB_PATH):
     lib.cgpu_load_restart.argtypes = [C.c_void_p, C.c_char_p]
     lib.cgpu_batch_save_restart.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
     lib.cgpu_batch_load_restart.argtypes = [C.c_void_p, C.c_char_p]
+    for name in ("cgpu_autotune", "cgpu_batch_autotune"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_char_p, C.c_int]
+    for name in ("cgpu_get_tiles", "cgpu_set_tiles", "cgpu_batch_get_tiles", "cgpu_batch_set_tiles"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     _lib = lib
     return lib
 
@@ -120,6 +132,49 @@ class _PinnedBlock:
         if getattr(self, "_ptr", None):
             self._lib.cgpu_host_free(C.c_void_p(self._ptr))
             self._ptr = None
+
+
+def tiles_to_dict(t):
+    """The 10-entry tile table as {"W": (bn, compact, splits), "Z": ..., "H2": ..., "lz_blocks": n}."""
+    t = [int(v) for v in t]
+    d = {k: tuple(t[3 * i:3 * i + 3]) for i, k in enumerate(TILE_KEYS)}
+    d["lz_blocks"] = t[9]
+    return d
+
+
+def tiles_from_dict(d):
+    t = []
+    for k in TILE_KEYS:
+        t.extend(int(v) for v in d[k])
+    t.append(int(d["lz_blocks"]))
+    return (C.c_int * 10)(*t)
+
+
+class _Tunable:
+    """Tile table and autotuner of a context (cgpu_autotune / cgpu_get_tiles /
+    cgpu_set_tiles), shared by Engine and Batch."""
+
+    _tune_fns = ("cgpu_autotune", "cgpu_get_tiles", "cgpu_set_tiles")
+
+    def autotune(self, cache_path=DEFAULT_TILE_CACHE, force=False):
+        """Time the tile candidates on the resident states and apply the
+        fastest (or the cached entry of this shape); returns the report dict."""
+        import json
+        fn = getattr(self.lib, self._tune_fns[0])
+        buf = C.create_string_buffer(65536)
+        path = None if cache_path is None else str(cache_path).encode()
+        if cache_path is not None:
+            os.makedirs(os.path.dirname(os.path.abspath(str(cache_path))), exist_ok=True)
+        self._check(fn(self.h, path, TUNE_FORCE if force else TUNE_CACHED, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    def tiles(self):
+        t = (C.c_int * 10)()
+        self._check(getattr(self.lib, self._tune_fns[1])(self.h, t))
+        return tiles_to_dict(t)
+
+    def set_tiles(self, d):
+        self._check(getattr(self.lib, self._tune_fns[2])(self.h, tiles_from_dict(d)))
 
 
 def select_device(device):
@@ -181,7 +236,7 @@ def make_desc(spec: SystemSpec, precision: str = "fp64", max_krylov: int = 32, k
     return d, keep
 
 
-class Engine:
+class Engine(_Tunable):
     """The GB300 MCTDHX/TDCI engine for one system (one cgpu_ctx, one CUDA stream)."""
 
     def __init__(self, spec: SystemSpec, precision: str = "fp64", max_krylov: int = 32, krylov_window: int = 0):
@@ -290,6 +345,47 @@ class Engine:
         e = C.c_double()
         self._check(self.lib.cgpu_energy(self.h, _p(s), _d(t), C.byref(e)))
         return e.value
+
+    # Sys* operators on one orbital ---------------------------------------------
+    def _vec(self, a):
+        return np.ascontiguousarray(a, dtype=np.complex128)
+
+    def sys_kinetic_multiply(self, orb, t=0.0, bt=1):
+        """SysKinetic_MultiplyWithKineticOp: T orb with the mass of body type bt (1-based)."""
+        out = np.zeros(self.nG, dtype=np.complex128)
+        self._check(self.lib.cgpu_sys_kinetic_multiply(self.h, _p(out), _p(self._vec(orb)), _d(t), int(bt)))
+        return out
+
+    def sys_potential_fill(self, t=0.0, bt=1):
+        """SysPotential_FillExternalPotential: V(x) + E(t) x."""
+        out = np.zeros(self.nG, dtype=np.complex128)
+        self._check(self.lib.cgpu_sys_potential_fill(self.h, _p(out), _d(t), int(bt)))
+        return out
+
+    def sys_potential_multiply(self, potential, orb):
+        out = np.zeros(self.nG, dtype=np.complex128)
+        self._check(self.lib.cgpu_sys_potential_multiply(self.h, _p(out), _p(self._vec(potential)),
+                                                         _p(self._vec(orb))))
+        return out
+
+    def sys_interaction_src(self, orb_conjg, orb):
+        """SysInteraction_FillInteractionSrc: conj(orb_conjg) orb w."""
+        out = np.zeros(self.nG, dtype=np.complex128)
+        self._check(self.lib.cgpu_sys_interaction_src(self.h, _p(out), _p(self._vec(orb_conjg)), _p(self._vec(orb))))
+        return out
+
+    def sys_interaction_potential(self, src, t=0.0, bt1=1, bt2=1):
+        """SysInteraction_FillInteractionPotential: sum_j K(x_i, x_j) src_j."""
+        out = np.zeros(self.nG, dtype=np.complex128)
+        self._check(self.lib.cgpu_sys_interaction_potential(self.h, _p(out), _p(self._vec(src)), _d(t), int(bt1),
+                                                            int(bt2)))
+        return out
+
+    def sys_interaction_multiply(self, potential, orb):
+        out = np.zeros(self.nG, dtype=np.complex128)
+        self._check(self.lib.cgpu_sys_interaction_multiply(self.h, _p(out), _p(self._vec(potential)),
+                                                           _p(self._vec(orb))))
+        return out
 
     # Coeffs -------------------------------------------------------------------
     def rdm1(self, coeffs):
@@ -445,6 +541,26 @@ class Engine:
         o = self._orbs(orbs)
         self._check(self.lib.cgpu_tdci_set_orbitals(self.h, _p(o)))
 
+    def mc_adjoint_forward(self, state0, field, dt, krylov_dim=12, checkpoint=64, ref_state=None):
+        """MCTDHF pulse objective J = 1 - |<ref|Psi_N>|^2 after len(field)
+        Strang steps with E(t) = field[floor(t / dt)]; keeps checkpoints for
+        mc_adjoint_backward.  Returns (J, overlap, final state)."""
+        s0 = np.ascontiguousarray(state0, dtype=np.complex128)
+        ref = None if ref_state is None else np.ascontiguousarray(ref_state, dtype=np.complex128)
+        f = np.ascontiguousarray(field, dtype=np.float64)
+        self._mc_field_len = len(f)
+        J, ov = C.c_double(), (C.c_double * 2)()
+        fin = np.zeros_like(s0)
+        self._check(self.lib.cgpu_mc_adjoint_forward(self.h, _p(s0), _p(ref), _p(f), len(f), _d(dt), int(krylov_dim),
+                                                     int(checkpoint), C.byref(J), ov, _p(fin)))
+        return J.value, complex(ov[0], ov[1]), fin
+
+    def mc_adjoint_backward(self):
+        """dJ/dfield[n] for the last mc_adjoint_forward."""
+        g = np.zeros(getattr(self, "_mc_field_len", 0))
+        self._check(self.lib.cgpu_mc_adjoint_backward(self.h, _p(g)))
+        return g
+
     def tdci_adjoint(self, c0, field, dt, checkpoint=64, gradient=True):
         """J = 1 - |<c0|C_N>|^2 after len(field) RK4 steps (field constant per
         step) and, with gradient, dJ/dfield from the adjoint sweep.
@@ -468,10 +584,12 @@ class BatchSystem:
         self.x, self.w = x, w
 
 
-class Batch:
+class Batch(_Tunable):
     """Independent systems of arbitrary sizes advanced together: every kernel
     of the step covers all systems in one launch, one CUDA-graph launch per
     time step (cgpu_batch_propagate)."""
+
+    _tune_fns = ("cgpu_batch_autotune", "cgpu_batch_get_tiles", "cgpu_batch_set_tiles")
 
     def __init__(self, specs, precision: str = "fp64", max_krylov: int = 32, krylov_window: int = 0):
         self.lib = load_library()

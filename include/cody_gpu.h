@@ -162,6 +162,34 @@ int cgpu_apply_correlation_op(cgpu_ctx* ctx, cgpu_complex* d_orbs, const cgpu_co
 /* Method_GetEnergy (S_Method_Mb_OrbBased.f90:132-161) of the given state. */
 int cgpu_energy(cgpu_ctx* ctx, const cgpu_complex* state, double time, double* energy);
 
+/* ---- Sys* operators on one orbital (single-system contexts) -------------- */
+/* The procedure pointers a configuration binds when it moves only sysKinetic,
+ * sysPotential or sysInteraction to the GPU; nG-point host arrays.  Body
+ * types are 1-based as in Fortran; 0 stands for an absent optional bt_. */
+/* I_SysKinetic_MultiplyWithKineticOp (src/SysKinetic/M_SysKinetic.f90:141-160):
+ * d_orb = T orb with the mass of body type bt (FEDVR or finite differences). */
+int cgpu_sys_kinetic_multiply(cgpu_ctx* ctx, cgpu_complex* d_orb, const cgpu_complex* orb, double time, int bt);
+/* I_SysPotential_FillExternalPotential (src/SysPotential/M_SysPotential.f90:71-84):
+ * potential = V(x) + E(t) x on the grid (soft-Yukawa nuclei; the 1D
+ * length-gauge laser is carried by the external potential). */
+int cgpu_sys_potential_fill(cgpu_ctx* ctx, cgpu_complex* potential, double time, int bt);
+/* I_SysPotential_MultiplyWithExternalPotential (src/SysPotential/M_SysPotential.f90:89-101):
+ * d_orb = potential * orb point by point. */
+int cgpu_sys_potential_multiply(cgpu_ctx* ctx, cgpu_complex* d_orb, const cgpu_complex* potential,
+                                const cgpu_complex* orb);
+/* I_SysInteraction_FillInteractionSrc (src/SysInteraction/M_SysInteraction.f90:114-128;
+ * src/SysInteraction/Linear/S_SysInteraction_Linear.f90:57-72): src = conj(orb_conjg) orb w. */
+int cgpu_sys_interaction_src(cgpu_ctx* ctx, cgpu_complex* src, const cgpu_complex* orb_conjg, const cgpu_complex* orb);
+/* I_SysInteraction_FillInteractionPotential (src/SysInteraction/M_SysInteraction.f90:94-111):
+ * potential(x_i) = sum_j K(x_i, x_j) src_j with the context's interaction
+ * kernel (CGPU_INT_TOEPLITZ or CGPU_INT_DENSE). */
+int cgpu_sys_interaction_potential(cgpu_ctx* ctx, cgpu_complex* potential, const cgpu_complex* src, double time,
+                                   int bt1, int bt2);
+/* I_SysInteraction_MultiplyWithInteractionPotential (src/SysInteraction/M_SysInteraction.f90:145-157):
+ * res = potential * orb point by point. */
+int cgpu_sys_interaction_multiply(cgpu_ctx* ctx, cgpu_complex* res, const cgpu_complex* potential,
+                                  const cgpu_complex* orb);
+
 /* ---- CI vector (Coeffs pointers) ---------------------------------------- */
 /* I_Coeffs_ApplyH1FillRdm1 (src/Coeffs/M_Coeffs.f90:119-135; Generic :103-178).
  * NULL optional arguments select the mode, as the Fortran optionals do. */
@@ -279,6 +307,28 @@ int cgpu_tdci_adjoint(cgpu_ctx* ctx, const cgpu_complex* c0, const double* field
                       int checkpoint, double* objective, double* overlap, cgpu_complex* c_final,
                       double* d_objective);
 
+/* MCTDHF pulse gradient, as an explicit forward / backward pair.  No
+ * counterpart in the reference.  For a single FP64 MCTDHX context that is
+ * restricted, with two body types of one particle each (the two-electron
+ * problem of the 1D helium model, M <= 16 spatial orbitals):
+ * cgpu_mc_adjoint_forward propagates state0 over n_steps Strang steps of dt
+ * (fixed-order SIL of krylov_dim <= 32 with the metric [1 | w] on OrbsLin,
+ * RK4 on NonLin: the map of cgpu_propagate_split2) with the piecewise-
+ * constant field E(t) = field[floor(t / dt)] (zero from n_steps dt on) in the
+ * length gauge, in place of the context's laser.  It returns
+ * objective = 1 - |<ref|Psi_N>|^2 with the MCTDHF overlap
+ * sum conj(C_ref[a,b]) (S C S^T)[a,b], S = phi_ref^H W phi (ref_state NULL =
+ * state0), overlap[2] = <ref|Psi_N>, and state_final (may be NULL), and keeps
+ * the state every `checkpoint` steps (0 = 64) on the device.
+ * cgpu_mc_adjoint_backward then returns d_objective[n] = d objective / d field[n]
+ * for every n: the exact gradient of the discrete map, from the co-state
+ * propagated backward through the Krylov, RK4 and Lanczos steps, each segment
+ * of `checkpoint` steps recomputed from its checkpoint. */
+int cgpu_mc_adjoint_forward(cgpu_ctx* ctx, const cgpu_complex* state0, const cgpu_complex* ref_state,
+                            const double* field, int n_steps, double dt, int krylov_dim, int checkpoint,
+                            double* objective, double* overlap, cgpu_complex* state_final);
+int cgpu_mc_adjoint_backward(cgpu_ctx* ctx, double* d_objective);
+
 /* ---- batched trajectories ------------------------------------------------ */
 /* No counterpart in the reference, whose module-global state allows one
  * trajectory per process (src/Method/M_Method.f90:47).  A batch holds n
@@ -325,6 +375,37 @@ long cgpu_batch_launch_count(cgpu_batch* batch, int reset);
  * trajectory's grid is a contiguous piece), 0 when each trajectory keeps its own. */
 int cgpu_batch_shared_interactions(const cgpu_batch* batch);
 
+/* ---- tile autotuner ------------------------------------------------------ */
+/* No counterpart in the reference.  The tile table of a context or batch:
+ * tiles[0..8] = for the fixed-point contractions W = V S, Z = W R'' and
+ * h2 = S^T W in turn: N-tile width, compact flag (two CTAs per SM), K splits
+ * (zero outside CGPU_PREC_MIXED_FX / _FX6); tiles[9] = blocks per trajectory
+ * of the Lanczos reductions.  The set-up heuristics choose the initial table.
+ * cgpu_autotune times the candidates on the resident states (upload them
+ * first) with CUDA events on the context's stream and applies the fastest:
+ * every instantiated tile configuration and feasible K split of each
+ * contraction, and half / one / two times the heuristic's Lanczos blocks.
+ * cache_path (may be NULL) is a JSON-lines file of winners keyed by the
+ * precision, device, Krylov order and window and the trajectories' sizes:
+ * CGPU_TUNE_CACHED applies the cached entry of this shape if there is one and
+ * otherwise tunes and adds it; CGPU_TUNE_FORCE always tunes and replaces it.
+ * report (may be NULL) receives a JSON object with the source ("tuned" or
+ * "cache"), the key, the timed candidates [tile..., ms] and the chosen table.
+ * The tile choice leaves the fixed-point contractions' results unchanged (exact
+ * digit sums); K splits and Lanczos blocks change FP64 summation orders only.
+ * A changed table is used from the next step on (a captured step graph is
+ * re-captured). */
+#define CGPU_TUNE_CACHED 0
+#define CGPU_TUNE_FORCE 1
+int cgpu_autotune(cgpu_ctx* ctx, const char* cache_path, int mode, char* report, int report_len);
+int cgpu_get_tiles(const cgpu_ctx* ctx, int* tiles);
+/* Applies a table (validated against the instantiated configurations, the
+ * digits' exact range and the partial buffers; CGPU_ERR_ARG otherwise). */
+int cgpu_set_tiles(cgpu_ctx* ctx, const int* tiles);
+int cgpu_batch_autotune(cgpu_batch* batch, const char* cache_path, int mode, char* report, int report_len);
+int cgpu_batch_get_tiles(const cgpu_batch* batch, int* tiles);
+int cgpu_batch_set_tiles(cgpu_batch* batch, const int* tiles);
+
 /* ---- no-allocation variant ---------------------------------------------- */
 /* No counterpart in the reference.  Weighted Gram matrix of two orbital sets,
  *   gram(i,j) = sum_g conj(a[g + n_grid*i]) * b[g + n_grid*j] * weights[g],
@@ -338,7 +419,11 @@ int cgpu_batch_shared_interactions(const cgpu_batch* batch);
  * until exit.  Limits: 1 <= n_cols <= 32, n_grid >= 1; larger sizes are
  * rejected with CGPU_ERR_ARG and a message in cgpu_last_global_error().
  * The first call on each device looks up that array's device address (with
- * the device current); make that first call before any stream capture.
+ * the device current) and keeps it for the life of the process; make that
+ * first call before any stream capture.  Calls after cudaDeviceReset (or any
+ * other teardown of the device's primary context) are not supported.  A CUDA
+ * error already pending on the calling thread is reported (CGPU_ERR_CUDA) and
+ * left pending; nothing is launched then.
  * The kernels run asynchronously on `stream` (a cudaStream_t, NULL = legacy
  * default stream).  All calls share the one array: calls that overlap on the
  * GPU (concurrent streams) race on it and must be serialised by the caller. */

@@ -12,6 +12,7 @@ for p in (ROOT, os.path.join(ROOT, "oracle")):
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a GB300 (sm_103a) GPU and the built CUDA library")
+    config.addinivalue_line("markers", "slow: long propagation (minutes); still part of the GPU suite")
 
 
 @pytest.fixture(scope="session")

@@ -1,7 +1,7 @@
 """Extract the reference's golden values for the hot path into he1d_golden.json.
 
-Run in a checkout that has the CodyFortran sources at $CODY_REFERENCE
-(default /root/reference).  The values are read from the reference's own
+Usage: python make_golden.py <path to the CodyFortran sources>, or with the
+path in $CODY_REFERENCE; there is no default.  The values are read from the reference's own
 test programs (their `check(error, value, golden, thr=...)` calls), so the
 JSON is a verbatim record of what the reference tests assert.
 """
@@ -10,7 +10,16 @@ import os
 import re
 import sys
 
-REF = os.environ.get("CODY_REFERENCE", "/root/reference")
+
+def reference_root():
+    """The CodyFortran checkout: first argument, else $CODY_REFERENCE."""
+    if len(sys.argv) > 1:
+        return sys.argv[1]
+    if os.environ.get("CODY_REFERENCE"):
+        return os.environ["CODY_REFERENCE"]
+    sys.exit("make_golden.py: give the CodyFortran source directory as the argument or in $CODY_REFERENCE")
+
+
 TESTS = {
     "he1d_01_exact_diag": "test/simulationTests/He1d/T_He1d_01_ExactDiagGridBasedFullExpansion.f90",
     "he1d_02_tdci_exact_diag": "test/simulationTests/He1d/T_He1d_02_ExactDiagTdci.f90",
@@ -25,6 +34,7 @@ PAT = re.compile(r"call check\(error,\s*([^,]+),\s*([-+0-9.eE_R64]+)?,?\s*(?:thr
 
 
 def main():
+    REF = reference_root()
     out = {}
     for key, rel in TESTS.items():
         path = os.path.join(REF, rel)

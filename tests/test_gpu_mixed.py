@@ -141,3 +141,24 @@ def test_mixed_trajectory_orbital_span(precision):
     assert ds < 1e-9
     f.close()
     m.close()
+
+
+@pytest.mark.slow
+def test_mixed_fx6_batch_horizon_1500_steps():
+    """The headline form over the whole batch horizon: the first 32 trajectories
+    of the seed-1234 batch (uneven grids, orbital counts and pulses) advanced
+    1500 steps of dt = 0.02 (K = 12) in mixed_fx6 and in FP64 from the same
+    states; every 10 steps each trajectory's energy within 1e-8 relative and
+    its norm within 1e-8 of the FP64 run."""
+    import bench
+    specs, cfg = bench.workload("batch512")
+    rows = bench.accuracy_horizon(specs[:32], cfg, "mixed_fx6", 1500, every=10, window=1)
+    e_max = max(r[1] for r in rows)
+    n_max = max(r[4] for r in rows)
+    a_max = max(r[7] for r in rows)
+    f_max = max(r[8] for r in rows)
+    worst = max(rows, key=lambda r: r[1])
+    print(f"mixed_fx6 32 trajectories x 1500 steps: max |dE|/|E| {e_max:.3e} (step {worst[0]}, trajectory "
+          f"{worst[5]}, |E| {worst[6]:.3e}), max |dE| {a_max:.3e} Eh, max |dE|/max(|E|, 1) {f_max:.3e}, "
+          f"max |d||C||| {n_max:.3e}")
+    assert f_max < 1e-8 and a_max < 1e-8 and n_max < 1e-8

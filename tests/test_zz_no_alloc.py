@@ -99,3 +99,39 @@ def test_noalloc_gram_matches_fill_h1_on_two_calls():
         for buf in (a, b, w, g):
             buf.free()
         e.close()
+
+
+def test_noalloc_gram_wide_and_long_against_numpy():
+    """Caller-owned random buffers at the edges of the fixed scratch: 17 and 32
+    columns (every accumulator slot of a thread in use), a grid longer than the
+    64 blocks x 32 points one pass covers (blocks loop), then a short grid on
+    the same buffers (fewer blocks than the call before), each against numpy."""
+    from codyfortran_gb300 import build
+    from codyfortran_gb300.engine import load_library
+    build.build()
+    lib = load_library()
+    rt = _cudart()
+    rng = np.random.default_rng(17)
+    for n in (17, 32):
+        nG = 5000
+        A = np.asfortranarray(rng.normal(size=(nG, n)) + 1j * rng.normal(size=(nG, n)))
+        B = np.asfortranarray(rng.normal(size=(nG, n)) + 1j * rng.normal(size=(nG, n)))
+        w = rng.uniform(0.1, 2.0, size=nG)
+        a, b, wd = DeviceBuffer(rt, A), DeviceBuffer(rt, B), DeviceBuffer(rt, w)
+        g = DeviceBuffer(rt, np.zeros((n, n), dtype=np.complex128, order="F"))
+        try:
+            for n_grid in (nG, 300):
+                rc = lib.cgpu_weighted_gram_noalloc(a.ptr, b.ptr, wd.ptr, n_grid, n, g.ptr, None)
+                assert rc == 0, lib.cgpu_last_global_error().decode()
+                assert rt.cudaDeviceSynchronize() == 0
+                out = np.zeros((n, n), dtype=np.complex128, order="F")
+                g.download(out)
+                # the first n_grid rows of each column (column stride n_grid)
+                Ak = A.ravel(order="F")[: n_grid * n].reshape(n, n_grid).T
+                Bk = B.ravel(order="F")[: n_grid * n].reshape(n, n_grid).T
+                ref = Ak.conj().T @ (w[:n_grid, None] * Bk)
+                err = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+                assert err < TOL, (n, n_grid, err)
+        finally:
+            for buf in (a, b, wd, g):
+                buf.free()
