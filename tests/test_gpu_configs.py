@@ -162,24 +162,14 @@ def test_cfg1_free_run_100_steps(chain):
 
 @pytest.mark.slow
 def test_cfg1_free_run_1000_steps(chain):
-    """After 1000 free-running steps the GPU is as close to the oracle as the
-    oracle is to itself run on one host thread instead of all (reduction
-    orders only): each quantity within 20 times that self-difference (floor
-    1e-12).  Measured on GB300: GPU vs oracle 1.2e-9 (state), 9.6e-12 (energy);
-    oracle vs itself 9.1e-10, 7.0e-12 (x86 host)."""
+    """After 1000 free-running steps the GPU is about as close to the oracle as
+    the oracle is to itself under another reduction order.  Measured on GB300:
+    GPU vs oracle 1.2e-9 (state), 9.6e-12 (energy), 2.1e-9 (wavefunction);
+    the oracle on one x86 host thread vs eight: 9.1e-10 (state), 7.0e-12
+    (energy).  Bounds: eight times the measured GPU values."""
     w = _free_run(chain, 1000)
-    o1 = Oracle(chain.sp, n_threads=1)
-    a, b, m = chain.states[0].copy(), chain.oracle_state(1000), chain.m
-    for k in range(1000):
-        a = o1.propagate_split2(a, k * DT, (k + 1) * DT, krylov_dim=K, metric=m)
-    t = 1000 * DT
-    self_diff = dict(state=rel(a, b), energy=abs(o1.energy(a, t) - chain.o.energy(b, t)) / abs(chain.o.energy(b, t)),
-                     wavefunction=wavefunction_distance(chain.sp, chain.o.nG, chain.o.w, a, b))
-    print("oracle 1 thread vs default threads after 1000 steps: " +
-          ", ".join(f"{k} {v:.2e}" for k, v in self_diff.items()))
-    for k in ("state", "energy", "wavefunction"):
-        assert w[k] < 20.0 * max(self_diff[k], TOL), (k, w[k], self_diff[k])
     assert w["norm"] < 1e-11 and w["metric_norm"] < 1e-10, w
+    assert w["state"] < 1e-8 and w["energy"] < 1e-10 and w["wavefunction"] < 2e-8, w
 
 
 def test_cfg2_trimer_strang_steps():
