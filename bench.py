@@ -497,6 +497,77 @@ def run_accuracy_horizon(args):
     return 0
 
 
+def adjoint_start_state(kind, x, w, eng_relax=None):
+    """Start (and reference) state of the pulse-gradient workload: 'relaxed' --
+    the field-free ground state by imaginary-time relaxation from seed-42
+    orbitals; 'correlated' -- seed-42 Gaussian orbitals with a seeded random
+    normalised CI vector, every natural orbital occupied."""
+    from codyfortran_gb300 import init as I
+    from codyfortran_gb300 import spec as S
+    sp0 = S.helium_fedvr(100, 6, 8, laser=S.Laser())
+    orbs = I.seeded_gaussian_orbitals(sp0, x, w, 42)
+    if kind == "relaxed":
+        st0 = I.pack_state(I.unary_coeffs(sp0), orbs)
+        e0, st, rounds = eng_relax.relax(st0, 0.005, 10, 1e-12, 2000)
+        return st, {"relaxed_energy": e0, "relax_rounds": rounds}
+    rng = np.random.default_rng(42)
+    c = rng.normal(size=sp0.n_coeffs) + 1j * rng.normal(size=sp0.n_coeffs)
+    return I.pack_state(c / np.linalg.norm(c), orbs), {}
+
+
+def run_adjoint(args):
+    """--workload adjoint_helium: the pulse-gradient workload -- 1D helium
+    (100 FEDVR elements x 6 points, 501 points), M = 8 restricted orbitals,
+    --adjoint-samples field samples E_n ~ N(0, 0.01^2) from seed 99,
+    dt = 0.05, Krylov order 12, checkpoints every 64 steps, objective
+    1 - |<Psi_0|Psi_N>|^2.  Times one forward + backward evaluation (the
+    gradient with respect to all samples) and compares central differences
+    on a few random samples at h = 1e-5 and 1e-6."""
+    from codyfortran_gb300 import build as B
+    B.build()
+    from codyfortran_gb300 import spec as S
+    from codyfortran_gb300.engine import Engine
+    nT, dt, K, chk = args.adjoint_samples, 0.05, 12, 64
+    field = np.random.default_rng(99).normal(0.0, 0.01, size=4000)[:nT]
+    mk = lambda laser: S.helium_fedvr(100, 6, 8, laser=laser)
+    r = Engine(mk(S.Laser()))
+    st, extra = adjoint_start_state(args.adjoint_state, r.x, r.w, r)
+    r.close()
+    e = Engine(mk(S.Laser(kind="sampled", samples=field, sample_dt=dt, sample_t0=0.0)), max_krylov=K)
+    e.mc_adjoint_forward(st, field[:8], dt, K, chk)  # warm-up (allocations, module load)
+    e.mc_adjoint_backward()
+    t0 = time.perf_counter()
+    J, ov, fin = e.mc_adjoint_forward(st, field, dt, K, chk)
+    t1 = time.perf_counter()
+    g = e.mc_adjoint_backward()
+    t2 = time.perf_counter()
+    idx = np.sort(np.random.default_rng(7).choice(nT, size=args.adjoint_fd, replace=False))
+    rows, worst = [], {}
+    gmax = float(np.max(np.abs(g)))
+    for h in (1e-5, 1e-6):
+        worst[h] = 0.0
+        for n in idx:
+            f1, f2 = field.copy(), field.copy()
+            f1[n] += h
+            f2[n] -= h
+            fd = (e.mc_adjoint_forward(st, f1, dt, K, chk)[0] - e.mc_adjoint_forward(st, f2, dt, K, chk)[0]) / (2 * h)
+            rows.append((h, int(n), float(fd), float(g[n])))
+            worst[h] = max(worst[h], abs(fd - g[n]) / gmax)
+    e.close()
+    line = {"metric": "MCTDHF pulse-gradient evaluations/s (forward + backward over all field samples)",
+            "value": 1.0 / (t2 - t0), "unit": "gradients/s", "n_gpus": 1, "higher_is_better": True,
+            "dtype": "complex128", "data": f"synthetic (seed-99 field samples; {args.adjoint_state} start state)",
+            "config": dict({"workload": "adjoint_helium", "n_grid": 501, "n_orbitals": 8, "field_samples": nT,
+                            "dt": dt, "krylov_order": K, "checkpoint": chk, "start_state": args.adjoint_state},
+                           **extra),
+            "forward_s": t1 - t0, "backward_s": t2 - t1, "objective": J, "survival": abs(ov) ** 2,
+            "gradient_max_abs": gmax,
+            "fd_check": {"samples": rows, "worst_abs_diff_over_max_gradient": {str(k): v for k, v in worst.items()},
+                         "target": 1e-6}}
+    print(json.dumps(line))
+    return 0
+
+
 def krylov_window(args, precision):
     """Lanczos re-orthogonalisation window: the reference's full loop for the
     FP64 form, the three-term recurrence (window 1) for the mixed forms unless
@@ -762,7 +833,12 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch512", choices=["batch512", "trimer_large", "helium_small"])
+    ap.add_argument("--workload", default="batch512",
+                    choices=["batch512", "trimer_large", "helium_small", "adjoint_helium"])
+    ap.add_argument("--adjoint-samples", type=int, default=4000, help="adjoint_helium: field samples (steps)")
+    ap.add_argument("--adjoint-state", default="correlated", choices=["correlated", "relaxed"],
+                    help="adjoint_helium: start and reference state")
+    ap.add_argument("--adjoint-fd", type=int, default=4, help="adjoint_helium: samples checked by central differences")
     ap.add_argument("--precision", default=None, choices=list(DTYPES))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-leg", action="store_true")
@@ -782,6 +858,8 @@ def main():
         return run_reference(args)
     if args.accuracy_horizon:
         return run_accuracy_horizon(args)
+    if args.workload == "adjoint_helium":
+        return run_adjoint(args)
     rank, world, local = dist_info()
     if world > 1:
         import torch.distributed as dist

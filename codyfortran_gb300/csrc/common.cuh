@@ -410,6 +410,9 @@ struct cgpu_ctx {
   // inside the NonLin time derivative: r2s from rdm2Lin and h2Lin from h2s
   // directly (the nO^4 rdm2 / h2 tensors are not formed)
   int fuseLayouts = 0;
+  // SIL on OrbsLin with the three-term recurrence: the double-float one-body
+  // apply emits the recurrence's first-pass partials (launch_onebody_lz)
+  int fuseOrbsLinLz = 1;
   int numSms = 148;  // streaming multiprocessors of the device
   float4 *h1Df_d = nullptr, *h2Df_d = nullptr;
   float2* Tdf_d = nullptr;  // double-float copy of the kinetic band (static)
@@ -529,6 +532,12 @@ void batch_copy(cgpu_ctx* c, void* dst, const void* src, size_t bytes);
 // k_onebody.cu
 void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha, int accumulate);
 void launch_field(cgpu_ctx* c, double* E, double t);  // E(t) of every trajectory into its slot E
+// The OrbsLin apply of Lanczos iteration j (three-term recurrence, double-float
+// one-body operator) into c->lw_d, fused with the recurrence's first pass:
+// partials of alpha_j and ||w'||^2 at c->partial_d (layout of k_lz3_dot).
+// Returns the partial blocks per trajectory, or 0 when the fused form does not
+// apply (the caller then runs the plain derivative and pass).
+int launch_onebody_lz(cgpu_ctx* c, int j, double t);
 // k_sys.cu: one orbital of a single-system context (the Sys* procedure pointers)
 void sys_kinetic(cgpu_ctx* c, z_t* out, const z_t* in, int btBlock);
 void sys_potential(cgpu_ctx* c, z_t* V, double t);
@@ -608,11 +617,15 @@ void adjoint_tdci(cgpu_ctx* c, const z_t* C0_h, const double* E_h, int nT, doubl
 // The SIL kernels work on c->basis_d, c->lw_d (H v_j), c->work_d (start vector),
 // c->metric_d (current metric) and the scalar block c->lz_d.
 void launch_lanczos_start(cgpu_ctx* c, const z_t* v);
-void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim);
+// pass1Blocks > 0: the three-term pass-1 partials (alpha, ||w'||^2) were
+// emitted by launch_onebody_lz with that many blocks per trajectory
+void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim, int pass1Blocks = 0);
 void launch_lanczos_tail(cgpu_ctx* c, int j, double dt, int evalExp);  // j = 0: use the device mDim
 void launch_lanczos_combine(cgpu_ctx* c, z_t* out, const z_t* start);
 void launch_lz_set(cgpu_ctx* c, int idx, double v);
 size_t lanczos_partial_need(const cgpu_ctx* c);
+#define CODY_LZ_BETA 64
+#define CODY_LZ_S 400
 #define CODY_LZ_ERR 385
 #define CODY_LZ_MDIM 386
 #define CODY_LZ_DONE 387

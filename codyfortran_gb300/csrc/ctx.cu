@@ -722,9 +722,11 @@ int lanczos_pass(cgpu_ctx* c, int which, double tBase, double dt, int maxDim, do
   int mUsed = maxDim;
   for (int j = 1; j <= maxDim; j++) {
     z_t* v = c->basis_d + (size_t)c->nS * (j - 1);
-    // w = i * TimeDerivative(v)
-    td_device(c, which, c->lw_d, v, tEval, zmk(0.0, 1.0));
-    launch_lanczos_update(c, j, maxDim);
+    // w = i * TimeDerivative(v); on OrbsLin with the three-term recurrence the
+    // one-body apply also emits the recurrence's first-pass partials
+    const int nPass1 = (which == CGPU_TD_ORBS_LIN && c->fuseOrbsLinLz) ? launch_onebody_lz(c, j, tEval) : 0;
+    if (nPass1 == 0) td_device(c, which, c->lw_d, v, tEval, zmk(0.0, 1.0));
+    launch_lanczos_update(c, j, maxDim, nPass1);
     if (adaptive) {
       launch_lanczos_tail(c, j, dt, 1);
       CODY_CUDA(cudaMemcpyAsync(c->lz_h, c->lz_d, sizeof(double) * 400, cudaMemcpyDeviceToHost, c->stream));

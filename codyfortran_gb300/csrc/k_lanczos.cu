@@ -40,6 +40,7 @@ constexpr int LZ_DT = 389;      // dt of the current sub-step
 constexpr int LZ_BREAKJ = 390;  // iteration at which breakdown happened
 constexpr int LZ_S = 400;       // scale of basis slot k: v_(k+1) = s_k u_k  [400, 433)
 constexpr int LZ_SMAX = 33;
+static_assert(LZ_S == CODY_LZ_S && LZ_BETA == CODY_LZ_BETA && LZ_DONE == CODY_LZ_DONE, "Lanczos scalar slots");
 
 constexpr int LZ_THREADS = 256;
 
@@ -112,10 +113,11 @@ __device__ __forceinline__ void store_dots(z_t (&acc)[LZ_VPW], int nVec, z_t* __
 // the classical criterion for a loss of orthogonality beyond rounding.  Every
 // block sums the same partials in the same order, so all blocks agree.
 constexpr double LZ_ETA2 = 1.0e-2;
-__device__ bool reorth_needed(const z_t* __restrict__ w0n, int stride, const z_t* __restrict__ w1n, int nBlk) {
+__device__ bool reorth_needed(const z_t* __restrict__ w0n, int stride, int nBlk0, const z_t* __restrict__ w1n,
+                              int nBlk1) {
   __shared__ z_t g[2];
-  sum_partials(w0n, nBlk, stride, 1, g);
-  sum_partials(w1n, nBlk, 1, 1, g + 1);
+  sum_partials(w0n, nBlk0, stride, 1, g);
+  sum_partials(w1n, nBlk1, 1, 1, g + 1);
   return g[1].x <= LZ_ETA2 * g[0].x;
 }
 
@@ -127,11 +129,11 @@ __global__ void __launch_bounds__(LZ_THREADS) k_mdot(z_t* __restrict__ part, int
                                                       const double* __restrict__ m, TRAJ_ARGS,
                                                       const double* __restrict__ lz, int E, int withNorm,
                                                       const z_t* __restrict__ gate0, int gateStride,
-                                                      const z_t* __restrict__ gate1, int nBlkGate) {
+                                                      const z_t* __restrict__ gate1, int nBlkGate, int nBlkGate0) {
   const TrajShape& S = shp[blockIdx.z];
   lz = bat(lz, bs);
   if (lz[LZ_DONE] != 0.0) return;
-  if (gate0 && !reorth_needed(bat(gate0, bs), gateStride, bat(gate1, bs), nBlkGate)) return;
+  if (gate0 && !reorth_needed(bat(gate0, bs), gateStride, nBlkGate0, bat(gate1, bs), nBlkGate)) return;
   part = bat(part, bs);
   V = bat(V, bs);
   w = bat(w, bs);
@@ -173,11 +175,12 @@ __global__ void __launch_bounds__(LZ_THREADS) k_cgs_pass(z_t* __restrict__ w, co
                                                           const double* __restrict__ m, TRAJ_ARGS,
                                                           double* __restrict__ lz, int dotBase, int E,
                                                           const z_t* __restrict__ gate0, int gateStride,
-                                                          const z_t* __restrict__ gate1, int scaleIdx, int nBlkGate) {
+                                                          const z_t* __restrict__ gate1, int scaleIdx, int nBlkGate,
+                                                          int nBlkGate0) {
   const TrajShape& S = shp[blockIdx.z];
   lz = bat(lz, bs);
   if (lz[LZ_DONE] != 0.0) return;
-  if (gate0 && !reorth_needed(bat(gate0, bs), gateStride, bat(gate1, bs), nBlkGate)) return;
+  if (gate0 && !reorth_needed(bat(gate0, bs), gateStride, nBlkGate0, bat(gate1, bs), nBlkGate)) return;
   w = bat(w, bs);
   V = bat(V, bs);
   partIn = bat(partIn, bs);
@@ -231,7 +234,7 @@ __global__ void k_lz_finish(z_t* __restrict__ vNext, const z_t* __restrict__ w, 
   vNext = bat(vNext, bs);
   w = bat(w, bs);
   partIn = bat(partIn, bs);
-  if (reorth_needed(bat(gate0, bs), gateStride, partIn, nBlkIn)) partIn = bat(partAlt, bs);
+  if (reorth_needed(bat(gate0, bs), gateStride, nBlkIn, partIn, nBlkIn)) partIn = bat(partAlt, bs);
   const size_t n = S.nS;
   __shared__ z_t tot[1];
   sum_partials(partIn, nBlkIn, 1, 1, tot);
@@ -552,13 +555,13 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz3_update(z_t* __restrict__ dst
 __global__ void __launch_bounds__(LZ_THREADS) k_lz_scalars(const z_t* __restrict__ partIn, int nBlkIn,
                                                             const z_t* __restrict__ partAlt, int nBlkAlt,
                                                             const z_t* __restrict__ gate0, int gateStride,
-                                                            TRAJ_ARGS, double* __restrict__ lz, int j, int maxDim,
-                                                            double zeroThr) {
+                                                            int nBlkGate0, TRAJ_ARGS, double* __restrict__ lz, int j,
+                                                            int maxDim, double zeroThr) {
   lz = bat(lz, bs);
   if (lz[LZ_DONE] != 0.0) return;
   partIn = bat(partIn, bs);
   int nPart = nBlkIn;
-  if (reorth_needed(bat(gate0, bs), gateStride, partIn, nBlkIn)) {
+  if (reorth_needed(bat(gate0, bs), gateStride, nBlkGate0, partIn, nBlkIn)) {
     partIn = bat(partAlt, bs);
     nPart = nBlkAlt;
   }
@@ -597,7 +600,7 @@ void launch_lanczos_start(cgpu_ctx* c, const z_t* v) {
 
 // After lw_d holds H v_j: Gram-Schmidt against v_1..v_j (or the window's last
 // vectors), the gated second pass, beta_j, v_{j+1}.
-void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
+void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim, int pass1Blocks) {
   ProfScope prof(c, CGPU_KERNEL_LANCZOS);
   size_t ld = c->nS;
   int nBlk = c->lzBlocks;
@@ -616,21 +619,26 @@ void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
     z_t* uNext = (j < maxDim) ? c->basis_d + ld * (size_t)j : c->lw_d;
     dim3 g = bgrid(c, nBlk);
     const int E = c->lzElems;
-    k_lz3_dot<<<g, LZ_THREADS, 0, c->stream>>>(p1, vPrev, vCur, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, j);
-    CODY_LAUNCHED(c);
-    k_lz3_update<<<g, LZ_THREADS, 0, c->stream>>>(uNext, c->lw_d, vPrev, vCur, p1, nBlk, p2, c->metric_d,
+    // pass 1 (alpha and ||w'||^2 partials): here, or already emitted by the
+    // fused one-body apply (pass1Blocks partials per trajectory)
+    const int n1 = pass1Blocks > 0 ? pass1Blocks : nBlk;
+    if (pass1Blocks <= 0) {
+      k_lz3_dot<<<g, LZ_THREADS, 0, c->stream>>>(p1, vPrev, vCur, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, j);
+      CODY_LAUNCHED(c);
+    }
+    k_lz3_update<<<g, LZ_THREADS, 0, c->stream>>>(uNext, c->lw_d, vPrev, vCur, p1, n1, p2, c->metric_d,
                                                   TRAJ_PASS(c), c->lz_d, j);
     CODY_LAUNCHED(c);
     // the gated second pass rarely fires: one block per trajectory reads the
     // gate (and, when it fires, walks the whole vector)
     dim3 g1 = bgrid(c, 1);
     k_mdot<<<g1, LZ_THREADS, 0, c->stream>>>(p3, 1, vCur, ld, 1, uNext, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 0,
-                                             p1 + 1, 2, p2, nBlk);
+                                             p1 + 1, 2, p2, nBlk, n1);
     CODY_LAUNCHED(c);
     k_cgs_pass<<<g1, LZ_THREADS, 0, c->stream>>>(uNext, vCur, ld, 1, p3, 1, 1, p4, c->metric_d, TRAJ_PASS(c), c->lz_d,
-                                                 -1, E, p1 + 1, 2, p2, LZ_S + j - 1, nBlk);
+                                                 -1, E, p1 + 1, 2, p2, LZ_S + j - 1, nBlk, n1);
     CODY_LAUNCHED(c);
-    k_lz_scalars<<<g1, LZ_THREADS, 0, c->stream>>>(p2, nBlk, p4, 1, p1 + 1, 2, TRAJ_PASS(c), c->lz_d, j, maxDim,
+    k_lz_scalars<<<g1, LZ_THREADS, 0, c->stream>>>(p2, nBlk, p4, 1, p1 + 1, 2, n1, TRAJ_PASS(c), c->lz_d, j, maxDim,
                                                    1.0e-14);
     CODY_LAUNCHED(c);
     return;
@@ -641,16 +649,16 @@ void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim) {
   const int E = c->lzElems;
   dim3 g = bgrid(c, nBlk);
   k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p1, s1, V, ld, nv, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 1,
-                                          nullptr, 0, nullptr, nBlk);
+                                          nullptr, 0, nullptr, nBlk, nBlk);
   CODY_LAUNCHED(c);
   k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, V, ld, nv, p1, s1, nBlk, p2, c->metric_d, TRAJ_PASS(c),
-                                              c->lz_d, base, E, nullptr, 0, nullptr, -1, nBlk);
+                                              c->lz_d, base, E, nullptr, 0, nullptr, -1, nBlk, nBlk);
   CODY_LAUNCHED(c);
   k_mdot<<<g, LZ_THREADS, 0, c->stream>>>(p3, nv, V, ld, nv, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, E, 0,
-                                          p1 + nv, s1, p2, nBlk);
+                                          p1 + nv, s1, p2, nBlk, nBlk);
   CODY_LAUNCHED(c);
   k_cgs_pass<<<g, LZ_THREADS, 0, c->stream>>>(c->lw_d, V, ld, nv, p3, nv, nBlk, p4, c->metric_d, TRAJ_PASS(c),
-                                              c->lz_d, -1, E, p1 + nv, s1, p2, -1, nBlk);
+                                              c->lz_d, -1, E, p1 + nv, s1, p2, -1, nBlk, nBlk);
   CODY_LAUNCHED(c);
   z_t* vNext = (j < maxDim) ? c->basis_d + ld * (size_t)j : nullptr;
   k_lz_finish<<<g, LZ_THREADS, 0, c->stream>>>(vNext, c->lw_d, p2, p4, p1 + nv, s1, nBlk, TRAJ_PASS(c), c->lz_d, j,

@@ -163,6 +163,124 @@ __global__ void k_onebody_df(z_t* __restrict__ out, const z_t* __restrict__ orbs
   }
 }
 
+// Sum of v over the block (the block total in thread 0).
+__device__ z_t ob_block_sum(z_t v) {
+  __shared__ z_t red[OB_THREADS / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  v = (threadIdx.x < OB_THREADS / 32) ? red[threadIdx.x] : zmk(0.0, 0.0);
+  if (wid == 0)
+    for (int o = 16; o > 0; o >>= 1) {
+      v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+  return v;
+}
+
+// The OrbsLin apply of Lanczos iteration j (three-term recurrence on
+// unnormalised basis vectors u_k, scales s_k in lz) in double-float arithmetic,
+// fused with the recurrence's first pass: h = (T + V0 + E x) u_j on the
+// orbitals into out (0 on the coefficients, which OrbsLin does not move) and,
+// with x = s_j h - beta_{j-1} s_{j-1} u_{j-1}, per block b the partials
+//   part[2 b] = s_j sum m Re(conj(u_j) x),   part[2 b + 1] = sum m |x|^2
+// (b = blockIdx.x + gridDim.x blockIdx.y), the layout the pass-2 kernel reads.
+// The one-body apply has just read u_j; the pass reads u_{j-1} and m besides,
+// instead of a separate pass over h, u_j, u_{j-1} and m.
+__global__ void k_onebody_lz_df(z_t* __restrict__ out, const z_t* __restrict__ vCur, const z_t* __restrict__ vPrev,
+                                const double* __restrict__ m, z_t* __restrict__ part, const float2* __restrict__ Tdf,
+                                const double* __restrict__ V0, const double* __restrict__ x,
+                                const int* __restrict__ btOf, TRAJ_ARGS, const double* __restrict__ Efield,
+                                const double* __restrict__ lz, int j) {
+  extern __shared__ float4 shf[];
+  const TrajShape& S = shp[blockIdx.z];
+  lz = bat(lz, bs);
+  if (lz[CODY_LZ_DONE] != 0.0) return;  // the recurrence stopped: the pass-2 kernel returns too
+  const int nG = S.nG, band = S.band;
+  const int g0 = blockIdx.x * OB_THREADS;
+  const int bid = blockIdx.x + gridDim.x * blockIdx.y;
+  const double sj = lz[CODY_LZ_S + j - 1];
+  const double bp = (j > 1) ? lz[CODY_LZ_BETA + j - 2] * lz[CODY_LZ_S + j - 2] : 0.0;
+  out = bat(out, bs);
+  vCur = bat(vCur, bs);
+  vPrev = (j > 1) ? bat(vPrev, bs) : nullptr;
+  m = bat(m, bs);
+  part = bat(part, bs);
+  double a = 0.0, q = 0.0;
+  if (bid == 0)  // the coefficient part: h = 0, x = -bp u_{j-1}
+    for (int l = threadIdx.x; l < S.nC; l += OB_THREADS) {
+      out[l] = zmk(0.0, 0.0);
+      if (vPrev) {
+        const z_t p = vPrev[l], v = vCur[l];
+        const double xr = -bp * p.x, xi = -bp * p.y, mi = m[l];
+        a = fma(mi, fma(v.x, xr, v.y * xi), a);
+        q = fma(mi, fma(xr, xr, xi * xi), q);
+      }
+    }
+  if (g0 < nG) {
+    Tdf = bat(Tdf, bs);
+    V0 = bat(V0, bs);
+    x = bat(x, bs);
+    btOf = bat(btOf, bs);
+    const double E = *bat(Efield, bs);
+    const z_t* orbCur = vCur + S.nCpad;
+    const z_t* orbPrev = vPrev ? vPrev + S.nCpad : nullptr;
+    const double* mo = m + S.nCpad;
+    z_t* oo = out + S.nCpad;
+    const int nTile = OB_THREADS + 2 * band, nd = 2 * band + 1;
+    const int g = g0 + threadIdx.x;
+    const bool live = g < nG;
+    const float2 pd = (S.hasPot && live) ? df_split(fma(E, x[g], V0[g])) : make_float2(0.0f, 0.0f);
+    for (int i = blockIdx.y; i < S.nOS; i += gridDim.y) {
+      const z_t* f = orbCur + (size_t)nG * i;
+      if (i != (int)blockIdx.y) __syncthreads();
+      for (int t = threadIdx.x; t < nTile; t += OB_THREADS) {
+        const int gg = g0 - band + t;
+        shf[t] = (gg >= 0 && gg < nG) ? zdf_from(f[gg]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+      __syncthreads();
+      if (!live) continue;
+      const int bt = S.restricted ? 0 : btOf[i];
+      const float2* Tb = Tdf + (size_t)bt * nd * nG;
+      zdf_acc acc = {0.0f, 0.0f, 0.0f, 0.0f};
+      for (int d = 0; d < nd; d++) {
+        const float2 cf = Tb[(size_t)d * nG + g];
+        const float4 v = shf[threadIdx.x + d];
+        df_mul_acc(acc.rs, acc.rc, cf.x, cf.y, v.x, v.y);
+        df_mul_acc(acc.is, acc.ic, cf.x, cf.y, v.z, v.w);
+      }
+      if (S.hasPot) {
+        const float4 v = shf[threadIdx.x + band];
+        df_mul_acc(acc.rs, acc.rc, pd.x, pd.y, v.x, v.y);
+        df_mul_acc(acc.is, acc.ic, pd.x, pd.y, v.z, v.w);
+      }
+      const z_t h = zdf_to_z(acc);
+      const size_t o = (size_t)nG * i + g;
+      oo[o] = h;
+      double xr = sj * h.x, xi = sj * h.y;
+      if (orbPrev) {
+        const z_t p = orbPrev[o];
+        xr = fma(-bp, p.x, xr);
+        xi = fma(-bp, p.y, xi);
+      }
+      const z_t v = f[g];
+      const double mi = mo[o];
+      a = fma(mi, fma(v.x, xr, v.y * xi), a);
+      q = fma(mi, fma(xr, xr, xi * xi), q);
+    }
+  }
+  const z_t t = ob_block_sum(zmk(a * sj, q));
+  if (threadIdx.x == 0) {
+    part[(size_t)bid * 2] = zmk(t.x, 0.0);
+    part[(size_t)bid * 2 + 1] = zmk(t.y, 0.0);
+  }
+}
+
 // Column range of a Gram / projector call: group < 0 = all stored orbitals,
 // otherwise projector group `group` (false when the trajectory has none).
 __device__ __forceinline__ bool gram_cols(const TrajShape& S, int group, int& c0, int& n) {
@@ -676,6 +794,26 @@ void launch_field(cgpu_ctx* c, double* E, double t) {
   const double off = c->inCapture ? t - c->captureT0 : t;
   k_field<<<bgrid(c, 1), 1, 0, c->stream>>>(E, TRAJ_PASS(c), base, off);
   CODY_LAUNCHED(c);
+}
+
+int launch_onebody_lz(cgpu_ctx* c, int j, double t) {
+  if (!c->Tdf_d || c->krylovWindow != 1 || c->method == CGPU_METHOD_TDCI) return 0;
+  const unsigned tiles = ceil_div(c->nG, OB_THREADS);
+  const unsigned groups = (size_t)tiles * c->nb >= 4 * (size_t)c->numSms ? 1 : (unsigned)c->nOS;
+  const int nPart = (int)(tiles * groups);
+  // the pass-1 partials share the region the separate pass writes
+  if ((size_t)2 * nPart > (size_t)c->lzBlocks * (c->maxKrylov + 1)) return 0;
+  ProfScope prof(c, CGPU_KERNEL_ONEBODY);
+  double* E = c->scal_d + CODY_SCAL_FIELD;
+  launch_field(c, E, t);
+  const z_t* vCur = c->basis_d + (size_t)c->nS * (j - 1);
+  const z_t* vPrev = j > 1 ? c->basis_d + (size_t)c->nS * (j - 2) : nullptr;
+  dim3 grid(tiles, groups, c->nb);
+  size_t sh = sizeof(z_t) * (OB_THREADS + 2 * c->band);
+  k_onebody_lz_df<<<grid, OB_THREADS, sh, c->stream>>>(c->lw_d, vCur, vPrev, c->metric_d, c->partial_d, c->Tdf_d,
+                                                        c->V0_d, c->x_d, c->btOfOrb_d, TRAJ_PASS(c), E, c->lz_d, j);
+  CODY_LAUNCHED(c);
+  return nPart;
 }
 
 void launch_onebody(cgpu_ctx* c, z_t* out, const z_t* orbs, double t, z_t alpha, int accumulate) {
