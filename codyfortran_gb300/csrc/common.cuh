@@ -205,6 +205,28 @@ __device__ __forceinline__ void df_mul_acc(float& s, float& c, float a1, float a
   e = fmaf(a2, b1, e);
   df_acc(s, c, p, e);
 }
+// (s, c) from df_acc as a normalised double-float (hi, lo) by a fast two-sum
+__device__ __forceinline__ float2 df_norm(float s, float c) {
+  const float hi = s + c;
+  return make_float2(hi, c - (hi - s));
+}
+// a b + c d for double-floats, normalised
+__device__ __forceinline__ float2 df_dot2(float2 a, float2 b, float2 c, float2 d) {
+  float s = 0.0f, e = 0.0f;
+  df_mul_acc(s, e, a.x, a.y, b.x, b.y);
+  df_mul_acc(s, e, c.x, c.y, d.x, d.y);
+  return df_norm(s, e);
+}
+// a b + c d + e f for double-floats, normalised
+__device__ __forceinline__ float2 df_dot3(float2 a, float2 b, float2 c, float2 d, float2 e, float2 f) {
+  float s = 0.0f, r = 0.0f;
+  df_mul_acc(s, r, a.x, a.y, b.x, b.y);
+  df_mul_acc(s, r, c.x, c.y, d.x, d.y);
+  df_mul_acc(s, r, e.x, e.y, f.x, f.y);
+  return df_norm(s, r);
+}
+// a double-float as FP64 (both parts exact, one FP64 add)
+__device__ __forceinline__ double df_to_d(float2 a) { return f2d_exact(a.x) + f2d_exact(a.y); }
 // a += conj(b) * c
 __host__ __device__ __forceinline__ void zcfma(z_t& a, z_t b, z_t c) {
   a.x = fma(b.x, c.x, fma(b.y, c.y, a.x));

@@ -500,6 +500,9 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz3_dot(z_t* __restrict__ part, 
 // Pass 2: alpha_j from the pass-1 partials (stored at lz[LZ_D + 2 (j-1)]),
 // u_(j+1) = s_j h - beta_{j-1} v_{j-1} - alpha_j v_j into dst (the next basis
 // slot, or h itself after the last iteration), partials of ||u_(j+1)||_m^2.
+// DF: the update and the norm in double-float arithmetic (the fixed-point
+// forms), each new entry rounded once to FP64.
+template <bool DF>
 __global__ void __launch_bounds__(LZ_THREADS) k_lz3_update(z_t* __restrict__ dst, const z_t* __restrict__ w,
                                                             const z_t* __restrict__ vPrev,
                                                             const z_t* __restrict__ vCur, const z_t* __restrict__ partIn,
@@ -528,6 +531,26 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz3_update(z_t* __restrict__ dst
   const double as = alpha * sj;
   const size_t n = S.nS;
   double q = 0.0;
+  if (DF) {
+    const float2 sj2 = df_split(sj), nbp2 = df_split(-bp), nas2 = df_split(-as), zero2 = make_float2(0.0f, 0.0f);
+    float qs = 0.0f, qc = 0.0f;
+    for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
+      const size_t i = vidx(S, l);
+      const z_t h = w[i], v = vCur[i];
+      float2 pr = zero2, pi = zero2;
+      if (vPrev) {
+        const z_t p = vPrev[i];
+        pr = df_split(p.x);
+        pi = df_split(p.y);
+      }
+      const float2 xr = df_dot3(sj2, df_split(h.x), nbp2, pr, nas2, df_split(v.x));
+      const float2 xi = df_dot3(sj2, df_split(h.y), nbp2, pi, nas2, df_split(v.y));
+      dst[i] = zmk(df_to_d(xr), df_to_d(xi));
+      const float2 u = df_dot2(xr, xr, xi, xi), m2 = df_split(m[i]);
+      df_mul_acc(qs, qc, m2.x, m2.y, u.x, u.y);
+    }
+    q = f2d_exact(qs) + f2d_exact(qc);
+  } else
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
     const size_t i = vidx(S, l);
     const z_t h = w[i];
@@ -626,8 +649,9 @@ void launch_lanczos_update(cgpu_ctx* c, int j, int maxDim, int pass1Blocks) {
       k_lz3_dot<<<g, LZ_THREADS, 0, c->stream>>>(p1, vPrev, vCur, c->lw_d, c->metric_d, TRAJ_PASS(c), c->lz_d, j);
       CODY_LAUNCHED(c);
     }
-    k_lz3_update<<<g, LZ_THREADS, 0, c->stream>>>(uNext, c->lw_d, vPrev, vCur, p1, n1, p2, c->metric_d,
-                                                  TRAJ_PASS(c), c->lz_d, j);
+    auto update = c->ciDf ? k_lz3_update<true> : k_lz3_update<false>;
+    update<<<g, LZ_THREADS, 0, c->stream>>>(uNext, c->lw_d, vPrev, vCur, p1, n1, p2, c->metric_d, TRAJ_PASS(c),
+                                            c->lz_d, j);
     CODY_LAUNCHED(c);
     // the gated second pass rarely fires: one block per trajectory reads the
     // gate (and, when it fires, walks the whole vector)

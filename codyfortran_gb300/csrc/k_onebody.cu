@@ -211,15 +211,23 @@ __global__ void k_onebody_lz_df(z_t* __restrict__ out, const z_t* __restrict__ v
   vPrev = (j > 1) ? bat(vPrev, bs) : nullptr;
   m = bat(m, bs);
   part = bat(part, bs);
-  double a = 0.0, q = 0.0;
+  // the pass is summed in double-float arithmetic (the FP64 pipe is the scarce one)
+  const float2 sj2 = df_split(sj), nbp2 = df_split(-bp), zero2 = make_float2(0.0f, 0.0f);
+  float as = 0.0f, ac = 0.0f, qs = 0.0f, qc = 0.0f;
+  // a += m Re(conj(v) x), q += m |x|^2 for the double-floats x, v, m
+  auto pass = [&](float2 xr, float2 xi, const z_t v, double mi) {
+    const float2 vr = df_split(v.x), vi = df_split(v.y), m2 = df_split(mi);
+    const float2 t = df_dot2(vr, xr, vi, xi), u = df_dot2(xr, xr, xi, xi);
+    df_mul_acc(as, ac, m2.x, m2.y, t.x, t.y);
+    df_mul_acc(qs, qc, m2.x, m2.y, u.x, u.y);
+  };
   if (bid == 0)  // the coefficient part: h = 0, x = -bp u_{j-1}
     for (int l = threadIdx.x; l < S.nC; l += OB_THREADS) {
       out[l] = zmk(0.0, 0.0);
       if (vPrev) {
-        const z_t p = vPrev[l], v = vCur[l];
-        const double xr = -bp * p.x, xi = -bp * p.y, mi = m[l];
-        a = fma(mi, fma(v.x, xr, v.y * xi), a);
-        q = fma(mi, fma(xr, xr, xi * xi), q);
+        const z_t p = vPrev[l];
+        const float2 pr = df_split(p.x), pi = df_split(p.y);
+        pass(df_dot2(nbp2, pr, zero2, zero2), df_dot2(nbp2, pi, zero2, zero2), vCur[l], m[l]);
       }
     }
   if (g0 < nG) {
@@ -259,21 +267,19 @@ __global__ void k_onebody_lz_df(z_t* __restrict__ out, const z_t* __restrict__ v
         df_mul_acc(acc.rs, acc.rc, pd.x, pd.y, v.x, v.y);
         df_mul_acc(acc.is, acc.ic, pd.x, pd.y, v.z, v.w);
       }
-      const z_t h = zdf_to_z(acc);
       const size_t o = (size_t)nG * i + g;
-      oo[o] = h;
-      double xr = sj * h.x, xi = sj * h.y;
+      oo[o] = zdf_to_z(acc);
+      const float2 hr = df_norm(acc.rs, acc.rc), hi = df_norm(acc.is, acc.ic);
+      float2 pr = zero2, pi = zero2;
       if (orbPrev) {
         const z_t p = orbPrev[o];
-        xr = fma(-bp, p.x, xr);
-        xi = fma(-bp, p.y, xi);
+        pr = df_split(p.x);
+        pi = df_split(p.y);
       }
-      const z_t v = f[g];
-      const double mi = mo[o];
-      a = fma(mi, fma(v.x, xr, v.y * xi), a);
-      q = fma(mi, fma(xr, xr, xi * xi), q);
+      pass(df_dot2(sj2, hr, nbp2, pr), df_dot2(sj2, hi, nbp2, pi), f[g], mo[o]);
     }
   }
+  const double a = f2d_exact(as) + f2d_exact(ac), q = f2d_exact(qs) + f2d_exact(qc);
   const z_t t = ob_block_sum(zmk(a * sj, q));
   if (threadIdx.x == 0) {
     part[(size_t)bid * 2] = zmk(t.x, 0.0);
