@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/cody_gpu.h"
+#include "dfloat.cuh"
 
 // ---------------------------------------------------------------------------
 // Complex arithmetic on double2 (layout-compatible with Fortran complex(R64)).
@@ -92,86 +93,7 @@ __device__ __forceinline__ z_t h2lin_value(const int* __restrict__ btOf, int i1,
   return v;
 }
 
-// ---- double-float arithmetic (a value as an unevaluated sum hi + lo of two
-// FP32 numbers, about 47 bits): the mixed forms' CI arithmetic, where FP64
-// issue (two FMA per cycle per SM) is the bound and FP32 runs 64 times faster.
-// A complex value is float4 {re.hi, re.lo, im.hi, im.lo} (16 bytes, as z_t).
-
-// x as hi + lo by integer operations: hi = the leading 24 bits (truncated),
-// lo = the next 29 bits rounded down to 24; |x| < 2^-100 becomes 0.
-__device__ __forceinline__ float2 df_split(double x) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
-  const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
-  const int e = (int)((u >> 52) & 0x7FF) - 1023;
-  if (e < -100) return make_float2(0.0f, 0.0f);
-  if (e > 127) return make_float2(__int_as_float((int)(sign | 0x7F800000u)), 0.0f);
-  const float hi = __int_as_float((int)(sign | ((unsigned)(e + 127) << 23) | (unsigned)((u >> 29) & 0x7FFFFF)));
-  const unsigned r = (unsigned)(u & 0x1FFFFFFF);  // value r 2^(e-52)
-  if (r == 0) return make_float2(hi, 0.0f);
-  const int msb = 31 - __clz(r);
-  const int elo = e - 52 + msb;
-  if (elo < -126) return make_float2(hi, 0.0f);
-  const unsigned mlo = (msb >= 23) ? ((r >> (msb - 23)) & 0x7FFFFF) : ((r << (23 - msb)) & 0x7FFFFF);
-  return make_float2(hi, __int_as_float((int)(sign | ((unsigned)(elo + 127) << 23) | mlo)));
-}
-
-__device__ __forceinline__ float4 zdf_from(z_t z) {
-  const float2 r = df_split(z.x), i = df_split(z.y);
-  return make_float4(r.x, r.y, i.x, i.y);
-}
-
-// (s, c) += p + q with an exact FP32 two-sum of s + p; the rounding errors and
-// q accumulate in c.
-__device__ __forceinline__ void df_acc(float& s, float& c, float p, float q) {
-  const float t = s + p;
-  const float bp = t - s;
-  const float err = (s - (t - bp)) + (p - bp);
-  s = t;
-  c += err + q;
-}
-
-// acc += h * x for complex double-float h, x; x negated when neg (sign bits).
-struct zdf_acc {
-  float rs, rc, is, ic;
-};
-__device__ __forceinline__ void zdf_fma(zdf_acc& a, float4 h, float4 x, bool neg) {
-  if (neg) {
-    x.x = -x.x;
-    x.y = -x.y;
-    x.z = -x.z;
-    x.w = -x.w;
-  }
-  // products a b of double-floats: p = a1 b1 exactly as p + e, plus the cross terms
-  float p, e;
-  p = h.x * x.x;
-  e = fmaf(h.x, x.x, -p);
-  e = fmaf(h.x, x.y, e);
-  e = fmaf(h.y, x.x, e);
-  df_acc(a.rs, a.rc, p, e);  // + hr xr
-  p = h.z * x.z;
-  e = fmaf(h.z, x.z, -p);
-  e = fmaf(h.z, x.w, e);
-  e = fmaf(h.w, x.z, e);
-  df_acc(a.rs, a.rc, -p, -e);  // - hi xi
-  p = h.x * x.z;
-  e = fmaf(h.x, x.z, -p);
-  e = fmaf(h.x, x.w, e);
-  e = fmaf(h.y, x.z, e);
-  df_acc(a.is, a.ic, p, e);  // + hr xi
-  p = h.z * x.x;
-  e = fmaf(h.z, x.x, -p);
-  e = fmaf(h.z, x.y, e);
-  e = fmaf(h.w, x.x, e);
-  df_acc(a.is, a.ic, p, e);  // + hi xr
-}
-
-// acc += conj(h) * x for complex double-floats; x negated when neg.
-__device__ __forceinline__ void zdf_cfma(zdf_acc& a, float4 h, float4 x, bool neg) {
-  h.z = -h.z;
-  h.w = -h.w;
-  zdf_fma(a, h, x, neg);
-}
-
+// ---- double-float arithmetic: dfloat.cuh; the warp sum of an accumulator here.
 __device__ __forceinline__ zdf_acc zdf_warp_sum(zdf_acc a) {
   for (int o = 16; o > 0; o >>= 1) {
     const float rs = __shfl_xor_sync(0xffffffffu, a.rs, o), rc = __shfl_xor_sync(0xffffffffu, a.rc, o);
@@ -182,51 +104,6 @@ __device__ __forceinline__ zdf_acc zdf_warp_sum(zdf_acc a) {
   return a;
 }
 
-// An FP32 value as FP64 by integer operations (exact; zero and FP32
-// subnormals, below 2^-126, give 0).
-__device__ __forceinline__ double f2d_exact(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned e = (u >> 23) & 0xFFu;
-  if (e == 0) return 0.0;
-  const unsigned long long be = (e == 0xFFu) ? 0x7FFull : (unsigned long long)(e - 127 + 1023);
-  return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) | (be << 52) |
-                                          ((unsigned long long)(u & 0x7FFFFFu) << 29)));
-}
-
-__device__ __forceinline__ z_t zdf_to_z(const zdf_acc& a) {
-  return zmk(f2d_exact(a.rs) + f2d_exact(a.rc), f2d_exact(a.is) + f2d_exact(a.ic));
-}
-
-// (s, c) += a * b for double-floats a, b (error-free FP32 product plus cross terms).
-__device__ __forceinline__ void df_mul_acc(float& s, float& c, float a1, float a2, float b1, float b2) {
-  const float p = a1 * b1;
-  float e = fmaf(a1, b1, -p);
-  e = fmaf(a1, b2, e);
-  e = fmaf(a2, b1, e);
-  df_acc(s, c, p, e);
-}
-// (s, c) from df_acc as a normalised double-float (hi, lo) by a fast two-sum
-__device__ __forceinline__ float2 df_norm(float s, float c) {
-  const float hi = s + c;
-  return make_float2(hi, c - (hi - s));
-}
-// a b + c d for double-floats, normalised
-__device__ __forceinline__ float2 df_dot2(float2 a, float2 b, float2 c, float2 d) {
-  float s = 0.0f, e = 0.0f;
-  df_mul_acc(s, e, a.x, a.y, b.x, b.y);
-  df_mul_acc(s, e, c.x, c.y, d.x, d.y);
-  return df_norm(s, e);
-}
-// a b + c d + e f for double-floats, normalised
-__device__ __forceinline__ float2 df_dot3(float2 a, float2 b, float2 c, float2 d, float2 e, float2 f) {
-  float s = 0.0f, r = 0.0f;
-  df_mul_acc(s, r, a.x, a.y, b.x, b.y);
-  df_mul_acc(s, r, c.x, c.y, d.x, d.y);
-  df_mul_acc(s, r, e.x, e.y, f.x, f.y);
-  return df_norm(s, r);
-}
-// a double-float as FP64 (both parts exact, one FP64 add)
-__device__ __forceinline__ double df_to_d(float2 a) { return f2d_exact(a.x) + f2d_exact(a.y); }
 // a += conj(b) * c
 __host__ __device__ __forceinline__ void zcfma(z_t& a, z_t b, z_t c) {
   a.x = fma(b.x, c.x, fma(b.y, c.y, a.x));

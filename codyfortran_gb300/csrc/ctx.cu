@@ -381,30 +381,6 @@ void put(cgpu_ctx* c, int b, T* dst0, const std::vector<T>& v) {
   CODY_CUDA(cudaMemcpy((char*)dst0 + (size_t)b * c->bs, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
 }
 
-// hi + lo FP32 split of x, as the device df_split (leading 24 bits truncated,
-// the next 29 rounded down to 24; |x| < 2^-100 gives 0).
-float2 df_split_host(double x) {
-  unsigned long long u;
-  std::memcpy(&u, &x, 8);
-  const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
-  const int e = (int)((u >> 52) & 0x7FF) - 1023;
-  auto asf = [](unsigned v) {
-    float f;
-    std::memcpy(&f, &v, 4);
-    return f;
-  };
-  if (e < -100) return make_float2(0.0f, 0.0f);
-  if (e > 127) return make_float2(asf(sign | 0x7F800000u), 0.0f);
-  const float hi = asf(sign | ((unsigned)(e + 127) << 23) | (unsigned)((u >> 29) & 0x7FFFFF));
-  const unsigned r = (unsigned)(u & 0x1FFFFFFF);
-  if (r == 0) return make_float2(hi, 0.0f);
-  int msb = 31;
-  while (!((r >> msb) & 1u)) msb--;
-  const int elo = e - 52 + msb;
-  if (elo < -126) return make_float2(hi, 0.0f);
-  const unsigned mlo = (msb >= 23) ? ((r >> (msb - 23)) & 0x7FFFFF) : ((r << (23 - msb)) & 0x7FFFFF);
-  return make_float2(hi, asf(sign | ((unsigned)(elo + 127) << 23) | mlo));
-}
 
 // Fixed-point form of a batch: when every trajectory has the same dense
 // interaction and its grid is a contiguous, bitwise-equal piece of one of a
@@ -539,7 +515,7 @@ void build_ctx(cgpu_ctx* c, const cgpu_desc* descs, int nSys) {
     put(c, b, c->T_d, s.band_h);
     if (c->Tdf_d) {
       std::vector<float2> tdf(s.band_h.size());
-      for (size_t k = 0; k < s.band_h.size(); k++) tdf[k] = df_split_host(s.band_h[k]);
+      for (size_t k = 0; k < s.band_h.size(); k++) tdf[k] = df_split(s.band_h[k]);
       put(c, b, c->Tdf_d, tdf);
     }
     put(c, b, c->btOfOrb_d, s.btOfOrb);

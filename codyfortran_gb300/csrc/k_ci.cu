@@ -20,6 +20,11 @@
 
 namespace {
 
+// threads of an RDM pair-gather block (one pair of singles codes per thread):
+// the staged CI vector (up to 72 KB) allows three blocks per SM, so the block
+// size sets the warps in flight for these latency-bound gathers
+constexpr int CI_PAIR_THREADS = 256;
+
 __device__ __forceinline__ unsigned long long bitmask_below(int p) {  // bits [0, p)
   return p >= 64 ? ~0ULL : ((1ULL << p) - 1ULL);
 }
@@ -272,6 +277,34 @@ __global__ void k_ci_apply_df(const z_t* __restrict__ C0, z_t* __restrict__ dC0,
           int n2 = v.sN[b2][c2 - 1];
           size_t col2 = (size_t)v.maxS[b2] * (c2 - 1);
           int st2 = v.stride[b2];
+          if (n1 <= 32 && n2 <= 32) {
+            // the n1 x n2 pairs of singles spread over all lanes: lane k holds
+            // entry k of both tables (integral row / column, configuration
+            // offset, sign in bit 0 of the packed code), pair t = (t / n2, t % n2)
+            int p1 = 0, e1 = 0, p2 = 0, e2 = 0;
+            if (lane < n1) {
+              p1 = ((v.sCode[b][col1 + lane] - 1) * nO2) * 2 + (v.sFac[b][col1 + lane] < 0);
+              e1 = (v.sExc[b][col1 + lane] - c) * st;
+            }
+            if (lane < n2) {
+              p2 = v.sCode[b2][col2 + lane] * 2 + (v.sFac[b2][col2 + lane] < 0);
+              e2 = (v.sExc[b2][col2 + lane] - c2) * st2;
+            }
+            const int total = n1 * n2, q = 32 / n2, r = 32 - q * n2;
+            int k1 = lane / n2, k2 = lane - k1 * n2;
+            for (int base = 0; base < total; base += 32) {
+              const int a1 = __shfl_sync(0xffffffffu, p1, k1 & 31), x1 = __shfl_sync(0xffffffffu, e1, k1 & 31);
+              const int a2 = __shfl_sync(0xffffffffu, p2, k2), x2 = __shfl_sync(0xffffffffu, e2, k2);
+              if (base + lane < total)
+                zdf_fma(acc, h2[(a1 >> 1) + (a2 >> 1)], C[I - 1 + x1 + x2], ((a1 ^ a2) & 1) != 0);
+              k1 += q;
+              k2 += r;
+              if (k2 >= n2) {
+                k2 -= n2;
+                k1++;
+              }
+            }
+          } else
           for (int k2b = 0; k2b < n2; k2b += 32) {
             int k2 = k2b + lane;
             bool has2 = k2 < n2;
@@ -787,7 +820,8 @@ void ci_build_work(cgpu_ctx* c) {
       }
     }
   };
-  // a block holds at least ~8 configurations (one per warp) / ~128 RDM tasks (one per thread) on average
+  // a block holds at least ~8 configurations (one per warp) / ~CI_PAIR_THREADS RDM pair tasks (one per
+  // thread) on average
   long nConfTot = 0, nTaskTot = 0, nPairTot = 0;
   for (int t = 0; t < c->nb; t++) {
     nConfTot += (long)aw[t].size();
@@ -796,7 +830,7 @@ void ci_build_work(cgpu_ctx* c) {
   }
   cut(aw, std::max({64L, aTot / (8 * 152), 8 * aTot / std::max(1L, nConfTot)}), 1 << 20, apply);
   cut(rw, std::max({64L, rTot / (8 * 152), 8 * rTot / std::max(1L, nTaskTot)}), 1 << 20, rdm);
-  cut(pw, std::max({64L, pTot / (8 * 152), 128 * pTot / std::max(1L, nPairTot)}), 1 << 20, pairs);
+  cut(pw, std::max({64L, pTot / (8 * 152), (long)CI_PAIR_THREADS * pTot / std::max(1L, nPairTot)}), 1 << 20, pairs);
   c->nApplyWork = (int)apply.size();
   c->nRdmWork = (int)rdm.size();
   c->nPairWork = (int)pairs.size();
@@ -847,10 +881,11 @@ void launch_ci_rdm(cgpu_ctx* c, const z_t* C, int want1, int want2) {
   }
   if (want2 && c->nPairWork > 0) {
     if (df)
-      k_ci_rdm_pairs_df<<<c->nPairWork, 128, c->ciSmem, c->stream>>>(C, c->rdm2Lin_d, TRAJ_PASS(c), c->pairWork_d);
+      k_ci_rdm_pairs_df<<<c->nPairWork, CI_PAIR_THREADS, c->ciSmem, c->stream>>>(C, c->rdm2Lin_d, TRAJ_PASS(c),
+                                                                              c->pairWork_d);
     else
-      k_ci_rdm_pairs<<<c->nPairWork, 128, c->ciSmem, c->stream>>>(C, c->rdm2Lin_d, TRAJ_PASS(c), c->pairWork_d,
-                                                                  c->ciSmem > 0);
+      k_ci_rdm_pairs<<<c->nPairWork, CI_PAIR_THREADS, c->ciSmem, c->stream>>>(C, c->rdm2Lin_d, TRAJ_PASS(c),
+                                                                              c->pairWork_d, c->ciSmem > 0);
     CODY_LAUNCHED(c);
   }
   if (want1) {

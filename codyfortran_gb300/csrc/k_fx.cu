@@ -26,7 +26,9 @@
 // warps.  Per 64-wide K block the producer loads the L slices of the B tile
 // (in 16-row boxes, only the rows of the trajectory's own columns) into one
 // ring stage and the L slices of the A tile into L stages of a second ring; the issuer runs the L(L+1)/2 slice products of the block from
-// shared memory with the MMA width cut to the trajectory's own N.  The
+// shared memory with the MMA width cut to the trajectory's own N, the L - i
+// products of A slice i back to back per 16-wide K step so that A comes from
+// the tensor core's collector buffer after its first read.  The
 // epilogue stages the FP64 tile in shared memory for coalesced stores.  The
 // wide configuration (two B stages, deep A ring) holds one CTA per SM; the
 // compact one (one B stage, L A stages, <= 256 TMEM columns) two.  Every wait
@@ -255,13 +257,19 @@ __global__ void __launch_bounds__(192)
             consumedA = ca;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint64_t ad = adesc0 + (uint64_t)((sa * C::A_BYTES) >> 4);
+            // the L - i products of A slice i share each 16-wide K step of A:
+            // issued back to back, A is read from shared memory once per step
+            // and reused from the collector buffer
 #pragma unroll
-            for (int j = 0; j < L - i; j++) {
-              const uint32_t d = tmem + (uint32_t)((i + j) * BN);
-              const uint64_t bdj = bd + (uint64_t)((j * C::B_BYTES) >> 4);
+            for (int k = 0; k < TC_BK / 16; k++) {
 #pragma unroll
-              for (int k = 0; k < TC_BK / 16; k++)
-                umma_bf16(d, ad + 2 * k, bdj + 2 * k, idesc, (kb > 0 || i > 0 || k > 0) ? 1u : 0u);
+              for (int j = 0; j < L - i; j++) {
+                const int last = L - i - 1;
+                const int coll = last == 0 ? 0 : (j == 0 ? 1 : (j == last ? 3 : 2));
+                umma_bf16_coll(coll, tmem + (uint32_t)((i + j) * BN), ad + 2 * k,
+                               bd + (uint64_t)((j * C::B_BYTES) >> 4) + 2 * k, idesc,
+                               (kb > 0 || i > 0 || k > 0) ? 1u : 0u);
+              }
             }
             umma_commit(&aEmpty[sa]);
           }

@@ -143,6 +143,35 @@ __device__ __forceinline__ void umma_bf16(uint32_t tmemD, uint64_t adesc, uint64
       : "memory");
 }
 
+// The same MMA with the A operand's collector buffer: coll 1 reads A from
+// shared memory and keeps it (fill), 2 reuses the kept A (use), 3 reuses it a
+// last time (lastuse); 0 = umma_bf16.  A run fill, use..., lastuse carries
+// the same A descriptor and is issued back to back by one thread.  Callers
+// pass coll from unrolled loops, so the branches fold away.
+__device__ __forceinline__ void umma_bf16_coll(int coll, uint32_t tmemD, uint64_t adesc, uint64_t bdesc,
+                                               uint32_t idesc, uint32_t accumulate) {
+  if (coll == 1)
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%0], %1, %2, %3, p;\n}\n" ::"r"(tmemD),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  else if (coll == 2)
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16.collector::a::use [%0], %1, %2, %3, p;\n}\n" ::"r"(tmemD),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  else if (coll == 3)
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [%0], %1, %2, %3, p;\n}\n" ::"r"(tmemD),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  else
+    umma_bf16(tmemD, adesc, bdesc, idesc, accumulate);
+}
+
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
