@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libcodygpu.so")
 SOURCES = ["ctx.cu", "k_onebody.cu", "k_ci.cu", "k_mf.cu", "k_lanczos.cu", "noalloc.cu", "k_tc.cu", "k_fx.cu", "k_mixed.cu", "k_adjoint.cu", "autotune.cu", "k_sys.cu", "k_adjoint_mc.cu"]
-HEADERS = ["common.cuh", "tc.cuh"]
+HEADERS = ["common.cuh", "tc.cuh", "dfloat.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

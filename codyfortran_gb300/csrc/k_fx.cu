@@ -22,8 +22,10 @@
 // the operand truncation (2^-(bL+1) of each row maximum) they bound the error
 // at about 2^-bL max|a| max|b| K.
 //
-// Pipeline: one TMA producer thread, one MMA issuer thread, four epilogue
-// warps.  Per 64-wide K block the producer loads the L slices of the B tile
+// Pipeline: one TMA producer thread, one MMA issuer thread, eight epilogue
+// warps (the tile's accumulators fill the tensor memory, so the epilogue of
+// one tile cannot overlap the MMAs of the next; two warps per lane quarter
+// halve its latency-bound duration).  Per 64-wide K block the producer loads the L slices of the B tile
 // (in 16-row boxes, only the rows of the trajectory's own columns) into one
 // ring stage and the L slices of the A tile into L stages of a second ring; the issuer runs the L(L+1)/2 slice products of the block from
 // shared memory with the MMA width cut to the trajectory's own N, the L - i
@@ -103,8 +105,9 @@ struct FxTile {
 };
 
 // out[traj][split][M][N] = C (FP64) over the tile list; a persistent CTA takes
-// tiles blockIdx.x, blockIdx.x + gridDim.x, ...  Warps 0-3: epilogue (TMEM lanes
-// 32w..32w+31); warp 4: TMA producer; warp 5: MMA issuer.  The rings and their
+// tiles blockIdx.x, blockIdx.x + gridDim.x, ...  Warps 0..EW-1: epilogue (TMEM
+// lanes 32(w%4)..32(w%4)+31, column batches of CB); warp EW: TMA producer;
+// warp EW+1: MMA issuer.  The rings and their
 // phases run on across tiles; the accumulator hand-off uses accFull (MMA ->
 // epilogue) and accEmpty (epilogue -> MMA), so the producer loads the next
 // tile while the epilogue drains the current one.  K splits: a trajectory of
@@ -114,14 +117,15 @@ struct FxTile {
 // aShared: A is shared by the trajectories (3D map with one plane per root
 // grid); the trajectory's rows start at vRow of plane vRoot, its K range at
 // vRow - gShift, its row exponents at expA[vExp].
-template <int BN, int L, int NA_, int NB_>
-__global__ void __launch_bounds__(192)
+template <int BN, int L, int NA_, int NB_, int EW, int CB>
+__global__ void __launch_bounds__(32 * (EW + 2), NA_ > 0 ? 2 : 1)
     k_fx_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, double* __restrict__ out,
               const int* __restrict__ expA, const int* __restrict__ expB, unsigned* __restrict__ maxRow,
               unsigned* __restrict__ maxCol, TRAJ_ARGS, int gemmId, int segPitchA, int segPitch, int aShared,
               int kPer, int digitBits, const FxTile* __restrict__ tiles, int nTiles, int* __restrict__ err) {
   using C = FxCfg<BN, L, NA_, NB_>;
   constexpr int NA = C::NA, NB = C::NB;
+  static_assert(EW % 4 == 0 && (CB == 8 || CB == 16) && BN % CB == 0, "epilogue warps / column batch");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* ringA = smem;
@@ -144,7 +148,7 @@ __global__ void __launch_bounds__(192)
       mbar_init(&bEmpty[s], 1);
     }
     mbar_init(&accFull, 1);
-    mbar_init(&accEmpty, 4);
+    mbar_init(&accEmpty, EW);
     mbar_init(&finalBar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -170,7 +174,7 @@ __global__ void __launch_bounds__(192)
     nk = tl.split < sT ? max(0, min(segTiles, kt0 + per) - kt0) : 0;
   };
 
-  if (warp == 4) {
+  if (warp == EW) {
     if (lane == 0) {
       // TMA producer: per K block the L B slices (16-row boxes of the tile's rows), then the L A slices
       int ta = 0, tb = 0;
@@ -211,7 +215,7 @@ __global__ void __launch_bounds__(192)
         }
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == EW + 1) {
     if (lane == 0) {
       // MMA issuer: kind::f16, D=F32, A=B=BF16, K-major, M=128; descriptors
       // advance by address / 16: +2 per 16-wide K step, +B_BYTES/16 per B slice
@@ -282,18 +286,21 @@ __global__ void __launch_bounds__(192)
       umma_commit(&finalBar);  // arrives when every issued MMA has completed
     }
   } else {
-    // epilogue: warp w owns TMEM lanes [32w, 32w+32) = tile rows
+    // epilogue: warp w owns TMEM lanes [32q, 32q+32) = tile rows, q = w % 4
+    // (the lane quarter a warp may access), and every (EW/4)-th batch of CB
+    // columns starting at batch w / 4
     const long long base = 1LL << digitBits;
+    const int q = warp & 3, cg = warp >> 2;
     int ph = 0;
     for (int t = blockIdx.x; t < nTiles; t += gridDim.x) {
       const FxTile tl = tiles[t];
       int M, N, nT, kt0, nk;
       geometry(tl, M, N, nT, kt0, nk);
       double* Oz = batn(out, bs, tl.traj) + (size_t)tl.split * (size_t)M * N;
-      const int r = warp * 32 + lane, row = tl.m0 + r;
+      const int r = q * 32 + lane, row = tl.m0 + r;
       const bool rowOk = row < M;
       if (nk == 0) {  // empty split: its partial is zero
-        if (rowOk)
+        if (rowOk && cg == 0)
           for (int col = tl.n0; col < min(N, tl.n0 + BN); col++) Oz[(size_t)row * N + col] = 0.0;
         continue;
       }
@@ -309,15 +316,19 @@ __global__ void __launch_bounds__(192)
       const int ea = rowOk ? eA[row] - digitBits * (L + 1) : 0;
       unsigned rowMaxEx = 0;
 #pragma unroll 1
-      for (int c = 0; c < nT; c += 16) {
-        uint32_t acc[L][16];
+      for (int c = cg * CB; c < nT; c += (EW / 4) * CB) {
+        uint32_t acc[L][CB];
 #pragma unroll
-        for (int l = 0; l < L; l++)
-          TMEM_LD_X16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * BN + c), acc[l]);
+        for (int l = 0; l < L; l++) {
+          if (CB == 16)
+            TMEM_LD_X16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(l * BN + c), acc[l]);
+          else
+            TMEM_LD_X8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(l * BN + c), acc[l]);
+        }
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        double v[16];
+        double v[CB];
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
+        for (int j = 0; j < CB; j++) {
           const int col = tl.n0 + c + j;
           unsigned ex = 0;
           v[j] = 0.0;
@@ -337,7 +348,7 @@ __global__ void __launch_bounds__(192)
         if (rowOk) {
           double* dst = Oz + (size_t)row * N + tl.n0 + c;
 #pragma unroll
-          for (int j = 0; j < 16; j += 2)
+          for (int j = 0; j < CB; j += 2)
             if (tl.n0 + c + j < N) *reinterpret_cast<double2*>(dst + j) = make_double2(v[j], v[j + 1]);
         }
       }
@@ -351,7 +362,7 @@ __global__ void __launch_bounds__(192)
   __syncthreads();
   // every issued MMA has completed before the tensor memory is freed; after an
   // abort also the TMA copies that were issued but never consumed (bounded waits)
-  if (warp == 4 && lane == 0) {
+  if (warp == EW && lane == 0) {
     volatile int dummy = 0;
     mbar_wait(&finalBar, 0, &dummy);
     if (abortFlag) {
@@ -370,16 +381,20 @@ void launch_fx_t(cgpu_ctx* c, const CUtensorMap& ta, const CUtensorMap& tb, doub
                  const int* expB, unsigned* maxRow, unsigned* maxCol, int gemmId, int segPitchA, int segPitch,
                  int aShared, int kPer, int digitBits, const FxTile* tiles, int nTiles, int ctasPerSm, int* err) {
   using C = FxCfg<BN, L, NA_, NB_>;
+  // eight epilogue warps (two per tensor-memory lane quarter); the compact
+  // configuration (two CTAs per SM) loads eight columns per batch to stay
+  // inside half the register file
+  constexpr int EW = 8, CB = NA_ > 0 ? 8 : 16;
+  auto kern = k_fx_gemm<BN, L, NA_, NB_, EW, CB>;
   static bool attr = false;
   if (!attr) {
-    CODY_CUDA(cudaFuncSetAttribute(k_fx_gemm<BN, L, NA_, NB_>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+    CODY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
     attr = true;
   }
   if (nTiles <= 0) return;
   const int grid = std::min(nTiles, c->numSms * ctasPerSm);
-  k_fx_gemm<BN, L, NA_, NB_><<<grid, 192, C::SMEM, c->stream>>>(ta, tb, out, expA, expB, maxRow, maxCol, TRAJ_PASS(c),
-                                                                gemmId, segPitchA, segPitch, aShared, kPer,
-                                                                digitBits, tiles, nTiles, err);
+  kern<<<grid, 32 * (EW + 2), C::SMEM, c->stream>>>(ta, tb, out, expA, expB, maxRow, maxCol, TRAJ_PASS(c), gemmId,
+                                                    segPitchA, segPitch, aShared, kPer, digitBits, tiles, nTiles, err);
   CODY_LAUNCHED(c);
 }
 
