@@ -386,6 +386,19 @@ __global__ void k_ci_rdm_codes(const z_t* __restrict__ C0, z_t* __restrict__ r1L
     z_t acc = zmk(0.0, 0.0);
     if (nRest == 1) {
       for (int e = e0 + lane; e < e1; e += 32) zcfma(acc, C[dst[e] * st], zsign(C[src[e] * st], fac[e] < 0));
+    } else if (v.nBt == 2) {  // as in k_ci_rdm_codes_df: (e, r) advanced without divisions
+      const int sto = v.stride[1 - b], q = 32 / nRest, rr = 32 - q * nRest;
+      int e = e0 + lane / nRest, r = lane % nRest;
+      for (int t = lane; t < (e1 - e0) * nRest; t += 32) {
+        const int base = r * sto;
+        zcfma(acc, C[base + dst[e] * st], zsign(C[base + src[e] * st], fac[e] < 0));
+        e += q;
+        r += rr;
+        if (r >= nRest) {
+          r -= nRest;
+          e++;
+        }
+      }
     } else {
       for (int t = lane; t < (e1 - e0) * nRest; t += 32) {
         int e = e0 + t / nRest, r = t % nRest;
@@ -475,6 +488,21 @@ __global__ void k_ci_rdm_codes_df(const z_t* __restrict__ C0, z_t* __restrict__ 
     zdf_acc acc = {0.0f, 0.0f, 0.0f, 0.0f};
     if (nRest == 1) {
       for (int e = e0 + lane; e < e1; e += 32) zdf_cfma(acc, C[dst[e] * st], C[src[e] * st], fac[e] < 0);
+    } else if (v.nBt == 2) {
+      // term t = (excitation e0 + t / nRest, configuration r = t % nRest of the
+      // other body type), advanced by 32 terms per step without divisions
+      const int sto = v.stride[1 - b], q = 32 / nRest, rr = 32 - q * nRest;
+      int e = e0 + lane / nRest, r = lane % nRest;
+      for (int t = lane; t < (e1 - e0) * nRest; t += 32) {
+        const int base = r * sto;
+        zdf_cfma(acc, C[base + dst[e] * st], C[base + src[e] * st], fac[e] < 0);
+        e += q;
+        r += rr;
+        if (r >= nRest) {
+          r -= nRest;
+          e++;
+        }
+      }
     } else {
       for (int t = lane; t < (e1 - e0) * nRest; t += 32) {
         int e = e0 + t / nRest, r = t % nRest;

@@ -192,7 +192,7 @@ __device__ z_t ob_block_sum(z_t v) {
 // (b = blockIdx.x + gridDim.x blockIdx.y), the layout the pass-2 kernel reads.
 // The one-body apply has just read u_j; the pass reads u_{j-1} and m besides,
 // instead of a separate pass over h, u_j, u_{j-1} and m.
-__global__ void k_onebody_lz_df(z_t* __restrict__ out, const z_t* __restrict__ vCur, const z_t* __restrict__ vPrev,
+__global__ void __launch_bounds__(OB_THREADS, 4) k_onebody_lz_df(z_t* __restrict__ out, const z_t* __restrict__ vCur, const z_t* __restrict__ vPrev,
                                 const double* __restrict__ m, z_t* __restrict__ part, const float2* __restrict__ Tdf,
                                 const double* __restrict__ V0, const double* __restrict__ x,
                                 const int* __restrict__ btOf, TRAJ_ARGS, const double* __restrict__ Efield,
@@ -215,11 +215,14 @@ __global__ void k_onebody_lz_df(z_t* __restrict__ out, const z_t* __restrict__ v
   const float2 sj2 = df_split(sj), nbp2 = df_split(-bp), zero2 = make_float2(0.0f, 0.0f);
   float as = 0.0f, ac = 0.0f, qs = 0.0f, qc = 0.0f;
   // a += m Re(conj(v) x), q += m |x|^2 for the double-floats x, v, m
-  auto pass = [&](float2 xr, float2 xi, const z_t v, double mi) {
-    const float2 vr = df_split(v.x), vi = df_split(v.y), m2 = df_split(mi);
+  auto pass_df = [&](float2 xr, float2 xi, float2 vr, float2 vi, double mi) {
+    const float2 m2 = df_split(mi);
     const float2 t = df_dot2(vr, xr, vi, xi), u = df_dot2(xr, xr, xi, xi);
     df_mul_acc(as, ac, m2.x, m2.y, t.x, t.y);
     df_mul_acc(qs, qc, m2.x, m2.y, u.x, u.y);
+  };
+  auto pass = [&](float2 xr, float2 xi, const z_t v, double mi) {
+    pass_df(xr, xi, df_split(v.x), df_split(v.y), mi);
   };
   if (bid == 0)  // the coefficient part: h = 0, x = -bp u_{j-1}
     for (int l = threadIdx.x; l < S.nC; l += OB_THREADS) {
@@ -244,23 +247,63 @@ __global__ void k_onebody_lz_df(z_t* __restrict__ out, const z_t* __restrict__ v
     const int g = g0 + threadIdx.x;
     const bool live = g < nG;
     const float2 pd = (S.hasPot && live) ? df_split(fma(E, x[g], V0[g])) : make_float2(0.0f, 0.0f);
-    for (int i = blockIdx.y; i < S.nOS; i += gridDim.y) {
-      const z_t* f = orbCur + (size_t)nG * i;
-      if (i != (int)blockIdx.y) __syncthreads();
-      for (int t = threadIdx.x; t < nTile; t += OB_THREADS) {
-        const int gg = g0 - band + t;
-        shf[t] = (gg >= 0 && gg < nG) ? zdf_from(f[gg]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    // restricted orbitals share one band: its coefficients for this grid tile
+    // are staged in shared memory once (after the orbital tile, nd rows of
+    // OB_THREADS double-floats)
+    float2* shT = reinterpret_cast<float2*>(shf + nTile);
+    if (S.restricted) {
+      for (int d = 0; d < nd; d++) shT[d * OB_THREADS + threadIdx.x] = live ? Tdf[(size_t)d * nG + g] : zero2;
+    }
+    // the orbital tile (entries threadIdx.x and threadIdx.x + OB_THREADS) and
+    // this thread's v_{j-1} and metric entries are fetched one orbital ahead
+    auto tile_at = [&](int i, int t) {
+      const int gg = g0 - band + t;
+      return (t < nTile && gg >= 0 && gg < nG) ? orbCur[(size_t)nG * i + gg] : zmk(0.0, 0.0);
+    };
+    const int i0 = blockIdx.y;
+    z_t nx0 = zmk(0.0, 0.0), nx1 = zmk(0.0, 0.0), np = zmk(0.0, 0.0);
+    double nm = 0.0;
+    if (i0 < S.nOS) {
+      nx0 = tile_at(i0, threadIdx.x);
+      nx1 = tile_at(i0, threadIdx.x + OB_THREADS);
+      if (live) {
+        if (orbPrev) np = orbPrev[(size_t)nG * i0 + g];
+        nm = mo[(size_t)nG * i0 + g];
+      }
+    }
+    for (int i = i0; i < S.nOS; i += gridDim.y) {
+      if (i != i0) __syncthreads();
+      shf[threadIdx.x] = zdf_from(nx0);
+      if (threadIdx.x + OB_THREADS < nTile) shf[threadIdx.x + OB_THREADS] = zdf_from(nx1);
+      const z_t p = np;
+      const double mi = nm;
+      const int in = i + gridDim.y;
+      if (in < S.nOS) {
+        nx0 = tile_at(in, threadIdx.x);
+        nx1 = tile_at(in, threadIdx.x + OB_THREADS);
+        if (live) {
+          if (orbPrev) np = orbPrev[(size_t)nG * in + g];
+          nm = mo[(size_t)nG * in + g];
+        }
       }
       __syncthreads();
       if (!live) continue;
-      const int bt = S.restricted ? 0 : btOf[i];
-      const float2* Tb = Tdf + (size_t)bt * nd * nG;
       zdf_acc acc = {0.0f, 0.0f, 0.0f, 0.0f};
-      for (int d = 0; d < nd; d++) {
-        const float2 cf = Tb[(size_t)d * nG + g];
-        const float4 v = shf[threadIdx.x + d];
-        df_mul_acc(acc.rs, acc.rc, cf.x, cf.y, v.x, v.y);
-        df_mul_acc(acc.is, acc.ic, cf.x, cf.y, v.z, v.w);
+      if (S.restricted) {
+        for (int d = 0; d < nd; d++) {
+          const float2 cf = shT[d * OB_THREADS + threadIdx.x];
+          const float4 v = shf[threadIdx.x + d];
+          df_mul_acc(acc.rs, acc.rc, cf.x, cf.y, v.x, v.y);
+          df_mul_acc(acc.is, acc.ic, cf.x, cf.y, v.z, v.w);
+        }
+      } else {
+        const float2* Tb = Tdf + (size_t)btOf[i] * nd * nG;
+        for (int d = 0; d < nd; d++) {
+          const float2 cf = Tb[(size_t)d * nG + g];
+          const float4 v = shf[threadIdx.x + d];
+          df_mul_acc(acc.rs, acc.rc, cf.x, cf.y, v.x, v.y);
+          df_mul_acc(acc.is, acc.ic, cf.x, cf.y, v.z, v.w);
+        }
       }
       if (S.hasPot) {
         const float4 v = shf[threadIdx.x + band];
@@ -272,11 +315,12 @@ __global__ void k_onebody_lz_df(z_t* __restrict__ out, const z_t* __restrict__ v
       const float2 hr = df_norm(acc.rs, acc.rc), hi = df_norm(acc.is, acc.ic);
       float2 pr = zero2, pi = zero2;
       if (orbPrev) {
-        const z_t p = orbPrev[o];
         pr = df_split(p.x);
         pi = df_split(p.y);
       }
-      pass(df_dot2(sj2, hr, nbp2, pr), df_dot2(sj2, hi, nbp2, pi), f[g], mo[o]);
+      const float4 vc = shf[threadIdx.x + band];  // u_j at g, already split
+      pass_df(df_dot2(sj2, hr, nbp2, pr), df_dot2(sj2, hi, nbp2, pi), make_float2(vc.x, vc.y),
+              make_float2(vc.z, vc.w), mi);
     }
   }
   const double a = f2d_exact(as) + f2d_exact(ac), q = f2d_exact(qs) + f2d_exact(qc);
@@ -815,7 +859,8 @@ int launch_onebody_lz(cgpu_ctx* c, int j, double t) {
   const z_t* vCur = c->basis_d + (size_t)c->nS * (j - 1);
   const z_t* vPrev = j > 1 ? c->basis_d + (size_t)c->nS * (j - 2) : nullptr;
   dim3 grid(tiles, groups, c->nb);
-  size_t sh = sizeof(z_t) * (OB_THREADS + 2 * c->band);
+  // the orbital tile (double-floats) and the band coefficients of the tile
+  size_t sh = sizeof(float4) * (OB_THREADS + 2 * c->band) + sizeof(float2) * (2 * c->band + 1) * OB_THREADS;
   k_onebody_lz_df<<<grid, OB_THREADS, sh, c->stream>>>(c->lw_d, vCur, vPrev, c->metric_d, c->partial_d, c->Tdf_d,
                                                         c->V0_d, c->x_d, c->btOfOrb_d, TRAJ_PASS(c), E, c->lz_d, j);
   CODY_LAUNCHED(c);
