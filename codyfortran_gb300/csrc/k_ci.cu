@@ -24,6 +24,9 @@ namespace {
 // the staged CI vector (up to 72 KB) allows three blocks per SM, so the block
 // size sets the warps in flight for these latency-bound gathers
 constexpr int CI_PAIR_THREADS = 256;
+// threads of an H.C block (one configuration per warp): with 55 registers per
+// thread two 512-thread blocks fit an SM, 32 warps sharing two staged CI vectors
+constexpr int CI_APPLY_THREADS = 512;
 
 __device__ __forceinline__ unsigned long long bitmask_below(int p) {  // bits [0, p)
   return p >= 64 ? ~0ULL : ((1ULL << p) - 1ULL);
@@ -856,7 +859,8 @@ void ci_build_work(cgpu_ctx* c) {
     nTaskTot += (long)rw[t].size();
     nPairTot += (long)pw[t].size();
   }
-  cut(aw, std::max({64L, aTot / (8 * 152), 8 * aTot / std::max(1L, nConfTot)}), 1 << 20, apply);
+  cut(aw, std::max({64L, aTot / (8 * 152), (long)(CI_APPLY_THREADS / 32) * aTot / std::max(1L, nConfTot)}), 1 << 20,
+      apply);
   cut(rw, std::max({64L, rTot / (8 * 152), 8 * rTot / std::max(1L, nTaskTot)}), 1 << 20, rdm);
   cut(pw, std::max({64L, pTot / (8 * 152), (long)CI_PAIR_THREADS * pTot / std::max(1L, nPairTot)}), 1 << 20, pairs);
   c->nApplyWork = (int)apply.size();
@@ -885,8 +889,9 @@ void ci_build_work(cgpu_ctx* c) {
 void launch_ci_apply(cgpu_ctx* c, const z_t* C, z_t* dC, int useH1, int useH2) {
   ProfScope prof(c, CGPU_KERNEL_CI_APPLY);
   if (c->ciDf && c->ciSmem > 0)
-    k_ci_apply_df<<<c->nApplyWork, 256, c->ciSmem, c->stream>>>(C, dC, c->h1Df_d, c->h2Df_d, TRAJ_PASS(c),
-                                                               c->applyWork_d, useH1, useH2);
+    k_ci_apply_df<<<c->nApplyWork, CI_APPLY_THREADS, c->ciSmem, c->stream>>>(C, dC, c->h1Df_d, c->h2Df_d,
+                                                                            TRAJ_PASS(c), c->applyWork_d, useH1,
+                                                                            useH2);
   else
     k_ci_apply<<<c->nApplyWork, 256, c->ciSmem, c->stream>>>(C, dC, c->h1Lin_d, c->h2Lin_d, TRAJ_PASS(c),
                                                             c->applyWork_d, c->ciSmem > 0, useH1, useH2);

@@ -379,6 +379,9 @@ __global__ void k_lz_expsub(double* __restrict__ lz, int mFixed, double dt, doub
 
 
 // out = nrm * sum_{j < mDim} phi_j s_j V_j   (or out = in when the start vector had zero norm)
+// DF: the sum in double-float arithmetic (the fixed-point forms; the FP64 form
+// costs 4 m FP64 FMA per entry on the scarce FP64 pipe), rounded once to FP64.
+template <bool DF>
 __global__ void k_lz_combine(z_t* __restrict__ out, const z_t* __restrict__ in, const z_t* __restrict__ V,
                              size_t ldv, TRAJ_ARGS, const double* __restrict__ lz) {
   const TrajShape& S = shp[blockIdx.z];
@@ -388,11 +391,15 @@ __global__ void k_lz_combine(z_t* __restrict__ out, const z_t* __restrict__ in, 
   lz = bat(lz, bs);
   const size_t n = S.nS;
   __shared__ z_t phi[CODY_MAX_KRYLOV];
+  __shared__ float4 phiDf[CODY_MAX_KRYLOV];
   int m = (int)lz[LZ_MDIM];
   double nrm = lz[LZ_NRM];
   bool zero = lz[LZ_ZERO] != 0.0;
-  for (int k = threadIdx.x; k < m; k += blockDim.x)
+  for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    // the coefficient with the norm folded in (one rounding)
     phi[k] = zscale(zmk(lz[LZ_PHI + 2 * k], lz[LZ_PHI + 2 * k + 1]), lz[LZ_S + k]);
+    if (DF) phiDf[k] = zdf_from(zscale(phi[k], nrm));
+  }
   __syncthreads();
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
     size_t i = vidx(S, l);
@@ -400,9 +407,15 @@ __global__ void k_lz_combine(z_t* __restrict__ out, const z_t* __restrict__ in, 
       out[i] = in[i];
       continue;
     }
-    z_t acc = zmk(0.0, 0.0);
-    for (int k = 0; k < m; k++) zfma(acc, V[ldv * k + i], phi[k]);
-    out[i] = zscale(acc, nrm);
+    if (DF) {
+      zdf_acc acc = {0.0f, 0.0f, 0.0f, 0.0f};
+      for (int k = 0; k < m; k++) zdf_fma(acc, phiDf[k], zdf_from(V[ldv * k + i]), false);
+      out[i] = zdf_to_z(acc);
+    } else {
+      z_t acc = zmk(0.0, 0.0);
+      for (int k = 0; k < m; k++) zfma(acc, V[ldv * k + i], phi[k]);
+      out[i] = zscale(acc, nrm);
+    }
   }
 }
 
@@ -701,8 +714,8 @@ void launch_lanczos_tail(cgpu_ctx* c, int j, double dt, int evalExp) {
 
 void launch_lanczos_combine(cgpu_ctx* c, z_t* out, const z_t* start) {
   ProfScope prof(c, CGPU_KERNEL_VECTOR);
-  k_lz_combine<<<bgrid(c, c->lzBlocks), LZ_THREADS, 0, c->stream>>>(out, start, c->basis_d, c->nS, TRAJ_PASS(c),
-                                                                    c->lz_d);
+  auto comb = c->ciDf ? k_lz_combine<true> : k_lz_combine<false>;
+  comb<<<bgrid(c, c->lzBlocks), LZ_THREADS, 0, c->stream>>>(out, start, c->basis_d, c->nS, TRAJ_PASS(c), c->lz_d);
   CODY_LAUNCHED(c);
 }
 

@@ -431,8 +431,12 @@ __global__ void __launch_bounds__(256) k_fx_split_V(__nv_bfloat16* __restrict__ 
   fx_row(out + (size_t)g * L * pitch, eV + g, nG, T.Kg, pitch, b, L, 0, [&](int k) { return row[k]; });
 }
 
-// Row 2p + s of S: (re, im)[conj(phi_l) phi_k w] over the grid (p = (l, k)).
-// Block 0 of a trajectory also clears the W exponent maxima for GEMM1.
+// Rows 2p (real part) and 2p + 1 (imaginary part) of S = conj(phi_l) phi_k w
+// over the grid (p = (l, k)), one block per pair: the complex product and the
+// weight in double-float arithmetic (FP32 pipe; ~2^-44 relative, far below the
+// digits' 2^-36 of the row maximum), both rows staged in shared memory, each
+// with the exponent of its own maximum.  Block 0 of a trajectory also clears
+// the W exponent maxima for GEMM1.
 template <int BT, int LT>
 __global__ void __launch_bounds__(256) k_fx_split_S(__nv_bfloat16* __restrict__ out, int* __restrict__ eS,
                                                      unsigned* __restrict__ mWr, unsigned* __restrict__ mWc,
@@ -440,27 +444,55 @@ __global__ void __launch_bounds__(256) k_fx_split_S(__nv_bfloat16* __restrict__ 
                                                      const int* __restrict__ pl, const int* __restrict__ pk, int pitch,
                                                      int b, int L, TRAJ_ARGS) {
   const TrajShape& T = shp[blockIdx.z];
-  const int row = blockIdx.x, nG = T.nG, nP = T.nPairs;
-  if (row >= 2 * nP) return;
+  const int p = blockIdx.x, nG = T.nG, nP = T.nPairs;
+  if (p >= nP) return;
   out = bat(out, bs);
   eS = bat(eS, bs);
   orbs = bat(orbs, bs);
   w = bat(w, bs);
   pl = bat(pl, bs);
   pk = bat(pk, bs);
-  if (row == 0) {
+  if (p == 0) {
     mWr = bat(mWr, bs);
     mWc = bat(mWc, bs);
     for (int i = threadIdx.x; i < nG; i += blockDim.x) mWr[i] = 0u;
     for (int i = threadIdx.x; i < 2 * nP; i += blockDim.x) mWc[i] = 0u;
   }
-  const int p = row >> 1, s = row & 1;
+  extern __shared__ double fxbuf[];  // [2][pitch]: the real and the imaginary row
   const z_t* a = orbs + (size_t)nG * pl[p];
   const z_t* bo = orbs + (size_t)nG * pk[p];
-  fx_row<BT, LT>(out + (size_t)row * L * pitch, eS + row, nG, T.Kg, pitch, b, L, T.gShift, [&](int g) {
-    const z_t v = zcmul(a[g], bo[g]);
-    return (s ? v.y : v.x) * w[g];
-  });
+  unsigned mr = 0, mi = 0;
+  for (int g = threadIdx.x; g < nG; g += blockDim.x) {
+    const z_t av = a[g], bv = bo[g];
+    const float2 ar = df_split(av.x), ai = df_split(av.y), br = df_split(bv.x), bi = df_split(bv.y);
+    const float2 wg = df_split(w[g]);
+    // conj(a) b = (ar br + ai bi) + i (ar bi - ai br)
+    const float2 re = df_dot2(ar, br, ai, bi);
+    const float2 im = df_dot2(ar, bi, make_float2(-ai.x, -ai.y), br);
+    float s0 = 0.0f, c0 = 0.0f, s1 = 0.0f, c1 = 0.0f;
+    df_mul_acc(s0, c0, re.x, re.y, wg.x, wg.y);
+    df_mul_acc(s1, c1, im.x, im.y, wg.x, wg.y);
+    const double vr = df_to_d(make_float2(s0, c0)), vi = df_to_d(make_float2(s1, c1));
+    fxbuf[g] = vr;
+    fxbuf[pitch + g] = vi;
+    mr = max(mr, fx_biased_exp(vr));
+    mi = max(mi, fx_biased_exp(vi));
+  }
+  const int er = fx_exp(fx_block_max(mr));
+  const int ei = fx_exp(fx_block_max(mi));
+  if (threadIdx.x == 0) {
+    eS[2 * p] = er;
+    eS[2 * p + 1] = ei;
+  }
+  __nv_bfloat16* rowR = out + (size_t)(2 * p) * L * pitch;
+  __nv_bfloat16* rowI = out + (size_t)(2 * p + 1) * L * pitch;
+  const int Kpad = T.Kg, shift = T.gShift;
+  for (int k = threadIdx.x; k < Kpad; k += blockDim.x) {
+    const int src = k - shift;
+    const bool valid = src >= 0 && src < nG;
+    fx_store_t<BT, LT>(rowR, pitch, k, valid, valid ? fxbuf[src] : 0.0, er, b, L);
+    fx_store_t<BT, LT>(rowI, pitch, k, valid, valid ? fxbuf[pitch + src] : 0.0, ei, b, L);
+  }
 }
 
 // Row n = 2q + s of R'' (K = 2p + t), as k_split_R.
@@ -896,7 +928,10 @@ void correlation_fx(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs, int wantH2) {
     auto split_s = k_fx_split_S<0, 0>;
     if (m->b1 == 6 && m->LS == 6) split_s = k_fx_split_S<6, 6>;
     else if (m->b1 == 6 && m->LS == 5) split_s = k_fx_split_S<6, 5>;
-    split_s<<<dim3(2 * nP, 1, c->nb), 256, sizeof(double) * m->KgMax, c->stream>>>(
+    const size_t shS = 2 * sizeof(double) * m->KgMax;
+    if (shS > 48 * 1024)
+      CODY_CUDA(cudaFuncSetAttribute(split_s, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shS));
+    split_s<<<dim3(nP, 1, c->nb), 256, shS, c->stream>>>(
         m->SxA, m->eS, m->mWr, m->mWc, orbs, c->w_d, c->pairL_d, c->pairK_d, m->KgMax, m->b1, m->LS, TRAJ_PASS(c));
     CODY_LAUNCHED(c);
     fx_run_W(c);
