@@ -602,23 +602,41 @@ __global__ void k_fold_h2(z_t* __restrict__ h2Lin, float4* __restrict__ h2Df, co
 // (FP64) is written when non-null, h2Df when non-null.  Only the codes of
 // FillH2Lin's rule are written: the CI apply reads no other code, and the
 // others keep the zeros of the set-up.
+// The valid entries i1 < i2, j1 < j2 as pairs p1 = (i1, i2), p2 = (j1, j2) in
+// the triangle order (a shared-memory table of P = nO (nO - 1) / 2 pairs): each
+// block takes FOLD_CHUNK consecutive p1, its threads all p2; entry
+// e = ((i1 nO + j1) nO + i2) nO + j2.
+constexpr int FOLD_CHUNK = 8;
+constexpr int FOLD_MAX_NO = 64;
 __global__ void k_fold_h2s(z_t* __restrict__ h2Lin, float4* __restrict__ h2Df, const z_t* __restrict__ H2s,
                            const int* __restrict__ btOf, TRAJ_ARGS) {
   const TrajShape& T = shp[blockIdx.z];
-  const int nO = T.nO, n = T.nOS, restricted = T.restricted;
-  size_t n4 = (size_t)nO * nO * nO * nO;
+  const int nO = T.nO, n = T.nOS, restricted = T.restricted, P = nO * (nO - 1) / 2;
+  const int p1a = blockIdx.x * FOLD_CHUNK;
+  if (p1a >= P) return;
   h2Lin = bat(h2Lin, bs);
   h2Df = bat(h2Df, bs);
   H2s = bat(H2s, bs);
   btOf = bat(btOf, bs);
-  GRID_STRIDE(e, n4) {
-    int j2 = (int)(e % nO), i2 = (int)((e / nO) % nO), j1 = (int)((e / nO / nO) % nO), i1 = (int)(e / nO / nO / nO);
-    if (!(i1 < i2 && j1 < j2 && bt_rule_ok(btOf, i1, i2, j1, j2))) continue;
-    const z_t v = h2lin_value(btOf, i1, j1, i2, j2, [&](int a, int b, int c, int d) {
-      return h2_from_h2s(H2s, btOf, restricted, n, a, b, c, d);
-    });
-    if (h2Lin) h2Lin[e + 1] = v;
-    if (h2Df) h2Df[e + 1] = zdf_from(v);
+  __shared__ unsigned char pa[FOLD_MAX_NO * (FOLD_MAX_NO - 1) / 2], pb[FOLD_MAX_NO * (FOLD_MAX_NO - 1) / 2];
+  for (int u = 0, base = 0; u < nO - 1; base += nO - 1 - u, u++)
+    for (int v = u + 1 + (int)threadIdx.x; v < nO; v += blockDim.x) {
+      pa[base + v - u - 1] = (unsigned char)u;
+      pb[base + v - u - 1] = (unsigned char)v;
+    }
+  __syncthreads();
+  for (int p1 = p1a; p1 < min(P, p1a + FOLD_CHUNK); p1++) {
+    const int i1 = pa[p1], i2 = pb[p1];
+    for (int p2 = threadIdx.x; p2 < P; p2 += blockDim.x) {
+      const int j1 = pa[p2], j2 = pb[p2];
+      if (!bt_rule_ok(btOf, i1, i2, j1, j2)) continue;
+      const z_t v = h2lin_value(btOf, i1, j1, i2, j2, [&](int a, int b, int c, int d) {
+        return h2_from_h2s(H2s, btOf, restricted, n, a, b, c, d);
+      });
+      const size_t e = (((size_t)i1 * nO + j1) * nO + i2) * nO + j2;
+      if (h2Lin) h2Lin[e + 1] = v;
+      if (h2Df) h2Df[e + 1] = zdf_from(v);
+    }
   }
 }
 
@@ -946,9 +964,10 @@ void launch_fold_h2(cgpu_ctx* c) {
   if (c->fuseLayouts) {
     // h2Lin from the spatial H2s; the FP64 copy only when the FP64 CI apply reads it
     const bool dfOnly = c->ciDf && c->ciSmem > 0;
-    k_fold_h2s<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(dfOnly ? nullptr : c->h2Lin_d,
-                                                                  c->ciDf ? c->h2Df_d : nullptr, c->h2s_d,
-                                                                  c->btOfOrb_d, TRAJ_PASS(c));
+    if (c->nO > FOLD_MAX_NO) throw std::string("FillH2Lin: more than 64 spin orbitals is not supported");
+    const int P = c->nO * (c->nO - 1) / 2;
+    k_fold_h2s<<<dim3((unsigned)ceil_div(P, FOLD_CHUNK), 1, c->nb), 128, 0, c->stream>>>(
+        dfOnly ? nullptr : c->h2Lin_d, c->ciDf ? c->h2Df_d : nullptr, c->h2s_d, c->btOfOrb_d, TRAJ_PASS(c));
   } else {
     k_fold_h2<<<bgrid(c, ew_blocks(c, n4)), 256, 0, c->stream>>>(c->h2Lin_d, c->ciDf ? c->h2Df_d : nullptr, c->h2_d,
                                                                  c->btOfOrb_d, TRAJ_PASS(c));

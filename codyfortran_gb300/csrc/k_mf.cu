@@ -473,9 +473,10 @@ __global__ void k_build_r2s_lin(z_t* __restrict__ r2s, const z_t* __restrict__ l
   btOf = bat(btOf, bs);
   const size_t N = T.nO;
   auto R2 = [&](int a, int b, int c, int d) { return rdm2_from_lin(lin, btOf, N, a, b, c, d); };
-  GRID_STRIDE(e, Q * Q) {
-    int row = (int)(e / Q), col = (int)(e % Q);
-    int l2 = row / n, k2 = row % n, k1 = col / n, k = col % n;
+  const int Qi = (int)Q;
+  GRID_STRIDE(e, Q * Q) {  // Q^2 < 2^31: 32-bit index arithmetic
+    const int ei = (int)e, row = ei / Qi, col = ei - row * Qi;
+    const int l2 = row / n, k2 = row - l2 * n, k1 = col / n, k = col - k1 * n;
     z_t r = zmk(0.0, 0.0);
     if (restricted)
       r = zadd(zadd(zadd(R2(k1, k2, k, l2), R2(n + k1, k2, n + k, l2)), R2(k1, n + k2, k, n + l2)),
@@ -487,25 +488,38 @@ __global__ void k_build_r2s_lin(z_t* __restrict__ r2s, const z_t* __restrict__ l
 }
 
 // R'[(l2*n+k2)][(k1*n+j)] = sum_k r2s[(l2,k2)][(k1,k)] Mreg(k,j), masked by body types.
+// One block per row (l2, k2) of R' (blockIdx.x), threads over its Q columns.
+// DF: the products in double-float arithmetic (the fixed-point forms: 4 n FP64
+// FMA per entry would hold the FP64 pipe), Mreg staged as double-floats.
+template <bool DF>
 __global__ void k_build_R(z_t* __restrict__ Rp, const z_t* __restrict__ r2s, const z_t* __restrict__ Mreg,
                           const int* __restrict__ btOf, TRAJ_ARGS) {
   const TrajShape& T = shp[blockIdx.z];
-  const int n = T.nOS, restricted = T.restricted;
-  size_t Q = (size_t)n * n;
+  const int n = T.nOS, restricted = T.restricted, Q = n * n, row = blockIdx.x;
+  if (row >= Q) return;
   Rp = bat(Rp, bs);
   r2s = bat(r2s, bs);
   Mreg = bat(Mreg, bs);
   btOf = bat(btOf, bs);
-  GRID_STRIDE(e, Q * Q) {
-    int row = (int)(e / Q), col = (int)(e % Q);
-    int l2 = row / n, k2 = row % n, k1 = col / n, j = col % n;
+  __shared__ float4 mdf[JB_MAX * JB_MAX];  // n <= JB_MAX (checked by the launcher)
+  if (DF) {
+    for (int i = threadIdx.x; i < Q; i += blockDim.x) mdf[i] = zdf_from(Mreg[i]);
+    __syncthreads();
+  }
+  const int l2 = row / n, k2 = row - l2 * n;
+  for (int col = threadIdx.x; col < Q; col += blockDim.x) {
+    const int k1 = col / n, j = col - k1 * n;
+    const bool ok = restricted || (btOf[l2] == btOf[k2] && btOf[k1] == btOf[j]);
+    const z_t* rr = r2s + (size_t)row * Q + (size_t)k1 * n;
     z_t v = zmk(0.0, 0.0);
-    bool ok = restricted || (btOf[l2] == btOf[k2] && btOf[k1] == btOf[j]);
-    if (ok) {
-      const z_t* rr = r2s + (size_t)row * Q + (size_t)k1 * n;
+    if (ok && DF) {
+      zdf_acc a = {0.0f, 0.0f, 0.0f, 0.0f};
+      for (int k = 0; k < n; k++) zdf_fma(a, zdf_from(rr[k]), mdf[k + n * j], false);
+      v = zdf_to_z(a);
+    } else if (ok) {
       for (int k = 0; k < n; k++) zfma(v, rr[k], Mreg[k + (size_t)n * j]);
     }
-    Rp[e] = v;
+    Rp[(size_t)row * Q + col] = v;
   }
 }
 
@@ -605,8 +619,9 @@ void launch_rdm_inverse(cgpu_ctx* c) {
     k_build_r2s<<<bgrid(c, ew_blocks(c, Q * Q)), 256, 0, c->stream>>>(c->r2s_d, c->rdm2_d, c->btOfOrb_d,
                                                                      TRAJ_PASS(c));
   CODY_LAUNCHED(c);
-  k_build_R<<<bgrid(c, ew_blocks(c, Q * Q)), 256, 0, c->stream>>>(c->Rp_d, c->r2s_d, c->Mreg_d, c->btOfOrb_d,
-                                                                    TRAJ_PASS(c));
+  auto buildR = c->ciDf ? k_build_R<true> : k_build_R<false>;
+  buildR<<<dim3((unsigned)Q, 1, c->nb), 128, 0, c->stream>>>(c->Rp_d, c->r2s_d, c->Mreg_d, c->btOfOrb_d,
+                                                             TRAJ_PASS(c));
   CODY_LAUNCHED(c);
 }
 
