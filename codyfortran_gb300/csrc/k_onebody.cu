@@ -448,6 +448,47 @@ __global__ void k_project_apply(z_t* __restrict__ dOrbs, const z_t* __restrict__
   dOrbs[o] = zsub(dOrbs[o], acc);
 }
 
+// k_project_apply in double-float arithmetic (the fixed-point forms): one
+// thread per grid point for all j, PA_J at a time, G staged as double-floats
+// (n <= PA_MAXN), phi_i(g) split once per batch of j.
+constexpr int PA_J = 8, PA_MAXN = 32;
+__global__ void __launch_bounds__(128) k_project_apply_df(z_t* __restrict__ dOrbs, const z_t* __restrict__ orbs,
+                                                           const z_t* __restrict__ G, TRAJ_ARGS, int group) {
+  const TrajShape& S = shp[blockIdx.z];
+  int c0, n;
+  if (!gram_cols(S, group, c0, n)) return;
+  const int nG = S.nG;
+  dOrbs = bat(dOrbs, bs);
+  orbs = bat(orbs, bs);
+  G = bat(G, bs);
+  __shared__ float4 gdf[PA_MAXN * PA_MAXN];
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {  // -G, so that the sums subtract
+    const z_t v = G[e];
+    gdf[e] = zdf_from(zmk(-v.x, -v.y));
+  }
+  __syncthreads();
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nG) return;
+  for (int j0 = 0; j0 < n; j0 += PA_J) {
+    zdf_acc acc[PA_J];
+#pragma unroll
+    for (int q = 0; q < PA_J; q++) {
+      const float4 d =
+          (j0 + q < n) ? zdf_from(dOrbs[(size_t)nG * (c0 + j0 + q) + g]) : make_float4(0.f, 0.f, 0.f, 0.f);
+      acc[q] = {d.x, d.y, d.z, d.w};
+    }
+    for (int i = 0; i < n; i++) {
+      const float4 o = zdf_from(orbs[(size_t)nG * (c0 + i) + g]);
+#pragma unroll
+      for (int q = 0; q < PA_J; q++)
+        if (j0 + q < n) zdf_fma(acc[q], gdf[i + n * (j0 + q)], o, false);
+    }
+#pragma unroll
+    for (int q = 0; q < PA_J; q++)
+      if (j0 + q < n) dOrbs[(size_t)nG * (c0 + j0 + q) + g] = zdf_to_z(acc[q]);
+  }
+}
+
 // h1 (nO x nO) from the stored-orbital Gram G (nOS x nOS): same body type only,
 // restricted runs duplicate the block for the second spin (FillH1 :203-222).
 __global__ void k_h1_layout(z_t* __restrict__ h1, const z_t* __restrict__ G, const int* __restrict__ btOf,
@@ -767,6 +808,11 @@ __global__ void k_gram_partial_df(z_t* __restrict__ part, const z_t* __restrict_
   float4* sa = shg;              // chunk x n
   float4* sb = shg + chunk * n;  // chunk x n
   int nn = n * n;
+  // small blocks (n^2 <= blockDim / 2): the rows of a chunk spread over R phases;
+  // their R x n^2 partials reuse the tiles' 2 chunk n >= 2 chunk n (batch maximum)
+  // double-floats, hence R <= 2 chunk / n
+  const int R = nn * 2 <= (int)blockDim.x ? min(min(chunk, (int)blockDim.x / nn), 2 * chunk / n) : 1;
+  const int e0 = threadIdx.x % nn, ph = threadIdx.x / nn, ii0 = e0 % n, jj0 = e0 / n;
   zdf_acc acc[GR_PER_THREAD];
   for (int q = 0; q < GR_PER_THREAD; q++) acc[q] = {0.0f, 0.0f, 0.0f, 0.0f};
   for (int r0 = blockIdx.x * chunk; r0 < nG; r0 += gridDim.x * chunk) {
@@ -788,15 +834,39 @@ __global__ void k_gram_partial_df(z_t* __restrict__ part, const z_t* __restrict_
       sb[r * n + col] = b;
     }
     __syncthreads();
+    if (R > 1) {  // entry threadIdx.x % nn, rows of phase threadIdx.x / nn
+      if (ph < R) {
+        zdf_acc s = acc[0];
+        for (int r = ph; r < chunk; r += R) zdf_cfma(s, sa[r * n + ii0], sb[r * n + jj0], false);
+        acc[0] = s;
+      }
+    } else {
 #pragma unroll
-    for (int q = 0; q < GR_PER_THREAD; q++) {
-      int e = threadIdx.x + q * blockDim.x;
-      if (e >= nn) break;
-      int ii = e % n, jj = e / n;
-      zdf_acc s = acc[q];
-      for (int r = 0; r < chunk; r++) zdf_cfma(s, sa[r * n + ii], sb[r * n + jj], false);
-      acc[q] = s;
+      for (int q = 0; q < GR_PER_THREAD; q++) {
+        int e = threadIdx.x + q * blockDim.x;
+        if (e >= nn) break;
+        int ii = e % n, jj = e / n;
+        zdf_acc s = acc[q];
+        for (int r = 0; r < chunk; r++) zdf_cfma(s, sa[r * n + ii], sb[r * n + jj], false);
+        acc[q] = s;
+      }
     }
+  }
+  if (R > 1) {  // the R phase partials of each entry, summed in a fixed order
+    __syncthreads();
+    float4* red = shg;  // R x nn <= blockDim entries (the tiles are no longer read)
+    if (ph < R) red[ph * nn + e0] = make_float4(acc[0].rs, acc[0].rc, acc[0].is, acc[0].ic);
+    __syncthreads();
+    if (threadIdx.x < nn) {
+      zdf_acc t = {0.0f, 0.0f, 0.0f, 0.0f};
+      for (int k = 0; k < R; k++) {
+        const float4 v = red[k * nn + threadIdx.x];
+        df_acc(t.rs, t.rc, v.x, v.y);
+        df_acc(t.is, t.ic, v.z, v.w);
+      }
+      part[(size_t)blockIdx.x * nn + threadIdx.x] = zdf_to_z(t);
+    }
+    return;
   }
 #pragma unroll
   for (int q = 0; q < GR_PER_THREAD; q++) {
@@ -897,8 +967,13 @@ void launch_project_orbs(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs) {
     int n = max_group_size(c, g);
     if (n <= 0) continue;
     launch_gram(c, c->gram_d, orbs, dOrbs, g, n, 1.0);
-    dim3 grid(ceil_div(c->nG, 256), n, c->nb);
-    k_project_apply<<<grid, 256, 0, c->stream>>>(dOrbs, orbs, c->gram_d, TRAJ_PASS(c), g);
+    if (c->ciDf && n <= PA_MAXN) {
+      k_project_apply_df<<<dim3(ceil_div(c->nG, 128), 1, c->nb), 128, 0, c->stream>>>(dOrbs, orbs, c->gram_d,
+                                                                                     TRAJ_PASS(c), g);
+    } else {
+      dim3 grid(ceil_div(c->nG, 256), n, c->nb);
+      k_project_apply<<<grid, 256, 0, c->stream>>>(dOrbs, orbs, c->gram_d, TRAJ_PASS(c), g);
+    }
     CODY_LAUNCHED(c);
   }
 }
