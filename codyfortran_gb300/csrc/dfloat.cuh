@@ -63,8 +63,10 @@ DF_HD int df_msb(unsigned r) {
 }
 
 // x as hi + lo: hi = the leading 24 bits (truncated), lo = the next 29 bits
-// rounded down to 24 (an FP32 subnormal, with fewer bits, below 2^-126);
-// |x| < 2^-100 becomes 0 and |x| >= 2^128 infinity.
+// rounded to the nearest 24 (an FP32 subnormal, with fewer bits, below
+// 2^-126); |x| < 2^-100 becomes 0 and |x| >= 2^128 infinity.  Rounding, not
+// truncation: a value split and converted back many times (a state advanced
+// over thousands of steps) must not drift by a one-sided bias.
 DF_HD float2 df_split(double x) {
   const unsigned long long u = df_bits64(x);
   const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
@@ -72,9 +74,14 @@ DF_HD float2 df_split(double x) {
   if (e < -100) return make_float2(0.0f, 0.0f);
   if (e > 127) return make_float2(df_float(sign | 0x7F800000u), 0.0f);
   const float hi = df_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)((u >> 29) & 0x7FFFFF));
-  const unsigned r = (unsigned)(u & 0x1FFFFFFF);  // value r 2^(e-52)
+  unsigned r = (unsigned)(u & 0x1FFFFFFF);  // value r 2^(e-52)
   if (r == 0) return make_float2(hi, 0.0f);
-  const int msb = df_msb(r);
+  int msb = df_msb(r);
+  if (msb > 23) {  // round r to its leading 24 bits (half to even); may carry to 2^(msb+1)
+    const int sh = msb - 23;
+    r = ((r + (1u << (sh - 1)) - 1u + ((r >> sh) & 1u)) >> sh) << sh;
+    msb = df_msb(r);
+  }
   const int elo = e - 52 + msb;
   if (elo < -126) {  // lo = r 2^(e-52) in units of 2^-149 (below 2^23 here)
     const int sh = e + 97;
@@ -150,8 +157,8 @@ DF_HD double f2d_exact(float f) {
 // scaled lo is or-ed into those bits when the signs agree and subtracted from
 // the 64-bit pattern when they differ -- in units one place finer when hi is
 // a power of two, whose lower neighbours are twice as dense.  Bits of lo below
-// the FP64 last place are dropped (truncation: relative error below 2^-52); a
-// subnormal lo counts with its exponent 2^-126 and no leading bit; hi below
+// the FP64 last place are rounded to the nearest place (half to even);
+// a subnormal lo counts with its exponent 2^-126 and no leading bit; hi below
 // 2^-126 gives 0, an infinite or NaN hi passes through.
 DF_HD double df_to_d(float2 a) {
   const float2 n = df_two_sum(a.x, a.y);
@@ -165,7 +172,8 @@ DF_HD double df_to_d(float2 a) {
   const bool opp = ((H ^ L) & 0x80000000u) != 0;
   const int s = (eL ? eL : 1) - eH + 29 + ((opp && mH == 0) ? 1 : 0);
   const unsigned mL = (L & 0x7FFFFFu) | (eL ? 0x800000u : 0u);
-  const unsigned k = (s >= 0) ? (mL << s) : (s > -24 ? (mL >> -s) : 0u);
+  const unsigned k =
+      (s >= 0) ? (mL << s) : (s > -25 ? ((mL + (1u << (-s - 1)) - 1u + ((mL >> -s) & 1u)) >> -s) : 0u);
   const unsigned long long u = ((unsigned long long)hiw << 32) | low;
   return df_double(opp ? u - k : (u | k));
 }

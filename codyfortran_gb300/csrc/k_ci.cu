@@ -21,9 +21,12 @@
 namespace {
 
 // threads of an RDM pair-gather block (one pair of singles codes per thread):
-// the staged CI vector (up to 72 KB) allows three blocks per SM, so the block
-// size sets the warps in flight for these latency-bound gathers
-constexpr int CI_PAIR_THREADS = 256;
+// the staged CI vector (up to 72 KB) allows three blocks per SM and the
+// registers two of 512 threads, so the block size sets the warps in flight for
+// these latency-bound gathers
+constexpr int CI_PAIR_THREADS = 512;
+// threads of an RDM code-gather block (one code per warp)
+constexpr int CI_RDM_THREADS = 512;
 // threads of an H.C block (one configuration per warp): with 55 registers per
 // thread two 512-thread blocks fit an SM, 32 warps sharing two staged CI vectors
 constexpr int CI_APPLY_THREADS = 512;
@@ -459,7 +462,7 @@ __global__ void k_ci_rdm_pairs(const z_t* __restrict__ C0, z_t* __restrict__ r2L
 // The RDM gathers in double-float arithmetic (the fixed-point forms): as
 // k_ci_rdm_codes / k_ci_rdm_pairs with C staged as double-floats and every
 // product conj(C_J) C_I an FP32 error-free product with two-sum accumulation.
-__global__ void k_ci_rdm_codes_df(const z_t* __restrict__ C0, z_t* __restrict__ r1Lin0, z_t* __restrict__ r2Lin0,
+__global__ void __launch_bounds__(CI_RDM_THREADS, 2) k_ci_rdm_codes_df(const z_t* __restrict__ C0, z_t* __restrict__ r1Lin0, z_t* __restrict__ r2Lin0,
                                   TRAJ_ARGS, const CiWork* __restrict__ work, int want1, int want2) {
   extern __shared__ float4 cdf[];
   const CiWork wk = work[blockIdx.x];
@@ -518,7 +521,7 @@ __global__ void k_ci_rdm_codes_df(const z_t* __restrict__ C0, z_t* __restrict__ 
   }
 }
 
-__global__ void k_ci_rdm_pairs_df(const z_t* __restrict__ C0, z_t* __restrict__ r2Lin0, TRAJ_ARGS,
+__global__ void __launch_bounds__(CI_PAIR_THREADS, 2) k_ci_rdm_pairs_df(const z_t* __restrict__ C0, z_t* __restrict__ r2Lin0, TRAJ_ARGS,
                                   const CiWork* __restrict__ work) {
   extern __shared__ float4 cdf[];
   const CiWork wk = work[blockIdx.x];
@@ -879,7 +882,8 @@ void ci_build_work(cgpu_ctx* c) {
   }
   cut(aw, std::max({64L, aTot / (8 * 152), (long)(CI_APPLY_THREADS / 32) * aTot / std::max(1L, nConfTot)}), 1 << 20,
       apply);
-  cut(rw, std::max({64L, rTot / (8 * 152), 8 * rTot / std::max(1L, nTaskTot)}), 1 << 20, rdm);
+  cut(rw, std::max({64L, rTot / (8 * 152), (long)(CI_RDM_THREADS / 32) * rTot / std::max(1L, nTaskTot)}), 1 << 20,
+      rdm);
   cut(pw, std::max({64L, pTot / (8 * 152), (long)CI_PAIR_THREADS * pTot / std::max(1L, nPairTot)}), 1 << 20, pairs);
   c->nApplyWork = (int)apply.size();
   c->nRdmWork = (int)rdm.size();
@@ -923,7 +927,7 @@ void launch_ci_rdm(cgpu_ctx* c, const z_t* C, int want1, int want2) {
   const bool df = c->ciDf && c->ciSmem > 0;
   if (c->nRdmWork > 0) {
     if (df)
-      k_ci_rdm_codes_df<<<c->nRdmWork, 256, c->ciSmem, c->stream>>>(C, c->rdm1Lin_d, c->rdm2Lin_d, TRAJ_PASS(c),
+      k_ci_rdm_codes_df<<<c->nRdmWork, CI_RDM_THREADS, c->ciSmem, c->stream>>>(C, c->rdm1Lin_d, c->rdm2Lin_d, TRAJ_PASS(c),
                                                                     c->rdmWork_d, want1, want2);
     else
       k_ci_rdm_codes<<<c->nRdmWork, 256, c->ciSmem, c->stream>>>(C, c->rdm1Lin_d, c->rdm2Lin_d, TRAJ_PASS(c),

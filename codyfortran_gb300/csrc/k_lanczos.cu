@@ -379,8 +379,9 @@ __global__ void k_lz_expsub(double* __restrict__ lz, int mFixed, double dt, doub
 
 
 // out = nrm * sum_{j < mDim} phi_j s_j V_j   (or out = in when the start vector had zero norm)
-// DF: the sum in double-float arithmetic (the fixed-point forms; the FP64 form
-// costs 4 m FP64 FMA per entry on the scarce FP64 pipe), rounded once to FP64.
+// DF: the sum in double-float arithmetic on the orbital entries (the
+// fixed-point forms; the FP64 form costs 4 m FP64 FMA per entry on the scarce
+// FP64 pipe), rounded once to FP64; the CI coefficients stay FP64.
 template <bool DF>
 __global__ void k_lz_combine(z_t* __restrict__ out, const z_t* __restrict__ in, const z_t* __restrict__ V,
                              size_t ldv, TRAJ_ARGS, const double* __restrict__ lz) {
@@ -407,7 +408,7 @@ __global__ void k_lz_combine(z_t* __restrict__ out, const z_t* __restrict__ in, 
       out[i] = in[i];
       continue;
     }
-    if (DF) {
+    if (DF && l >= (size_t)S.nC) {  // orbital entries; the coefficients stay FP64
       zdf_acc acc = {0.0f, 0.0f, 0.0f, 0.0f};
       for (int k = 0; k < m; k++) zdf_fma(acc, phiDf[k], zdf_from(V[ldv * k + i]), false);
       out[i] = zdf_to_z(acc);
@@ -513,8 +514,10 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz3_dot(z_t* __restrict__ part, 
 // Pass 2: alpha_j from the pass-1 partials (stored at lz[LZ_D + 2 (j-1)]),
 // u_(j+1) = s_j h - beta_{j-1} v_{j-1} - alpha_j v_j into dst (the next basis
 // slot, or h itself after the last iteration), partials of ||u_(j+1)||_m^2.
-// DF: the update and the norm in double-float arithmetic (the fixed-point
-// forms), each new entry rounded once to FP64.
+// DF: the update and the norm in double-float arithmetic on the orbital
+// entries (the fixed-point forms), each new entry rounded once to FP64; the
+// CI coefficients (the first nC entries, a small share) stay FP64, so that
+// their norm is conserved to FP64 rounding over long runs.
 template <bool DF>
 __global__ void __launch_bounds__(LZ_THREADS) k_lz3_update(z_t* __restrict__ dst, const z_t* __restrict__ w,
                                                             const z_t* __restrict__ vPrev,
@@ -547,8 +550,24 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz3_update(z_t* __restrict__ dst
   if (DF) {
     const float2 sj2 = df_split(sj), nbp2 = df_split(-bp), nas2 = df_split(-as), zero2 = make_float2(0.0f, 0.0f);
     float qs = 0.0f, qc = 0.0f;
+    double qC = 0.0;  // the coefficient entries' norm part, FP64
     for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
       const size_t i = vidx(S, l);
+      if (l < (size_t)S.nC) {
+        const z_t h = w[i];
+        z_t x = zmk(sj * h.x, sj * h.y);
+        if (vPrev) {
+          const z_t p = vPrev[i];
+          x.x = fma(-bp, p.x, x.x);
+          x.y = fma(-bp, p.y, x.y);
+        }
+        const z_t v = vCur[i];
+        x.x = fma(-as, v.x, x.x);
+        x.y = fma(-as, v.y, x.y);
+        dst[i] = x;
+        qC = fma(m[i], fma(x.x, x.x, x.y * x.y), qC);
+        continue;
+      }
       const z_t h = w[i], v = vCur[i];
       float2 pr = zero2, pi = zero2;
       if (vPrev) {
@@ -562,7 +581,7 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lz3_update(z_t* __restrict__ dst
       const float2 u = df_dot2(xr, xr, xi, xi), m2 = df_split(m[i]);
       df_mul_acc(qs, qc, m2.x, m2.y, u.x, u.y);
     }
-    q = f2d_exact(qs) + f2d_exact(qc);
+    q = (f2d_exact(qs) + f2d_exact(qc)) + qC;
   } else
   for (size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x; l < n; l += (size_t)gridDim.x * blockDim.x) {
     const size_t i = vidx(S, l);

@@ -449,8 +449,8 @@ __global__ void k_project_apply(z_t* __restrict__ dOrbs, const z_t* __restrict__
 }
 
 // k_project_apply in double-float arithmetic (the fixed-point forms): one
-// thread per grid point for all j, PA_J at a time, G staged as double-floats
-// (n <= PA_MAXN), phi_i(g) split once per batch of j.
+// thread per grid point and batch of PA_J orbitals j (blockIdx.y), G staged as
+// double-floats (n <= PA_MAXN), phi_i(g) split once per batch.
 constexpr int PA_J = 8, PA_MAXN = 32;
 __global__ void __launch_bounds__(128) k_project_apply_df(z_t* __restrict__ dOrbs, const z_t* __restrict__ orbs,
                                                            const z_t* __restrict__ G, TRAJ_ARGS, int group) {
@@ -468,8 +468,9 @@ __global__ void __launch_bounds__(128) k_project_apply_df(z_t* __restrict__ dOrb
   }
   __syncthreads();
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= nG) return;
-  for (int j0 = 0; j0 < n; j0 += PA_J) {
+  const int j0 = blockIdx.y * PA_J;
+  if (g >= nG || j0 >= n) return;
+  {
     zdf_acc acc[PA_J];
 #pragma unroll
     for (int q = 0; q < PA_J; q++) {
@@ -968,8 +969,8 @@ void launch_project_orbs(cgpu_ctx* c, z_t* dOrbs, const z_t* orbs) {
     if (n <= 0) continue;
     launch_gram(c, c->gram_d, orbs, dOrbs, g, n, 1.0);
     if (c->ciDf && n <= PA_MAXN) {
-      k_project_apply_df<<<dim3(ceil_div(c->nG, 128), 1, c->nb), 128, 0, c->stream>>>(dOrbs, orbs, c->gram_d,
-                                                                                     TRAJ_PASS(c), g);
+      k_project_apply_df<<<dim3(ceil_div(c->nG, 128), ceil_div(n, PA_J), c->nb), 128, 0, c->stream>>>(
+          dOrbs, orbs, c->gram_d, TRAJ_PASS(c), g);
     } else {
       dim3 grid(ceil_div(c->nG, 256), n, c->nb);
       k_project_apply<<<grid, 256, 0, c->stream>>>(dOrbs, orbs, c->gram_d, TRAJ_PASS(c), g);

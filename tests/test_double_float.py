@@ -1,9 +1,12 @@
 """The double-float helpers of the fixed-point forms (codyfortran_gb300/csrc/dfloat.cuh)
 on the host: tests/df_check.cu is compiled by nvcc as host code and checks
-  * the FP64 -> double-float split and back (the low part truncated to 24 bits),
+  * the FP64 -> double-float split and back (the low part rounded to 24 bits),
+    and that the round trip carries no one-sided bias (mean signed relative
+    error over 2e6 values below 1e-17; the earlier truncating split gave
+    -1.5e-15, a drift of the state norm over long runs),
   * the integer FP64 conversion of any (hi, lo) pair against the correctly
-    rounded FP64 sum: within one unit in the last place, exact where the sum
-    is representable,
+    rounded FP64 sum: equal to it (round to nearest, ties to even), and exact
+    where the sum is representable,
   * complex double-float dot products of up to 600 terms against long double
     sums: within 2^-41 of the sum of magnitudes (measured 1.9e-13, about
     2^-42.3: the operands keep 48 bits, the low parts add in FP32),
@@ -30,7 +33,8 @@ def test_double_float_helpers(tmp_path):
     r = json.loads(subprocess.run([exe], check=True, capture_output=True, text=True).stdout)
     assert r["split_bad"] == 0
     assert r["split_rel_max"] < 2.0 ** -46
-    assert r["conv_bad"] == 0 and r["conv_ulps_max"] <= 1.0
+    assert r["conv_bad"] == 0 and r["conv_ulps_max"] <= 0.5
     assert r["conv_exact_cases"] > 100000 and r["conv_exact_bad"] == 0
     assert r["dot_rel_max"] < 2.0 ** -41
     assert r["specials"]
+    assert abs(r["split_bias"]) < 1e-17
