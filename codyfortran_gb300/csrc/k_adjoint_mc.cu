@@ -81,19 +81,53 @@ __global__ void k_mc_zgemm(int M, int N, int K, z_t alpha, const z_t* __restrict
   }
 }
 
-// C = V B (+ C when acc): V the real symmetric nG x nG interaction matrix
+// k_mc_zgemm with one warp per output element (small outputs, long K): lanes
+// stride K, a fixed-order shuffle tree sums them
+__global__ void k_mc_zgemm_w(int M, int N, int K, z_t alpha, const z_t* __restrict__ A, int lda, int opA,
+                             const z_t* __restrict__ B, int ldb, int opB, const double* __restrict__ wk, z_t beta,
+                             z_t* __restrict__ C, int ldc) {
+  const int lane = threadIdx.x & 31;
+  const size_t nw = ((size_t)gridDim.x * blockDim.x) >> 5;
+  for (size_t e = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5; e < (size_t)M * N; e += nw) {
+    const int i = (int)(e % M), j = (int)(e / M);
+    z_t s = zmk(0.0, 0.0);
+    for (int k = lane; k < K; k += 32) {
+      z_t a = opget(A, lda, opA, i, k);
+      if (wk) a = zscale(a, wk[k]);
+      zfma(s, a, opget(B, ldb, opB, k, j));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+      s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+    }
+    if (lane == 0) {
+      z_t r = zmul(alpha, s);
+      if (beta.x != 0.0 || beta.y != 0.0) r = zadd(r, zmul(beta, C[i + (size_t)ldc * j]));
+      C[i + (size_t)ldc * j] = r;
+    }
+  }
+}
+
+// C = V B (+ C when acc): V the real symmetric nG x nG interaction matrix; one
+// warp per output element (lanes over the row of V and the column of B)
 __global__ void k_mc_vgemm(int nG, int N, const double* __restrict__ V, const z_t* __restrict__ B, z_t* __restrict__ C,
                            int acc) {
-  MC_LOOP(e, (size_t)nG * N) {
+  const int lane = threadIdx.x & 31;
+  const size_t nw = ((size_t)gridDim.x * blockDim.x) >> 5;
+  for (size_t e = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5; e < (size_t)nG * N; e += nw) {
     const int x = (int)(e % nG), j = (int)(e / nG);
     const double* Vr = V + (size_t)x * nG;
     const z_t* b = B + (size_t)nG * j;
     z_t s = zmk(0.0, 0.0);
-    for (int y = 0; y < nG; y++) {
+    for (int y = lane; y < nG; y += 32) {
       s.x = fma(Vr[y], b[y].x, s.x);
       s.y = fma(Vr[y], b[y].y, s.y);
     }
-    C[e] = acc ? zadd(C[e], s) : s;
+    for (int o = 16; o > 0; o >>= 1) {
+      s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+      s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+    }
+    if (lane == 0) C[e] = acc ? zadd(C[e], s) : s;
   }
 }
 
@@ -203,20 +237,41 @@ __device__ void herm_jacobi(z_t (*A)[JM + 1], z_t (*V)[JM + 1], int n, double* e
   }
   __syncthreads();
   const int ne = (n + 1) & ~1, half = ne / 2;
+  __shared__ double redOff[32], redDg[32];
+  double prevOffs = -1.0;
   for (int sweep = 0; sweep < 40 && n > 1; sweep++) {
-    if (tid == 0) {
+    {  // off-diagonal and diagonal mass: per-thread strided sums, warp trees, warps in order
       double off = 0.0, dg = 0.0;
-      for (int j = 0; j < n; j++)
-        for (int i = 0; i < n; i++) {
-          const double a2 = A[i][j].x * A[i][j].x + A[i][j].y * A[i][j].y;
-          if (i == j) dg += a2;
-          else off += a2;
+      for (int e = tid; e < n * n; e += blockDim.x) {
+        const int i = e % n, j = e / n;
+        const double a2 = A[i][j].x * A[i][j].x + A[i][j].y * A[i][j].y;
+        if (i == j) dg += a2;
+        else off += a2;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        off += __shfl_xor_sync(0xffffffffu, off, o);
+        dg += __shfl_xor_sync(0xffffffffu, dg, o);
+      }
+      if ((tid & 31) == 0) {
+        redOff[tid >> 5] = off;
+        redDg[tid >> 5] = dg;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        double o2 = 0.0, d2 = 0.0;
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) {
+          o2 += redOff[w];
+          d2 += redDg[w];
         }
-      offs = off;
-      diags = dg;
+        offs = o2;
+        diags = d2;
+      }
+      __syncthreads();
     }
-    __syncthreads();
+    // converged, or at the rounding floor (below 1e-24 of the mass and no longer halving)
     if (offs <= 1e-30 * (diags + offs) || offs == 0.0) break;
+    if (offs <= 1e-24 * (diags + offs) && prevOffs >= 0.0 && offs > 0.5 * prevOffs) break;
+    prevOffs = offs;
     for (int r = 0; r < ne - 1; r++) {
       if (tid < half) {
         const int k = tid;
@@ -479,18 +534,29 @@ __global__ void k_mc_build_R(z_t* __restrict__ R, const z_t* __restrict__ r2, co
 }
 
 // dphi0[x, j] = sum_{a, k, l} Wp[x, l + M k] phi[x, a] R[a, k, j, l]
-__global__ void k_mc_meanfield(z_t* __restrict__ dphi, const z_t* __restrict__ Wp, const z_t* __restrict__ phi,
+// the l-th term of k_mc_meanfield's sum, Y[x, j + M l], one thread each
+// (nG M^2 threads; the sum over l follows in k_mc_meanfield_sum in order)
+__global__ void k_mc_meanfield(z_t* __restrict__ Y, const z_t* __restrict__ Wp, const z_t* __restrict__ phi,
                                const z_t* __restrict__ R, int nG, int M) {
   const int Q = M * M;
+  MC_LOOP(e, (size_t)nG * Q) {
+    const int x = (int)(e % nG), jl = (int)(e / nG), j = jl % M, l = jl / M;
+    z_t s = zmk(0.0, 0.0);
+    for (int k = 0; k < M; k++) {
+      z_t t = zmk(0.0, 0.0);
+      for (int a = 0; a < M; a++) zfma(t, phi[x + (size_t)nG * a], R[a + M * k + (size_t)Q * (j + M * l)]);
+      zfma(s, Wp[x + (size_t)nG * (l + M * k)], t);
+    }
+    Y[e] = s;
+  }
+}
+
+// dphi[x, j] = sum_l Y[x, j + M l] (fixed order)
+__global__ void k_mc_meanfield_sum(z_t* __restrict__ dphi, const z_t* __restrict__ Y, int nG, int M) {
   MC_LOOP(e, (size_t)nG * M) {
     const int x = (int)(e % nG), j = (int)(e / nG);
     z_t s = zmk(0.0, 0.0);
-    for (int l = 0; l < M; l++)
-      for (int k = 0; k < M; k++) {
-        z_t t = zmk(0.0, 0.0);
-        for (int a = 0; a < M; a++) zfma(t, phi[x + (size_t)nG * a], R[a + M * k + (size_t)Q * (j + M * l)]);
-        zfma(s, Wp[x + (size_t)nG * (l + M * k)], t);
-      }
+    for (int l = 0; l < M; l++) s = zadd(s, Y[x + (size_t)nG * (j + M * l)]);
     dphi[e] = s;
   }
 }
@@ -926,7 +992,14 @@ double field_at(const McAdjoint& A, double t, int* idx) {
 
 void mc_zgemm(cgpu_ctx* c, int M, int N, int K, z_t alpha, const z_t* A, int lda, int opA, const z_t* B, int ldb,
               int opB, const double* wk, z_t beta, z_t* C, int ldc) {
-  k_mc_zgemm<<<nblk((size_t)M * N), MC_T, 0, c->stream>>>(M, N, K, alpha, A, lda, opA, B, ldb, opB, wk, beta, C, ldc);
+  // small outputs over a long K (the M x M and Q x Q products over the grid,
+  // whose operands are K-contiguous): a warp per output; otherwise a thread
+  if ((size_t)M * N <= 8192 && K >= 128)
+    k_mc_zgemm_w<<<nblk((size_t)M * N * 32), MC_T, 0, c->stream>>>(M, N, K, alpha, A, lda, opA, B, ldb, opB, wk, beta,
+                                                                     C, ldc);
+  else
+    k_mc_zgemm<<<nblk((size_t)M * N), MC_T, 0, c->stream>>>(M, N, K, alpha, A, lda, opA, B, ldb, opB, wk, beta, C,
+                                                             ldc);
   CODY_LAUNCHED(c);
 }
 
@@ -952,7 +1025,7 @@ void nonlin_forward(cgpu_ctx* c, McAdjoint& A, const z_t* s, z_t* out, double E)
   mc_zgemm(c, M, M, nG, ONE, phi, nG, 2, A.Aphi, nG, 0, c->w_d, ZERO, A.h1, M);
   k_mc_pairs<<<nblk((size_t)nG * Q), MC_T, 0, c->stream>>>(A.Sp, phi, c->w_d, nG, M);
   CODY_LAUNCHED(c);
-  k_mc_vgemm<<<nblk((size_t)nG * Q), MC_T, 0, c->stream>>>(nG, Q, c->Vint_d, A.Sp, A.Wp, 0);
+  k_mc_vgemm<<<nblk((size_t)nG * Q * 32), MC_T, 0, c->stream>>>(nG, Q, c->Vint_d, A.Sp, A.Wp, 0);
   CODY_LAUNCHED(c);
   mc_zgemm(c, Q, Q, nG, ONE, A.Sp, nG, 1, A.Wp, nG, 0, nullptr, ZERO, A.g2, Q);
   k_mc_dc0<<<nblk(Q), MC_T, 0, c->stream>>>(A.dC0, A.h1, C, A.g2, M);
@@ -963,7 +1036,9 @@ void nonlin_forward(cgpu_ctx* c, McAdjoint& A, const z_t* s, z_t* out, double E)
   CODY_LAUNCHED(c);
   k_mc_build_R<<<nblk((size_t)Q * Q), MC_T, 0, c->stream>>>(A.R, A.r2, A.Mreg, M);
   CODY_LAUNCHED(c);
-  k_mc_meanfield<<<nblk((size_t)nG * M), MC_T, 0, c->stream>>>(A.dphi0, A.Wp, phi, A.R, nG, M);
+  k_mc_meanfield<<<nblk((size_t)nG * Q), MC_T, 0, c->stream>>>(A.Q1, A.Wp, phi, A.R, nG, M);  // Q1: scratch here
+  CODY_LAUNCHED(c);
+  k_mc_meanfield_sum<<<nblk((size_t)nG * M), MC_T, 0, c->stream>>>(A.dphi0, A.Q1, nG, M);
   CODY_LAUNCHED(c);
   mc_dot(c, A.sc, C, A.dC0, nullptr, Q);
   mc_zgemm(c, M, M, nG, ONE, phi, nG, 2, A.dphi0, nG, 0, c->w_d, ZERO, A.Gp, M);
@@ -1037,7 +1112,7 @@ void nonlin_vjp(cgpu_ctx* c, McAdjoint& A, const z_t* s, const z_t* obar, z_t* s
   k_mc_rdm_vjp<<<nblk(Q), MC_T, 0, c->stream>>>(A.Cbar, A.r1bar, A.r2bar, C, M);
   CODY_LAUNCHED(c);
   // pair potentials
-  k_mc_vgemm<<<nblk((size_t)nG * Q), MC_T, 0, c->stream>>>(nG, Q, c->Vint_d, A.Wpbar, A.Spbar, 0);
+  k_mc_vgemm<<<nblk((size_t)nG * Q * 32), MC_T, 0, c->stream>>>(nG, Q, c->Vint_d, A.Wpbar, A.Spbar, 0);
   CODY_LAUNCHED(c);
   k_mc_pairs_vjp<<<nblk((size_t)nG * M), MC_T, 0, c->stream>>>(A.phibar, A.Spbar, phi, c->w_d, nG, M);
   CODY_LAUNCHED(c);
